@@ -1,0 +1,371 @@
+// C ABI of the GB300 BTA solver (declared in include/pyinla_gb300.h).
+//
+// A gbta_solver plays the role of the reference's SerinvSolver object
+// (src/pyinla/solvers/structured_solver.py:19-70) without the block buffers, which
+// the caller owns: it holds the geometry, the device workspace of the dataflow
+// kernels (tile flags, task lists, partial buffers, the selected-inversion output
+// blocks) and the stream the work is enqueued on.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/pyinla_gb300.h"
+#include "bta_internal.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+#define GBTA_CUDA(call)                                                                   \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess)                                                                \
+      return fail(GBTA_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+  } while (0)
+
+constexpr int CTRL_INTS = 8;
+constexpr int CTRL_INFO = 2, CTRL_ERR = 3;   // sticky status words of the control block
+
+}  // namespace
+
+struct gbta_solver {
+  gbta::Geom g;
+  int device = 0;
+  int nsm = 0;
+  int ctas_per_sm = 1;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  unsigned long long wait_ns = 20ull * 1000 * 1000 * 1000;
+  int epoch = 0;
+
+  int* d_ctrl = nullptr;
+  int* d_flags = nullptr;
+  int4* d_ftasks = nullptr;
+  int n_ftasks = 0;
+  int4* d_stasks = nullptr;
+  int n_stasks = 0;
+  double* d_tip_part = nullptr;
+  double* d_arrow_part = nullptr;
+  double* d_ld = nullptr;   // logdet partials [nt + 1] + result [1]
+  double* d_sig = nullptr;  // selected-inversion output blocks (lazy)
+  size_t sig_elems = 0;
+  int* h_ctrl = nullptr;    // pinned
+  size_t ws_bytes = 0;
+};
+
+namespace {
+
+int grid_of(const gbta_solver* s, int ntasks) {
+  int g = s->nsm * s->ctas_per_sm;
+  if (ntasks < g) g = ntasks;
+  return g < 1 ? 1 : g;
+}
+
+gbta::LaunchCtl next_launch(gbta_solver* s, int ntasks) {
+  gbta::LaunchCtl lc;
+  s->epoch += 1;
+  lc.ctrl = s->d_ctrl;
+  lc.flags = s->d_flags;
+  lc.epoch = s->epoch;
+  lc.wait_ns = s->wait_ns;
+  lc.grid = grid_of(s, ntasks);
+  lc.stream = s->stream;
+  return lc;
+}
+
+// Reset the ticket counter and the abort flag of the next launch (not the sticky
+// status words).
+int reset_ticket(gbta_solver* s) {
+  GBTA_CUDA(cudaMemsetAsync(s->d_ctrl, 0, 2 * sizeof(int), s->stream));
+  return GBTA_OK;
+}
+
+std::vector<int4> factor_tasks(const gbta::Geom& g) {
+  std::vector<int4> t;
+  for (int i = 0; i < g.nt; ++i)
+    for (int c = 0; c < g.B; ++c) {
+      t.push_back(make_int4(gbta::FT_DIAG, i, c, c));
+      for (int r = c + 1; r < g.B; ++r) t.push_back(make_int4(gbta::FT_OFFD, i, r, c));
+      if (i < g.nt - 1)
+        for (int r = 0; r < g.B; ++r) t.push_back(make_int4(gbta::FT_LOW, i, r, c));
+      if (g.a > 0) t.push_back(make_int4(gbta::FT_ARW, i, 0, c));
+    }
+  if (g.a > 0) t.push_back(make_int4(gbta::FT_TIP, 0, 0, 0));
+  return t;
+}
+
+std::vector<int4> selinv_tasks(const gbta::Geom& g) {
+  std::vector<int4> t;
+  if (g.a > 0) t.push_back(make_int4(gbta::ST_TIP, 0, 0, 0));
+  for (int i = g.nt - 1; i >= 0; --i)
+    for (int c = g.B - 1; c >= 0; --c) {
+      if (g.a > 0) t.push_back(make_int4(gbta::ST_OFF, i, 2 * g.B, c));
+      if (i < g.nt - 1)
+        for (int r = 0; r < g.B; ++r) t.push_back(make_int4(gbta::ST_OFF, i, g.B + r, c));
+      for (int r = c + 1; r < g.B; ++r) t.push_back(make_int4(gbta::ST_OFF, i, r, c));
+      t.push_back(make_int4(gbta::ST_DIAG, i, c, c));
+    }
+  return t;
+}
+
+int check_solver(const gbta_solver* s) {
+  if (!s) return fail(GBTA_ERR_ARG, "null solver");
+  return GBTA_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gbta_version(void) { return 100; }
+
+int gbta_set_error(int code, const char* msg) { return fail(code, msg ? msg : ""); }
+
+int gbta_geometry(const gbta_solver* s, int* b, int* nt, int* a, void** stream) {
+  if (!s) return fail(GBTA_ERR_ARG, "null solver");
+  if (b) *b = s->g.b;
+  if (nt) *nt = s->g.nt;
+  if (a) *a = s->g.a;
+  if (stream) *stream = (void*)s->stream;
+  return GBTA_OK;
+}
+
+const char* gbta_last_error(void) { return g_last_error.c_str(); }
+
+int gbta_create(int b, int nt, int a, gbta_solver** out) {
+  if (!out) return fail(GBTA_ERR_ARG, "out is null");
+  *out = nullptr;
+  if (b < 1 || nt < 1 || a < 0) return fail(GBTA_ERR_ARG, "require b >= 1, nt >= 1, a >= 0");
+  if (a > gbta::TS)
+    return fail(GBTA_ERR_ARG, "arrowhead block size above " + std::to_string(gbta::TS) + " is not supported");
+  auto* s = new gbta_solver();
+  s->g.b = b;
+  s->g.nt = nt;
+  s->g.a = a;
+  s->g.B = (b + gbta::TS - 1) / gbta::TS;
+  const long long nflags = (long long)(2 * nt - 1) * s->g.B * s->g.B + (long long)nt * s->g.B + 1;
+  if (nflags > (1ll << 31) - 1) {
+    delete s;
+    return fail(GBTA_ERR_ARG, "problem too large for 32-bit tile indices");
+  }
+  auto cleanup = [&](int code) {
+    gbta_destroy(s);
+    return code;
+  };
+  cudaError_t e;
+#define CREATE_CUDA(call)                                                                     \
+  if ((e = (call)) != cudaSuccess) {                                                           \
+    const std::string m = std::string(#call) + ": " + cudaGetErrorString(e);                   \
+    cleanup(0);                                                                                \
+    return fail(GBTA_ERR_CUDA, m);                                                             \
+  }
+  CREATE_CUDA(cudaGetDevice(&s->device));
+  CREATE_CUDA(cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device));
+  if (const char* v = std::getenv("GBTA_CTAS_PER_SM")) {
+    const int k = std::atoi(v);
+    if (k >= 1 && k <= 8) s->ctas_per_sm = k;
+  }
+  CREATE_CUDA(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
+  s->stream = s->own_stream;
+
+  const std::vector<int4> ft = factor_tasks(s->g), st = selinv_tasks(s->g);
+  s->n_ftasks = (int)ft.size();
+  s->n_stasks = (int)st.size();
+  const size_t ntile = (size_t)nt * s->g.B;
+  CREATE_CUDA(cudaMalloc(&s->d_ctrl, CTRL_INTS * sizeof(int)));
+  CREATE_CUDA(cudaMalloc(&s->d_flags, (size_t)nflags * sizeof(int)));
+  CREATE_CUDA(cudaMalloc(&s->d_ftasks, ft.size() * sizeof(int4)));
+  CREATE_CUDA(cudaMalloc(&s->d_stasks, st.size() * sizeof(int4)));
+  CREATE_CUDA(cudaMalloc(&s->d_tip_part, ntile * gbta::TS * gbta::TS * sizeof(double)));
+  CREATE_CUDA(cudaMalloc(&s->d_arrow_part, ntile * gbta::TS * gbta::SOLVE_NC * sizeof(double)));
+  CREATE_CUDA(cudaMalloc(&s->d_ld, (nt + 2) * sizeof(double)));
+  CREATE_CUDA(cudaMallocHost(&s->h_ctrl, CTRL_INTS * sizeof(int)));
+  CREATE_CUDA(cudaMemsetAsync(s->d_ctrl, 0, CTRL_INTS * sizeof(int), s->stream));
+  CREATE_CUDA(cudaMemsetAsync(s->d_flags, 0, (size_t)nflags * sizeof(int), s->stream));
+  CREATE_CUDA(cudaMemcpyAsync(s->d_ftasks, ft.data(), ft.size() * sizeof(int4), cudaMemcpyHostToDevice, s->stream));
+  CREATE_CUDA(cudaMemcpyAsync(s->d_stasks, st.data(), st.size() * sizeof(int4), cudaMemcpyHostToDevice, s->stream));
+  CREATE_CUDA(cudaStreamSynchronize(s->stream));
+#undef CREATE_CUDA
+  s->ws_bytes = CTRL_INTS * sizeof(int) + (size_t)nflags * sizeof(int) + (ft.size() + st.size()) * sizeof(int4) +
+                ntile * gbta::TS * (gbta::TS + gbta::SOLVE_NC) * sizeof(double) + (nt + 2) * sizeof(double);
+  *out = s;
+  g_last_error.clear();
+  return GBTA_OK;
+}
+
+int gbta_destroy(gbta_solver* s) {
+  if (!s) return GBTA_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  cudaFree(s->d_ctrl);
+  cudaFree(s->d_flags);
+  cudaFree(s->d_ftasks);
+  cudaFree(s->d_stasks);
+  cudaFree(s->d_tip_part);
+  cudaFree(s->d_arrow_part);
+  cudaFree(s->d_ld);
+  cudaFree(s->d_sig);
+  if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
+  if (s->own_stream) cudaStreamDestroy(s->own_stream);
+  delete s;
+  return GBTA_OK;
+}
+
+int gbta_set_stream(gbta_solver* s, void* stream) {
+  if (int r = check_solver(s)) return r;
+  s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+  return GBTA_OK;
+}
+
+int gbta_set_wait_limit_ms(gbta_solver* s, double ms) {
+  if (int r = check_solver(s)) return r;
+  if (!(ms > 0)) return fail(GBTA_ERR_ARG, "wait limit must be positive");
+  s->wait_ns = (unsigned long long)(ms * 1e6);
+  return GBTA_OK;
+}
+
+size_t gbta_workspace_bytes(const gbta_solver* s) {
+  return s ? s->ws_bytes + s->sig_elems * sizeof(double) : 0;
+}
+
+int gbta_status(gbta_solver* s) {
+  if (int r = check_solver(s)) return r;
+  GBTA_CUDA(cudaStreamSynchronize(s->stream));
+  GBTA_CUDA(cudaGetLastError());
+  GBTA_CUDA(cudaMemcpy(s->h_ctrl, s->d_ctrl, CTRL_INTS * sizeof(int), cudaMemcpyDeviceToHost));
+  const int info = s->h_ctrl[CTRL_INFO], err = s->h_ctrl[CTRL_ERR];
+  if (info != 0 || err != 0) {
+    GBTA_CUDA(cudaMemsetAsync(s->d_ctrl, 0, CTRL_INTS * sizeof(int), s->stream));
+    GBTA_CUDA(cudaStreamSynchronize(s->stream));
+  }
+  if (err == 1) return fail(GBTA_ERR_TIMEOUT, "a kernel wait exceeded the wait limit; the launch was abandoned");
+  if (info > 0)
+    return fail(info, "matrix is not positive definite (non-positive pivot at global row " + std::to_string(info) + ")");
+  return GBTA_OK;
+}
+
+// ---------------------------------------------------------------- factorization
+static int factor_async(gbta_solver* s, double* D, double* L, double* R, double* T, int use_arrow) {
+  if (int r = check_solver(s)) return r;
+  if (!D || (s->g.nt > 1 && !L)) return fail(GBTA_ERR_ARG, "D/L must be device pointers");
+  if (use_arrow && (!R || !T)) return fail(GBTA_ERR_ARG, "R/T must be device pointers for the bta factorization");
+  if (int r = reset_ticket(s)) return r;
+  const gbta::LaunchCtl lc = next_launch(s, s->n_ftasks);
+  gbta::launch_factor(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part, lc);
+  GBTA_CUDA(cudaGetLastError());
+  return GBTA_OK;
+}
+
+int gbta_pobtaf_async(gbta_solver* s, double* D, double* L, double* R, double* T) {
+  return factor_async(s, D, L, R, T, s && s->g.a > 0);
+}
+int gbta_pobtf_async(gbta_solver* s, double* D, double* L) { return factor_async(s, D, L, nullptr, nullptr, 0); }
+int gbta_pobtaf(gbta_solver* s, double* D, double* L, double* R, double* T) {
+  if (int r = gbta_pobtaf_async(s, D, L, R, T)) return r;
+  return gbta_status(s);
+}
+int gbta_pobtf(gbta_solver* s, double* D, double* L) {
+  if (int r = gbta_pobtf_async(s, D, L)) return r;
+  return gbta_status(s);
+}
+
+// ---------------------------------------------------------------- solves
+static int solve_async(gbta_solver* s, const double* D, const double* L, const double* R, const double* T, double* B,
+                       int nrhs, int trans, int use_arrow) {
+  if (int r = check_solver(s)) return r;
+  if (!D || !B || (s->g.nt > 1 && !L)) return fail(GBTA_ERR_ARG, "D/L/B must be device pointers");
+  if (use_arrow && (!R || !T)) return fail(GBTA_ERR_ARG, "R/T must be device pointers for the bta solve");
+  if (nrhs < 1) return fail(GBTA_ERR_ARG, "nrhs must be >= 1");
+  if (trans != 0 && trans != 1) return fail(GBTA_ERR_ARG, "trans must be 0 (N) or 1 (C)");
+  const int ntasks = s->g.nt * s->g.B + (use_arrow ? 1 : 0);
+  for (int c0 = 0; c0 < nrhs; c0 += gbta::SOLVE_NC) {
+    const int nc = nrhs - c0 < gbta::SOLVE_NC ? nrhs - c0 : gbta::SOLVE_NC;
+    if (int r = reset_ticket(s)) return r;
+    const gbta::LaunchCtl lc = next_launch(s, ntasks);
+    gbta::launch_solve(s->g, D, L, R, T, B + c0, nrhs, nc, trans, use_arrow, s->d_arrow_part, lc);
+    GBTA_CUDA(cudaGetLastError());
+  }
+  return GBTA_OK;
+}
+
+int gbta_pobtas_async(gbta_solver* s, const double* D, const double* L, const double* R, const double* T, double* B,
+                      int nrhs, int trans) {
+  return solve_async(s, D, L, R, T, B, nrhs, trans, s && s->g.a > 0);
+}
+int gbta_pobtas(gbta_solver* s, const double* D, const double* L, const double* R, const double* T, double* B,
+                int nrhs, int trans) {
+  if (int r = gbta_pobtas_async(s, D, L, R, T, B, nrhs, trans)) return r;
+  return gbta_status(s);
+}
+int gbta_pobts(gbta_solver* s, const double* D, const double* L, double* B, int nrhs, int trans) {
+  if (int r = solve_async(s, D, L, nullptr, nullptr, B, nrhs, trans, 0)) return r;
+  return gbta_status(s);
+}
+
+// ---------------------------------------------------------------- logdet
+int gbta_logdet(gbta_solver* s, const double* D, const double* T, int with_tip, double* out) {
+  if (int r = check_solver(s)) return r;
+  if (!D || !out) return fail(GBTA_ERR_ARG, "D and out are required");
+  const int tip = with_tip && s->g.a > 0;
+  if (tip && !T) return fail(GBTA_ERR_ARG, "T is required for the bta logdet");
+  gbta::launch_logdet(s->g, D, T, tip, s->d_ld, s->d_ld + s->g.nt + 1, s->stream);
+  GBTA_CUDA(cudaGetLastError());
+  double v = 0.0;
+  GBTA_CUDA(cudaMemcpyAsync(&v, s->d_ld + s->g.nt + 1, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  GBTA_CUDA(cudaStreamSynchronize(s->stream));
+  *out = v;
+  if (std::isnan(v)) return fail(GBTA_ERR_ARG, "Logdet is NaN. Check the input matrix.");
+  return GBTA_OK;
+}
+
+// ---------------------------------------------------------------- selected inversion
+static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double* T, int use_arrow) {
+  if (int r = check_solver(s)) return r;
+  if (!D || (s->g.nt > 1 && !L)) return fail(GBTA_ERR_ARG, "D/L must be device pointers");
+  if (use_arrow && (!R || !T)) return fail(GBTA_ERR_ARG, "R/T must be device pointers for the bta selected inversion");
+  const gbta::Geom& g = s->g;
+  const size_t bb = (size_t)g.b * g.b;
+  const size_t need = g.nt * bb + (g.nt - 1) * bb + (size_t)g.nt * g.a * g.b + (size_t)g.a * g.a;
+  if (s->sig_elems < need) {
+    GBTA_CUDA(cudaStreamSynchronize(s->stream));
+    cudaFree(s->d_sig);
+    s->d_sig = nullptr;
+    s->sig_elems = 0;
+    GBTA_CUDA(cudaMalloc(&s->d_sig, need * sizeof(double)));
+    s->sig_elems = need;
+  }
+  double* SD = s->d_sig;
+  double* SL = SD + g.nt * bb;
+  double* SR = SL + (g.nt - 1) * bb;
+  double* ST = SR + (size_t)g.nt * g.a * g.b;
+  if (int r = reset_ticket(s)) return r;
+  const gbta::LaunchCtl lc = next_launch(s, s->n_stasks);
+  gbta::launch_selinv(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks, lc);
+  GBTA_CUDA(cudaGetLastError());
+  gbta::launch_selinv_writeback(g, SD, SL, SR, ST, D, L, R, T, use_arrow, s->stream);
+  GBTA_CUDA(cudaGetLastError());
+  return GBTA_OK;
+}
+
+int gbta_pobtasi_async(gbta_solver* s, double* D, double* L, double* R, double* T) {
+  return selinv_async(s, D, L, R, T, s && s->g.a > 0);
+}
+int gbta_pobtasi(gbta_solver* s, double* D, double* L, double* R, double* T) {
+  if (int r = gbta_pobtasi_async(s, D, L, R, T)) return r;
+  return gbta_status(s);
+}
+int gbta_pobtsi(gbta_solver* s, double* D, double* L) {
+  if (int r = selinv_async(s, D, L, nullptr, nullptr, 0)) return r;
+  return gbta_status(s);
+}
+
+}  // extern "C"

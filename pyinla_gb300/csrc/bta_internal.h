@@ -1,0 +1,59 @@
+// Internal launch interface between the C ABI (bta_api.cu) and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gbta {
+
+constexpr int TS = 32;  // tile edge (FP64 elements)
+
+// Task codes of the factorization DAG.
+enum FactorTask { FT_DIAG = 0, FT_OFFD = 1, FT_LOW = 2, FT_ARW = 3, FT_TIP = 4 };
+// Task codes of the selected-inversion DAG.
+enum SelinvTask { ST_TIP = 0, ST_OFF = 1, ST_DIAG = 2 };
+
+// Geometry of one BTA matrix and the flag layout shared by all kernels.
+struct Geom {
+  int b, nt, a, B;   // block size, number of diagonal blocks, arrow size, tiles per block edge
+  __host__ __device__ int fD(int i, int r, int c) const { return (i * B + r) * B + c; }
+  __host__ __device__ int fL(int i, int r, int c) const { return nt * B * B + (i * B + r) * B + c; }
+  __host__ __device__ int fR(int i, int c) const { return (2 * nt - 1) * B * B + i * B + c; }
+  __host__ __device__ int fT() const { return (2 * nt - 1) * B * B + nt * B; }
+  __host__ __device__ int nflags() const { return (2 * nt - 1) * B * B + nt * B + 1; }
+  __host__ __device__ int vrows(int r) const {   // valid rows of block-tile r
+    const int v = b - r * TS;
+    return v < TS ? v : TS;
+  }
+};
+
+struct LaunchCtl {
+  int* ctrl;
+  int* flags;
+  int epoch;
+  unsigned long long wait_ns;
+  int grid;
+  cudaStream_t stream;
+};
+
+void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow,
+                   const int4* tasks, int ntasks, double* tip_part, const LaunchCtl& lc);
+
+constexpr int SOLVE_NC = 4;   // right-hand-side columns per solve launch
+
+void launch_solve(const Geom& g, const double* D, const double* L, const double* R, const double* T,
+                  double* Bv, int ldb, int nc, int trans, int use_arrow, double* arrow_part,
+                  const LaunchCtl& lc);
+
+void launch_selinv(const Geom& g, const double* D, const double* L, const double* R, const double* T,
+                   double* SD, double* SL, double* SR, double* ST, int use_arrow, const int4* tasks,
+                   int ntasks, const LaunchCtl& lc);
+
+void launch_selinv_writeback(const Geom& g, const double* SD, const double* SL, const double* SR,
+                             const double* ST, double* D, double* L, double* R, double* T, int use_arrow,
+                             cudaStream_t stream);
+
+void launch_logdet(const Geom& g, const double* D, const double* T, int with_tip, double* partial,
+                   double* out, cudaStream_t stream);
+
+}  // namespace gbta

@@ -1,0 +1,76 @@
+"""Device plumbing: solver handles of libpyinla_gb300.so and the torch stream they use.
+
+PyTorch provides device memory and the current CUDA stream; all arithmetic runs in
+the library's kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+
+from . import _lib
+
+_handles: dict = {}
+_hlock = threading.Lock()
+
+
+def require_torch_cuda():
+    """Return the torch module, raising if no CUDA device is usable (no CPU fallback)."""
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("pyinla_gb300 needs a CUDA device (GB300); none is visible")
+    _lib.load()
+    return torch
+
+
+def current_stream_ptr() -> int:
+    import torch
+
+    return torch.cuda.current_stream().cuda_stream
+
+
+class BtaHandle:
+    """Owns one ``gbta_solver`` (geometry b, nt, a on the current device)."""
+
+    def __init__(self, b: int, nt: int, a: int):
+        self.lib = _lib.load()
+        self.b, self.nt, self.a = int(b), int(nt), int(a)
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.gbta_create(self.b, self.nt, self.a, ctypes.byref(h)))
+        self.ptr = h
+
+    @classmethod
+    def get(cls, b: int, nt: int, a: int) -> "BtaHandle":
+        import torch
+
+        key = (int(b), int(nt), int(a), torch.cuda.current_device())
+        with _hlock:
+            h = _handles.get(key)
+            if h is None:
+                h = cls(b, nt, a)
+                _handles[key] = h
+            return h
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        _lib.check(self.lib.gbta_set_stream(self.ptr, stream_ptr))
+
+    def set_wait_limit_ms(self, ms: float) -> None:
+        _lib.check(self.lib.gbta_set_wait_limit_ms(self.ptr, float(ms)))
+
+    def workspace_bytes(self) -> int:
+        return int(self.lib.gbta_workspace_bytes(self.ptr))
+
+    def status(self) -> int:
+        return _lib.check(self.lib.gbta_status(self.ptr))
+
+    def close(self) -> None:
+        if self.ptr:
+            self.lib.gbta_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,184 @@
+"""``GB300SerinvSolver``: drop-in for the reference's ``SerinvSolver``.
+
+Mirrors src/pyinla/solvers/structured_solver.py:19-550 method for method --
+``cholesky``, ``solve``, ``logdet``, ``selected_inversion``,
+``_structured_to_spmatrix``, ``get_solver_memory`` and the ``t_cholesky`` /
+``t_solve`` timers that ``PyINLA`` resets and reads (src/pyinla/core/pyinla.py:216-217,
+531-532, 588) -- with the block buffers resident in GB300 memory as torch float64
+tensors and every step (sparse-to-BTA scatter, factorization, sweeps, logdet,
+selected inversion, pattern gather) running in libpyinla_gb300.so.
+
+It does not import pyinla.  To use it inside the reference, replace the class the
+driver instantiates (``pyinla.core.pyinla.SerinvSolver``) with this one, or inject
+:mod:`pyinla_gb300.algs` as ``serinv.algs``; both are shown in INTEGRATION.md.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+
+import numpy as np
+import scipy.sparse as sps
+
+from . import _lib
+from .device import BtaHandle, current_stream_ptr, require_torch_cuda
+
+
+class GB300SerinvSolver:
+    """BTA solver on one GB300 (reference: ``SerinvSolver``, structured_solver.py:19)."""
+
+    def __init__(self, config=None, diagonal_blocksize: int = None, n_diag_blocks: int = None,
+                 arrowhead_blocksize: int = 0, **kwargs) -> None:
+        torch = require_torch_cuda()
+        self.config = config
+        self.diagonal_blocksize = int(diagonal_blocksize)
+        self.arrowhead_blocksize = int(arrowhead_blocksize)
+        self.n_diag_blocks = int(n_diag_blocks)
+        b, nt, a = self.diagonal_blocksize, self.n_diag_blocks, self.arrowhead_blocksize
+        dev = torch.device("cuda", torch.cuda.current_device())
+        f64 = torch.float64
+        # structured_solver.py:37-61
+        self.A_diagonal_blocks = torch.empty((nt, b, b), dtype=f64, device=dev)
+        self.A_lower_diagonal_blocks = torch.empty((max(nt - 1, 0), b, b), dtype=f64, device=dev)
+        self.A_arrow_bottom_blocks = torch.empty((nt, a, b), dtype=f64, device=dev) if a > 0 else None
+        self.A_arrow_tip_block = torch.empty((a, a), dtype=f64, device=dev) if a > 0 else None
+        self._h = BtaHandle.get(b, nt, a)
+        self._torch = torch
+        self.total_bytes = 0
+        self.t_cholesky = 0.0
+        self.t_solve = 0.0
+
+    # ------------------------------------------------------------------ helpers
+    def _ptrs(self, sparsity: str):
+        D = self.A_diagonal_blocks.data_ptr()
+        L = self.A_lower_diagonal_blocks.data_ptr() if self.n_diag_blocks > 1 else None
+        if sparsity == "bta" and self.arrowhead_blocksize > 0:
+            return D, L, self.A_arrow_bottom_blocks.data_ptr(), self.A_arrow_tip_block.data_ptr()
+        return D, L, None, None
+
+    @staticmethod
+    def _check_sparsity(sparsity: str) -> None:
+        if sparsity not in ("bt", "bta"):
+            raise ValueError(f"Unknown sparsity pattern: {sparsity}. Use 'bt' or 'bta'.")
+
+    def _sync(self) -> None:
+        self._torch.cuda.current_stream().synchronize()
+
+    # ------------------------------------------------------------------ API
+    def cholesky(self, A, sparsity: str) -> None:
+        """Map the sparse matrix into BTA blocks and factor it (structured_solver.py:72-100)."""
+        self._check_sparsity(sparsity)
+        self._spmatrix_to_structured(A, sparsity)
+        tic = time.perf_counter()
+        self._sync()
+        h = self._h
+        h.set_stream(current_stream_ptr())
+        D, L, R, T = self._ptrs(sparsity)
+        if sparsity == "bta" and self.arrowhead_blocksize > 0:
+            _lib.check(h.lib.gbta_pobtaf(h.ptr, D, L, R, T))
+        else:
+            _lib.check(h.lib.gbta_pobtf(h.ptr, D, L))
+        self._sync()
+        self.t_cholesky += time.perf_counter() - tic
+
+    def solve(self, rhs, sparsity: str):
+        """Forward then backward sweep, overwriting and returning ``rhs``
+        (structured_solver.py:102-149)."""
+        self._check_sparsity(sparsity)
+        torch = self._torch
+        tic = time.perf_counter()
+        self._sync()
+        on_dev = isinstance(rhs, torch.Tensor) and rhs.device.type == "cuda"
+        nb = self.n_diag_blocks * self.diagonal_blocksize
+        n = nb + (self.arrowhead_blocksize if sparsity == "bta" else 0)
+        if on_dev:
+            x = rhs[:n] if rhs.is_contiguous() else rhs[:n].contiguous()
+        else:
+            x = torch.from_numpy(np.ascontiguousarray(np.asarray(rhs, dtype=np.float64)[:n])).cuda()
+        nrhs = 1 if x.ndim == 1 else int(np.prod(x.shape[1:]))
+        h = self._h
+        h.set_stream(current_stream_ptr())
+        D, L, R, T = self._ptrs(sparsity)
+        if R is not None:
+            _lib.check(h.lib.gbta_pobtas_async(h.ptr, D, L, R, T, x.data_ptr(), nrhs, 0))
+            _lib.check(h.lib.gbta_pobtas(h.ptr, D, L, R, T, x.data_ptr(), nrhs, 1))
+        else:
+            _lib.check(h.lib.gbta_pobts(h.ptr, D, L, x.data_ptr(), nrhs, 0))
+            _lib.check(h.lib.gbta_pobts(h.ptr, D, L, x.data_ptr(), nrhs, 1))
+        if on_dev:
+            if x.data_ptr() != rhs.data_ptr():
+                rhs[:n].copy_(x)
+        else:
+            rhs[:n] = x.cpu().numpy()
+        self._sync()
+        self.t_solve += time.perf_counter() - tic
+        return rhs
+
+    def logdet(self, sparsity: str) -> float:
+        """2 * sum(log diag) of the factor; "bt" excludes the tip (structured_solver.py:151-166)."""
+        self._check_sparsity(sparsity)
+        h = self._h
+        h.set_stream(current_stream_ptr())
+        D, _, _, T = self._ptrs(sparsity)
+        out = ctypes.c_double(0.0)
+        code = h.lib.gbta_logdet(h.ptr, D, T, 1 if T is not None else 0, ctypes.byref(out))
+        if code == _lib.GBTA_ERR_ARG and np.isnan(out.value):
+            raise ValueError("Logdet is NaN. Check the input matrix.")
+        _lib.check(code)
+        return float(out.value)
+
+    def selected_inversion(self, sparsity: str) -> None:
+        """Overwrite the factor blocks with Sigma on the BTA pattern (structured_solver.py:168-190)."""
+        self._check_sparsity(sparsity)
+        h = self._h
+        h.set_stream(current_stream_ptr())
+        D, L, R, T = self._ptrs(sparsity)
+        if R is not None:
+            _lib.check(h.lib.gbta_pobtasi(h.ptr, D, L, R, T))
+        else:
+            _lib.check(h.lib.gbta_pobtsi(h.ptr, D, L))
+
+    def _spmatrix_to_structured(self, A, sparsity: str) -> None:
+        """Zero-fill and scatter the symmetric sparse matrix into the BTA blocks
+        (structured_solver.py:192-250) with one device scatter."""
+        self._check_sparsity(sparsity)
+        torch = self._torch
+        coo = sps.coo_matrix(A)
+        rows = torch.from_numpy(coo.row.astype(np.int64)).cuda()
+        cols = torch.from_numpy(coo.col.astype(np.int64)).cuda()
+        vals = torch.from_numpy(np.ascontiguousarray(coo.data, dtype=np.float64)).cuda()
+        h = self._h
+        h.set_stream(current_stream_ptr())
+        D, L, R, T = self._ptrs("bta")
+        _lib.check(h.lib.gbta_scatter_coo(h.ptr, rows.data_ptr(), cols.data_ptr(), vals.data_ptr(), int(coo.nnz),
+                                          D, L, R, T, 1 if R is not None else 0))
+
+    def _structured_to_spmatrix(self, A, sparsity: str):
+        """Sigma (or the factor) on the lower pattern of ``A``, symmetrised, as CSC
+        (structured_solver.py:470-538)."""
+        self._check_sparsity(sparsity)
+        torch = self._torch
+        Bl = sps.tril(sps.csc_matrix(A)).tocoo()
+        b, nt = self.diagonal_blocksize, self.n_diag_blocks
+        nb = nt * b
+        r, c = Bl.row.astype(np.int64), Bl.col.astype(np.int64)
+        in_bt = (r < nb) & (c < nb) & ((r // b == c // b) | (r // b == c // b + 1))
+        keep = in_bt | ((r >= nb) if sparsity == "bta" else np.zeros_like(in_bt))
+        r, c = r[keep], c[keep]
+        rows, cols = torch.from_numpy(r).cuda(), torch.from_numpy(c).cuda()
+        vals = torch.empty(r.size, dtype=torch.float64, device="cuda")
+        h = self._h
+        h.set_stream(current_stream_ptr())
+        D, L, R, T = self._ptrs(sparsity)
+        _lib.check(h.lib.gbta_gather_coo(h.ptr, rows.data_ptr(), cols.data_ptr(), int(r.size), D, L, R, T,
+                                         1 if R is not None else 0, vals.data_ptr()))
+        out = sps.coo_matrix((vals.cpu().numpy(), (r, c)), shape=Bl.shape).tocsc()
+        return out + sps.tril(out, k=-1).T
+
+    def get_solver_memory(self) -> int:
+        """Bytes of the block buffers plus the library workspace (structured_solver.py:540-550)."""
+        n = self.A_diagonal_blocks.nbytes + self.A_lower_diagonal_blocks.nbytes
+        if self.A_arrow_bottom_blocks is not None:
+            n += self.A_arrow_bottom_blocks.nbytes + self.A_arrow_tip_block.nbytes
+        self.total_bytes = n + self._h.workspace_bytes()
+        return self.total_bytes
