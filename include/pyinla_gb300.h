@@ -54,6 +54,13 @@ typedef struct gbta_solver gbta_solver;
 /* Version of this ABI (major*10000 + minor*100 + patch). */
 int gbta_version(void);
 
+/* Number of kernels this library has launched in the process so far. */
+long long gbta_kernel_launches(void);
+
+/* Measure the chip's FP64 FMA throughput (TFLOP/s) with a DFMA-bound kernel on every
+ * SM (`iters` FMA rounds per thread); the roofline denominator of the FP64 kernels. */
+int gbta_probe_fp64_peak(int iters, double* tflops);
+
 /* Text of the last error raised on the calling thread ("" if none). */
 const char* gbta_last_error(void);
 
@@ -71,8 +78,8 @@ int gbta_set_error(int code, const char* msg);
 int gbta_create(int b, int nt, int a, gbta_solver** out);
 int gbta_destroy(gbta_solver* s);
 
-/* Make the solver enqueue its work on `stream` (a cudaStream_t; NULL restores the
- * private stream). */
+/* Make the solver enqueue its work on `stream` (a cudaStream_t, used as given: NULL
+ * is the CUDA default stream).  A new solver uses a private non-blocking stream. */
 int gbta_set_stream(gbta_solver* s, void* stream);
 
 /* Limit, in milliseconds, on any inter-CTA wait inside a kernel; after it the
@@ -126,6 +133,42 @@ int gbta_scatter_coo(gbta_solver* s, const long long* rows, const long long* col
 int gbta_gather_coo(gbta_solver* s, const long long* rows, const long long* cols, long long nnz,
                     const double* D, const double* L, const double* R, const double* T, int with_arrow,
                     double* vals);
+
+/* ---- on-device assembly of Kronecker-sum precisions ----------------------- */
+/* Overwrite D, L (R, T) with the BTA blocks of
+ *     Q = sum_k  M_k(theta) (x) S_k  +  lik_scale * A^T A  +  tip_diag * I_a
+ * where S_k are fixed ns x ns spatial matrices placed at variate block (v_k, w_k) of
+ * the b = nv * ns diagonal block, with temporal coefficients
+ *     D_t += alpha[k*nt + t] * S_k,     L_t += beta[k*(nt-1) + t] * S_k.
+ * The S_k share one union pattern (CSR upat_rowptr[ns+1], upat_col); uval[e*nterms + k]
+ * is S_k's value at union entry e (0 when absent); term_vw[2k], term_vw[2k+1] = (v_k, w_k).
+ * A^T A (theta-independent) is given as CSR rows of the diagonal blocks (lik_rowptr
+ * [nt*b+1] over block rows t*b + rho, lik_col block-local) plus dense arrow parts
+ * lik_R (nt, a, b) and lik_T (a, a); any of them may be NULL.  All arrays are device
+ * pointers.  Replaces the per-evaluation Q construction of the reference
+ * (src/pyinla/submodels/spatio_temporal.py:114-149, src/pyinla/core/model.py:306-423,
+ * src/pyinla/models/coregional_model.py:274-597) and the sparse-to-BTA scatter
+ * (structured_solver.py:192-468).  Deterministic.  Asynchronous on the solver's stream. */
+int gbta_assemble_kron(gbta_solver* s, int ns, int nv, int nterms, const int* upat_rowptr,
+                       const int* upat_col, const double* uval, const int* term_vw, const double* alpha,
+                       const double* beta, const long long* lik_rowptr, const int* lik_col,
+                       const double* lik_val, const double* lik_R, const double* lik_T, double lik_scale,
+                       double tip_diag, double* D, double* L, double* R, double* T);
+
+/* Contractions for the adjoint theta-gradient (no counterpart in the reference, which
+ * differentiates by central finite differences, src/pyinla/core/pyinla.py:512-600):
+ * with Sigma given by SD, SL, SR, ST (selected inverse blocks, any may be NULL) and
+ * mu (N vector, may be NULL), writes out[4*K*nt + 2*(nt+1)] (K = nterms):
+ *   out[0*K*nt + k*nt + t] = <Sigma_tt, S_k>       out[1*K*nt + k*nt + t] = <Sigma_{t+1,t}, S_k>
+ *   out[2*K*nt + k*nt + t] = mu_t' S_k mu_t        out[3*K*nt + k*nt + t] = mu_{t+1}' S_k mu_t
+ *   out[4*K*nt + t]        = <Sigma, A^T A> on block t (t = nt: tip part)
+ *   out[4*K*nt + nt+1 + t] = the same with mu mu'.
+ * Deterministic.  Asynchronous on the solver's stream. */
+int gbta_contract_kron(gbta_solver* s, int ns, int nv, int nterms, const int* upat_rowptr,
+                       const int* upat_col, const double* uval, const int* term_vw,
+                       const long long* lik_rowptr, const int* lik_col, const double* lik_val,
+                       const double* lik_R, const double* lik_T, const double* SD, const double* SL,
+                       const double* SR, const double* ST, const double* mu, double* out);
 
 #ifdef __cplusplus
 }

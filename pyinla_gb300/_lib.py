@@ -31,6 +31,8 @@ _dp = ctypes.POINTER(ctypes.c_double)
 # name -> (restype, argtypes); the exact list of symbols declared in the header.
 SIGNATURES = {
     "gbta_version": (_c_int, []),
+    "gbta_kernel_launches": (_c_ll, []),
+    "gbta_probe_fp64_peak": (_c_int, [_c_int, _dp]),
     "gbta_last_error": (ctypes.c_char_p, []),
     "gbta_geometry": (_c_int, [_vp, ctypes.POINTER(_c_int), ctypes.POINTER(_c_int), ctypes.POINTER(_c_int),
                                ctypes.POINTER(_vp)]),
@@ -54,6 +56,10 @@ SIGNATURES = {
     "gbta_pobtasi_async": (_c_int, [_vp, _vp, _vp, _vp, _vp]),
     "gbta_scatter_coo": (_c_int, [_vp, _vp, _vp, _vp, _c_ll, _vp, _vp, _vp, _vp, _c_int]),
     "gbta_gather_coo": (_c_int, [_vp, _vp, _vp, _c_ll, _vp, _vp, _vp, _vp, _c_int, _vp]),
+    "gbta_assemble_kron": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                    _vp, _vp, ctypes.c_double, ctypes.c_double, _vp, _vp, _vp, _vp]),
+    "gbta_contract_kron": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                    _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
 

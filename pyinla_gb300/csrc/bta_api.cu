@@ -222,7 +222,7 @@ int gbta_destroy(gbta_solver* s) {
 
 int gbta_set_stream(gbta_solver* s, void* stream) {
   if (int r = check_solver(s)) return r;
-  s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+  s->stream = (cudaStream_t)stream;   // NULL is the CUDA default stream
   return GBTA_OK;
 }
 

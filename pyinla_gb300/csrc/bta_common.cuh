@@ -58,20 +58,27 @@ __device__ __forceinline__ void raise_abort(const Ctl& c) { atomicExch(c.ctrl + 
 
 // Thread-0 helper: spin (bounded in time) until flag >= epoch.  Returns false on
 // abort or timeout (timeout also records ERR_TIMEOUT and aborts the launch).
+// Only thread 0 of a CTA polls, and a persistent kernel runs one CTA per SM, so the
+// first SPIN_NS of a wait are a tight acquire-load loop (the hop latency of the
+// dependency chains is what bounds these kernels); longer waits back off with a
+// short sleep.
+constexpr unsigned long long SPIN_NS = 200000;
+
 static __device__ bool spin_ready(const Ctl& c, const int* flag) {
   if (ld_acquire(flag) >= c.epoch) return true;
   const unsigned long long t0 = gtimer();
-  unsigned ns = 32;
-  while (true) {
+  for (unsigned it = 1;; ++it) {
     if (ld_acquire(flag) >= c.epoch) return true;
-    if (ld_relaxed(c.ctrl + CTRL_ABORT)) return false;
-    if (gtimer() - t0 > c.wait_ns) {
-      atomicCAS(c.ctrl + CTRL_ERR, ERR_NONE, ERR_TIMEOUT);
-      raise_abort(c);
-      return false;
+    if ((it & 63) == 0) {
+      if (ld_relaxed(c.ctrl + CTRL_ABORT)) return false;
+      const unsigned long long dt = gtimer() - t0;
+      if (dt > c.wait_ns) {
+        atomicCAS(c.ctrl + CTRL_ERR, ERR_NONE, ERR_TIMEOUT);
+        raise_abort(c);
+        return false;
+      }
+      if (dt > SPIN_NS) __nanosleep(256);
     }
-    __nanosleep(ns);
-    if (ns < 2048) ns <<= 1;
   }
 }
 
@@ -312,10 +319,46 @@ static __device__ bool kloop(Acc& acc, int nsteps, StepFn step_of, const Ctl& c,
 // Small dense kernels on shared tiles (whole CTA).
 // ---------------------------------------------------------------------------
 
+// Scalar FP64 helpers.  On GB300 one warp-wide FP64 instruction occupies an SM
+// sub-partition's FP64 unit for ~64 cycles, so the sequential per-column work of the
+// small tile kernels is kept to a few FP64 instructions: reciprocals and inverse
+// square roots are Newton-Raphson refinements (y <- y (2 - x y), resp.
+// y <- y (3 - x y^2) / 2, each doubling the correct bits) of the hardware
+// approximations rcp.approx / rsqrt.approx, computed once per tile or per pivot.
+__device__ __forceinline__ double nr_recip(double x) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
+}
+__device__ __forceinline__ double nr_rsqrt(double x) {
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  const double h = 0.5 * x;
+  double r = fma(-h * y, y, 0.5);
+  y = fma(y, r, y);
+  r = fma(-h * y, y, 0.5);
+  y = fma(y, r, y);
+  r = fma(-h * y, y, 0.5);
+  return fma(y, r, y);
+}
+
+// rd[j] = 1 / F[j][j] for the TS diagonal entries (one lane each).  Caller syncs.
+__device__ __forceinline__ void tile_diag_recip(const double* F, double* rd) {
+  if (threadIdx.x < TS) rd[threadIdx.x] = nr_recip(F[threadIdx.x * LDS + threadIdx.x]);
+}
+
 // In-place lower Cholesky of S (TS x TS; entries past n must already be identity).
 // Returns 0, or the 1-based column of the first non-positive (or NaN) pivot.
-// The strict upper triangle is zeroed on success.
-static __device__ int smem_potrf(double* S) {
+// One barrier per column: step j updates the trailing matrix with the unscaled
+// column j and 1/d_j; the columns are scaled by 1/sqrt(d_j) in a final pass (column
+// j is not modified after step j).  The strict upper triangle is zeroed on success.
+// `ybuf` is a TS-double shared scratch.
+static __device__ int smem_potrf(double* S, double* ybuf) {
   for (int j = 0; j < TS; ++j) {
     __syncthreads();
     const double d = S[j * LDS + j];
@@ -323,53 +366,55 @@ static __device__ int smem_potrf(double* S) {
       __syncthreads();
       return j + 1;
     }
-    const double s = sqrt(d);
-    __syncthreads();
-    for (int r = j + threadIdx.x; r < TS; r += NT) S[r * LDS + j] = (r == j) ? s : S[r * LDS + j] / s;
-    __syncthreads();
+    const double y = nr_rsqrt(d);
+    const double inv = y * y;
+    if (threadIdx.x == 0) ybuf[j] = y;
     const int m = TS - 1 - j;
     for (int idx = threadIdx.x; idx < m * m; idx += NT) {
       const int rr = j + 1 + idx / m, kk = j + 1 + idx % m;
-      if (kk <= rr) S[rr * LDS + kk] = fma(-S[rr * LDS + j], S[kk * LDS + j], S[rr * LDS + kk]);
+      if (kk <= rr) S[rr * LDS + kk] = fma(-S[rr * LDS + j] * inv, S[kk * LDS + j], S[rr * LDS + kk]);
     }
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < TS * TS; idx += NT) {
     const int r = idx / TS, c = idx % TS;
-    if (c > r) S[r * LDS + c] = 0.0;
+    S[r * LDS + c] = (c > r) ? 0.0 : S[r * LDS + c] * ybuf[c];
   }
   __syncthreads();
   return 0;
 }
 
-// X <- X * F^{-T} with F lower triangular (right-looking column sweep).
-static __device__ void smem_trsm_rlt(double* X, const double* F) {
-  for (int j = 0; j < TS; ++j) {
+// X <- X * F^{-T} with F lower triangular; rd = 1/diag(F) (tile_diag_recip, synced).
+// One barrier per column: column j stays unscaled until a final pass, updates use
+// X[r][j] * rd[j].
+static __device__ void smem_trsm_rlt(double* X, const double* F, const double* rd) {
+  for (int j = 0; j < TS - 1; ++j) {
     __syncthreads();
-    const double d = F[j * LDS + j];
-    for (int r = threadIdx.x; r < TS; r += NT) X[r * LDS + j] = X[r * LDS + j] / d;
-    __syncthreads();
+    const double rj = rd[j];
     const int m = TS - 1 - j;
     for (int idx = threadIdx.x; idx < TS * m; idx += NT) {
       const int r = idx / m, col = j + 1 + idx % m;
-      X[r * LDS + col] = fma(-X[r * LDS + j], F[col * LDS + j], X[r * LDS + col]);
+      X[r * LDS + col] = fma(-X[r * LDS + j] * rj, F[col * LDS + j], X[r * LDS + col]);
     }
   }
   __syncthreads();
+  for (int idx = threadIdx.x; idx < TS * TS; idx += NT) X[(idx / TS) * LDS + idx % TS] *= rd[idx % TS];
+  __syncthreads();
 }
 
-// X <- X * F^{-1} with F lower triangular (solve X F = X, backward column sweep).
-static __device__ void smem_trsm_rln(double* X, const double* F) {
-  for (int j = TS - 1; j >= 0; --j) {
+// X <- X * F^{-1} with F lower triangular (solve X F = X, backward column sweep);
+// rd = 1/diag(F).  Same one-barrier-per-column scheme.
+static __device__ void smem_trsm_rln(double* X, const double* F, const double* rd) {
+  for (int j = TS - 1; j > 0; --j) {
     __syncthreads();
-    const double d = F[j * LDS + j];
-    for (int r = threadIdx.x; r < TS; r += NT) X[r * LDS + j] = X[r * LDS + j] / d;
-    __syncthreads();
+    const double rj = rd[j];
     for (int idx = threadIdx.x; idx < TS * j; idx += NT) {
       const int r = idx / j, col = idx % j;
-      X[r * LDS + col] = fma(-X[r * LDS + j], F[j * LDS + col], X[r * LDS + col]);
+      X[r * LDS + col] = fma(-X[r * LDS + j] * rj, F[j * LDS + col], X[r * LDS + col]);
     }
   }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < TS * TS; idx += NT) X[(idx / TS) * LDS + idx % TS] *= rd[idx % TS];
   __syncthreads();
 }
 

@@ -58,6 +58,7 @@ __device__ bool load_diag_factor(const FactorArgs& p, int i, int c, double* F, i
 
 __global__ void __launch_bounds__(NT, 1) k_factor(FactorArgs p) {
   __shared__ double sm[4 * TILE_SMEM];
+  __shared__ double vec[TS];            // pivots' 1/sqrt, or reciprocals of a factor tile's diagonal
   __shared__ int s_ok, s_t;
   double* bufs = sm;                    // 4 tiles: K-loop double buffer
   double* X = sm;                       // target tile (aliases the K-loop buffers:
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor(FactorArgs p) {
         const int rr = idx / TS, cc = idx % TS;
         if (rr >= g.a || cc >= g.a) X[rr * LDS + cc] = (rr == cc) ? 1.0 : 0.0;
       }
-      const int info = smem_potrf(X);
+      const int info = smem_potrf(X, vec);
       if (info) {
         if (threadIdx.x == 0) {
           atomicCAS(c.ctrl + CTRL_INFO, 0, g.nt * g.b + info);
@@ -173,7 +174,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor(FactorArgs p) {
 
     if (type == FT_DIAG) {
       tile_pad_identity(X, g.vrows(col));
-      const int info = smem_potrf(X);
+      const int info = smem_potrf(X, vec);
       if (info) {
         if (threadIdx.x == 0) {
           atomicCAS(c.ctrl + CTRL_INFO, 0, i * g.b + col * TS + info);
@@ -188,7 +189,8 @@ __global__ void __launch_bounds__(NT, 1) k_factor(FactorArgs p) {
 
     // Off-diagonal targets: X <- X * D_i(col,col)^{-T}.
     if (!load_diag_factor(p, i, col, F, &s_ok)) break;
-    smem_trsm_rlt(X, F);
+    tile_diag_recip(F, vec);
+    smem_trsm_rlt(X, F, vec);
     tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
     if (type == FT_OFFD) {
       // The factor's strict upper triangle is zero: clear the mirrored tile.
@@ -230,6 +232,7 @@ void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, in
   p.c.epoch = lc.epoch;
   p.c.wait_ns = lc.wait_ns;
   k_factor<<<lc.grid, NT, 0, lc.stream>>>(p);
+  count_launches(1);
 }
 
 }  // namespace gbta

@@ -36,6 +36,9 @@ struct LaunchCtl {
   cudaStream_t stream;
 };
 
+// Host-side count of kernel launches issued by this library (see gbta_kernel_launches).
+void count_launches(int n);
+
 void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow,
                    const int4* tasks, int ntasks, double* tip_part, const LaunchCtl& lc);
 

@@ -39,6 +39,7 @@ void launch_logdet(const Geom& g, const double* D, const double* T, int with_tip
                    cudaStream_t stream) {
   k_logdet_blocks<<<g.nt + 1, LD_THREADS, 0, stream>>>(D, T, g, with_tip, partial);
   k_logdet_final<<<1, 32, 0, stream>>>(partial, g.nt + 1, out);
+  count_launches(2);
 }
 
 }  // namespace gbta

@@ -137,19 +137,19 @@ __device__ __forceinline__ int pat_code(const SelinvArgs& p, int i, int c, int s
   return g.B - 1 - s;
 }
 
-// X <- (F^{-T} - X) F^{-1} (diagonal tile of Sigma), then symmetrise.
-__device__ void diag_finish(double* X, double* W, const double* F) {
+// X <- (F^{-T} - X) F^{-1} (diagonal tile of Sigma), then symmetrise; rd = 1/diag(F).
+__device__ void diag_finish(double* X, double* W, const double* F, const double* rd) {
   // W = I * F^{-T}
   for (int idx = threadIdx.x; idx < TS * TS; idx += NT) {
     const int r = idx / TS, cc = idx % TS;
     W[r * LDS + cc] = (r == cc) ? 1.0 : 0.0;
   }
-  smem_trsm_rlt(W, F);
+  smem_trsm_rlt(W, F, rd);
   for (int idx = threadIdx.x; idx < TS * TS; idx += NT) {
     const int r = idx / TS, cc = idx % TS;
     W[r * LDS + cc] -= X[r * LDS + cc];
   }
-  smem_trsm_rln(W, F);
+  smem_trsm_rln(W, F, rd);
   for (int idx = threadIdx.x; idx < TS * TS; idx += NT) {
     const int r = idx / TS, cc = idx % TS;
     X[r * LDS + cc] = 0.5 * (W[r * LDS + cc] + W[cc * LDS + r]);
@@ -159,6 +159,7 @@ __device__ void diag_finish(double* X, double* W, const double* F) {
 
 __global__ void __launch_bounds__(NT, 1) k_selinv(SelinvArgs p) {
   __shared__ double sm[4 * TILE_SMEM];
+  __shared__ double rd[TS];   // reciprocals of the diagonal factor tile's diagonal
   __shared__ int s_ok, s_t;
   double* bufs = sm;
   double* X = sm;
@@ -181,7 +182,9 @@ __global__ void __launch_bounds__(NT, 1) k_selinv(SelinvArgs p) {
       tile_pad_identity(F, g.a);
       for (int idx = threadIdx.x; idx < TS * TS; idx += NT) X[idx / TS * LDS + idx % TS] = 0.0;
       __syncthreads();
-      diag_finish(X, W, F);
+      tile_diag_recip(F, rd);
+      __syncthreads();
+      diag_finish(X, W, F, rd);
       tile_store(p.ST, g.a, g.a, g.a, X);
       cta_publish(c, c.flags + g.fT());
       continue;
@@ -210,7 +213,9 @@ __global__ void __launch_bounds__(NT, 1) k_selinv(SelinvArgs p) {
       tile_load(F, fac_tile(p, i, col, col));
       __syncthreads();
       tile_pad_identity(F, g.vrows(col));
-      smem_trsm_rln(X, F);
+      __syncthreads();
+      tile_diag_recip(F, rd);
+      smem_trsm_rln(X, F, rd);
       const SigTile d = sig_dest(p, i, j, col);
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
       cta_publish(c, const_cast<int*>(d.flag));
@@ -235,7 +240,9 @@ __global__ void __launch_bounds__(NT, 1) k_selinv(SelinvArgs p) {
       __syncthreads();
       tile_pad_identity(F, g.vrows(col));
       __syncthreads();
-      diag_finish(X, W, F);
+      tile_diag_recip(F, rd);
+      __syncthreads();
+      diag_finish(X, W, F, rd);
       const SigTile d = sig_dest(p, i, col, col);
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
       cta_publish(c, const_cast<int*>(d.flag));
@@ -287,11 +294,13 @@ void launch_selinv(const Geom& g, const double* D, const double* L, const double
   p.c.epoch = lc.epoch;
   p.c.wait_ns = lc.wait_ns;
   k_selinv<<<lc.grid, NT, 0, lc.stream>>>(p);
+  count_launches(1);
 }
 
 void launch_selinv_writeback(const Geom& g, const double* SD, const double* SL, const double* SR, const double* ST,
                              double* D, double* L, double* R, double* T, int use_arrow, cudaStream_t stream) {
   k_writeback<<<1024, 256, 0, stream>>>(SD, SL, SR, ST, D, L, R, T, g, use_arrow);
+  count_launches(1);
 }
 
 }  // namespace gbta

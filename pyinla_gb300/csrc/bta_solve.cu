@@ -46,39 +46,27 @@ __device__ __forceinline__ void vec_load(double* Vs, const SolveArgs& p, int row
   Vs[row * NC + col] = (row < rows && col < p.nc) ? __ldcg(p.B + (size_t)(row0 + row) * p.ldb + col) : 0.0;
 }
 
-// Warp 0: forward (lower) or backward (upper = F^T) substitution of the NC columns of
-// Ss with the TS x TS lower factor tile F (identity padded).  In place on Ss.
-__device__ void warp_trsv(double* Ss, const double* F, bool upper) {
-  if (threadIdx.x >= 32) return;
-  const int lane = threadIdx.x;
-  double s[NC];
-#pragma unroll
-  for (int q = 0; q < NC; ++q) s[q] = Ss[lane * NC + q];
+// Substitution of the NC columns of Ss (TS x NC, row-major) with the TS x TS lower
+// factor tile F (identity padded): forward (L y = s) or backward (L^T x = s).  Warp q
+// handles column q; rd = 1/diag(F), so each step is one multiply and one FMA.
+__device__ void warp_trsv(double* Ss, const double* F, const double* rd, bool upper, int ncols) {
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (q >= ncols) return;
+  double s = Ss[lane * NC + q];
   if (!upper) {
     for (int j = 0; j < TS; ++j) {
-      const double d = F[j * LDS + j];
-      const double f = F[lane * LDS + j];
-#pragma unroll
-      for (int q = 0; q < NC; ++q) {
-        const double yj = __shfl_sync(0xffffffffu, s[q], j) / d;
-        if (lane == j) s[q] = yj;
-        else if (lane > j) s[q] = fma(-f, yj, s[q]);
-      }
+      const double yj = __shfl_sync(0xffffffffu, s, j) * rd[j];
+      if (lane == j) s = yj;
+      else if (lane > j) s = fma(-F[lane * LDS + j], yj, s);
     }
   } else {
     for (int j = TS - 1; j >= 0; --j) {
-      const double d = F[j * LDS + j];
-      const double f = F[j * LDS + lane];
-#pragma unroll
-      for (int q = 0; q < NC; ++q) {
-        const double xj = __shfl_sync(0xffffffffu, s[q], j) / d;
-        if (lane == j) s[q] = xj;
-        else if (lane < j) s[q] = fma(-f, xj, s[q]);
-      }
+      const double xj = __shfl_sync(0xffffffffu, s, j) * rd[j];
+      if (lane == j) s = xj;
+      else if (lane < j) s = fma(-F[j * LDS + lane], xj, s);
     }
   }
-#pragma unroll
-  for (int q = 0; q < NC; ++q) Ss[lane * NC + q] = s[q];
+  Ss[lane * NC + q] = s;
 }
 
 __global__ void __launch_bounds__(NT, 1) k_solve(SolveArgs p) {
@@ -86,6 +74,7 @@ __global__ void __launch_bounds__(NT, 1) k_solve(SolveArgs p) {
   __shared__ double Fs[TILE_SMEM];
   __shared__ double Vs[TS * NC];
   __shared__ double Ss[TS * NC];
+  __shared__ double rd[TS];
   __shared__ int s_ok, s_t;
   const Geom& g = p.g;
   const Ctl& c = p.c;
@@ -124,7 +113,9 @@ __global__ void __launch_bounds__(NT, 1) k_solve(SolveArgs p) {
       __syncthreads();
       tile_pad_identity(Fs, g.a);
       __syncthreads();
-      warp_trsv(Ss, Fs, p.trans != 0);
+      tile_diag_recip(Fs, rd);
+      __syncthreads();
+      warp_trsv(Ss, Fs, rd, p.trans != 0, p.nc);
       __syncthreads();
       if (row < g.a && col < p.nc) p.B[(size_t)(arrow_row0 + row) * p.ldb + col] = Ss[threadIdx.x];
       cta_publish(c, c.flags + ntile);
@@ -135,6 +126,13 @@ __global__ void __launch_bounds__(NT, 1) k_solve(SolveArgs p) {
     const int rows = g.vrows(r);
     const int row0 = i * g.b + r * TS;
     double s = (row < rows && col < p.nc) ? __ldcg(p.B + (size_t)(row0 + row) * p.ldb + col) : 0.0;
+    // The diagonal factor tile and its reciprocals do not depend on other tasks:
+    // stage them before waiting on any dependency.
+    tile_load(Fs, make_tile(p.D + i * bb, g.b, r * TS, r * TS, g.b, g.b));
+    __syncthreads();
+    tile_pad_identity(Fs, rows);
+    __syncthreads();
+    tile_diag_recip(Fs, rd);
     bool ok = true;
     if (p.trans == 0) {
       // s -= L_{i-1}(r,k) y(i-1,k) for all k; s -= D_i(r,k) y(i,k) for k < r
@@ -189,11 +187,8 @@ __global__ void __launch_bounds__(NT, 1) k_solve(SolveArgs p) {
     }
     if (!ok) break;
     Ss[threadIdx.x] = s;
-    tile_load(Fs, make_tile(p.D + i * bb, g.b, r * TS, r * TS, g.b, g.b));
     __syncthreads();
-    tile_pad_identity(Fs, rows);
-    __syncthreads();
-    warp_trsv(Ss, Fs, p.trans != 0);
+    warp_trsv(Ss, Fs, rd, p.trans != 0, p.nc);
     __syncthreads();
     if (row < rows && col < p.nc) p.B[(size_t)(row0 + row) * p.ldb + col] = Ss[threadIdx.x];
     if (p.trans == 0 && p.use_arrow) {
@@ -227,6 +222,7 @@ void launch_solve(const Geom& g, const double* D, const double* L, const double*
   p.c.epoch = lc.epoch;
   p.c.wait_ns = lc.wait_ns;
   k_solve<<<lc.grid, NT, 0, lc.stream>>>(p);
+  count_launches(1);
 }
 
 }  // namespace gbta

@@ -91,6 +91,7 @@ extern "C" int gbta_scatter_coo(gbta_solver* s, const long long* rows, const lon
     gbta::k_scatter<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, stream>>>(g, p, with_arrow, rows, cols, vals,
                                                                                   nnz);
   }
+  gbta::count_launches(1 + (nt > 1) + 2 * (with_arrow && a > 0) + (nnz > 0));
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return gbta_set_error(GBTA_ERR_CUDA, cudaGetErrorString(e));
   return GBTA_OK;
@@ -110,6 +111,7 @@ extern "C" int gbta_gather_coo(gbta_solver* s, const long long* rows, const long
   const long long blocks = (nnz + 255) / 256;
   gbta::k_gather<<<(unsigned)(blocks < 4096 ? blocks : 4096), 256, 0, (cudaStream_t)st>>>(g, p, with_arrow, rows, cols,
                                                                                          vals, nnz);
+  gbta::count_launches(1);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return gbta_set_error(GBTA_ERR_CUDA, cudaGetErrorString(e));
   return GBTA_OK;

@@ -1,0 +1,417 @@
+"""Gaussian spatio-temporal models with a Kronecker-sum prior, evaluated on the GB300.
+
+A model here is the reference's Gaussian-likelihood ``Model`` reduced to what the
+BTA path needs (src/pyinla/core/model.py:306-449):
+
+    Q_prior(theta) = sum_k  M_k(theta) (x) S_k   (+ tip_prec * I on the fixed effects)
+    Q_cond(theta)  = Q_prior(theta) + tau_y(theta) A^T A
+    b(theta)       = tau_y(theta) A^T y
+
+with fixed sparse spatial matrices ``S_k`` and tridiagonal temporal coefficient
+matrices ``M_k(theta)`` given by their diagonal ``alpha[k, t]`` and sub-diagonal
+``beta[k, t]``.  The objective is the reference's ``_evaluate_f`` for a Gaussian
+likelihood evaluated at x = 0 (src/pyinla/core/pyinla.py:602-745, 1076-1167):
+
+    f(theta) = -log pi(theta) - l(y | eta=0) - 1/2 logdet_bt Q_prior
+               + 1/2 logdet Q_cond - 1/2 mu^T Q_cond mu,      mu = Q_cond^{-1} b
+
+and its gradient is computed by the adjoint (no counterpart in the reference, which
+spends 2 dim(theta) + 1 evaluations on central differences, pyinla.py:512-600):
+
+    df/dtheta = -dlog pi - dl - 1/2 tr(Q_prior^{-1} dQ_prior) + 1/2 tr(Q_cond^{-1} dQ_cond)
+                - mu^T db + 1/2 mu^T dQ_cond mu
+
+where the traces only need Q^{-1} on the BTA pattern -- exactly what the selected
+inversion produces -- contracted against the sparse dQ blocks on the device.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import scipy.sparse as sps
+
+from . import _lib, spde
+from .device import BtaHandle, current_stream_ptr, require_torch_cuda
+
+
+@dataclass
+class Coefficients:
+    alpha: np.ndarray        # (K, nt)
+    beta: np.ndarray         # (K, nt-1)
+    tau_y: float
+
+
+@dataclass
+class CoefficientDerivatives:
+    dalpha: np.ndarray       # (d, K, nt)
+    dbeta: np.ndarray        # (d, K, nt-1)
+    dtau_y: np.ndarray       # (d,)
+
+
+def union_pattern(mats: list[sps.csr_matrix]):
+    """Union CSR pattern of same-shape sparse matrices and each matrix's values on it."""
+    n = mats[0].shape[0]
+    U = sum(abs(m) for m in mats).tocsr()
+    U.sum_duplicates()
+    U.sort_indices()
+    rowptr = U.indptr.astype(np.int32)
+    col = U.indices.astype(np.int32)
+    vals = np.zeros((col.size, len(mats)))
+    rows = np.repeat(np.arange(n), np.diff(U.indptr))
+    for k, m in enumerate(mats):
+        mc = m.tocsr()
+        mc.sum_duplicates()
+        vals[:, k] = np.asarray(mc[rows, col]).ravel()
+    return rowptr, col, vals
+
+
+class KronSpec:
+    """Host description of a Kronecker-sum Gaussian model (no device state).
+
+    Subclasses define the theta -> coefficient maps.  Fields: ``terms`` (spatial
+    matrices S_k), ``term_vw`` (variate block of each term), ``ns``, ``nv``, ``nt``,
+    ``nb``, ``A`` (n_obs x N design matrix, time-major field then fixed effects),
+    ``y`` and ``tip_prec``.
+    """
+
+    terms: list
+    term_vw: list
+    ns: int
+    nv: int
+    nt: int
+    nb: int
+    A: sps.csr_matrix
+    y: np.ndarray
+    tip_prec: float
+
+    @property
+    def K(self) -> int:
+        return len(self.terms)
+
+    @property
+    def b(self) -> int:
+        return self.ns * self.nv
+
+    @property
+    def N(self) -> int:
+        return self.nt * self.b + self.nb
+
+    def coefficients(self, theta: np.ndarray) -> Coefficients:
+        raise NotImplementedError
+
+    def coefficient_derivatives(self, theta: np.ndarray) -> CoefficientDerivatives:
+        raise NotImplementedError
+
+    def log_prior(self, theta: np.ndarray) -> float:
+        raise NotImplementedError
+
+    def log_prior_grad(self, theta: np.ndarray) -> np.ndarray:
+        raise NotImplementedError
+
+    def lik_theta_index(self) -> int:
+        """Index of theta_y = log tau_y in theta."""
+        raise NotImplementedError
+
+    def sparse_precisions(self, theta: np.ndarray):
+        """Host sparse (CSR) Q_prior and Q_cond at theta, in the form the reference's
+        Model hands to its solver (src/pyinla/core/model.py:306-423): the input of
+        the sparse drop-in path (``GB300SerinvSolver.cholesky``)."""
+        c = self.coefficients(theta)
+        b, nt, ns = self.b, self.nt, self.ns
+        N = self.N
+        rows, cols, vals = [], [], []
+        for k, S in enumerate(self.terms):
+            v, w = self.term_vw[k]
+            Sc = S.tocoo()
+            for t in range(nt):
+                rows.append(t * b + v * ns + Sc.row)
+                cols.append(t * b + w * ns + Sc.col)
+                vals.append(c.alpha[k, t] * Sc.data)
+                if t < nt - 1:
+                    for (r0, c0) in ((t + 1, t), (t, t + 1)):
+                        rows.append(r0 * b + v * ns + Sc.row)
+                        cols.append(c0 * b + w * ns + Sc.col)
+                        vals.append(c.beta[k, t] * Sc.data)
+        if self.nb:
+            rows.append(nt * b + np.arange(self.nb))
+            cols.append(nt * b + np.arange(self.nb))
+            vals.append(np.full(self.nb, self.tip_prec))
+        Qp = sps.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(N, N))
+        Qp.sum_duplicates()
+        Qc = (Qp + c.tau_y * (self.A.T @ self.A)).tocsr()
+        Qc.sum_duplicates()
+        return Qp, Qc
+
+
+class KronGaussianModel:
+    """Device-resident evaluation of a :class:`KronSpec` model (see module docstring)."""
+
+    def __init__(self, spec: KronSpec):
+        torch = require_torch_cuda()
+        self.spec = spec
+        self.torch = torch
+        self.ns, self.nv, self.nt, self.nb = int(spec.ns), int(spec.nv), int(spec.nt), int(spec.nb)
+        self.b = self.ns * self.nv
+        self.N = self.nt * self.b + self.nb
+        self.K = spec.K
+        self.tip_prec = float(spec.tip_prec)
+        A, y = spec.A, spec.y
+        self.n_obs = int(y.shape[0])
+        if A.shape != (self.n_obs, self.N):
+            raise ValueError(f"A has shape {A.shape}, expected {(self.n_obs, self.N)}")
+        # --- theta-independent device data (built once, like the reference's pattern reuse,
+        #     src/pyinla/core/model.py:356-380)
+        dev = "cuda"
+        rowptr, col, uval = union_pattern(spec.terms)
+        self._upat_rowptr = torch.from_numpy(rowptr).to(dev)
+        self._upat_col = torch.from_numpy(col).to(dev)
+        self._uval = torch.from_numpy(np.ascontiguousarray(uval)).to(dev)
+        self._term_vw = torch.from_numpy(np.asarray(spec.term_vw, dtype=np.int32).reshape(-1)).to(dev)
+        At = A.T.tocsr()
+        AtA = (At @ A).tocsr()
+        AtA.sum_duplicates()
+        nbk = self.nt * self.b
+        # diagonal-block rows of A^T A as CSR with block-local columns
+        blk = AtA[:nbk, :nbk].tocoo()
+        keep = (blk.row // self.b) == (blk.col // self.b)
+        if int(np.count_nonzero(~keep)):
+            raise ValueError("A^T A couples different time blocks: each observation must touch one time step")
+        D_lik = sps.csr_matrix((blk.data[keep], (blk.row[keep], blk.col[keep] % self.b)), shape=(nbk, self.b))
+        D_lik.sum_duplicates()
+        D_lik.sort_indices()
+        self._lik_rowptr = torch.from_numpy(D_lik.indptr.astype(np.int64)).to(dev)
+        self._lik_col = torch.from_numpy(D_lik.indices.astype(np.int32)).to(dev)
+        self._lik_val = torch.from_numpy(D_lik.data.astype(np.float64)).to(dev)
+        if self.nb > 0:
+            Rl = np.asarray(AtA[nbk:, :nbk].todense()).reshape(self.nb, self.nt, self.b).transpose(1, 0, 2)
+            Tl = np.asarray(AtA[nbk:, nbk:].todense())
+            self._lik_R = torch.from_numpy(np.ascontiguousarray(Rl)).to(dev)
+            self._lik_T = torch.from_numpy(np.ascontiguousarray(Tl)).to(dev)
+        else:
+            self._lik_R = self._lik_T = None
+        self._Aty = torch.from_numpy(np.asarray(At @ y, dtype=np.float64)).to(dev)
+        self.yty = float(y @ y)
+        # --- block buffers: conditional (bta) and prior (bt) precisions
+        f64 = torch.float64
+        b, nt, a = self.b, self.nt, self.nb
+        self.Dc = torch.empty((nt, b, b), dtype=f64, device=dev)
+        self.Lc = torch.empty((max(nt - 1, 1), b, b), dtype=f64, device=dev)
+        self.Rc = torch.empty((nt, max(a, 1), b), dtype=f64, device=dev)
+        self.Tc = torch.empty((max(a, 1), max(a, 1)), dtype=f64, device=dev)
+        self.Dp = torch.empty_like(self.Dc)
+        self.Lp = torch.empty_like(self.Lc)
+        self.Rp = torch.empty_like(self.Rc)
+        self.Tp = torch.empty_like(self.Tc)
+        self.mu = torch.empty(self.N, dtype=f64, device=dev)
+        self._coef = torch.empty(2 * self.K * nt, dtype=f64, device=dev)
+        self._contract_out = torch.empty(4 * self.K * nt + 2 * (nt + 1), dtype=f64, device=dev)
+        self.h = BtaHandle.get(b, nt, a)
+        self.last = {}
+
+    def coefficients(self, theta):
+        return self.spec.coefficients(theta)
+
+    def coefficient_derivatives(self, theta):
+        return self.spec.coefficient_derivatives(theta)
+
+    def log_prior(self, theta):
+        return self.spec.log_prior(theta)
+
+    def log_prior_grad(self, theta):
+        return self.spec.log_prior_grad(theta)
+
+    def lik_theta_index(self):
+        return self.spec.lik_theta_index()
+
+    # ---------------------------------------------------------------- device steps
+    def _ptr(self, t):
+        return None if t is None else t.data_ptr()
+
+    def _upload_coef(self, c: Coefficients):
+        K, nt = self.K, self.nt
+        buf = np.zeros(2 * K * nt)
+        buf[: K * nt] = c.alpha.reshape(-1)
+        if nt > 1:
+            buf[K * nt: K * nt + K * (nt - 1)] = c.beta.reshape(-1)
+        self._coef.copy_(self.torch.from_numpy(buf), non_blocking=False)
+        return self._coef.data_ptr(), self._coef.data_ptr() + 8 * K * nt
+
+    def _assemble(self, alpha_p, beta_p, lik_scale, D, L, R, T, with_lik: bool):
+        lib, h = self.h.lib, self.h
+        _lib.check(lib.gbta_assemble_kron(
+            h.ptr, self.ns, self.nv, self.K, self._upat_rowptr.data_ptr(), self._upat_col.data_ptr(),
+            self._uval.data_ptr(), self._term_vw.data_ptr(), alpha_p, beta_p,
+            self._lik_rowptr.data_ptr() if with_lik else None, self._lik_col.data_ptr() if with_lik else None,
+            self._lik_val.data_ptr() if with_lik else None, self._ptr(self._lik_R) if with_lik else None,
+            self._ptr(self._lik_T) if with_lik else None, float(lik_scale), self.tip_prec,
+            D.data_ptr(), L.data_ptr(), R.data_ptr(), T.data_ptr()))
+
+    def _contract(self, SD, SL, SR, ST, mu) -> np.ndarray:
+        lib, h = self.h.lib, self.h
+        _lib.check(lib.gbta_contract_kron(
+            h.ptr, self.ns, self.nv, self.K, self._upat_rowptr.data_ptr(), self._upat_col.data_ptr(),
+            self._uval.data_ptr(), self._term_vw.data_ptr(), self._lik_rowptr.data_ptr(), self._lik_col.data_ptr(),
+            self._lik_val.data_ptr(), self._ptr(self._lik_R), self._ptr(self._lik_T),
+            self._ptr(SD), self._ptr(SL), self._ptr(SR), self._ptr(ST), self._ptr(mu),
+            self._contract_out.data_ptr()))
+        return self._contract_out.cpu().numpy()
+
+    def _logdet(self, D, T, with_tip: bool) -> float:
+        out = ctypes.c_double(0.0)
+        code = self.h.lib.gbta_logdet(self.h.ptr, D.data_ptr(), T.data_ptr() if with_tip else None,
+                                      1 if with_tip else 0, ctypes.byref(out))
+        if code == _lib.GBTA_ERR_ARG and np.isnan(out.value):
+            raise ValueError("Logdet is NaN. Check the input matrix.")
+        _lib.check(code)
+        return float(out.value)
+
+    def _split(self, out: np.ndarray):
+        K, nt = self.K, self.nt
+        KN = K * nt
+        c = out[0:KN].reshape(K, nt)
+        d = out[KN:2 * KN].reshape(K, nt)[:, : nt - 1]
+        qc = out[2 * KN:3 * KN].reshape(K, nt)
+        qd = out[3 * KN:4 * KN].reshape(K, nt)[:, : nt - 1]
+        lc = float(out[4 * KN:4 * KN + nt + 1].sum())
+        lq = float(out[4 * KN + nt + 1:4 * KN + 2 * (nt + 1)].sum())
+        return c, d, qc, qd, lc, lq
+
+    # ---------------------------------------------------------------- public
+    def evaluate(self, theta, gradient: bool = False):
+        """f(theta) (and, with ``gradient=True``, its adjoint gradient)."""
+        theta = np.asarray(theta, dtype=np.float64)
+        h = self.h
+        h.set_stream(current_stream_ptr())
+        lib = h.lib
+        coef = self.coefficients(theta)
+        alpha_p, beta_p = self._upload_coef(coef)
+        has_arrow = self.nb > 0
+        # prior: bt factorization, tip excluded from the logdet (pyinla.py:1102-1103)
+        self._assemble(alpha_p, beta_p, 0.0, self.Dp, self.Lp, self.Rp, self.Tp, with_lik=False)
+        _lib.check(lib.gbta_pobtf(h.ptr, self.Dp.data_ptr(), self.Lp.data_ptr()))
+        logdet_p = self._logdet(self.Dp, self.Tp, with_tip=False)
+        # conditional: bta factorization (pyinla.py:650-662)
+        self._assemble(alpha_p, beta_p, coef.tau_y, self.Dc, self.Lc, self.Rc, self.Tc, with_lik=True)
+        R, T = (self.Rc.data_ptr(), self.Tc.data_ptr()) if has_arrow else (None, None)
+        _lib.check(lib.gbta_pobtaf(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T))
+        logdet_c = self._logdet(self.Dc, self.Tc, with_tip=has_arrow)
+        # mean: mu = Q_cond^{-1} tau_y A^T y (model.py:425-449 at x = 0)
+        self.mu.copy_(self._Aty)
+        self.mu.mul_(coef.tau_y)
+        bvec = self.mu.clone()
+        _lib.check(lib.gbta_pobtas_async(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T,
+                                         self.mu.data_ptr(), 1, 0))
+        _lib.check(lib.gbta_pobtas(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T, self.mu.data_ptr(), 1, 1))
+        quad = float(self.torch.dot(self.mu, bvec))   # mu^T Q_cond mu = mu^T b
+        ty = self.lik_theta_index()
+        lik = 0.5 * self.n_obs * theta[ty] - 0.5 * coef.tau_y * self.yty   # gaussian.py:58-60, eta = 0
+        lp = self.log_prior(theta)
+        f = -(lp + lik + 0.5 * logdet_p) + 0.5 * logdet_c - 0.5 * quad
+        self.last = dict(logdet_prior=logdet_p, logdet_cond=logdet_c, quad=quad, lik=lik, log_prior=lp)
+        if not gradient:
+            return f
+        return f, self._adjoint_gradient(theta, coef, quad)
+
+    def _adjoint_gradient(self, theta, coef: Coefficients, quad: float) -> np.ndarray:
+        h = self.h
+        lib = h.lib
+        dc = self.coefficient_derivatives(theta)
+        has_arrow = self.nb > 0
+        # conditional selected inverse (in place over the factor) + contractions with mu
+        R, T = (self.Rc.data_ptr(), self.Tc.data_ptr()) if has_arrow else (None, None)
+        _lib.check(lib.gbta_pobtasi(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T))
+        cc, dd, qc, qd, lc, lq = self._split(self._contract(
+            self.Dc, self.Lc if self.nt > 1 else None, self.Rc if has_arrow else None,
+            self.Tc if has_arrow else None, self.mu))
+        # prior selected inverse (bt)
+        _lib.check(lib.gbta_pobtsi(h.ptr, self.Dp.data_ptr(), self.Lp.data_ptr()))
+        pc, pd, _, _, _, _ = self._split(self._contract(self.Dp, self.Lp if self.nt > 1 else None, None, None, None))
+        d = dc.dalpha.shape[0]
+        grad = np.zeros(d)
+        for k in range(d):
+            da, db = dc.dalpha[k], dc.dbeta[k]
+            tr_c = float(np.sum(da * cc) + 2.0 * np.sum(db * dd) + dc.dtau_y[k] * lc)
+            tr_p = float(np.sum(da * pc) + 2.0 * np.sum(db * pd))
+            mqm = float(np.sum(da * qc) + 2.0 * np.sum(db * qd) + dc.dtau_y[k] * lq)
+            mdb = dc.dtau_y[k] / coef.tau_y * quad        # mu^T d(b) with b = tau_y A^T y
+            grad[k] = -0.5 * tr_p + 0.5 * tr_c - mdb + 0.5 * mqm
+        ty = self.lik_theta_index()
+        grad[ty] -= 0.5 * self.n_obs - 0.5 * coef.tau_y * self.yty
+        grad -= self.log_prior_grad(theta)
+        return grad
+
+
+class SeparableSpdeAr1(KronSpec):
+    """Q_prior = tau * (T_AR1(rho) (x) Q_s(kappa)) (+) tip_prec * I_nb, Gaussian likelihood.
+
+    theta = (log kappa, log r_t, log tau, log tau_y) with rho = exp(-1 / r_t);
+    Gaussian priors N(theta0, 1 / prior_prec) on every component (the form of the
+    reference's GaussianPriorHyperparameters, src/pyinla/prior_hyperparameters/gaussian.py:26-29).
+    """
+
+    def __init__(self, mesh: spde.Mesh, nt: int, nb: int, obs: spde.Observations, theta0: np.ndarray,
+                 prior_prec: float = 0.5, tip_prec: float = 1e-3):
+        self.mesh = mesh
+        self.theta0 = np.asarray(theta0, dtype=np.float64)
+        self.prior_prec = float(prior_prec)
+        self.terms = spde.spde_terms(mesh)
+        self.term_vw = [(0, 0)] * len(self.terms)
+        self.ns, self.nv, self.nt, self.nb = mesh.ns, 1, int(nt), int(nb)
+        self.A = spde.design_matrix(obs, mesh.ns, nt, nb)
+        self.y = obs.y
+        self.tip_prec = float(tip_prec)
+
+    @staticmethod
+    def unpack(theta):
+        kappa = np.exp(theta[0])
+        r_t = np.exp(theta[1])
+        rho = np.exp(-1.0 / r_t)
+        return kappa, r_t, rho, np.exp(theta[2]), np.exp(theta[3])
+
+    def coefficients(self, theta) -> Coefficients:
+        kappa, r_t, rho, tau, tau_y = self.unpack(theta)
+        w = spde.spde_weights(kappa)
+        tdiag, toff = spde.ar1_bands(rho, self.nt)
+        return Coefficients(alpha=tau * np.outer(w, tdiag), beta=tau * np.outer(w, toff).reshape(len(w), -1),
+                            tau_y=tau_y)
+
+    def coefficient_derivatives(self, theta) -> CoefficientDerivatives:
+        kappa, r_t, rho, tau, tau_y = self.unpack(theta)
+        w = spde.spde_weights(kappa)
+        dw = spde.spde_weights_dlogkappa(kappa)
+        tdiag, toff = spde.ar1_bands(rho, self.nt)
+        ddiag, doff = spde.ar1_bands_drho(rho, self.nt)
+        drho = rho / r_t                         # d rho / d log r_t
+        dalpha = np.stack([tau * np.outer(dw, tdiag), tau * drho * np.outer(w, ddiag),
+                           tau * np.outer(w, tdiag), np.zeros((self.K, self.nt))])
+        dbeta = np.stack([tau * np.outer(dw, toff), tau * drho * np.outer(w, doff),
+                          tau * np.outer(w, toff), np.zeros((self.K, max(self.nt - 1, 0)))])
+        return CoefficientDerivatives(dalpha=dalpha, dbeta=dbeta, dtau_y=np.array([0.0, 0.0, 0.0, tau_y]))
+
+    @classmethod
+    def synthetic(cls, n_side: int, nt: int, nb: int, n_obs: int, seed: int, theta0=None):
+        """The benchmark's synthetic instance: n_side x n_side mesh, n_obs observations."""
+        mesh = spde.unit_square_mesh(n_side)
+        obs = spde.make_observations(mesh, nt, n_obs, nb, seed)
+        th = default_theta() if theta0 is None else np.asarray(theta0, dtype=np.float64)
+        return cls(mesh, nt, nb, obs, th)
+
+    def log_prior(self, theta) -> float:
+        return float(-0.5 * self.prior_prec * np.sum((theta - self.theta0) ** 2))
+
+    def log_prior_grad(self, theta) -> np.ndarray:
+        return -self.prior_prec * (theta - self.theta0)
+
+    def lik_theta_index(self) -> int:
+        return 3
+
+
+def default_theta(rho: float = 0.9, kappa: float = None, tau: float = 1.0, tau_y: float = 4.0, ns: int = 1024):
+    """theta = (log kappa, log r_t, log tau, log tau_y) for the benchmark model; kappa
+    defaults to a spatial range of a third of the domain (kappa = sqrt(8) / 0.33)."""
+    if kappa is None:
+        kappa = np.sqrt(8.0) / 0.33
+    r_t = -1.0 / np.log(rho)
+    return np.array([np.log(kappa), np.log(r_t), np.log(tau), np.log(tau_y)])

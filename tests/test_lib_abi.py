@@ -13,7 +13,7 @@ HEADER = Path(__file__).resolve().parents[1] / "include" / "pyinla_gb300.h"
 
 def header_symbols():
     text = HEADER.read_text()
-    return sorted(set(re.findall(r"\b(gbta_[a-z_]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(gbta_[a-z0-9_]+)\s*\(", text)))
 
 
 def test_library_builds_and_loads():
