@@ -99,6 +99,25 @@ int gbta_pobtf(gbta_solver* s, double* D, double* L);
 int gbta_pobtaf_async(gbta_solver* s, double* D, double* L, double* R, double* T);
 int gbta_pobtf_async(gbta_solver* s, double* D, double* L);
 
+/* ---- factorization without device allocation ----------------------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device memory
+ * when they factor -- hosts that own a fixed device-memory pool and forbid
+ * allocations outside it, or loops that cannot afford the implicit device
+ * synchronisation of cudaMalloc/cudaFree -- gbta_pobtaf_noalloc factors like
+ * gbta_pobtaf (same kernel, same results, same return codes, synchronous on
+ * `stream`; NULL = the CUDA default stream) without a solver object and without
+ * calling cudaMalloc, cudaFree or any allocating routine.  Its scratch lives in one
+ * fixed array of GBTA_NOALLOC_SCRATCH_BYTES in device memory, held by every GPU that
+ * loads the library until the process exits; problems whose scratch
+ * (gbta_noalloc_scratch_bytes) exceeds it are rejected with GBTA_ERR_ARG.  All calls
+ * on a device share the array and it keeps the last call's contents (each call
+ * clears what must start at zero): calls that overlap on the GPU race.  The first
+ * call on a device looks up the array's device address (with that device current);
+ * make that first call before any stream capture. */
+#define GBTA_NOALLOC_SCRATCH_BYTES (64u << 20)
+size_t gbta_noalloc_scratch_bytes(int b, int nt, int a);
+int gbta_pobtaf_noalloc(int b, int nt, int a, double* D, double* L, double* R, double* T, void* stream);
+
 /* ---- triangular sweeps: Serinv pobtas / pobts ---------------------------- */
 int gbta_pobtas(gbta_solver* s, const double* D, const double* L, const double* R,
                 const double* T, double* B, int nrhs, int trans);

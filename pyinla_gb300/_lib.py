@@ -47,6 +47,8 @@ SIGNATURES = {
     "gbta_pobtf": (_c_int, [_vp, _vp, _vp]),
     "gbta_pobtaf_async": (_c_int, [_vp, _vp, _vp, _vp, _vp]),
     "gbta_pobtf_async": (_c_int, [_vp, _vp, _vp]),
+    "gbta_noalloc_scratch_bytes": (ctypes.c_size_t, [_c_int, _c_int, _c_int]),
+    "gbta_pobtaf_noalloc": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp]),
     "gbta_pobtas": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _c_int, _c_int]),
     "gbta_pobts": (_c_int, [_vp, _vp, _vp, _vp, _c_int, _c_int]),
     "gbta_pobtas_async": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _c_int, _c_int]),

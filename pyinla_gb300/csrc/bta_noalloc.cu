@@ -1,0 +1,155 @@
+// BTA Cholesky factorization that allocates no device memory.
+//
+// Some callers cannot allocate device memory at the point where they need a
+// factorization: hosts that own a fixed device-memory pool and forbid allocations
+// outside it (custom-call hooks of other frameworks, long-running services that
+// reserve their whole arena up front), and latency-sensitive loops where the implicit
+// device-wide synchronisation of cudaMalloc/cudaFree is not acceptable.  For them,
+// gbta_pobtaf_noalloc runs the same dataflow factorization kernel as gbta_pobtaf, with
+// every piece of its scratch -- control words, per-tile ready flags, the task list and
+// the arrow-tip partial products -- placed in one file-scope __device__ array of
+// GBTA_NOALLOC_SCRATCH_BYTES (64 MiB).  The caller passes only the block buffers.
+//
+// That array exists on every GPU that loads this library and is held until the
+// process exits.  All calls on a device share it and it keeps the previous call's
+// contents: each call clears the part that must start at zero (control words and
+// ready flags) and regenerates the rest, and calls whose work overlaps on the GPU
+// (different streams, or different host threads, at the same time) race on it.
+//
+// In host code the array's name is only a host-side stand-in, not a device address,
+// so its device address is looked up with cudaGetSymbolAddress, once per device with
+// that device current, the first time the entry point runs there; that first call
+// should therefore come before any stream capture.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/pyinla_gb300.h"
+#include "bta_internal.h"
+
+namespace gbta {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[GBTA_NOALLOC_SCRATCH_BYTES];
+
+// Writes the factorization task list in the order the regular path builds it on the
+// host (bta_api.cu: factor_tasks): per block i, per column c: DIAG, OFFD (r > c),
+// LOW (i < nt-1), ARW (a > 0); then TIP (a > 0).  One thread per (i, c).
+__global__ void k_gen_factor_tasks(Geom g, int4* tasks) {
+  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ic >= g.nt * g.B) return;
+  const int i = ic / g.B, c = ic % g.B;
+  const int lb = g.nt > 1 ? g.B : 0;                 // LOW tasks per column of a non-final block
+  const int ab = g.a > 0 ? 1 : 0;
+  const long long per_block = (long long)g.B * (1 + lb + ab) + (long long)g.B * (g.B - 1) / 2;
+  const int lo = (i < g.nt - 1) ? g.B : 0;
+  long long off = (long long)i * per_block + (long long)c * (1 + lb + ab) + (long long)c * (g.B - 1) -
+                  (long long)c * (c - 1) / 2;
+  // the final block has no LOW tasks: its columns are shorter
+  if (i == g.nt - 1 && i > 0) off = (long long)i * per_block + (long long)c * (1 + ab) + (long long)c * (g.B - 1) -
+                                    (long long)c * (c - 1) / 2;
+  tasks[off++] = make_int4(FT_DIAG, i, c, c);
+  for (int r = c + 1; r < g.B; ++r) tasks[off++] = make_int4(FT_OFFD, i, r, c);
+  for (int r = 0; r < lo; ++r) tasks[off++] = make_int4(FT_LOW, i, r, c);
+  if (ab) tasks[off++] = make_int4(FT_ARW, i, 0, c);
+  if (ab && ic == g.nt * g.B - 1) tasks[off] = make_int4(FT_TIP, 0, 0, 0);
+}
+
+}  // namespace gbta
+
+extern "C" int gbta_set_error(int code, const char* msg);
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+void* g_addr[kMaxDevices] = {};
+
+size_t align256(size_t n) { return (n + 255) & ~size_t(255); }
+
+}  // namespace
+
+extern "C" size_t gbta_noalloc_scratch_bytes(int b, int nt, int a) {
+  if (b < 1 || nt < 1 || a < 0) return 0;
+  const long long B = (b + gbta::TS - 1) / gbta::TS;
+  const long long nflags = (2LL * nt - 1) * B * B + (long long)nt * B + 1;
+  const long long per_block = B * (1 + (nt > 1 ? B : 0) + (a > 0 ? 1 : 0)) + B * (B - 1) / 2;
+  const long long ntasks = nt * per_block - (nt > 1 ? B * B : 0) + (a > 0 ? 1 : 0);
+  size_t bytes = align256(8 * sizeof(int));
+  bytes += align256((size_t)nflags * sizeof(int));
+  bytes += align256((size_t)ntasks * sizeof(int4));
+  bytes += align256((size_t)nt * B * gbta::TS * gbta::TS * sizeof(double));
+  return bytes;
+}
+
+extern "C" int gbta_pobtaf_noalloc(int b, int nt, int a, double* D, double* L, double* R, double* T, void* stream) {
+  if (b < 1 || nt < 1 || a < 0) return gbta_set_error(GBTA_ERR_ARG, "noalloc pobtaf: require b >= 1, nt >= 1, a >= 0");
+  if (a > gbta::TS) return gbta_set_error(GBTA_ERR_ARG, "noalloc pobtaf: arrowhead block size above 32 is not supported");
+  if (!D || (nt > 1 && !L) || (a > 0 && (!R || !T)))
+    return gbta_set_error(GBTA_ERR_ARG, "noalloc pobtaf: D/L (and R/T when a > 0) must be device pointers");
+  const size_t need = gbta_noalloc_scratch_bytes(b, nt, a);
+  if (need > (size_t)GBTA_NOALLOC_SCRATCH_BYTES)
+    return gbta_set_error(GBTA_ERR_ARG, ("noalloc pobtaf: this problem needs " + std::to_string(need) +
+                                         " bytes of scratch, above the fixed limit of " +
+                                         std::to_string((size_t)GBTA_NOALLOC_SCRATCH_BYTES) + " bytes")
+                                            .c_str());
+  int dev = 0, nsm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+    return gbta_set_error(GBTA_ERR_CUDA, "noalloc pobtaf: no usable current device");
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
+    if (!g_addr[dev]) {
+      const cudaError_t e = cudaGetSymbolAddress(&g_addr[dev], gbta::g_noalloc_scratch);
+      if (e != cudaSuccess) {
+        g_addr[dev] = nullptr;
+        return gbta_set_error(GBTA_ERR_CUDA, (std::string("noalloc pobtaf: cudaGetSymbolAddress: ") +
+                                              cudaGetErrorString(e)).c_str());
+      }
+    }
+    base = g_addr[dev];
+  }
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return gbta_set_error(GBTA_ERR_CUDA, "noalloc pobtaf: cannot query the SM count");
+
+  gbta::Geom g{b, nt, a, (b + gbta::TS - 1) / gbta::TS};
+  const long long nflags = (2LL * nt - 1) * g.B * g.B + (long long)nt * g.B + 1;
+  const long long per_block = (long long)g.B * (1 + (nt > 1 ? g.B : 0) + (a > 0 ? 1 : 0)) + (long long)g.B * (g.B - 1) / 2;
+  const long long ntasks = nt * per_block - (nt > 1 ? (long long)g.B * g.B : 0) + (a > 0 ? 1 : 0);
+  unsigned char* p = static_cast<unsigned char*>(base);
+  int* ctrl = reinterpret_cast<int*>(p);
+  p += align256(8 * sizeof(int));
+  int* flags = reinterpret_cast<int*>(p);
+  p += align256((size_t)nflags * sizeof(int));
+  int4* tasks = reinterpret_cast<int4*>(p);
+  p += align256((size_t)ntasks * sizeof(int4));
+  double* tip_part = reinterpret_cast<double*>(p);
+
+  cudaStream_t st = (cudaStream_t)stream;
+  // Control words and ready flags must start at zero; the task list is regenerated;
+  // the tip partials are fully written before they are read.
+  cudaError_t e = cudaMemsetAsync(ctrl, 0, (size_t)(reinterpret_cast<unsigned char*>(tasks) -
+                                                     reinterpret_cast<unsigned char*>(ctrl)), st);
+  if (e != cudaSuccess) return gbta_set_error(GBTA_ERR_CUDA, cudaGetErrorString(e));
+  const int ncol = nt * g.B;
+  gbta::k_gen_factor_tasks<<<(ncol + 127) / 128, 128, 0, st>>>(g, tasks);
+  gbta::LaunchCtl lc;
+  lc.ctrl = ctrl;
+  lc.flags = flags;
+  lc.epoch = 1;
+  lc.wait_ns = 20ull * 1000 * 1000 * 1000;
+  lc.grid = (int)(ntasks < nsm ? ntasks : nsm);
+  lc.stream = st;
+  gbta::launch_factor(g, D, L, R, T, a > 0 ? 1 : 0, tasks, (int)ntasks, tip_part, lc);
+  gbta::count_launches(1);
+  if ((e = cudaGetLastError()) != cudaSuccess) return gbta_set_error(GBTA_ERR_CUDA, cudaGetErrorString(e));
+  int h_ctrl[8] = {0};
+  if ((e = cudaMemcpyAsync(h_ctrl, ctrl, sizeof(h_ctrl), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(st)) != cudaSuccess)
+    return gbta_set_error(GBTA_ERR_CUDA, cudaGetErrorString(e));
+  if (h_ctrl[3] != 0) return gbta_set_error(GBTA_ERR_TIMEOUT, "noalloc pobtaf: a kernel wait exceeded its limit");
+  if (h_ctrl[2] > 0)
+    return gbta_set_error(h_ctrl[2], ("matrix is not positive definite (non-positive pivot at global row " +
+                                      std::to_string(h_ctrl[2]) + ")").c_str());
+  return GBTA_OK;
+}
