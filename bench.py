@@ -40,7 +40,7 @@ UNIT = "TFLOP/s"
 # ----------------------------------------------------------------------------- shapes
 def workload(small: bool):
     if small:   # a reduced case for profiler captures only
-        return dict(name="spde16x16_ar1_nt16_nb6_obs20k", n_side=16, nt=16, nb=6, n_obs=20000, seed=11)
+        return dict(name="spde32x32_ar1_nt16_nb6_obs25k", n_side=32, nt=16, nb=6, n_obs=25000, seed=11)
     return dict(name="spde32x32_ar1_nt128_nb6_obs200k", n_side=32, nt=128, nb=6, n_obs=200000, seed=11)
 
 

@@ -49,6 +49,18 @@ extern "C" {
 #define GBTA_ERR_TIMEOUT (-3)
 #define GBTA_ERR_ALLOC (-5)
 
+/* How the factorization computes its tile products (gbta_set_method).
+ * GBTA_METHOD_FP64: FP64 FMAs on the CUDA cores.
+ * GBTA_METHOD_OZAKI (default): error-free splitting of each FP64 tile into nine 6-bit
+ * integer digit planes (per-row exponents from the matrix diagonal) multiplied on the
+ * tensor cores with exact fp32 accumulation and folded into FP64; the product error is
+ * bounded like an FP64 product's (a few units of 2^-53 of the operands' magnitudes).
+ * The selected inversion uses the same scheme for its products (factor tiles sliced
+ * once per inversion with per-column exponents, Sigma tiles sliced on the fly).  Tile
+ * Cholesky factors, tile inverses / triangular solves and the sweeps stay FP64. */
+#define GBTA_METHOD_FP64 0
+#define GBTA_METHOD_OZAKI 1
+
 typedef struct gbta_solver gbta_solver;
 
 /* Version of this ABI (major*10000 + minor*100 + patch). */
@@ -85,6 +97,17 @@ int gbta_set_stream(gbta_solver* s, void* stream);
 /* Limit, in milliseconds, on any inter-CTA wait inside a kernel; after it the
  * kernel records GBTA_ERR_TIMEOUT and returns instead of waiting further. */
 int gbta_set_wait_limit_ms(gbta_solver* s, double ms);
+
+/* Select / query the product method of the factorization (see GBTA_METHOD_*). */
+int gbta_set_method(gbta_solver* s, int method);
+int gbta_get_method(const gbta_solver* s);
+
+/* Task tracing (off by default).  When enabled, every dataflow kernel launched by
+ * the solver records one entry per task: [ticket, (task type << 16) | SM id,
+ * start ns, end ns] (GPU global timer).  gbta_get_trace copies the records of the
+ * last traced launch to host memory and returns how many were copied. */
+int gbta_set_trace(gbta_solver* s, int enable);
+long long gbta_get_trace(gbta_solver* s, long long* out, long long max_records);
 
 /* Bytes of device workspace held by the solver (SerinvSolver.get_solver_memory,
  * structured_solver.py:540-550, minus the caller-owned block buffers). */

@@ -19,6 +19,8 @@ GBTA_ERR_ARG = -1
 GBTA_ERR_CUDA = -2
 GBTA_ERR_TIMEOUT = -3
 GBTA_ERR_ALLOC = -5
+GBTA_METHOD_FP64 = 0
+GBTA_METHOD_OZAKI = 1
 
 _lib = None
 _lock = threading.Lock()
@@ -41,6 +43,10 @@ SIGNATURES = {
     "gbta_destroy": (_c_int, [_vp]),
     "gbta_set_stream": (_c_int, [_vp, _vp]),
     "gbta_set_wait_limit_ms": (_c_int, [_vp, ctypes.c_double]),
+    "gbta_set_method": (_c_int, [_vp, _c_int]),
+    "gbta_get_method": (_c_int, [_vp]),
+    "gbta_set_trace": (_c_int, [_vp, _c_int]),
+    "gbta_get_trace": (_c_ll, [_vp, _vp, _c_ll]),
     "gbta_workspace_bytes": (ctypes.c_size_t, [_vp]),
     "gbta_status": (_c_int, [_vp]),
     "gbta_pobtaf": (_c_int, [_vp, _vp, _vp, _vp, _vp]),

@@ -61,6 +61,13 @@ struct gbta_solver {
   size_t sig_elems = 0;
   int* h_ctrl = nullptr;    // pinned
   size_t ws_bytes = 0;
+  int method = GBTA_METHOD_OZAKI;  // how tile products are computed in the factorization
+  void* d_digits = nullptr;         // Ozaki digit planes (lazy)
+  int* d_erow = nullptr;            // Ozaki row exponents (lazy)
+  size_t digit_bytes = 0;
+  long long* d_trace = nullptr;   // task trace of the last launch (when enabled)
+  long long trace_cap = 0;        // records
+  long long trace_n = 0;          // records of the last traced launch
 };
 
 namespace {
@@ -80,6 +87,10 @@ gbta::LaunchCtl next_launch(gbta_solver* s, int ntasks) {
   lc.wait_ns = s->wait_ns;
   lc.grid = grid_of(s, ntasks);
   lc.stream = s->stream;
+  if (s->d_trace && ntasks <= s->trace_cap) {
+    lc.trace = s->d_trace;
+    s->trace_n = ntasks;
+  }
   return lc;
 }
 
@@ -214,6 +225,9 @@ int gbta_destroy(gbta_solver* s) {
   cudaFree(s->d_arrow_part);
   cudaFree(s->d_ld);
   cudaFree(s->d_sig);
+  cudaFree(s->d_trace);
+  cudaFree(s->d_digits);
+  cudaFree(s->d_erow);
   if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
   delete s;
@@ -226,6 +240,37 @@ int gbta_set_stream(gbta_solver* s, void* stream) {
   return GBTA_OK;
 }
 
+int gbta_set_method(gbta_solver* s, int method) {
+  if (int r = check_solver(s)) return r;
+  if (method != GBTA_METHOD_FP64 && method != GBTA_METHOD_OZAKI) return fail(GBTA_ERR_ARG, "unknown method");
+  s->method = method;
+  return GBTA_OK;
+}
+
+int gbta_get_method(const gbta_solver* s) { return s ? s->method : -1; }
+
+int gbta_set_trace(gbta_solver* s, int enable) {
+  if (int r = check_solver(s)) return r;
+  GBTA_CUDA(cudaStreamSynchronize(s->stream));
+  cudaFree(s->d_trace);
+  s->d_trace = nullptr;
+  s->trace_cap = s->trace_n = 0;
+  if (enable) {
+    const long long cap = s->n_ftasks > s->n_stasks ? s->n_ftasks : s->n_stasks;
+    GBTA_CUDA(cudaMalloc(&s->d_trace, (size_t)cap * 4 * sizeof(long long)));
+    s->trace_cap = cap;
+  }
+  return GBTA_OK;
+}
+
+long long gbta_get_trace(gbta_solver* s, long long* out, long long max_records) {
+  if (!s || !s->d_trace || !out) return 0;
+  const long long n = s->trace_n < max_records ? s->trace_n : max_records;
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) return 0;
+  if (cudaMemcpy(out, s->d_trace, (size_t)n * 4 * sizeof(long long), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+  return n;
+}
+
 int gbta_set_wait_limit_ms(gbta_solver* s, double ms) {
   if (int r = check_solver(s)) return r;
   if (!(ms > 0)) return fail(GBTA_ERR_ARG, "wait limit must be positive");
@@ -234,7 +279,7 @@ int gbta_set_wait_limit_ms(gbta_solver* s, double ms) {
 }
 
 size_t gbta_workspace_bytes(const gbta_solver* s) {
-  return s ? s->ws_bytes + s->sig_elems * sizeof(double) : 0;
+  return s ? s->ws_bytes + s->sig_elems * sizeof(double) + s->digit_bytes : 0;
 }
 
 int gbta_status(gbta_solver* s) {
@@ -253,14 +298,34 @@ int gbta_status(gbta_solver* s) {
   return GBTA_OK;
 }
 
+// ---------------------------------------------------------------- Ozaki workspace
+// Digit planes (one 9 x 32 x 32 fp16 block per tile slot) and per-row / per-column
+// exponents, shared by the factorization and the selected inversion.
+static int ensure_digits(gbta_solver* s) {
+  if (s->d_digits) return GBTA_OK;
+  GBTA_CUDA(cudaStreamSynchronize(s->stream));
+  const size_t bytes = gbta::factor_oz_digit_bytes(s->g);
+  const size_t ebytes = ((size_t)s->g.nt * s->g.b + s->g.a) * sizeof(int);
+  GBTA_CUDA(cudaMalloc(&s->d_digits, bytes));
+  GBTA_CUDA(cudaMalloc(&s->d_erow, ebytes));
+  s->digit_bytes = bytes + ebytes;
+  return GBTA_OK;
+}
+
 // ---------------------------------------------------------------- factorization
 static int factor_async(gbta_solver* s, double* D, double* L, double* R, double* T, int use_arrow) {
   if (int r = check_solver(s)) return r;
   if (!D || (s->g.nt > 1 && !L)) return fail(GBTA_ERR_ARG, "D/L must be device pointers");
   if (use_arrow && (!R || !T)) return fail(GBTA_ERR_ARG, "R/T must be device pointers for the bta factorization");
+  if (s->method == GBTA_METHOD_OZAKI)
+    if (int r = ensure_digits(s)) return r;
   if (int r = reset_ticket(s)) return r;
   const gbta::LaunchCtl lc = next_launch(s, s->n_ftasks);
-  gbta::launch_factor(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part, lc);
+  if (s->method == GBTA_METHOD_OZAKI)
+    gbta::launch_factor_oz(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part,
+                           (__half*)s->d_digits, s->d_erow, lc);
+  else
+    gbta::launch_factor(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part, lc);
   GBTA_CUDA(cudaGetLastError());
   return GBTA_OK;
 }
@@ -347,9 +412,15 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
   double* SL = SD + g.nt * bb;
   double* SR = SL + (g.nt - 1) * bb;
   double* ST = SR + (size_t)g.nt * g.a * g.b;
+  if (s->method == GBTA_METHOD_OZAKI)
+    if (int r = ensure_digits(s)) return r;
   if (int r = reset_ticket(s)) return r;
   const gbta::LaunchCtl lc = next_launch(s, s->n_stasks);
-  gbta::launch_selinv(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks, lc);
+  if (s->method == GBTA_METHOD_OZAKI)
+    gbta::launch_selinv_oz(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks,
+                           (__half*)s->d_digits, s->d_erow, lc);
+  else
+    gbta::launch_selinv(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks, lc);
   GBTA_CUDA(cudaGetLastError());
   gbta::launch_selinv_writeback(g, SD, SL, SR, ST, D, L, R, T, use_arrow, s->stream);
   GBTA_CUDA(cudaGetLastError());

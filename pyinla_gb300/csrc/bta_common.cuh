@@ -35,6 +35,7 @@ struct Ctl {
   int* flags;
   int epoch;
   unsigned long long wait_ns;
+  long long* trace;   // optional: 4 int64 per task (see trace_task), or null
 };
 
 __device__ __forceinline__ int ld_acquire(const int* p) {
@@ -52,6 +53,23 @@ __device__ __forceinline__ unsigned long long gtimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
+}
+
+__device__ __forceinline__ unsigned smid() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
+  return r;
+}
+// Task trace record (thread 0): [ticket, (type << 16) | sm, t_start, t_end] in
+// globaltimer nanoseconds; written only when tracing is enabled.
+__device__ __forceinline__ void trace_task(const Ctl& c, int ticket, int type, unsigned long long t0) {
+  if (c.trace && threadIdx.x == 0) {
+    long long* r = c.trace + 4ll * ticket;
+    r[0] = ticket;
+    r[1] = ((long long)type << 16) | smid();
+    r[2] = (long long)t0;
+    r[3] = (long long)gtimer();
+  }
 }
 
 __device__ __forceinline__ void raise_abort(const Ctl& c) { atomicExch(c.ctrl + CTRL_ABORT, 1); }

@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor(FactorArgs p) {
 
   while (true) {
     const int t = cta_ticket(c, &s_t);
+    const unsigned long long t_task0 = c.trace ? gtimer() : 0ull;
     if (t < 0 || t >= p.ntasks) break;
     const int4 tk = p.tasks[t];
     const int type = tk.x, i = tk.y, r = tk.z, col = tk.w;
@@ -106,6 +107,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor(FactorArgs p) {
       }
       tile_store(p.T, g.a, g.a, g.a, X);
       cta_publish(c, c.flags + g.fT());
+      trace_task(c, t, type, t_task0);
       continue;
     }
 
@@ -184,6 +186,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor(FactorArgs p) {
       }
       tile_store(const_cast<double*>(tgt.p), g.b, tgt.rows, tgt.cols, X);
       cta_publish(c, tgt_flag);
+      trace_task(c, t, type, t_task0);
       continue;
     }
 
@@ -212,6 +215,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor(FactorArgs p) {
         for (int q = 0; q < 4; ++q) P[acc_row(ii) * TS + acc_col(q)] = pacc.v[ii][q];
     }
     cta_publish(c, tgt_flag);
+    trace_task(c, t, type, t_task0);
   }
 }
 
@@ -231,6 +235,7 @@ void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, in
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;
   p.c.wait_ns = lc.wait_ns;
+  p.c.trace = lc.trace;
   k_factor<<<lc.grid, NT, 0, lc.stream>>>(p);
   count_launches(1);
 }

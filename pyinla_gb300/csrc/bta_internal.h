@@ -1,6 +1,7 @@
 // Internal launch interface between the C ABI (bta_api.cu) and the kernels.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -34,6 +35,7 @@ struct LaunchCtl {
   unsigned long long wait_ns;
   int grid;
   cudaStream_t stream;
+  long long* trace = nullptr;   // per-task trace records, or null
 };
 
 // Host-side count of kernel launches issued by this library (see gbta_kernel_launches).
@@ -43,6 +45,17 @@ void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, in
                    const int4* tasks, int ntasks, double* tip_part, const LaunchCtl& lc);
 
 constexpr int SOLVE_NC = 4;   // right-hand-side columns per solve launch
+
+// Tensor-core (Ozaki) factorization: digit-plane workspace bytes, and the launcher.
+size_t factor_oz_digit_bytes(const Geom& g);
+void launch_factor_oz(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow,
+                      const int4* tasks, int ntasks, double* tip_part, __half* digits, int* erow,
+                      const LaunchCtl& lc);
+
+size_t selinv_oz_digit_bytes(const Geom& g);
+void launch_selinv_oz(const Geom& g, const double* D, const double* L, const double* R, const double* T,
+                      double* SD, double* SL, double* SR, double* ST, int use_arrow, const int4* tasks,
+                      int ntasks, __half* fdig, int* ecol, const LaunchCtl& lc);
 
 void launch_solve(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                   double* Bv, int ldb, int nc, int trans, int use_arrow, double* arrow_part,

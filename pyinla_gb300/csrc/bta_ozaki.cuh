@@ -1,0 +1,192 @@
+// FP64 tile products on the tensor cores (Ozaki scheme with exact integer slices).
+//
+// GB300 executes FP64 FMAs at 1.2 TFLOP/s but fp16 mma.sync (f32 accumulate) at ~600
+// TFLOP/s.  A product acc -= X Y^T of FP64 tiles is therefore computed as follows
+// (Ozaki, Ogita, Oishi, Rump, "Error-free transformations of matrix multiplication
+// by using fast routines of matrix multiplication and its applications", Numer.
+// Algorithms 59 (2012); integer-slice variant as in Ootomo, Ozaki, Yokota, "DGEMM on
+// integer matrix multiplication unit", IJHPCA 2024):
+//
+//  * every element x of row g is written in fixed point relative to a per-row
+//    exponent E_g with |x| < 2^E_g:  x ~ sign(x) * sum_{s=1..9} d_s 2^(E_g - 6 s),
+//    d_s in [0, 63] (54 bits, rounded to nearest: error <= 2^(E_g - 55)).  The signed digits are
+//    exact in fp16 and are stored once per tile, as 9 "digit planes";
+//  * sum_k x_ik y_jk = sum_{s,t} 2^(E_i + E_j - 6(s+t)) sum_k d_s,ik g_t,jk.  Each
+//    inner sum is an integer matrix product computed by mma.sync; the 53 pairs with
+//    s + t <= 11 are kept (the dropped ones weigh below 2^(E_i+E_j-60) per term in
+//    total, under FP64 rounding of the result) and pairs of equal s + t share one
+//    fp32 accumulator;
+//  * every partial sum is an integer below 9 * 63^2 * 32 * OZ_CHUNK < 2^24, so the
+//    fp32 accumulation is exact; every OZ_CHUNK tile steps the nine diagonals are
+//    combined exactly in 64-bit integers and folded into the FP64 accumulator.
+//
+// For the Cholesky factor the per-row exponents come from the matrix itself: a row of
+// L satisfies sum_j L_gj^2 = Q_gg, so E_g = ilogb(sqrt(Q_gg)) + 2 bounds every element
+// of row g in every tile, and the same digits serve as left and right operand.
+#pragma once
+
+#include <cuda_fp16.h>
+
+#include "bta_common.cuh"
+
+namespace gbta {
+
+constexpr int OZ_S = 9;                       // digit planes per tile
+constexpr int OZ_W = 6;                       // bits per digit
+constexpr int OZ_ND = 10;                     // diagonals s + t = 2 .. 11
+constexpr int OZ_CHUNK = 12;                  // tile steps per exact fp32 accumulation
+constexpr int OZ_LD = 40;                     // shared row stride of a plane (halves): conflict-free ldmatrix
+constexpr int OZ_PLANE = TS * OZ_LD;          // halves per plane in shared memory
+constexpr int OZ_OPER = OZ_S * OZ_PLANE;      // halves per operand tile in shared memory
+constexpr int OZ_TILE = OZ_S * TS * TS;       // halves per tile in the global digit buffer
+constexpr int OZ_CHUNKS16 = OZ_S * TS * 4;    // 16-byte pieces per tile (9 * 32 rows * 64 B)
+
+static_assert(9 * 63 * 63 * TS * OZ_CHUNK < (1 << 24), "fp32 accumulation must stay exact");
+
+// Row exponent: E = ilogb(sqrt(q)) + 2 (q > 0), so |x| <= sqrt(q) < 2^(E-1).
+__device__ __forceinline__ int oz_row_exponent(double q) {
+  if (!(q > 0.0) || !isfinite(q)) return 0;
+  return ilogb(sqrt(q)) + 2;
+}
+
+// The nine signed digits of x relative to 2^E (sign applied to every digit).
+__device__ __forceinline__ void oz_digits(double x, int E, int (&d)[OZ_S]) {
+  const long long bits = __double_as_longlong(x);
+  const int ex = (int)((bits >> 52) & 0x7ff);
+  unsigned long long F = 0;
+  if (ex != 0x7ff && (bits & 0x7fffffffffffffffll) != 0) {
+    const unsigned long long m = (bits & 0xfffffffffffffull) | (ex ? (1ull << 52) : 0ull);
+    const int sh = (ex ? ex : 1) - 1075 + 54 - E;   // F = round(|x| 2^(54 - E)) = round(m 2^sh)
+    if (sh >= 0)
+      F = (sh <= 1) ? (m << sh) : ~0ull;
+    else if (sh > -54)
+      F = (m + (1ull << (-sh - 1))) >> (-sh);         // round half up on the magnitude
+    if (F >= (1ull << 54)) F = (1ull << 54) - 1;     // only reachable for out-of-bound input
+  }
+  const int sgn = bits < 0 ? -1 : 1;
+#pragma unroll
+  for (int s = 0; s < OZ_S; ++s) d[s] = sgn * (int)((F >> (54 - OZ_W * (s + 1))) & 63);
+}
+
+// Write the digit planes of the valid part of a shared FP64 tile X (rows x cols)
+// to dst ([plane][row][col] halves), rows scaled by E[row] (global exponents).
+__device__ __forceinline__ void oz_store_digits(__half* dst, const double* X, int rows, int cols, const int* E) {
+#pragma unroll
+  for (int k = 0; k < PER_THREAD; ++k) {
+    const int idx = threadIdx.x + k * NT;
+    const int r = idx / TS, c = idx % TS;
+    int d[OZ_S];
+    if (r < rows && c < cols) {
+      oz_digits(X[r * LDS + c], E[r], d);
+    } else {
+#pragma unroll
+      for (int s = 0; s < OZ_S; ++s) d[s] = 0;
+    }
+#pragma unroll
+    for (int s = 0; s < OZ_S; ++s) dst[s * TS * TS + idx] = __int2half_rn(d[s]);
+  }
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(sdst)), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Stage one tile's digit planes (global, compact rows) into shared memory (padded rows).
+__device__ __forceinline__ void oz_load_async(__half* sdst, const __half* gsrc) {
+  for (int q = threadIdx.x; q < OZ_CHUNKS16; q += NT) {
+    const int s = q / (TS * 4), row = (q / 4) % TS, part = q % 4;
+    cp_async16(sdst + s * OZ_PLANE + row * OZ_LD + part * 8, gsrc + s * TS * TS + row * TS + part * 8);
+  }
+}
+
+__device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const __half* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ void mma16816(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Per-thread state of an Ozaki K-loop: warp w owns the 16 x 16 output block at rows
+// (w/2)*16, cols (w%2)*16; each thread holds 2 n8-tiles x 4 elements (mma C layout).
+struct OzAcc {
+  float p[OZ_ND][2][4];   // exact integer partial sums per diagonal
+  double v[2][4];         // FP64 accumulator (same layout)
+};
+
+__device__ __forceinline__ int oz_row(int nt_, int j) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  return (w >> 1) * 16 + (lane >> 2) + (j >> 1) * 8;
+}
+__device__ __forceinline__ int oz_col(int nt_, int j) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  return (w & 1) * 16 + nt_ * 8 + 2 * (lane & 3) + (j & 1);
+}
+
+__device__ __forceinline__ void oz_clear_partials(OzAcc& a) {
+#pragma unroll
+  for (int d = 0; d < OZ_ND; ++d)
+#pragma unroll
+    for (int n = 0; n < 2; ++n)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) a.p[d][n][j] = 0.f;
+}
+
+// One tile step: p[s+t] += d_s(A) * d_t(B)^T for the 53 pairs s + t <= 11.
+__device__ __forceinline__ void oz_step(OzAcc& acc, const __half* As, const __half* Bs) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int m0 = (w >> 1) * 16, n0 = (w & 1) * 16;
+  const int ar = m0 + (lane & 7) + ((lane >> 3) & 1) * 8, ac = (lane >> 4) * 8;
+  const int br = n0 + (lane & 7) + (lane >> 4) * 8, bc = ((lane >> 3) & 1) * 8;
+#pragma unroll
+  for (int kk = 0; kk < TS; kk += 16) {
+    unsigned a[OZ_S][4], b[OZ_S][4];
+#pragma unroll
+    for (int s = 0; s < OZ_S; ++s) ldsm_x4(a[s], As + s * OZ_PLANE + ar * OZ_LD + kk + ac);
+#pragma unroll
+    for (int s = 0; s < OZ_S; ++s) ldsm_x4(b[s], Bs + s * OZ_PLANE + br * OZ_LD + kk + bc);
+#pragma unroll
+    for (int s = 0; s < OZ_S; ++s)
+#pragma unroll
+      for (int t = 0; t + s < OZ_ND && t < OZ_S; ++t) {
+        mma16816(acc.p[s + t][0], a[s], b[t][0], b[t][1]);
+        mma16816(acc.p[s + t][1], a[s], b[t][2], b[t][3]);
+      }
+  }
+}
+
+// Fold the exact partial sums into the FP64 accumulator: v -= sum_D p_D 2^(Ei+Ej-6D)
+// (D = 2..11).
+// `esum[n][j]` = E_i + E_j of the thread's elements.  Clears the partials.
+__device__ __forceinline__ void oz_fold_sub(OzAcc& acc, const int (&esum)[2][4]) {
+#pragma unroll
+  for (int n = 0; n < 2; ++n)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      int I[OZ_ND];
+#pragma unroll
+      for (int d = 0; d < OZ_ND; ++d) {
+        I[d] = __float2int_rn(acc.p[d][n][j]);
+        acc.p[d][n][j] = 0.f;
+      }
+      // diagonals 2..5, 6..9 and 10..11 in three exact 64-bit integers
+      const long long hi = (((long long)I[0] * 64 + I[1]) * 64 + I[2]) * 64 + I[3];
+      const long long mid = (((long long)I[4] * 64 + I[5]) * 64 + I[6]) * 64 + I[7];
+      const long long lo = (long long)I[8] * 64 + I[9];
+      const double vv = fma((double)mid, 0x1p-24, fma((double)lo, 0x1p-36, (double)hi));
+      const double sc = __longlong_as_double((long long)(1023 + esum[n][j] - 30) << 52);
+      acc.v[n][j] = fma(-vv, sc, acc.v[n][j]);
+    }
+}
+
+}  // namespace gbta

@@ -170,6 +170,7 @@ __global__ void __launch_bounds__(NT, 1) k_selinv(SelinvArgs p) {
 
   while (true) {
     const int t = cta_ticket(c, &s_t);
+    const unsigned long long t_task0 = c.trace ? gtimer() : 0ull;
     if (t < 0 || t >= p.ntasks) break;
     const int4 tk = p.tasks[t];
     const int type = tk.x, i = tk.y, j = tk.z, col = tk.w;
@@ -187,6 +188,7 @@ __global__ void __launch_bounds__(NT, 1) k_selinv(SelinvArgs p) {
       diag_finish(X, W, F, rd);
       tile_store(p.ST, g.a, g.a, g.a, X);
       cta_publish(c, c.flags + g.fT());
+      trace_task(c, t, type, t_task0);
       continue;
     }
 
@@ -219,6 +221,7 @@ __global__ void __launch_bounds__(NT, 1) k_selinv(SelinvArgs p) {
       const SigTile d = sig_dest(p, i, j, col);
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
       cta_publish(c, const_cast<int*>(d.flag));
+      trace_task(c, t, type, t_task0);
     } else {   // ST_DIAG
       // Z = sum_l Sigma(l,col)^T F(l,col)
       auto step_of = [&](int s) -> Step {
@@ -246,6 +249,7 @@ __global__ void __launch_bounds__(NT, 1) k_selinv(SelinvArgs p) {
       const SigTile d = sig_dest(p, i, col, col);
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
       cta_publish(c, const_cast<int*>(d.flag));
+      trace_task(c, t, type, t_task0);
     }
   }
 }
@@ -293,6 +297,7 @@ void launch_selinv(const Geom& g, const double* D, const double* L, const double
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;
   p.c.wait_ns = lc.wait_ns;
+  p.c.trace = lc.trace;
   k_selinv<<<lc.grid, NT, 0, lc.stream>>>(p);
   count_launches(1);
 }

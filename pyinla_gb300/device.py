@@ -55,6 +55,14 @@ class BtaHandle:
     def set_stream(self, stream_ptr: int | None) -> None:
         _lib.check(self.lib.gbta_set_stream(self.ptr, stream_ptr))
 
+    def set_method(self, method: int) -> None:
+        """GBTA_METHOD_FP64 (0) or GBTA_METHOD_OZAKI (1, default): how the
+        factorization computes its tile products."""
+        _lib.check(self.lib.gbta_set_method(self.ptr, int(method)))
+
+    def method(self) -> int:
+        return int(self.lib.gbta_get_method(self.ptr))
+
     def set_wait_limit_ms(self, ms: float) -> None:
         _lib.check(self.lib.gbta_set_wait_limit_ms(self.ptr, float(ms)))
 

@@ -35,6 +35,26 @@ def torch():
     return _t
 
 
+METHODS = [0, 1]   # GBTA_METHOD_FP64, GBTA_METHOD_OZAKI
+
+
+@pytest.fixture
+def use_method(torch):
+    """Set the product method of the cached solver handles for one test."""
+    from pyinla_gb300.device import BtaHandle
+
+    touched = []
+
+    def _set(b, nt, a, method):
+        h = BtaHandle.get(b, nt, a)
+        touched.append((h, h.method()))
+        h.set_method(method)
+
+    yield _set
+    for h, m in touched:
+        h.set_method(m)
+
+
 def dev(torch, *arrs):
     return [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in arrs]
 
@@ -53,11 +73,13 @@ def _golden(name):
     return g, D, L, R, T, rhs
 
 
+@pytest.mark.parametrize("method", METHODS)
 @pytest.mark.parametrize("name", GOLDEN_CASES)
-def test_bta_against_reference_golden(torch, name):
+def test_bta_against_reference_golden(torch, use_method, name, method):
     from pyinla_gb300 import algs
 
     g, D, L, R, T, rhs = _golden(name)
+    use_method(int(g["b"]), int(g["nt"]), int(g["a"]), method)
     Dd, Ld, Rd, Td = dev(torch, D, L, R, T)
     algs.pobtaf(Dd, Ld, Rd, Td)
     ld = algs.logdet(Dd, Td, "bta")
@@ -88,11 +110,13 @@ def test_bta_against_reference_golden(torch, name):
     assert np.array_equal(ST, ST.T)
 
 
+@pytest.mark.parametrize("method", METHODS)
 @pytest.mark.parametrize("name", GOLDEN_CASES)
-def test_bt_against_reference_golden(torch, name):
+def test_bt_against_reference_golden(torch, use_method, name, method):
     from pyinla_gb300 import algs
 
     g, D, L, R, T, rhs = _golden(name)
+    use_method(int(g["b"]), int(g["nt"]), 0, method)
     nt, b = D.shape[0], D.shape[1]
     Dd, Ld = dev(torch, D, L)
     algs.pobtf(Dd, Ld)
@@ -123,11 +147,13 @@ SHAPES = [
 ]
 
 
+@pytest.mark.parametrize("method", METHODS)
 @pytest.mark.parametrize("seed,nt,b,a", SHAPES)
-def test_against_oracle_shapes(torch, seed, nt, b, a):
+def test_against_oracle_shapes(torch, use_method, seed, nt, b, a, method):
     from pyinla_gb300 import algs
 
     D, L, R, T, rhs = orc.make_bta_c1(seed, nt=nt, b=b, a=a, nrhs=5)
+    use_method(b, nt, a, method)
     ref = [x.copy() for x in (D, L, R, T)]
     orc.pobtaf(*ref)
     Dd, Ld, Rd, Td = dev(torch, D, L, R, T)
@@ -170,9 +196,11 @@ def test_numpy_inputs_in_place(torch):
     assert relerr(x, xr) < RTOL
 
 
-def test_not_positive_definite_raises_with_row(torch):
+@pytest.mark.parametrize("method", METHODS)
+def test_not_positive_definite_raises_with_row(torch, use_method, method):
     from pyinla_gb300 import algs
 
+    use_method(40, 4, 3, method)
     D, L, R, T, rhs = orc.make_bta_c1(5, nt=4, b=40, a=3)
     D[2][7, 7] = -50.0   # global row 2*40 + 7 (0-based) fails first
     Dd, Ld, Rd, Td = dev(torch, D, L, R, T)
