@@ -115,6 +115,46 @@ static __device__ bool cta_wait(const Ctl& c, const int* f0, const int* f1, int*
   return ok;
 }
 
+// Readiness scan for pipelined product loops.  Thread 0 advances *s_ready (the
+// number of leading steps whose operand flags are all set) by checking up to
+// SCAN_AHEAD further steps with independent relaxed loads and a single acquire fence,
+// so one memory round trip covers many steps.  `flags_of(s, f0, f1)` returns the
+// step's flags (nullptr = none).  The caller synchronises the CTA afterwards.
+constexpr int SCAN_AHEAD = 8;
+
+__device__ __forceinline__ int ld_relaxed_gpu(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void fence_acquire_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+template <class FlagsOf>
+__device__ __forceinline__ void scan_ready(const Ctl& c, int nsteps, FlagsOf flags_of, int* s_ready) {
+  if (threadIdx.x == 0) {
+    const int r0 = *s_ready;
+    int v[SCAN_AHEAD];
+#pragma unroll
+    for (int k = 0; k < SCAN_AHEAD; ++k) {
+      v[k] = 1;
+      if (r0 + k < nsteps) {
+        const int* f0;
+        const int* f1;
+        flags_of(r0 + k, f0, f1);
+        const int a = f0 ? ld_relaxed_gpu(f0) : c.epoch;
+        const int b = f1 ? ld_relaxed_gpu(f1) : c.epoch;
+        v[k] = (a >= c.epoch) && (b >= c.epoch);
+      }
+    }
+    fence_acquire_gpu();
+    int r = r0;
+#pragma unroll
+    for (int k = 0; k < SCAN_AHEAD; ++k)
+      if (r == r0 + k && r < nsteps && v[k]) ++r;
+    *s_ready = r;
+  }
+}
+
 // CTA-wide non-blocking poll of up to two flags.  Contains __syncthreads().
 static __device__ bool cta_poll(const Ctl& c, const int* f0, const int* f1, int* s_ok) {
   if (threadIdx.x == 0) {
@@ -365,6 +405,26 @@ __device__ __forceinline__ double nr_rsqrt(double x) {
   return fma(y, r, y);
 }
 
+// sqrt(x) and 1/sqrt(x) together by Goldschmidt's iteration (R. E. Goldschmidt,
+// "Applications of division by convergence", MIT thesis, 1964): from y0 ~ 1/sqrt(x)
+// (rsqrt.approx, ~20 correct bits), g = x y0, h = y0/2 and r = 1/2 - g h,
+// g <- g + g r, h <- h + h r doubles the correct bits per step; g and h update in
+// parallel, so two steps are a chain of five FP64 operations instead of the eleven
+// of three dependent Newton steps.
+__device__ __forceinline__ void gs_sqrt_rsqrt(double x, double& sq, double& rs) {
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  double g = x * y, h = 0.5 * y;
+  double r = fma(-g, h, 0.5);
+  g = fma(g, r, g);
+  h = fma(h, r, h);
+  r = fma(-g, h, 0.5);
+  g = fma(g, r, g);
+  h = fma(h, r, h);
+  sq = g;
+  rs = 2.0 * h;
+}
+
 // rd[j] = 1 / F[j][j] for the TS diagonal entries (one lane each).  Caller syncs.
 __device__ __forceinline__ void tile_diag_recip(const double* F, double* rd) {
   if (threadIdx.x < TS) rd[threadIdx.x] = nr_recip(F[threadIdx.x * LDS + threadIdx.x]);
@@ -384,7 +444,8 @@ static __device__ int smem_potrf(double* S, double* ybuf) {
       __syncthreads();
       return j + 1;
     }
-    const double y = nr_rsqrt(d);
+    double sq, y;
+    gs_sqrt_rsqrt(d, sq, y);
     const double inv = y * y;
     if (threadIdx.x == 0) ybuf[j] = y;
     const int m = TS - 1 - j;

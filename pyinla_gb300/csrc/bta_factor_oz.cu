@@ -55,7 +55,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor_oz(FactorOzArgs p) {
   double* vec = F + TILE_SMEM;
   int* erow_t = reinterpret_cast<int*>(vec + TS);   // exponents of the target's rows
   int* ecol_t = erow_t + TS;                        // exponents of the target's columns
-  __shared__ int s_ok, s_t;
+  __shared__ int s_ok, s_t, s_ready;
   const Geom& g = p.g;
   const Ctl& c = p.c;
 
@@ -158,10 +158,17 @@ __global__ void __launch_bounds__(NT, 1) k_factor_oz(FactorOzArgs p) {
     };
     bool ok = true;
     if (nsteps > 0) {
+      auto flags_of = [&](int s, const int*& f0, const int*& f1) {
+        int sa, sb;
+        slots(s, sa, sb);
+        f0 = c.flags + sa;
+        f1 = (sa == sb) ? nullptr : c.flags + sb;
+      };
       int sa, sb;
       slots(0, sa, sb);
       ok = cta_wait(c, c.flags + sa, sa == sb ? nullptr : c.flags + sb, &s_ok);
       if (ok) {
+        if (threadIdx.x == 0) s_ready = 1;
         oz_load_async(stages, p.digits + (size_t)sa * OZ_TILE);
         oz_load_async(stages + OZ_OPER, p.digits + (size_t)sb * OZ_TILE);
         cp_async_commit();
@@ -175,8 +182,12 @@ __global__ void __launch_bounds__(NT, 1) k_factor_oz(FactorOzArgs p) {
         bool issued = false;
         int na = 0, nb = 0;
         if (more) {
-          slots(s + 1, na, nb);
-          if (cta_poll(c, c.flags + na, na == nb ? nullptr : c.flags + nb, &s_ok)) {
+          if (s_ready <= s + 1) {   // uniform: read after the barrier
+            scan_ready(c, nsteps, flags_of, &s_ready);
+            __syncthreads();
+          }
+          if (s_ready > s + 1) {
+            slots(s + 1, na, nb);
             oz_load_async(nxt, p.digits + (size_t)na * OZ_TILE);
             oz_load_async(nxt + OZ_OPER, p.digits + (size_t)nb * OZ_TILE);
             cp_async_commit();
@@ -186,8 +197,9 @@ __global__ void __launch_bounds__(NT, 1) k_factor_oz(FactorOzArgs p) {
         oz_step(acc, cur, cur + OZ_OPER);
         if ((s + 1) % OZ_CHUNK == 0 || !more) oz_fold_sub(acc, esum);
         if (more && !issued) {
+          slots(s + 1, na, nb);
           if (!(ok = cta_wait(c, c.flags + na, na == nb ? nullptr : c.flags + nb, &s_ok))) break;
-          __syncthreads();
+          if (threadIdx.x == 0) s_ready = s + 2;
           oz_load_async(nxt, p.digits + (size_t)na * OZ_TILE);
           oz_load_async(nxt + OZ_OPER, p.digits + (size_t)nb * OZ_TILE);
           cp_async_commit();

@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(NT, 1) k_selinv_oz(SelinvOzArgs p) {
   double* rd = W + TILE_SMEM;
   int* ecol_t = reinterpret_cast<int*>(rd + TS);
   double* red4 = reinterpret_cast<double*>(ecol_t + TS);
-  __shared__ int s_ok, s_t;
+  __shared__ int s_ok, s_t, s_ready;
   const Geom& g = p.g;
   const Ctl& c = p.c;
 
@@ -315,10 +315,15 @@ __global__ void __launch_bounds__(NT, 1) k_selinv_oz(SelinvOzArgs p) {
     bool ok = true;
     double vreg[PER_THREAD];
     int since_fold = 0;
+    auto flags_of = [&](int s, const int*& f0, const int*& f1) {
+      f0 = left_of(s).flag;
+      f1 = nullptr;
+    };
     if (np > 0) {
       SigTileOz lt = left_of(0);
       ok = cta_wait(c, lt.flag, nullptr, &s_ok);
       if (ok) {
+        if (threadIdx.x == 0) s_ready = 1;
         tile_ldg(vreg, lt.t);
         oz_load_async(stages + OZ_OPER, right_of(0));
         cp_async_commit();
@@ -337,7 +342,11 @@ __global__ void __launch_bounds__(NT, 1) k_selinv_oz(SelinvOzArgs p) {
         SigTileOz nt_;
         if (more) {
           nt_ = left_of(s + 1);
-          if (cta_poll(c, nt_.flag, nullptr, &s_ok)) {
+          if (s_ready <= s + 1) {   // uniform: read after the barrier
+            scan_ready(c, np, flags_of, &s_ready);
+            __syncthreads();
+          }
+          if (s_ready > s + 1) {
             tile_ldg(vreg, nt_.t);
             oz_load_async(nxt + OZ_OPER, right_of(s + 1));
             cp_async_commit();
@@ -349,6 +358,7 @@ __global__ void __launch_bounds__(NT, 1) k_selinv_oz(SelinvOzArgs p) {
         if (more) {
           if (!have) {
             if (!(ok = cta_wait(c, nt_.flag, nullptr, &s_ok))) break;
+            if (threadIdx.x == 0) s_ready = s + 2;
             tile_ldg(vreg, nt_.t);
             oz_load_async(nxt + OZ_OPER, right_of(s + 1));
             cp_async_commit();
