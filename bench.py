@@ -185,6 +185,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     stream = torch.cuda.current_stream()
     h.set_stream(stream.cuda_stream)
     coef = spec.coefficients(theta)
+    tau_dev = torch.from_numpy(coef.tau_y).cuda()
 
     Dc, Lc, Rc, Tc = model.Dc, model.Lc, model.Rc, model.Tc
     mu = model.mu
@@ -193,14 +194,13 @@ def run_ours(args, rank: int, world: int, local_rank: int):
 
     def step(record: bool):
         e = ev if record else None
-        alpha_p, beta_p = model._upload_coef(coef)
+        ptrs = model._upload_coef(coef)
         if e: e["asm"][0].record()
-        model._assemble(alpha_p, beta_p, coef.tau_y, Dc, Lc, Rc, Tc, with_lik=True)
+        model._assemble(ptrs, Dc, Lc, Rc, Tc, with_lik=True)
         if e: e["asm"][1].record(); e["fac"][0].record()
         _lib.check(lib.gbta_pobtaf_async(h.ptr, Dc.data_ptr(), Lc.data_ptr(), Rc.data_ptr(), Tc.data_ptr()))
         if e: e["fac"][1].record(); e["sol"][0].record()
-        mu.copy_(model._Aty)
-        mu.mul_(coef.tau_y)
+        torch.mv(model._Aty_v.t(), tau_dev, out=mu)
         _lib.check(lib.gbta_pobtas_async(h.ptr, Dc.data_ptr(), Lc.data_ptr(), Rc.data_ptr(), Tc.data_ptr(),
                                          mu.data_ptr(), 1, 0))
         _lib.check(lib.gbta_pobtas_async(h.ptr, Dc.data_ptr(), Lc.data_ptr(), Rc.data_ptr(), Tc.data_ptr(),
@@ -284,7 +284,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     # ---- e2e through the reference-facing drop-in (host sparse Q_cond in, host results out)
     if not args.no_e2e:
         Qp_host, Qc_host = spec.sparse_precisions(theta)
-        rhs_host = np.asarray(coef.tau_y * (spec.A.T @ spec.y), dtype=np.float64)
+        rhs_host = np.asarray(spec.A.T @ (coef.tau_y[spec.obs_variates()] * spec.y), dtype=np.float64)
         solver = GB300SerinvSolver(None, diagonal_blocksize=b, n_diag_blocks=nt, arrowhead_blocksize=a)
         Qc_coo = Qc_host.tocoo()
         nnz_lower = int(np.count_nonzero(Qc_coo.row >= Qc_coo.col))

@@ -177,8 +177,11 @@ int gbta_gather_coo(gbta_solver* s, const long long* rows, const long long* cols
                     double* vals);
 
 /* ---- on-device assembly of Kronecker-sum precisions ----------------------- */
+/* Largest number of variates (coregional components) a model may have. */
+#define GBTA_MAX_VARIATES 8
+
 /* Overwrite D, L (R, T) with the BTA blocks of
- *     Q = sum_k  M_k(theta) (x) S_k  +  lik_scale * A^T A  +  tip_diag * I_a
+ *     Q = sum_k  M_k(theta) (x) S_k  +  sum_v lik_scale[v] * A_v^T A_v  +  tip_diag * I_a
  * where S_k are fixed ns x ns spatial matrices placed at variate block (v_k, w_k) of
  * the b = nv * ns diagonal block, with temporal coefficients
  *     D_t += alpha[k*nt + t] * S_k,     L_t += beta[k*(nt-1) + t] * S_k.
@@ -186,31 +189,37 @@ int gbta_gather_coo(gbta_solver* s, const long long* rows, const long long* cols
  * is S_k's value at union entry e (0 when absent); term_vw[2k], term_vw[2k+1] = (v_k, w_k).
  * A^T A (theta-independent) is given as CSR rows of the diagonal blocks (lik_rowptr
  * [nt*b+1] over block rows t*b + rho, lik_col block-local) plus dense arrow parts
- * lik_R (nt, a, b) and lik_T (a, a); any of them may be NULL.  All arrays are device
- * pointers.  Replaces the per-evaluation Q construction of the reference
- * (src/pyinla/submodels/spatio_temporal.py:114-149, src/pyinla/core/model.py:306-423,
- * src/pyinla/models/coregional_model.py:274-597) and the sparse-to-BTA scatter
- * (structured_solver.py:192-468).  Deterministic.  Asynchronous on the solver's stream. */
+ * lik_R (nt, a, b) and lik_T (a, a); any of them may be NULL.  A_v^T A_v is the part
+ * of A^T A that belongs to the observations of variate v: diagonal-block rows and R
+ * columns of variate v's nodes, T rows of the fixed effects with arrow_variate[i] == v
+ * (arrow_variate: device [a], NULL = every fixed effect belongs to variate 0).
+ * lik_scale is a DEVICE array of nv noise precisions, read when the kernel runs (so a
+ * captured graph picks up new values); required when any A^T A part is given.
+ * All arrays are device pointers.  Replaces the per-evaluation Q construction of the
+ * reference (src/pyinla/submodels/spatio_temporal.py:114-149, src/pyinla/core/model.py:
+ * 306-423, src/pyinla/models/coregional_model.py:274-643) and the sparse-to-BTA
+ * scatter (structured_solver.py:192-468).  Deterministic.  Asynchronous on the
+ * solver's stream. */
 int gbta_assemble_kron(gbta_solver* s, int ns, int nv, int nterms, const int* upat_rowptr,
                        const int* upat_col, const double* uval, const int* term_vw, const double* alpha,
                        const double* beta, const long long* lik_rowptr, const int* lik_col,
-                       const double* lik_val, const double* lik_R, const double* lik_T, double lik_scale,
-                       double tip_diag, double* D, double* L, double* R, double* T);
+                       const double* lik_val, const double* lik_R, const double* lik_T, const double* lik_scale,
+                       const int* arrow_variate, double tip_diag, double* D, double* L, double* R, double* T);
 
 /* Contractions for the adjoint theta-gradient (no counterpart in the reference, which
  * differentiates by central finite differences, src/pyinla/core/pyinla.py:512-600):
  * with Sigma given by SD, SL, SR, ST (selected inverse blocks, any may be NULL) and
- * mu (N vector, may be NULL), writes out[4*K*nt + 2*(nt+1)] (K = nterms):
+ * mu (N vector, may be NULL), writes out[4*K*nt + 2*nv*(nt+1)] (K = nterms):
  *   out[0*K*nt + k*nt + t] = <Sigma_tt, S_k>       out[1*K*nt + k*nt + t] = <Sigma_{t+1,t}, S_k>
  *   out[2*K*nt + k*nt + t] = mu_t' S_k mu_t        out[3*K*nt + k*nt + t] = mu_{t+1}' S_k mu_t
- *   out[4*K*nt + t]        = <Sigma, A^T A> on block t (t = nt: tip part)
- *   out[4*K*nt + nt+1 + t] = the same with mu mu'.
+ *   out[4*K*nt + v*2*(nt+1) + t]          = <Sigma, A_v^T A_v> on block t (t = nt: tip part)
+ *   out[4*K*nt + v*2*(nt+1) + nt+1 + t]   = the same with mu mu'.
  * Deterministic.  Asynchronous on the solver's stream. */
 int gbta_contract_kron(gbta_solver* s, int ns, int nv, int nterms, const int* upat_rowptr,
                        const int* upat_col, const double* uval, const int* term_vw,
                        const long long* lik_rowptr, const int* lik_col, const double* lik_val,
-                       const double* lik_R, const double* lik_T, const double* SD, const double* SL,
-                       const double* SR, const double* ST, const double* mu, double* out);
+                       const double* lik_R, const double* lik_T, const int* arrow_variate, const double* SD,
+                       const double* SL, const double* SR, const double* ST, const double* mu, double* out);
 
 #ifdef __cplusplus
 }

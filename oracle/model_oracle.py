@@ -8,8 +8,10 @@ evaluation for a Gaussian likelihood:
   (``sp.sparse.kron(m_k, q_k)`` summed), with the fixed-effect block
   ``tip_prec * I`` of src/pyinla/submodels/regression.py:27-30 appended;
 * Q_cond = Q_prior - A^T D A with D = -tau_y I (src/pyinla/core/model.py:421,
-  src/pyinla/likelihoods/gaussian.py:127-129);
-* the information vector at x = 0, tau_y A^T y (model.py:445-447, gaussian.py:94);
+  src/pyinla/likelihoods/gaussian.py:127-129), or D = -diag(tau_y of each row's
+  variate) for the coregional model's per-variate likelihoods
+  (src/pyinla/models/coregional_model.py:599-643);
+* the information vector at x = 0, A^T D y (model.py:445-447, gaussian.py:94);
 * the sparse-to-BTA mapping of SerinvSolver (src/pyinla/solvers/structured_solver.py:192-250);
 * f(theta) of PyINLA._evaluate_f for the Gaussian branch
   (src/pyinla/core/pyinla.py:631-688, 1076-1167) with the BTA oracle of
@@ -67,23 +69,41 @@ def sparse_to_bta(Q, nt: int, b: int, a: int):
     return D, L, R, T
 
 
-def objective(spatial_terms, term_vw, ns, nv, nt, nb, A, y, tip_prec, alpha, beta, tau_y, theta_y, log_prior):
-    """f(theta) for the Gaussian branch of PyINLA._evaluate_f, on the CPU."""
+def _variate_arrays(y, tau_y, obs_variate):
+    tau_y = np.atleast_1d(np.asarray(tau_y, dtype=np.float64))
+    ov = np.zeros(y.size, dtype=np.int64) if obs_variate is None else np.asarray(obs_variate, dtype=np.int64)
+    return tau_y, ov, tau_y[ov]
+
+
+def objective(spatial_terms, term_vw, ns, nv, nt, nb, A, y, tip_prec, alpha, beta, tau_y, theta_y, log_prior,
+              obs_variate=None):
+    """f(theta) for the Gaussian branch of PyINLA._evaluate_f, on the CPU.
+
+    ``tau_y`` and ``theta_y`` hold one noise precision (and its log) per variate and
+    ``obs_variate`` the variate of each observation (default: all 0); several variates
+    are the coregional model's per-variate likelihoods: D = -diag(tau_y of each row)
+    (src/pyinla/models/coregional_model.py:599-643) and the likelihood summed over the
+    variates (:664-677)."""
     b = nv * ns
+    tau_y, ov, tau_row = _variate_arrays(y, tau_y, obs_variate)
+    theta_y = np.atleast_1d(np.asarray(theta_y, dtype=np.float64))
     Qp = kron_prior(spatial_terms, term_vw, alpha, beta, ns, nv, nt, nb, tip_prec)
-    Qc = (Qp + tau_y * (A.T @ A)).tocsr()
+    Qc = (Qp + A.T @ (sps.diags(tau_row) @ A)).tocsr()
     Dp, Lp, Rp, Tp = sparse_to_bta(Qp, nt, b, nb)
     orc.pobtf(Dp, Lp)
     logdet_p = orc.logdet(Dp, None, "bt")
     Dc, Lc, Rc, Tc = sparse_to_bta(Qc, nt, b, nb)
     orc.pobtaf(Dc, Lc, Rc, Tc)
     logdet_c = orc.logdet(Dc, Tc, "bta")
-    rhs = tau_y * (A.T @ y)
+    rhs = A.T @ (tau_row * y)
     mu = rhs.copy()
     orc.pobtas(Dc, Lc, Rc, Tc, mu, "N")
     orc.pobtas(Dc, Lc, Rc, Tc, mu, "C")
     quad = float(mu @ (Qc @ mu))                        # pyinla.py:1157-1158
-    lik = 0.5 * theta_y * y.size - 0.5 * tau_y * float(y @ y)   # gaussian.py:58-60 at eta = 0
+    lik = 0.0                                           # gaussian.py:58-60 at eta = 0, per variate
+    for v in range(tau_y.size):
+        yv = y[ov == v]
+        lik += 0.5 * theta_y[v] * yv.size - 0.5 * tau_y[v] * float(yv @ yv)
     f = -(log_prior + lik + 0.5 * logdet_p) + 0.5 * logdet_c - 0.5 * quad
     return f, dict(logdet_prior=logdet_p, logdet_cond=logdet_c, quad=quad, mu=mu, Qp=Qp, Qc=Qc)
 
@@ -100,28 +120,35 @@ def central_difference(fun, theta, eps):
 
 
 def dense_gradient(spatial_terms, term_vw, ns, nv, nt, nb, A, y, tip_prec, coef, dcoef, theta_y_index,
-                   log_prior_grad):
+                   log_prior_grad, obs_variate=None):
     """Exact gradient of f with dense FP64 linear algebra (small problems only):
-    tr(Q^{-1} dQ) with the full inverses, mu from a dense solve."""
+    tr(Q^{-1} dQ) with the full inverses, mu from a dense solve.  ``theta_y_index``
+    lists the index of log tau_y,v in theta for each variate v; ``dcoef.dtau_y[k, v]``
+    is d tau_y,v / d theta_k."""
     b = nv * ns
+    tau_y, ov, tau_row = _variate_arrays(y, coef.tau_y, obs_variate)
+    nvar = tau_y.size
+    dtau = np.asarray(dcoef.dtau_y, dtype=np.float64).reshape(dcoef.dalpha.shape[0], nvar)
     Qp = kron_prior(spatial_terms, term_vw, coef.alpha, coef.beta, ns, nv, nt, nb, tip_prec).toarray()
-    AtA = (A.T @ A).toarray()
-    Qc = Qp + coef.tau_y * AtA
+    AtA_v = [(A[ov == v].T @ A[ov == v]).toarray() for v in range(nvar)]
+    Aty_v = [A[ov == v].T @ y[ov == v] for v in range(nvar)]
+    Qc = Qp + sum(tau_y[v] * AtA_v[v] for v in range(nvar))
     nbk = nt * b
     Sp = np.linalg.inv(Qp[:nbk, :nbk])
     Sc = np.linalg.inv(Qc)
-    rhs = coef.tau_y * (A.T @ y)
+    rhs = sum(tau_y[v] * Aty_v[v] for v in range(nvar))
     mu = np.linalg.solve(Qc, rhs)
-    quad = float(mu @ rhs)
     d = dcoef.dalpha.shape[0]
     g = np.zeros(d)
     for k in range(d):
         dQp = kron_prior(spatial_terms, term_vw, dcoef.dalpha[k], dcoef.dbeta[k], ns, nv, nt, nb, 0.0).toarray()
-        dQc = dQp + dcoef.dtau_y[k] * AtA
+        dQc = dQp + sum(dtau[k, v] * AtA_v[v] for v in range(nvar))
         tr_p = float(np.sum(Sp * dQp[:nbk, :nbk]))
         tr_c = float(np.sum(Sc * dQc))
-        mdb = dcoef.dtau_y[k] / coef.tau_y * quad
+        mdb = float(sum(dtau[k, v] * (mu @ Aty_v[v]) for v in range(nvar)))
         g[k] = -0.5 * tr_p + 0.5 * tr_c - mdb + 0.5 * float(mu @ dQc @ mu)
-    g[theta_y_index] -= 0.5 * y.size - 0.5 * coef.tau_y * float(y @ y)
+    for v, idx in enumerate(np.atleast_1d(theta_y_index)):
+        yv = y[ov == v]
+        g[idx] -= 0.5 * yv.size - 0.5 * tau_y[v] * float(yv @ yv)
     g -= log_prior_grad
     return g

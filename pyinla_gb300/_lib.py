@@ -21,6 +21,7 @@ GBTA_ERR_TIMEOUT = -3
 GBTA_ERR_ALLOC = -5
 GBTA_METHOD_FP64 = 0
 GBTA_METHOD_OZAKI = 1
+GBTA_MAX_VARIATES = 8        # include/pyinla_gb300.h
 
 _lib = None
 _lock = threading.Lock()
@@ -65,9 +66,9 @@ SIGNATURES = {
     "gbta_scatter_coo": (_c_int, [_vp, _vp, _vp, _vp, _c_ll, _vp, _vp, _vp, _vp, _c_int]),
     "gbta_gather_coo": (_c_int, [_vp, _vp, _vp, _c_ll, _vp, _vp, _vp, _vp, _c_int, _vp]),
     "gbta_assemble_kron": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
-                                    _vp, _vp, ctypes.c_double, ctypes.c_double, _vp, _vp, _vp, _vp]),
+                                    _vp, _vp, _vp, _vp, ctypes.c_double, _vp, _vp, _vp, _vp]),
     "gbta_contract_kron": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
-                                    _vp, _vp, _vp, _vp, _vp, _vp]),
+                                    _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
 }
 
 

@@ -39,13 +39,20 @@ struct LikDesc {
   const double* val;
   const double* Rdense;     // [nt*a*b] or null
   const double* Tdense;     // [a*a] or null
+  const double* scale;      // [nv] noise precision of each variate (device)
+  const int* arrow_var;     // [a] variate of each fixed effect, or null (all variate 0)
 };
+
+// Variate of fixed effect i (out-of-range labels count as "no variate": -1).
+__device__ __forceinline__ int arrow_variate(const LikDesc& ld, int i, int nv) {
+  const int v = ld.arrow_var ? ld.arrow_var[i] : 0;
+  return (v >= 0 && v < nv) ? v : -1;
+}
 
 constexpr int AS_WARPS = 8;
 
 __global__ void __launch_bounds__(AS_WARPS * 32) k_assemble_rows(Geom g, KronDesc kd, LikDesc ld, const double* alpha,
-                                                                 const double* beta, double lik_scale, double* D,
-                                                                 double* L) {
+                                                                 const double* beta, double* D, double* L) {
   const int lane = threadIdx.x & 31;
   const long long wid = (long long)blockIdx.x * AS_WARPS + (threadIdx.x >> 5);
   const long long nrows = (long long)g.nt * g.b;
@@ -74,19 +81,23 @@ __global__ void __launch_bounds__(AS_WARPS * 32) k_assemble_rows(Geom g, KronDes
   if (ld.rowptr) {
     __syncwarp();
     const long long l0 = ld.rowptr[wid], l1 = ld.rowptr[wid + 1];
-    for (long long e = l0 + lane; e < l1; e += 32) drow[ld.col[e]] += lik_scale * ld.val[e];
+    const double sc = ld.scale[v];   // observations of variate v touch only its own nodes
+    for (long long e = l0 + lane; e < l1; e += 32) drow[ld.col[e]] += sc * ld.val[e];
   }
 }
 
-__global__ void k_assemble_arrow(Geom g, LikDesc ld, double lik_scale, double tip_diag, double* R, double* T) {
+// Arrow blocks: R entries take the scale of their column's variate, T entries that of
+// their row's fixed effect (A^T A couples a fixed effect only with its own variate).
+__global__ void k_assemble_arrow(Geom g, int ns, int nv, LikDesc ld, double tip_diag, double* R, double* T) {
   const size_t nR = (size_t)g.nt * g.a * g.b, nT = (size_t)g.a * g.a;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nR + nT; e += (size_t)gridDim.x * blockDim.x) {
     if (e < nR) {
-      R[e] = ld.Rdense ? lik_scale * ld.Rdense[e] : 0.0;
+      R[e] = ld.Rdense ? ld.scale[(int)(e % g.b) / ns] * ld.Rdense[e] : 0.0;
     } else {
       const size_t q = e - nR;
       const int i = (int)(q / g.a), j = (int)(q % g.a);
-      T[q] = (ld.Tdense ? lik_scale * ld.Tdense[q] : 0.0) + (i == j ? tip_diag : 0.0);
+      const int v = arrow_variate(ld, i, nv);
+      T[q] = ((ld.Tdense && v >= 0) ? ld.scale[v] * ld.Tdense[q] : 0.0) + (i == j ? tip_diag : 0.0);
     }
   }
 }
@@ -98,9 +109,11 @@ __global__ void k_assemble_arrow(Geom g, LikDesc ld, double lik_scale, double ti
 //   out[1*K*nt + k*nt + t]  <Sigma_{t+1,t}, S_k>         (SL[t]; 0 for t = nt-1)
 //   out[2*K*nt + k*nt + t]  mu_t^T S_k mu_t
 //   out[3*K*nt + k*nt + t]  mu_{t+1}^T S_k mu_t
-//   out[4*K*nt + t]         <Sigma, A^T A> restricted to block t (D part + 2 * R part);
-//                            index nt: the tip part
-//   out[4*K*nt + (nt+1) + t] the same with mu mu^T
+//   out[4*K*nt + v*2*(nt+1) + t]           <Sigma, A_v^T A_v> restricted to block t
+//                                           (D part + 2 * R part); index nt: the tip part
+//   out[4*K*nt + v*2*(nt+1) + (nt+1) + t]  the same with mu mu^T
+// where A_v^T A_v is the part of A^T A of variate v's observations (its rows and
+// columns lie in variate v's nodes and fixed effects).
 // ---------------------------------------------------------------------------
 constexpr int CT_THREADS = 256;
 constexpr int CT_CHUNK = 8;   // terms accumulated per pass
@@ -125,21 +138,25 @@ __global__ void __launch_bounds__(CT_THREADS) k_contract(Geom g, KronDesc kd, Li
   const int K = kd.nterms;
   const size_t KN = (size_t)K * g.nt;
   const size_t bb = (size_t)g.b * g.b;
+  const size_t LS = 2 * (size_t)(g.nt + 1);   // per-variate stride of the A^T A sums
   if (t == g.nt) {   // tip block of A^T A
-    double sc = 0.0, sq = 0.0;
-    if (ld.Tdense && g.a > 0) {
-      const double* mua = mu ? mu + (size_t)g.nt * g.b : nullptr;
-      for (int q = threadIdx.x; q < g.a * g.a; q += CT_THREADS) {
-        const int i = q / g.a, j = q % g.a;
-        if (ST) sc += ST[q] * ld.Tdense[q];
-        if (mua) sq += mua[i] * ld.Tdense[q] * mua[j];
+    for (int v = 0; v < kd.nv; ++v) {
+      double sc = 0.0, sq = 0.0;
+      if (ld.Tdense && g.a > 0) {
+        const double* mua = mu ? mu + (size_t)g.nt * g.b : nullptr;
+        for (int q = threadIdx.x; q < g.a * g.a; q += CT_THREADS) {
+          const int i = q / g.a, j = q % g.a;
+          if (arrow_variate(ld, i, kd.nv) != v) continue;
+          if (ST) sc += ST[q] * ld.Tdense[q];
+          if (mua) sq += mua[i] * ld.Tdense[q] * mua[j];
+        }
       }
-    }
-    sc = block_sum(sc, red);
-    sq = block_sum(sq, red);
-    if (threadIdx.x == 0) {
-      out[4 * KN + g.nt] = sc;
-      out[4 * KN + (g.nt + 1) + g.nt] = sq;
+      sc = block_sum(sc, red);
+      sq = block_sum(sq, red);
+      if (threadIdx.x == 0) {
+        out[4 * KN + v * LS + g.nt] = sc;
+        out[4 * KN + v * LS + (g.nt + 1) + g.nt] = sq;
+      }
     }
     return;
   }
@@ -181,32 +198,37 @@ __global__ void __launch_bounds__(CT_THREADS) k_contract(Geom g, KronDesc kd, Li
       }
     }
   }
-  // A^T A on block t: D part (CSR rows) and arrow part (dense R, counted twice).
-  double lc = 0.0, lq = 0.0;
-  if (ld.rowptr) {
-    for (int rho = threadIdx.x; rho < g.b; rho += CT_THREADS) {
-      const long long row = (long long)t * g.b + rho;
-      for (long long e = ld.rowptr[row]; e < ld.rowptr[row + 1]; ++e) {
-        const int cc = ld.col[e];
-        if (Dt) lc += Dt[(size_t)rho * g.b + cc] * ld.val[e];
-        if (mut) lq += mut[rho] * ld.val[e] * mut[cc];
+  // A^T A on block t, per variate: D part (CSR rows of the variate's nodes) and arrow
+  // part (dense R columns of the variate's nodes, counted twice).
+  for (int v = 0; v < kd.nv; ++v) {
+    double lc = 0.0, lq = 0.0;
+    if (ld.rowptr) {
+      for (int rho = v * kd.ns + threadIdx.x; rho < (v + 1) * kd.ns; rho += CT_THREADS) {
+        const long long row = (long long)t * g.b + rho;
+        for (long long e = ld.rowptr[row]; e < ld.rowptr[row + 1]; ++e) {
+          const int cc = ld.col[e];
+          if (Dt) lc += Dt[(size_t)rho * g.b + cc] * ld.val[e];
+          if (mut) lq += mut[rho] * ld.val[e] * mut[cc];
+        }
       }
     }
-  }
-  if (ld.Rdense && g.a > 0) {
-    const double* Rt = ld.Rdense + (size_t)t * g.a * g.b;
-    const double* SRt = SR ? SR + (size_t)t * g.a * g.b : nullptr;
-    const double* mua = mu ? mu + (size_t)g.nt * g.b : nullptr;
-    for (int q = threadIdx.x; q < g.a * g.b; q += CT_THREADS) {
-      if (SRt) lc += 2.0 * SRt[q] * Rt[q];
-      if (mua) lq += 2.0 * mua[q / g.b] * Rt[q] * mut[q % g.b];
+    if (ld.Rdense && g.a > 0) {
+      const double* Rt = ld.Rdense + (size_t)t * g.a * g.b;
+      const double* SRt = SR ? SR + (size_t)t * g.a * g.b : nullptr;
+      const double* mua = mu ? mu + (size_t)g.nt * g.b : nullptr;
+      for (int q = threadIdx.x; q < g.a * kd.ns; q += CT_THREADS) {
+        const int r = q / kd.ns, col = v * kd.ns + q % kd.ns;
+        const size_t e = (size_t)r * g.b + col;
+        if (SRt) lc += 2.0 * SRt[e] * Rt[e];
+        if (mua) lq += 2.0 * mua[r] * Rt[e] * mut[col];
+      }
     }
-  }
-  lc = block_sum(lc, red);
-  lq = block_sum(lq, red);
-  if (threadIdx.x == 0) {
-    out[4 * KN + t] = lc;
-    out[4 * KN + (g.nt + 1) + t] = lq;
+    lc = block_sum(lc, red);
+    lq = block_sum(lq, red);
+    if (threadIdx.x == 0) {
+      out[4 * KN + v * LS + t] = lc;
+      out[4 * KN + v * LS + (g.nt + 1) + t] = lq;
+    }
   }
 }
 
@@ -217,6 +239,7 @@ extern "C" int gbta_set_error(int code, const char* msg);
 static int kron_args_ok(int b, int ns, int nv, int nterms, const int* rp, const int* col, const double* uval,
                         const int* vw) {
   if (ns < 1 || nv < 1 || nv * ns != b) return gbta_set_error(GBTA_ERR_ARG, "kron: need nv * ns == b");
+  if (nv > GBTA_MAX_VARIATES) return gbta_set_error(GBTA_ERR_ARG, "kron: too many variates");
   if (nterms < 0 || (nterms > 0 && (!rp || !col || !uval || !vw)))
     return gbta_set_error(GBTA_ERR_ARG, "kron: null term pointer");
   return GBTA_OK;
@@ -225,8 +248,9 @@ static int kron_args_ok(int b, int ns, int nv, int nterms, const int* rp, const 
 extern "C" int gbta_assemble_kron(gbta_solver* s, int ns, int nv, int nterms, const int* upat_rowptr,
                                   const int* upat_col, const double* uval, const int* term_vw, const double* alpha,
                                   const double* beta, const long long* lik_rowptr, const int* lik_col,
-                                  const double* lik_val, const double* lik_R, const double* lik_T, double lik_scale,
-                                  double tip_diag, double* D, double* L, double* R, double* T) {
+                                  const double* lik_val, const double* lik_R, const double* lik_T,
+                                  const double* lik_scale, const int* arrow_variate, double tip_diag, double* D,
+                                  double* L, double* R, double* T) {
   int b, nt, a;
   void* st;
   if (int r = gbta_geometry(s, &b, &nt, &a, &st)) return r;
@@ -234,15 +258,17 @@ extern "C" int gbta_assemble_kron(gbta_solver* s, int ns, int nv, int nterms, co
   if (!D || (nt > 1 && !L) || (nterms > 0 && !alpha) || (nterms > 0 && nt > 1 && !beta))
     return gbta_set_error(GBTA_ERR_ARG, "assemble: null block or coefficient pointer");
   if (lik_rowptr && (!lik_col || !lik_val)) return gbta_set_error(GBTA_ERR_ARG, "assemble: incomplete A^T A CSR");
+  if ((lik_rowptr || lik_R || lik_T) && !lik_scale)
+    return gbta_set_error(GBTA_ERR_ARG, "assemble: A^T A given without lik_scale");
   if (a > 0 && (!R || !T)) return gbta_set_error(GBTA_ERR_ARG, "assemble: R/T required when a > 0");
   gbta::Geom g{b, nt, a, (b + gbta::TS - 1) / gbta::TS};
   gbta::KronDesc kd{ns, nv, nterms, upat_rowptr, upat_col, uval, term_vw};
-  gbta::LikDesc ld{lik_rowptr, lik_col, lik_val, lik_R, lik_T};
+  gbta::LikDesc ld{lik_rowptr, lik_col, lik_val, lik_R, lik_T, lik_scale, arrow_variate};
   cudaStream_t stream = (cudaStream_t)st;
   const long long rows = (long long)nt * b;
   const long long blocks = (rows + gbta::AS_WARPS - 1) / gbta::AS_WARPS;
-  gbta::k_assemble_rows<<<(unsigned)blocks, gbta::AS_WARPS * 32, 0, stream>>>(g, kd, ld, alpha, beta, lik_scale, D, L);
-  if (a > 0) gbta::k_assemble_arrow<<<256, 256, 0, stream>>>(g, ld, lik_scale, tip_diag, R, T);
+  gbta::k_assemble_rows<<<(unsigned)blocks, gbta::AS_WARPS * 32, 0, stream>>>(g, kd, ld, alpha, beta, D, L);
+  if (a > 0) gbta::k_assemble_arrow<<<256, 256, 0, stream>>>(g, ns, nv, ld, tip_diag, R, T);
   gbta::count_launches(1 + (a > 0));
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return gbta_set_error(GBTA_ERR_CUDA, cudaGetErrorString(e));
@@ -252,8 +278,9 @@ extern "C" int gbta_assemble_kron(gbta_solver* s, int ns, int nv, int nterms, co
 extern "C" int gbta_contract_kron(gbta_solver* s, int ns, int nv, int nterms, const int* upat_rowptr,
                                   const int* upat_col, const double* uval, const int* term_vw,
                                   const long long* lik_rowptr, const int* lik_col, const double* lik_val,
-                                  const double* lik_R, const double* lik_T, const double* SD, const double* SL,
-                                  const double* SR, const double* ST, const double* mu, double* out) {
+                                  const double* lik_R, const double* lik_T, const int* arrow_variate,
+                                  const double* SD, const double* SL, const double* SR, const double* ST,
+                                  const double* mu, double* out) {
   int b, nt, a;
   void* st;
   if (int r = gbta_geometry(s, &b, &nt, &a, &st)) return r;
@@ -262,7 +289,7 @@ extern "C" int gbta_contract_kron(gbta_solver* s, int ns, int nv, int nterms, co
   if (lik_rowptr && (!lik_col || !lik_val)) return gbta_set_error(GBTA_ERR_ARG, "contract: incomplete A^T A CSR");
   gbta::Geom g{b, nt, a, (b + gbta::TS - 1) / gbta::TS};
   gbta::KronDesc kd{ns, nv, nterms, upat_rowptr, upat_col, uval, term_vw};
-  gbta::LikDesc ld{lik_rowptr, lik_col, lik_val, lik_R, lik_T};
+  gbta::LikDesc ld{lik_rowptr, lik_col, lik_val, lik_R, lik_T, nullptr, arrow_variate};
   gbta::k_contract<<<nt + 1, gbta::CT_THREADS, 0, (cudaStream_t)st>>>(g, kd, ld, SD, SL, SR, ST, mu, out);
   gbta::count_launches(1);
   const cudaError_t e = cudaGetLastError();

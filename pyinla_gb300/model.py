@@ -40,14 +40,21 @@ from .device import BtaHandle, current_stream_ptr, require_torch_cuda
 class Coefficients:
     alpha: np.ndarray        # (K, nt)
     beta: np.ndarray         # (K, nt-1)
-    tau_y: float
+    tau_y: np.ndarray        # (nv,) noise precision of each variate's observations
+
+    def __post_init__(self):
+        self.tau_y = np.atleast_1d(np.asarray(self.tau_y, dtype=np.float64))
 
 
 @dataclass
 class CoefficientDerivatives:
     dalpha: np.ndarray       # (d, K, nt)
     dbeta: np.ndarray        # (d, K, nt-1)
-    dtau_y: np.ndarray       # (d,)
+    dtau_y: np.ndarray       # (d, nv)
+
+    def __post_init__(self):
+        dt = np.asarray(self.dtau_y, dtype=np.float64)
+        self.dtau_y = dt.reshape(dt.shape[0], -1)
 
 
 def union_pattern(mats: list[sps.csr_matrix]):
@@ -73,7 +80,9 @@ class KronSpec:
     Subclasses define the theta -> coefficient maps.  Fields: ``terms`` (spatial
     matrices S_k), ``term_vw`` (variate block of each term), ``ns``, ``nv``, ``nt``,
     ``nb``, ``A`` (n_obs x N design matrix, time-major field then fixed effects),
-    ``y`` and ``tip_prec``.
+    ``y``, ``tip_prec`` and, for several variates, ``obs_variate`` (variate of each
+    observation) and ``arrow_variate`` (variate of each fixed effect); both default
+    to variate 0.
     """
 
     terms: list
@@ -110,9 +119,17 @@ class KronSpec:
     def log_prior_grad(self, theta: np.ndarray) -> np.ndarray:
         raise NotImplementedError
 
-    def lik_theta_index(self) -> int:
-        """Index of theta_y = log tau_y in theta."""
+    def lik_theta_indices(self) -> list[int]:
+        """Index in theta of theta_y,v = log tau_y,v for each variate v."""
         raise NotImplementedError
+
+    def obs_variates(self) -> np.ndarray:
+        v = getattr(self, "obs_variate", None)
+        return np.zeros(self.y.shape[0], dtype=np.int64) if v is None else np.asarray(v, dtype=np.int64)
+
+    def arrow_variates(self) -> np.ndarray:
+        v = getattr(self, "arrow_variate", None)
+        return np.zeros(self.nb, dtype=np.int32) if v is None else np.asarray(v, dtype=np.int32)
 
     def sparse_precisions(self, theta: np.ndarray):
         """Host sparse (CSR) Q_prior and Q_cond at theta, in the form the reference's
@@ -140,7 +157,8 @@ class KronSpec:
             vals.append(np.full(self.nb, self.tip_prec))
         Qp = sps.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(N, N))
         Qp.sum_duplicates()
-        Qc = (Qp + c.tau_y * (self.A.T @ self.A)).tocsr()
+        DA = sps.diags(c.tau_y[self.obs_variates()]) @ self.A
+        Qc = (Qp + (self.A.T @ DA)).tocsr()
         Qc.sum_duplicates()
         return Qp, Qc
 
@@ -161,6 +179,15 @@ class KronGaussianModel:
         self.n_obs = int(y.shape[0])
         if A.shape != (self.n_obs, self.N):
             raise ValueError(f"A has shape {A.shape}, expected {(self.n_obs, self.N)}")
+        if self.nv > _lib.GBTA_MAX_VARIATES:
+            raise ValueError(f"at most {_lib.GBTA_MAX_VARIATES} variates")
+        ov = spec.obs_variates()
+        av = spec.arrow_variates()
+        if ov.shape != (self.n_obs,) or (ov.size and (ov.min() < 0 or ov.max() >= self.nv)):
+            raise ValueError("obs_variate must give a variate in [0, nv) per observation")
+        if av.shape != (self.nb,) or (av.size and (av.min() < 0 or av.max() >= self.nv)):
+            raise ValueError("arrow_variate must give a variate in [0, nv) per fixed effect")
+        self._check_variate_support(A, ov, av)
         # --- theta-independent device data (built once, like the reference's pattern reuse,
         #     src/pyinla/core/model.py:356-380)
         dev = "cuda"
@@ -191,8 +218,14 @@ class KronGaussianModel:
             self._lik_T = torch.from_numpy(np.ascontiguousarray(Tl)).to(dev)
         else:
             self._lik_R = self._lik_T = None
-        self._Aty = torch.from_numpy(np.asarray(At @ y, dtype=np.float64)).to(dev)
-        self.yty = float(y @ y)
+        Aty_v = np.zeros((self.nv, self.N))
+        for v in range(self.nv):
+            sel = ov == v
+            Aty_v[v] = A[sel].T @ y[sel]
+        self._Aty_v = torch.from_numpy(Aty_v).to(dev)
+        self.yty_v = np.array([float(y[ov == v] @ y[ov == v]) for v in range(self.nv)])
+        self.nobs_v = np.array([int(np.count_nonzero(ov == v)) for v in range(self.nv)])
+        self._arrow_var = torch.from_numpy(np.ascontiguousarray(av, dtype=np.int32)).to(dev) if self.nb else None
         # --- block buffers: conditional (bta) and prior (bt) precisions
         f64 = torch.float64
         b, nt, a = self.b, self.nt, self.nb
@@ -205,8 +238,8 @@ class KronGaussianModel:
         self.Rp = torch.empty_like(self.Rc)
         self.Tp = torch.empty_like(self.Tc)
         self.mu = torch.empty(self.N, dtype=f64, device=dev)
-        self._coef = torch.empty(2 * self.K * nt, dtype=f64, device=dev)
-        self._contract_out = torch.empty(4 * self.K * nt + 2 * (nt + 1), dtype=f64, device=dev)
+        self._coef = torch.empty(2 * self.K * nt + self.nv, dtype=f64, device=dev)
+        self._contract_out = torch.empty(4 * self.K * nt + 2 * self.nv * (nt + 1), dtype=f64, device=dev)
         self.h = BtaHandle.get(b, nt, a)
         self.last = {}
 
@@ -222,38 +255,59 @@ class KronGaussianModel:
     def log_prior_grad(self, theta):
         return self.spec.log_prior_grad(theta)
 
-    def lik_theta_index(self):
-        return self.spec.lik_theta_index()
+    def lik_theta_indices(self):
+        return self.spec.lik_theta_indices()
+
+    def _check_variate_support(self, A, ov, av):
+        """Every observation must touch only its own variate's nodes and fixed effects
+        (the block-diagonal A of the reference's CoregionalModel, coregional_model.py:
+        203-214); the per-variate scaling of A^T A relies on it."""
+        if self.nv == 1:
+            return
+        Ac = A.tocoo()
+        col = Ac.col.astype(np.int64)
+        nbk = self.nt * self.b
+        field = col < nbk
+        cv = np.empty(col.size, dtype=np.int64)
+        cv[field] = (col[field] % self.b) // self.ns
+        cv[~field] = av[col[~field] - nbk]
+        if np.any(cv != ov[Ac.row]):
+            raise ValueError("an observation touches another variate's latent parameters")
 
     # ---------------------------------------------------------------- device steps
     def _ptr(self, t):
         return None if t is None else t.data_ptr()
 
     def _upload_coef(self, c: Coefficients):
+        """Copy alpha, beta and the per-variate tau_y into one device buffer; returns
+        the device pointers (alpha, beta, tau_y)."""
         K, nt = self.K, self.nt
-        buf = np.zeros(2 * K * nt)
+        buf = np.zeros(2 * K * nt + self.nv)
         buf[: K * nt] = c.alpha.reshape(-1)
         if nt > 1:
             buf[K * nt: K * nt + K * (nt - 1)] = c.beta.reshape(-1)
+        buf[2 * K * nt:] = c.tau_y
         self._coef.copy_(self.torch.from_numpy(buf), non_blocking=False)
-        return self._coef.data_ptr(), self._coef.data_ptr() + 8 * K * nt
+        p0 = self._coef.data_ptr()
+        return p0, p0 + 8 * K * nt, p0 + 8 * 2 * K * nt
 
-    def _assemble(self, alpha_p, beta_p, lik_scale, D, L, R, T, with_lik: bool):
+    def _assemble(self, coef_ptrs, D, L, R, T, with_lik: bool):
+        alpha_p, beta_p, tau_p = coef_ptrs
         lib, h = self.h.lib, self.h
         _lib.check(lib.gbta_assemble_kron(
             h.ptr, self.ns, self.nv, self.K, self._upat_rowptr.data_ptr(), self._upat_col.data_ptr(),
             self._uval.data_ptr(), self._term_vw.data_ptr(), alpha_p, beta_p,
             self._lik_rowptr.data_ptr() if with_lik else None, self._lik_col.data_ptr() if with_lik else None,
             self._lik_val.data_ptr() if with_lik else None, self._ptr(self._lik_R) if with_lik else None,
-            self._ptr(self._lik_T) if with_lik else None, float(lik_scale), self.tip_prec,
-            D.data_ptr(), L.data_ptr(), R.data_ptr(), T.data_ptr()))
+            self._ptr(self._lik_T) if with_lik else None, tau_p if with_lik else None,
+            self._ptr(self._arrow_var), self.tip_prec, D.data_ptr(), L.data_ptr(), R.data_ptr(), T.data_ptr()))
 
     def _contract(self, SD, SL, SR, ST, mu) -> np.ndarray:
         lib, h = self.h.lib, self.h
         _lib.check(lib.gbta_contract_kron(
             h.ptr, self.ns, self.nv, self.K, self._upat_rowptr.data_ptr(), self._upat_col.data_ptr(),
             self._uval.data_ptr(), self._term_vw.data_ptr(), self._lik_rowptr.data_ptr(), self._lik_col.data_ptr(),
-            self._lik_val.data_ptr(), self._ptr(self._lik_R), self._ptr(self._lik_T),
+            self._lik_val.data_ptr(), self._ptr(self._lik_R), self._ptr(self._lik_T), self._ptr(self._arrow_var),
             self._ptr(SD), self._ptr(SL), self._ptr(SR), self._ptr(ST), self._ptr(mu),
             self._contract_out.data_ptr()))
         return self._contract_out.cpu().numpy()
@@ -274,9 +328,8 @@ class KronGaussianModel:
         d = out[KN:2 * KN].reshape(K, nt)[:, : nt - 1]
         qc = out[2 * KN:3 * KN].reshape(K, nt)
         qd = out[3 * KN:4 * KN].reshape(K, nt)[:, : nt - 1]
-        lc = float(out[4 * KN:4 * KN + nt + 1].sum())
-        lq = float(out[4 * KN + nt + 1:4 * KN + 2 * (nt + 1)].sum())
-        return c, d, qc, qd, lc, lq
+        lik = out[4 * KN:4 * KN + 2 * self.nv * (nt + 1)].reshape(self.nv, 2, nt + 1).sum(axis=2)
+        return c, d, qc, qd, lik[:, 0], lik[:, 1]
 
     # ---------------------------------------------------------------- public
     def evaluate(self, theta, gradient: bool = False):
@@ -286,27 +339,29 @@ class KronGaussianModel:
         h.set_stream(current_stream_ptr())
         lib = h.lib
         coef = self.coefficients(theta)
-        alpha_p, beta_p = self._upload_coef(coef)
+        ptrs = self._upload_coef(coef)
         has_arrow = self.nb > 0
         # prior: bt factorization, tip excluded from the logdet (pyinla.py:1102-1103)
-        self._assemble(alpha_p, beta_p, 0.0, self.Dp, self.Lp, self.Rp, self.Tp, with_lik=False)
+        self._assemble(ptrs, self.Dp, self.Lp, self.Rp, self.Tp, with_lik=False)
         _lib.check(lib.gbta_pobtf(h.ptr, self.Dp.data_ptr(), self.Lp.data_ptr()))
         logdet_p = self._logdet(self.Dp, self.Tp, with_tip=False)
         # conditional: bta factorization (pyinla.py:650-662)
-        self._assemble(alpha_p, beta_p, coef.tau_y, self.Dc, self.Lc, self.Rc, self.Tc, with_lik=True)
+        self._assemble(ptrs, self.Dc, self.Lc, self.Rc, self.Tc, with_lik=True)
         R, T = (self.Rc.data_ptr(), self.Tc.data_ptr()) if has_arrow else (None, None)
         _lib.check(lib.gbta_pobtaf(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T))
         logdet_c = self._logdet(self.Dc, self.Tc, with_tip=has_arrow)
-        # mean: mu = Q_cond^{-1} tau_y A^T y (model.py:425-449 at x = 0)
-        self.mu.copy_(self._Aty)
-        self.mu.mul_(coef.tau_y)
+        # mean: mu = Q_cond^{-1} sum_v tau_y,v A_v^T y_v (model.py:425-449 at x = 0;
+        # per-variate likelihoods as in coregional_model.py:645-668)
+        tau_t = self.torch.from_numpy(coef.tau_y).to(self.mu.device)
+        self.mu.copy_(tau_t @ self._Aty_v)
         bvec = self.mu.clone()
         _lib.check(lib.gbta_pobtas_async(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T,
                                          self.mu.data_ptr(), 1, 0))
         _lib.check(lib.gbta_pobtas(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T, self.mu.data_ptr(), 1, 1))
         quad = float(self.torch.dot(self.mu, bvec))   # mu^T Q_cond mu = mu^T b
-        ty = self.lik_theta_index()
-        lik = 0.5 * self.n_obs * theta[ty] - 0.5 * coef.tau_y * self.yty   # gaussian.py:58-60, eta = 0
+        ty = np.asarray(self.lik_theta_indices(), dtype=np.int64)
+        # gaussian.py:58-60 at eta = 0, summed over the variates' likelihoods
+        lik = float(np.sum(0.5 * self.nobs_v * theta[ty] - 0.5 * coef.tau_y * self.yty_v))
         lp = self.log_prior(theta)
         f = -(lp + lik + 0.5 * logdet_p) + 0.5 * logdet_c - 0.5 * quad
         self.last = dict(logdet_prior=logdet_p, logdet_cond=logdet_c, quad=quad, lik=lik, log_prior=lp)
@@ -328,17 +383,18 @@ class KronGaussianModel:
         # prior selected inverse (bt)
         _lib.check(lib.gbta_pobtsi(h.ptr, self.Dp.data_ptr(), self.Lp.data_ptr()))
         pc, pd, _, _, _, _ = self._split(self._contract(self.Dp, self.Lp if self.nt > 1 else None, None, None, None))
+        mAty = (self._Aty_v @ self.mu).cpu().numpy()      # mu^T A_v^T y_v per variate
         d = dc.dalpha.shape[0]
         grad = np.zeros(d)
         for k in range(d):
-            da, db = dc.dalpha[k], dc.dbeta[k]
-            tr_c = float(np.sum(da * cc) + 2.0 * np.sum(db * dd) + dc.dtau_y[k] * lc)
+            da, db, dt = dc.dalpha[k], dc.dbeta[k], dc.dtau_y[k]
+            tr_c = float(np.sum(da * cc) + 2.0 * np.sum(db * dd) + dt @ lc)
             tr_p = float(np.sum(da * pc) + 2.0 * np.sum(db * pd))
-            mqm = float(np.sum(da * qc) + 2.0 * np.sum(db * qd) + dc.dtau_y[k] * lq)
-            mdb = dc.dtau_y[k] / coef.tau_y * quad        # mu^T d(b) with b = tau_y A^T y
+            mqm = float(np.sum(da * qc) + 2.0 * np.sum(db * qd) + dt @ lq)
+            mdb = float(dt @ mAty)                         # mu^T d(b), b = sum_v tau_y,v A_v^T y_v
             grad[k] = -0.5 * tr_p + 0.5 * tr_c - mdb + 0.5 * mqm
-        ty = self.lik_theta_index()
-        grad[ty] -= 0.5 * self.n_obs - 0.5 * coef.tau_y * self.yty
+        ty = np.asarray(self.lik_theta_indices(), dtype=np.int64)
+        grad[ty] -= 0.5 * self.nobs_v - 0.5 * coef.tau_y * self.yty_v
         grad -= self.log_prior_grad(theta)
         return grad
 
@@ -388,7 +444,7 @@ class SeparableSpdeAr1(KronSpec):
                            tau * np.outer(w, tdiag), np.zeros((self.K, self.nt))])
         dbeta = np.stack([tau * np.outer(dw, toff), tau * drho * np.outer(w, doff),
                           tau * np.outer(w, toff), np.zeros((self.K, max(self.nt - 1, 0)))])
-        return CoefficientDerivatives(dalpha=dalpha, dbeta=dbeta, dtau_y=np.array([0.0, 0.0, 0.0, tau_y]))
+        return CoefficientDerivatives(dalpha=dalpha, dbeta=dbeta, dtau_y=np.array([[0.0], [0.0], [0.0], [tau_y]]))
 
     @classmethod
     def synthetic(cls, n_side: int, nt: int, nb: int, n_obs: int, seed: int, theta0=None):
@@ -404,8 +460,8 @@ class SeparableSpdeAr1(KronSpec):
     def log_prior_grad(self, theta) -> np.ndarray:
         return -self.prior_prec * (theta - self.theta0)
 
-    def lik_theta_index(self) -> int:
-        return 3
+    def lik_theta_indices(self) -> list[int]:
+        return [3]
 
 
 def default_theta(rho: float = 0.9, kappa: float = None, tau: float = 1.0, tau_y: float = 4.0, ns: int = 1024):
@@ -415,3 +471,154 @@ def default_theta(rho: float = 0.9, kappa: float = None, tau: float = 1.0, tau_y
         kappa = np.sqrt(8.0) / 0.33
     r_t = -1.0 / np.log(rho)
     return np.array([np.log(kappa), np.log(r_t), np.log(tau), np.log(tau_y)])
+
+
+def coregional_loadings(lam: dict, nv: int) -> np.ndarray:
+    """Rows v_k of the coregional mixing: Q_re = sum_k sigma_k^-2 (v_k v_k^T) (x) Qu_k.
+
+    Read off the reference's block formulas (src/pyinla/models/coregional_model.py:
+    297-327 for two variates, :349-399 for three): v_0 = e_0, v_1 = (-l01, 1, 0),
+    v_2 = (-l12, -l02, 1), e.g. q21 = -l01/s1^2 Qu_1 + l02 l12/s2^2 Qu_2.
+    """
+    if nv == 1:
+        return np.ones((1, 1))
+    V = np.eye(nv)
+    V[1, 0] = -lam["0_1"]
+    if nv == 3:
+        V[2, 0] = -lam["1_2"]
+        V[2, 1] = -lam["0_2"]
+    elif nv != 2:
+        raise ValueError("the reference's coregional model has 2 or 3 variates")
+    return V
+
+
+class CoregionalSpdeAr1(KronSpec):
+    """nv-variate coregional spatio-temporal model with per-variate Gaussian likelihoods.
+
+    Mirrors the reference's CoregionalModel (src/pyinla/models/coregional_model.py):
+    each variate k has a unit-variance separable prior Qu_k = T_AR1(rho_k) (x)
+    Q_s(kappa_k) (its ``sigma`` hyperparameter is removed, coregional_model.py:107-118);
+    the mixing gives
+
+        Q_re = sum_k sigma_k^-2 (v_k v_k^T) (x) Qu_k          (coregional_loadings)
+
+    permuted to the BTA layout: block t = [variate 0 nodes, ..., variate nv-1 nodes]
+    (coregional_model.py:217-231, 754-786), fixed effects ordered per variate, each with
+    prior precision ``tip_prec`` (the regression submodel's block, appended with
+    bdiag_tiling at :490-497).  Q_cond = Q_prior + sum_v tau_y,v A_v^T A_v with the
+    block-diagonal A of the variates' design matrices (:203-214, 574-643).
+
+    The mixing (sigma_k, lambda) is held fixed; theta = (log kappa_k, log r_t,k,
+    log tau_y,k) for k = 0..nv-1 in that order (each variate's own parameters in
+    the reference's per-model order), with Gaussian priors N(theta0, 1/prior_prec).
+    The Kronecker terms are (S_j at variate block (p, q)) for the three spatial
+    matrices S_j and every pair (p, q): 3 nv^2 terms.
+    """
+
+    def __init__(self, mesh: spde.Mesh, nt: int, nb_per: int, nv: int, obs: spde.Observations, sigma, lam: dict,
+                 theta0: np.ndarray, prior_prec: float = 0.5, tip_prec: float = 1e-3):
+        self.mesh = mesh
+        self.nv, self.ns, self.nt = int(nv), mesh.ns, int(nt)
+        self.nb_per = int(nb_per)
+        self.nb = self.nv * self.nb_per
+        self.sigma = np.asarray(sigma, dtype=np.float64).reshape(self.nv)
+        self.lam = dict(lam)
+        self.V = coregional_loadings(self.lam, self.nv)
+        self.theta0 = np.asarray(theta0, dtype=np.float64).reshape(3 * self.nv)
+        self.prior_prec = float(prior_prec)
+        base = spde.spde_terms(mesh)
+        self.terms, self.term_vw, self._term_jpq = [], [], []
+        for j, S in enumerate(base):
+            for p in range(self.nv):
+                for q in range(self.nv):
+                    self.terms.append(S)
+                    self.term_vw.append((p, q))
+                    self._term_jpq.append((j, p, q))
+        self.A = spde.design_matrix(obs, mesh.ns, nt, self.nb_per, nv=self.nv)
+        self.y = obs.y
+        self.obs_variate = np.zeros(obs.y.shape[0], dtype=np.int64) if obs.v is None else np.asarray(obs.v)
+        self.arrow_variate = np.repeat(np.arange(self.nv), self.nb_per).astype(np.int32)
+        self.tip_prec = float(tip_prec)
+
+    def mixing_precision(self) -> np.ndarray:
+        """The nv x nv mixing precision sum_k sigma_k^-2 v_k v_k^T (SPD by construction)."""
+        return self.V.T @ np.diag(self.sigma ** -2.0) @ self.V
+
+    def _unpack(self, theta):
+        th = np.asarray(theta, dtype=np.float64).reshape(self.nv, 3)
+        kappa = np.exp(th[:, 0])
+        r_t = np.exp(th[:, 1])
+        rho = np.exp(-1.0 / r_t)
+        return kappa, r_t, rho, np.exp(th[:, 2])
+
+    def _mix(self, k, p, q):
+        return self.V[k, p] * self.V[k, q] / self.sigma[k] ** 2
+
+    def coefficients(self, theta) -> Coefficients:
+        kappa, r_t, rho, tau_y = self._unpack(theta)
+        nt, K = self.nt, self.K
+        alpha = np.zeros((K, nt))
+        beta = np.zeros((K, max(nt - 1, 0)))
+        for k in range(self.nv):
+            w = spde.spde_weights(kappa[k])
+            tdiag, toff = spde.ar1_bands(rho[k], nt)
+            for i, (j, p, q) in enumerate(self._term_jpq):
+                m = self._mix(k, p, q)
+                if m != 0.0:
+                    alpha[i] += m * w[j] * tdiag
+                    beta[i] += m * w[j] * toff
+        return Coefficients(alpha=alpha, beta=beta, tau_y=tau_y)
+
+    def coefficient_derivatives(self, theta) -> CoefficientDerivatives:
+        kappa, r_t, rho, tau_y = self._unpack(theta)
+        nt, K, nv = self.nt, self.K, self.nv
+        d = 3 * nv
+        dalpha = np.zeros((d, K, nt))
+        dbeta = np.zeros((d, K, max(nt - 1, 0)))
+        dtau = np.zeros((d, nv))
+        for k in range(nv):
+            w = spde.spde_weights(kappa[k])
+            dw = spde.spde_weights_dlogkappa(kappa[k])
+            tdiag, toff = spde.ar1_bands(rho[k], nt)
+            ddiag, doff = spde.ar1_bands_drho(rho[k], nt)
+            drho = rho[k] / r_t[k]
+            for i, (j, p, q) in enumerate(self._term_jpq):
+                m = self._mix(k, p, q)
+                if m == 0.0:
+                    continue
+                dalpha[3 * k, i] = m * dw[j] * tdiag
+                dbeta[3 * k, i] = m * dw[j] * toff
+                dalpha[3 * k + 1, i] = m * w[j] * drho * ddiag
+                dbeta[3 * k + 1, i] = m * w[j] * drho * doff
+            dtau[3 * k + 2, k] = tau_y[k]
+        return CoefficientDerivatives(dalpha=dalpha, dbeta=dbeta, dtau_y=dtau)
+
+    def log_prior(self, theta) -> float:
+        return float(-0.5 * self.prior_prec * np.sum((np.asarray(theta) - self.theta0) ** 2))
+
+    def log_prior_grad(self, theta) -> np.ndarray:
+        return -self.prior_prec * (np.asarray(theta) - self.theta0)
+
+    def lik_theta_indices(self) -> list[int]:
+        return [3 * k + 2 for k in range(self.nv)]
+
+    @classmethod
+    def synthetic(cls, n_side: int, nt: int, nb_per: int, nv: int, n_obs: int, seed: int, m_side: int = 0,
+                  theta0=None):
+        """Seeded synthetic instance: n_side x m_side mesh per variate, n_obs observations
+        split evenly over the variates, mixing sigma_k = exp(N(0, 0.2^2)) and
+        lambda ~ N(0, 0.5^2) drawn from the seed (so the nv x nv mixing precision is a
+        seeded SPD matrix)."""
+        mesh = spde.unit_square_mesh(n_side, m_side)
+        obs = spde.make_coregional_observations(mesh, nt, n_obs, nb_per, nv, seed)
+        rng = np.random.default_rng(seed + 7919)
+        sigma = np.exp(0.2 * rng.standard_normal(nv))
+        lam = {"0_1": 0.5 * rng.standard_normal(), "0_2": 0.5 * rng.standard_normal(),
+               "1_2": 0.5 * rng.standard_normal()}
+        if theta0 is None:
+            base = default_theta()
+            th = []
+            for k in range(nv):
+                th += [base[0] + 0.1 * k, base[1] - 0.1 * k, base[3] - 0.2 * k]
+            theta0 = np.array(th)
+        return cls(mesh, nt, nb_per, nv, obs, sigma, lam, np.asarray(theta0, dtype=np.float64))

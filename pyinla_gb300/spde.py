@@ -26,23 +26,31 @@ import scipy.sparse as sps
 
 @dataclass
 class Mesh:
-    n: int                   # nodes per side
+    n: int                   # nodes along x
     nodes: np.ndarray        # (ns, 2)
     tris: np.ndarray         # (ntri, 3)
     C: sps.csr_matrix        # lumped mass (diagonal)
     G: sps.csr_matrix        # P1 stiffness
+    m: int = 0               # nodes along y (0: same as n)
+
+    @property
+    def ny(self) -> int:
+        return self.m or self.n
 
     @property
     def ns(self) -> int:
-        return self.n * self.n
+        return self.n * self.ny
 
 
-def unit_square_mesh(n: int) -> Mesh:
-    """Regular n x n node grid on [0,1]^2, two triangles per cell, P1 FEM matrices."""
+def unit_square_mesh(n: int, m: int = 0) -> Mesh:
+    """Regular n x m node grid (m = n by default) on [0,1]^2, two triangles per cell,
+    P1 FEM matrices."""
+    m = m or n
     xs = np.linspace(0.0, 1.0, n)
-    X, Y = np.meshgrid(xs, xs, indexing="xy")
+    ys = np.linspace(0.0, 1.0, m)
+    X, Y = np.meshgrid(xs, ys, indexing="xy")
     nodes = np.stack([X.ravel(), Y.ravel()], axis=1)
-    idx = np.arange(n * n).reshape(n, n)   # idx[iy, ix]
+    idx = np.arange(n * m).reshape(m, n)   # idx[iy, ix]
     a = idx[:-1, :-1].ravel()
     b = idx[:-1, 1:].ravel()
     c = idx[1:, :-1].ravel()
@@ -55,13 +63,13 @@ def unit_square_mesh(n: int) -> Mesh:
     K = np.einsum("tid,tjd->tij", E, E) / (4.0 * area)[:, None, None]
     rows = np.repeat(tris, 3, axis=1).ravel()
     cols = np.tile(tris, (1, 3)).ravel()
-    ns = n * n
+    ns = n * m
     G = sps.csr_matrix((K.ravel(), (rows, cols)), shape=(ns, ns))
     G.sum_duplicates()
     cdiag = np.zeros(ns)
     np.add.at(cdiag, tris.ravel(), np.repeat(area / 3.0, 3))
     C = sps.diags(cdiag).tocsr()
-    return Mesh(n=n, nodes=nodes, tris=tris, C=C, G=G)
+    return Mesh(n=n, nodes=nodes, tris=tris, C=C, G=G, m=0 if m == n else m)
 
 
 def spde_terms(mesh: Mesh) -> list[sps.csr_matrix]:
@@ -116,18 +124,20 @@ class Observations:
     t: np.ndarray            # (nobs,) time step
     nodes: np.ndarray        # (nobs, 3) spatial node indices
     w: np.ndarray            # (nobs, 3) barycentric weights
-    z: np.ndarray            # (nobs, nb) covariates
+    z: np.ndarray            # (nobs, nb) covariates (nb per variate)
     y: np.ndarray            # (nobs,)
+    v: np.ndarray | None = None   # (nobs,) variate of each observation (None: all 0)
 
 
 def locate(mesh: Mesh, pts: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
     """Containing triangle's nodes and barycentric weights for points in [0,1]^2."""
-    n = mesh.n
-    h = 1.0 / (n - 1)
-    ix = np.clip((pts[:, 0] / h).astype(np.int64), 0, n - 2)
-    iy = np.clip((pts[:, 1] / h).astype(np.int64), 0, n - 2)
-    u = pts[:, 0] / h - ix
-    v = pts[:, 1] / h - iy
+    n, m = mesh.n, mesh.ny
+    hx = 1.0 / (n - 1)
+    hy = 1.0 / (m - 1)
+    ix = np.clip((pts[:, 0] / hx).astype(np.int64), 0, n - 2)
+    iy = np.clip((pts[:, 1] / hy).astype(np.int64), 0, m - 2)
+    u = pts[:, 0] / hx - ix
+    v = pts[:, 1] / hy - iy
     a = iy * n + ix
     b = a + 1
     c = a + n
@@ -148,13 +158,35 @@ def make_observations(mesh: Mesh, nt: int, nobs: int, nb: int, seed: int) -> Obs
     return Observations(t=t, nodes=nodes, w=w, z=z, y=y)
 
 
-def design_matrix(obs: Observations, ns: int, nt: int, nb: int) -> sps.csr_matrix:
-    """The observation matrix A (nobs x (nt*ns + nb)), latent order time-major then fixed effects."""
+def make_coregional_observations(mesh: Mesh, nt: int, nobs: int, nb_per: int, nv: int, seed: int) -> Observations:
+    """nobs observations split evenly over nv variates (ordered by variate, as the
+    reference concatenates its models' data, coregional_model.py:189-201); each has
+    the 3 barycentric weights of a uniform random location at a uniform random time
+    step of its own variate's field, nb_per N(0,1) covariates for its variate's fixed
+    effects, and y ~ N(0,1)."""
+    rng = np.random.default_rng(seed)
+    counts = [nobs // nv + (1 if v < nobs % nv else 0) for v in range(nv)]
+    v = np.repeat(np.arange(nv), counts)
+    pts = rng.random((nobs, 2))
+    t = rng.integers(0, nt, size=nobs)
+    nodes, w = locate(mesh, pts)
+    z = rng.standard_normal((nobs, nb_per))
+    y = rng.standard_normal(nobs)
+    return Observations(t=t, nodes=nodes, w=w, z=z, y=y, v=v)
+
+
+def design_matrix(obs: Observations, ns: int, nt: int, nb: int, nv: int = 1) -> sps.csr_matrix:
+    """The observation matrix A (nobs x (nt*nv*ns + nv*nb)), latent order time-major
+    (block t = [variate 0 nodes, ..., variate nv-1 nodes]) then the fixed effects
+    ordered per variate -- the coregional BTA layout (coregional_model.py:217-231,
+    754-786, 853-919).  ``nb`` is the number of fixed effects per variate."""
     nobs = obs.y.shape[0]
+    b = nv * ns
+    v = np.zeros(nobs, dtype=np.int64) if obs.v is None else np.asarray(obs.v, dtype=np.int64)
     rows = np.concatenate([np.repeat(np.arange(nobs), 3), np.repeat(np.arange(nobs), nb)])
-    cols = np.concatenate([(obs.t[:, None] * ns + obs.nodes).ravel(),
-                           np.tile(nt * ns + np.arange(nb), nobs)])
+    cols = np.concatenate([(obs.t[:, None] * b + v[:, None] * ns + obs.nodes).ravel(),
+                           (nt * b + v[:, None] * nb + np.arange(nb)[None, :]).ravel()])
     vals = np.concatenate([obs.w.ravel(), obs.z.ravel()])
-    A = sps.csr_matrix((vals, (rows, cols)), shape=(nobs, nt * ns + nb))
+    A = sps.csr_matrix((vals, (rows, cols)), shape=(nobs, nt * b + nv * nb))
     A.sum_duplicates()
     return A

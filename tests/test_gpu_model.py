@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from oracle import model_oracle as mo
-from pyinla_gb300.model import KronGaussianModel, SeparableSpdeAr1
+from pyinla_gb300.model import CoregionalSpdeAr1, KronGaussianModel, SeparableSpdeAr1
 
 pytestmark = pytest.mark.gpu
 
@@ -32,8 +32,8 @@ def built():
 def oracle_f(spec, theta):
     c = spec.coefficients(theta)
     f, aux = mo.objective(spec.terms, spec.term_vw, spec.ns, spec.nv, spec.nt, spec.nb, spec.A, spec.y,
-                          spec.tip_prec, c.alpha, c.beta, c.tau_y, theta[spec.lik_theta_index()],
-                          spec.log_prior(theta))
+                          spec.tip_prec, c.alpha, c.beta, c.tau_y, theta[spec.lik_theta_indices()],
+                          spec.log_prior(theta), spec.obs_variates())
     return f, aux
 
 
@@ -45,23 +45,33 @@ def test_device_assembly_matches_oracle(built, n_side, nt, nb, n_obs):
     m = KronGaussianModel(spec)
     theta = spec.theta0 + np.array([0.1, -0.1, 0.2, 0.3])
     c = spec.coefficients(theta)
-    ap, bp = m._upload_coef(c)
+    check_assembly(m, spec, theta)
+
+
+def check_assembly(m, spec, theta):
+    import torch
+
+    c = spec.coefficients(theta)
+    ptrs = m._upload_coef(c)
     m.h.set_stream(torch.cuda.current_stream().cuda_stream)
-    m._assemble(ap, bp, c.tau_y, m.Dc, m.Lc, m.Rc, m.Tc, with_lik=True)
-    m._assemble(ap, bp, 0.0, m.Dp, m.Lp, m.Rp, m.Tp, with_lik=False)
+    m._assemble(ptrs, m.Dc, m.Lc, m.Rc, m.Tc, with_lik=True)
+    m._assemble(ptrs, m.Dp, m.Lp, m.Rp, m.Tp, with_lik=False)
     torch.cuda.synchronize()
-    Qp = mo.kron_prior(spec.terms, spec.term_vw, c.alpha, c.beta, spec.ns, 1, nt, nb, spec.tip_prec)
-    Qc = Qp + c.tau_y * (spec.A.T @ spec.A)
+    nt, nb = spec.nt, spec.nb
+    Qp, Qc = spec.sparse_precisions(theta)
+    Qp_o = mo.kron_prior(spec.terms, spec.term_vw, c.alpha, c.beta, spec.ns, spec.nv, nt, nb, spec.tip_prec)
+    assert abs(Qp - Qp_o).max() <= 1e-13 * abs(Qp_o).max()
     for (D, L, R, T), Q in (((m.Dc, m.Lc, m.Rc, m.Tc), Qc), ((m.Dp, m.Lp, m.Rp, m.Tp), Qp)):
         Do, Lo, Ro, To = mo.sparse_to_bta(Q, nt, spec.b, nb)
         assert relerr(D.cpu().numpy(), Do) < 1e-13
         if nt > 1:
             assert relerr(L.cpu().numpy()[: nt - 1], Lo) < 1e-13
-        assert relerr(R.cpu().numpy(), Ro) < 1e-13
-        assert relerr(T.cpu().numpy(), To) < 1e-13
+        if nb:
+            assert relerr(R.cpu().numpy(), Ro) < 1e-13
+            assert relerr(T.cpu().numpy(), To) < 1e-13
     # deterministic: a second assembly is bit-identical
     D1 = m.Dc.clone()
-    m._assemble(ap, bp, c.tau_y, m.Dc, m.Lc, m.Rc, m.Tc, with_lik=True)
+    m._assemble(ptrs, m.Dc, m.Lc, m.Rc, m.Tc, with_lik=True)
     torch.cuda.synchronize()
     assert torch.equal(D1, m.Dc)
 
@@ -88,12 +98,16 @@ def test_adjoint_gradient_matches_dense_and_fd(built, n_side, nt, nb, n_obs):
     f, g = m.evaluate(theta, gradient=True)
     gd = mo.dense_gradient(spec.terms, spec.term_vw, spec.ns, spec.nv, spec.nt, spec.nb, spec.A, spec.y,
                            spec.tip_prec, spec.coefficients(theta), spec.coefficient_derivatives(theta),
-                           spec.lik_theta_index(), spec.log_prior_grad(theta))
+                           spec.lik_theta_indices(), spec.log_prior_grad(theta))
     assert relerr(g, gd) < 1e-8, (g, gd)
-    h = 1e-4
-    fd = np.zeros(4)
-    for k in range(4):
-        e = np.zeros(4)
+    check_fd(m, theta, g)
+
+
+def check_fd(m, theta, g, h=1e-4):
+    d = theta.size
+    fd = np.zeros(d)
+    for k in range(d):
+        e = np.zeros(d)
         e[k] = h
         fd[k] = (m.evaluate(theta + e) - m.evaluate(theta - e)) / (2 * h)
     assert relerr(g, fd) < 1e-6, (g, fd)
@@ -111,3 +125,30 @@ def test_autograd_function(built):
     f.backward()
     _, g = m.evaluate(th.detach().numpy(), gradient=True)
     assert relerr(th.grad.numpy(), g) < 1e-12
+
+
+# ---------------------------------------------------------------- coregional model
+@pytest.mark.parametrize("nv,n_side,m_side,nt,nb_per,n_obs", [(2, 4, 6, 4, 2, 800), (3, 5, 4, 3, 3, 1200),
+                                                               (2, 16, 24, 3, 2, 6000)])
+def test_coregional_assembly_matches_oracle(built, nv, n_side, m_side, nt, nb_per, n_obs):
+    """Coregional layout (block t = [variate nodes...]) with per-variate noise; the
+    last case is the 2-variate ns = 384 (b = 768) block of the mixed batch."""
+    spec = CoregionalSpdeAr1.synthetic(n_side, nt, nb_per, nv, n_obs, seed=11, m_side=m_side)
+    m = KronGaussianModel(spec)
+    check_assembly(m, spec, spec.theta0 + 0.05 * np.cos(np.arange(3 * nv)))
+
+
+@pytest.mark.parametrize("nv", [2, 3])
+def test_coregional_objective_and_gradient(built, nv):
+    spec = CoregionalSpdeAr1.synthetic(5, 4, 2, nv, 1500, seed=13, m_side=6)
+    m = KronGaussianModel(spec)
+    theta = spec.theta0 + 0.1 * np.sin(1.0 + np.arange(3 * nv))
+    f, g = m.evaluate(theta, gradient=True)
+    fo, aux = oracle_f(spec, theta)
+    assert abs(f - fo) <= 1e-10 * abs(fo), (f, fo)
+    assert relerr(m.mu.cpu().numpy(), aux["mu"]) < 1e-10
+    gd = mo.dense_gradient(spec.terms, spec.term_vw, spec.ns, spec.nv, spec.nt, spec.nb, spec.A, spec.y,
+                           spec.tip_prec, spec.coefficients(theta), spec.coefficient_derivatives(theta),
+                           spec.lik_theta_indices(), spec.log_prior_grad(theta), spec.obs_variates())
+    assert relerr(g, gd) < 1e-8, (g, gd)
+    check_fd(m, theta, g)

@@ -10,7 +10,7 @@ import pytest
 from oracle import bta_oracle as orc
 from oracle import model_oracle as mo
 from pyinla_gb300 import spde
-from pyinla_gb300.model import SeparableSpdeAr1, union_pattern
+from pyinla_gb300.model import CoregionalSpdeAr1, SeparableSpdeAr1, union_pattern
 
 
 def small_spec(seed=0, n_side=5, nt=4, nb=2, n_obs=300):
@@ -20,8 +20,8 @@ def small_spec(seed=0, n_side=5, nt=4, nb=2, n_obs=300):
 def oracle_f(spec, theta):
     c = spec.coefficients(theta)
     f, _ = mo.objective(spec.terms, spec.term_vw, spec.ns, spec.nv, spec.nt, spec.nb, spec.A, spec.y,
-                        spec.tip_prec, c.alpha, c.beta, c.tau_y, theta[spec.lik_theta_index()],
-                        spec.log_prior(theta))
+                        spec.tip_prec, c.alpha, c.beta, c.tau_y, theta[spec.lik_theta_indices()],
+                        spec.log_prior(theta), spec.obs_variates())
     return f
 
 
@@ -38,7 +38,7 @@ def test_oracle_objective_matches_dense():
     ld_c = np.linalg.slogdet(Qc)[1]
     assert abs(aux["logdet_prior"] - ld_p) < 1e-9 * abs(ld_p)
     assert abs(aux["logdet_cond"] - ld_c) < 1e-9 * abs(ld_c)
-    mu = np.linalg.solve(Qc, c.tau_y * (spec.A.T @ spec.y))
+    mu = np.linalg.solve(Qc, c.tau_y[0] * (spec.A.T @ spec.y))
     assert np.max(np.abs(aux["mu"] - mu)) < 1e-10 * np.max(np.abs(mu))
 
 
@@ -62,7 +62,7 @@ def test_dense_gradient_matches_central_differences():
     theta = spec.theta0 + np.array([0.2, 0.1, -0.3, 0.1])
     g = mo.dense_gradient(spec.terms, spec.term_vw, spec.ns, spec.nv, spec.nt, spec.nb, spec.A, spec.y,
                           spec.tip_prec, spec.coefficients(theta), spec.coefficient_derivatives(theta),
-                          spec.lik_theta_index(), spec.log_prior_grad(theta))
+                          spec.lik_theta_indices(), spec.log_prior_grad(theta))
     fd = mo.central_difference(lambda th: oracle_f(spec, th), theta, 1e-5)
     np.testing.assert_allclose(g, fd, rtol=1e-6, atol=1e-6 * np.max(np.abs(fd)))
 
@@ -75,3 +75,81 @@ def test_union_pattern_values():
         import scipy.sparse as sps
         R = sps.csr_matrix((uval[:, k], (rows, col)), shape=S.shape)
         assert abs(R - S).max() == 0.0
+
+
+# ---------------------------------------------------------------- coregional model
+def coreg_spec(nv, seed=0, n_side=4, m_side=5, nt=4, nb_per=2, n_obs=600):
+    return CoregionalSpdeAr1.synthetic(n_side, nt, nb_per, nv, n_obs, seed, m_side=m_side)
+
+
+def reference_coregional_prior(spec, theta):
+    """The reference's construction, restated: per-variate unit-variance priors Qu_k,
+    the q_ij blocks of src/pyinla/models/coregional_model.py:297-420 (variate-major
+    order), then the permutation to time-major interleaved blocks of
+    _generate_permutation_indices (:826-851)."""
+    import scipy.sparse as sps
+
+    kappa, r_t, rho, _ = spec._unpack(theta)
+    Qu = []
+    for k in range(spec.nv):
+        Qs = sum(w * S for w, S in zip(spde.spde_weights(kappa[k]), spde.spde_terms(spec.mesh)))
+        d, o = spde.ar1_bands(rho[k], spec.nt)
+        Qu.append(sps.kron(mo.temporal_matrix(d, o), Qs).tocsr())
+    s = spec.sigma
+    lam = spec.lam
+    if spec.nv == 2:
+        l01 = lam["0_1"]
+        q11 = Qu[0] / s[0] ** 2 + l01 ** 2 / s[1] ** 2 * Qu[1]
+        q21 = -l01 / s[1] ** 2 * Qu[1]
+        q22 = Qu[1] / s[1] ** 2
+        Q = sps.bmat([[q11, q21.T], [q21, q22]])
+    else:
+        l01, l02, l12 = lam["0_1"], lam["0_2"], lam["1_2"]
+        q11 = Qu[0] / s[0] ** 2 + l01 ** 2 / s[1] ** 2 * Qu[1] + l12 ** 2 / s[2] ** 2 * Qu[2]
+        q21 = -l01 / s[1] ** 2 * Qu[1] + l02 * l12 / s[2] ** 2 * Qu[2]
+        q31 = -l12 / s[2] ** 2 * Qu[2]
+        q22 = Qu[1] / s[1] ** 2 + l02 ** 2 / s[2] ** 2 * Qu[2]
+        q32 = -l02 / s[2] ** 2 * Qu[2]
+        q33 = Qu[2] / s[2] ** 2
+        Q = sps.bmat([[q11, q21.T, q31.T], [q21, q22, q32.T], [q31, q32, q33]])
+    n_re = spec.nt * spec.ns
+    idx = np.arange(n_re).reshape(spec.nt, spec.ns)
+    perm = np.hstack([idx + v * n_re for v in range(spec.nv)]).ravel()
+    return Q.tocsr()[perm][:, perm]
+
+
+@pytest.mark.parametrize("nv", [2, 3])
+def test_coregional_prior_matches_reference_blocks(nv):
+    spec = coreg_spec(nv)
+    theta = spec.theta0 + 0.05 * np.arange(3 * nv)
+    c = spec.coefficients(theta)
+    Qp = mo.kron_prior(spec.terms, spec.term_vw, c.alpha, c.beta, spec.ns, spec.nv, spec.nt, spec.nb, spec.tip_prec)
+    ref = reference_coregional_prior(spec, theta)
+    nbk = spec.nt * spec.b
+    assert abs(Qp[:nbk, :nbk] - ref).max() < 1e-12 * abs(ref).max()
+    tip = Qp[nbk:, nbk:].toarray()
+    assert np.array_equal(tip, spec.tip_prec * np.eye(spec.nb))
+    assert np.all(np.linalg.eigvalsh(spec.mixing_precision()) > 0)
+
+
+@pytest.mark.parametrize("nv", [2, 3])
+def test_coregional_design_matrix_layout(nv):
+    spec = coreg_spec(nv)
+    A = spec.A.tocoo()
+    ov = spec.obs_variates()
+    nbk = spec.nt * spec.b
+    field = A.col < nbk
+    assert np.all((A.col[field] % spec.b) // spec.ns == ov[A.row[field]])
+    assert np.all((A.col[~field] - nbk) // spec.nb_per == ov[A.row[~field]])
+    assert np.all(np.diff(ov) >= 0)
+
+
+@pytest.mark.parametrize("nv", [2, 3])
+def test_coregional_dense_gradient_matches_central_differences(nv):
+    spec = coreg_spec(nv, seed=4)
+    theta = spec.theta0 + 0.1 * np.sin(np.arange(3 * nv))
+    g = mo.dense_gradient(spec.terms, spec.term_vw, spec.ns, spec.nv, spec.nt, spec.nb, spec.A, spec.y,
+                          spec.tip_prec, spec.coefficients(theta), spec.coefficient_derivatives(theta),
+                          spec.lik_theta_indices(), spec.log_prior_grad(theta), spec.obs_variates())
+    fd = mo.central_difference(lambda th: oracle_f(spec, th), theta, 1e-5)
+    np.testing.assert_allclose(g, fd, rtol=1e-6, atol=1e-6 * np.max(np.abs(fd)))
