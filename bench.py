@@ -350,6 +350,186 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         dist.destroy_process_group()
 
 
+# ----------------------------------------------------------------------------- other workloads
+def batch41_shapes(seed: int = 41):
+    """41 instances (9 central-difference theta points + 32 grid points) of mixed
+    sizes, drawn from the seed: block size from univariate ns in {256, 512, 768} or a
+    2-variate coregional model with ns = 384 per variate (b = 768); nt in
+    {32, 64, 128, 256}; nb in {2, 4, 8}."""
+    rng = np.random.default_rng(seed)
+    kinds = [("uni256", 256), ("uni512", 512), ("uni768", 768), ("coreg2x384", 768)]
+    out = []
+    for _ in range(41):
+        kind, b = kinds[int(rng.integers(len(kinds)))]
+        nt = int(rng.choice([32, 64, 128, 256]))
+        nb = int(rng.choice([2, 4, 8]))
+        out.append((b, nt, nb, kind))
+    return out
+
+
+def run_batch41(args):
+    """All 41 instances in one graph-captured launch per run (factor, logdet, solve N+C,
+    selinv), methods from the autotuner; against the same instances one at a time
+    through the single-instance entry points."""
+    import torch
+
+    from pyinla_gb300 import _lib, autotune
+    from pyinla_gb300 import build as _build
+    from pyinla_gb300.batch import BtaBatch
+    from pyinla_gb300.device import BtaHandle
+    from pyinla_gb300.synthetic import random_bta
+
+    _build.build()
+    lib = _lib.load()
+    shapes4 = batch41_shapes()
+    shapes = [(b, nt, a) for (b, nt, a, _) in shapes4]
+    flops = sum(sum(bta_flops(nt, b, a)) for (b, nt, a) in shapes)
+    t0 = time.perf_counter()
+    methods = autotune.choose_methods(shapes)
+    t_tune_methods = time.perf_counter() - t0
+    bt = BtaBatch(shapes, methods=methods)
+
+    def refill():
+        for k, (b, nt, a) in enumerate(shapes):
+            D, L, R, T = random_bta(nt, b, a, seed=1000 + k)
+            bt.D[k].copy_(D)
+            bt.L[k].copy_(L)
+            bt.R[k].copy_(R)
+            bt.T[k].copy_(T)
+            bt.rhs[k].fill_(1.0)
+            del D, L, R, T
+
+    t0 = time.perf_counter()
+    order_ms = autotune.choose_order(bt, reload=refill)
+    t_tune_order = time.perf_counter() - t0
+    for _ in range(args.warmup):
+        refill()
+        bt.run(graph=True)
+    clocks = ClockSampler(0)
+    clocks.start()
+    times = []
+    launches0 = lib.gbta_kernel_launches()
+    for _ in range(args.steps):
+        refill()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        bt.run_async(graph=True)
+        e1.record()
+        bt.status()
+        times.append(e0.elapsed_time(e1))
+    launches = lib.gbta_kernel_launches() - launches0
+    clk = clocks.stop()
+    ms = statistics.median(times)
+    ws = bt.workspace_bytes()
+    graph_kernels = bt.graph_kernels()
+    # the same instances one at a time (single-instance entry points, same methods)
+    bt.close()
+    seq_ms = 0.0
+    stream = torch.cuda.current_stream()
+    for k, (b, nt, a) in enumerate(shapes):
+        h = BtaHandle(b, nt, a)
+        h.set_stream(stream.cuda_stream)
+        h.set_method(methods[k])
+        for rep in range(2):
+            D, L, R, T = random_bta(nt, b, a, seed=1000 + k)
+            x = torch.ones(nt * b + a, dtype=torch.float64, device="cuda")
+            ld = torch.zeros(1, dtype=torch.float64, device="cuda")
+            Rp, Tp = (R.data_ptr(), T.data_ptr()) if a else (None, None)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            _lib.check(lib.gbta_pobtaf_async(h.ptr, D.data_ptr(), L.data_ptr(), Rp, Tp))
+            _lib.check(lib.gbta_pobtas_async(h.ptr, D.data_ptr(), L.data_ptr(), Rp, Tp, x.data_ptr(), 1, 0))
+            _lib.check(lib.gbta_pobtas_async(h.ptr, D.data_ptr(), L.data_ptr(), Rp, Tp, x.data_ptr(), 1, 1))
+            _lib.check(lib.gbta_pobtasi_async(h.ptr, D.data_ptr(), L.data_ptr(), Rp, Tp))
+            e1.record()
+            h.status()
+            if rep:
+                seq_ms += e0.elapsed_time(e1)
+            del D, L, R, T
+        h.close()
+    line = {
+        "metric": METRIC, "value": flops / (ms * 1e-3) / 1e12, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded diagonally dominant SPD instances)",
+        "config": {"workload": "batch41_mixed", "instances": len(shapes),
+                   "shapes": [f"{kind}:b{b},nt{nt},nb{a}" for (b, nt, a, kind) in shapes4],
+                   "methods": methods, "order": bt.order, "order_ms": order_ms,
+                   "flops_per_step": flops, "workspace_bytes": ws,
+                   "step": "one graph launch: factor + logdet + solve N,C + selinv of all 41 instances",
+                   "tuning_s": {"methods": t_tune_methods, "order": t_tune_order}},
+        "graph_kernels": graph_kernels, "gpu_launches": int(launches),
+        "sequential_ms": seq_ms, "batch_speedup_vs_sequential": seq_ms / ms, "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_coreg3(args):
+    """3-variate coregional model (ns = 1024 per variate, b = 3072, nt = 64, nb = 9,
+    300 000 observations): factor and selected inversion throughput of Q_cond and the
+    adjoint theta-gradient (d = 9) against one plain evaluation and central FD."""
+    import torch
+
+    from pyinla_gb300 import _lib
+    from pyinla_gb300 import build as _build
+    from pyinla_gb300.model import CoregionalSpdeAr1, KronGaussianModel
+
+    _build.build()
+    lib = _lib.load()
+    t0 = time.perf_counter()
+    spec = CoregionalSpdeAr1.synthetic(32, 64, 3, 3, 300000, seed=5)
+    model = KronGaussianModel(spec)
+    t_setup = time.perf_counter() - t0
+    theta = spec.theta0
+    b, nt, a = model.b, model.nt, model.nb
+    ff, fs = bta_flops(nt, b, a)
+    h = model.h
+    h.set_stream(torch.cuda.current_stream().cuda_stream)
+    coef = spec.coefficients(theta)
+    Dc, Lc, Rc, Tc = model.Dc, model.Lc, model.Rc, model.Tc
+    fac, sel = [], []
+    for s in range(args.warmup + args.steps):
+        ptrs = model._upload_coef(coef)
+        model._assemble(ptrs, Dc, Lc, Rc, Tc, with_lik=True)
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record()
+        _lib.check(lib.gbta_pobtaf_async(h.ptr, Dc.data_ptr(), Lc.data_ptr(), Rc.data_ptr(), Tc.data_ptr()))
+        e[1].record()
+        _lib.check(lib.gbta_pobtasi_async(h.ptr, Dc.data_ptr(), Lc.data_ptr(), Rc.data_ptr(), Tc.data_ptr()))
+        e[2].record()
+        h.status()
+        if s >= args.warmup:
+            fac.append(e[0].elapsed_time(e[1]))
+            sel.append(e[1].elapsed_time(e[2]))
+    model.evaluate(theta)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    model.evaluate(theta)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    model.evaluate(theta, gradient=True)
+    torch.cuda.synchronize()
+    t_grad = time.perf_counter() - t0
+    d = theta.size
+    fm, sm = statistics.median(fac), statistics.median(sel)
+    line = {
+        "metric": METRIC, "value": (ff + fs) / ((fm + sm) * 1e-3) / 1e12, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": fm + sm, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": "coreg3_spde32x32_ar1_nt64_nb9_obs300k", "b": b, "nt": nt, "a": a,
+                   "flops_factor": ff, "flops_selinv": fs, "host_setup_s": t_setup},
+        "phases_ms": {"factor": fm, "selinv": sm},
+        "adjoint": {"plain_eval_ms": t_plain * 1e3, "value_and_grad_ms": t_grad * 1e3,
+                    "ratio_vs_plain": t_grad / t_plain, "central_fd_ratio": 2 * d + 1,
+                    "speedup_vs_fd": (2 * d + 1) * t_plain / t_grad, "dim_theta": int(d)},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--gpus", type=int, default=1)
@@ -360,7 +540,14 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["spde", "batch41", "coreg3"], default="spde",
+                    help="spde: the headline single-model step (default); batch41: the mixed 41-instance "
+                         "graph-captured launch; coreg3: the 3-variate coregional model with adjoint")
     args = ap.parse_args()
+    if args.impl == "ours" and args.workload == "batch41":
+        return run_batch41(args)
+    if args.impl == "ours" and args.workload == "coreg3":
+        return run_coreg3(args)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.impl == "reference" else 1)))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))

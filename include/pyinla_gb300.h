@@ -221,6 +221,56 @@ int gbta_contract_kron(gbta_solver* s, int ns, int nv, int nterms, const int* up
                        const double* lik_R, const double* lik_T, const int* arrow_variate, const double* SD,
                        const double* SL, const double* SR, const double* ST, const double* mu, double* out);
 
+/* ---- many instances in one persistent launch per phase -------------------- */
+/* A batch holds n independent BTA instances of arbitrary geometry (b[k], nt[k], a[k];
+ * a[k] = 0: block tridiagonal) -- the Q(theta) of a gradient's central-difference
+ * points, a Hessian or a theta grid (the reference evaluates them one at a time,
+ * src/pyinla/core/pyinla.py:512-600, 747-910), including coregional instances of other
+ * block sizes.  Each phase of all instances runs as ONE persistent launch that hands
+ * out the tasks of every instance from a merged ticket order.  No reference
+ * counterpart as an interface: per instance the results equal gbta_pobtaf /
+ * gbta_logdet / gbta_pobtas (N then C, one right-hand side) / gbta_pobtasi.
+ * methods[k] (NULL = all GBTA_METHOD_OZAKI) fixes each instance's product method and
+ * is chosen at creation because it sizes the workspace.  The batch owns its workspace
+ * and a non-blocking stream. */
+typedef struct gbta_batch gbta_batch;
+
+#define GBTA_PHASE_FACTOR 1   /* pobtaf (pobtf when a = 0) */
+#define GBTA_PHASE_LOGDET 2   /* logdet of the factor into logdet_out[k] (device) */
+#define GBTA_PHASE_SOLVE 4    /* pobtas N then C on rhs[k] (one column, in place) */
+#define GBTA_PHASE_SELINV 8   /* pobtasi: the factor blocks become Sigma */
+
+/* Ticket order of the merged task lists. */
+#define GBTA_BATCH_ORDER_PROPORTIONAL 0   /* every instance advances at the same fraction */
+#define GBTA_BATCH_ORDER_ROUND_ROBIN 1    /* one task of each instance in turn */
+#define GBTA_BATCH_ORDER_SEQUENTIAL 2     /* instance after instance */
+
+int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const int* methods, gbta_batch** out);
+int gbta_batch_destroy(gbta_batch* bt);
+size_t gbta_batch_workspace_bytes(const gbta_batch* bt);
+/* Work goes to `stream` (NULL = CUDA default stream; graph launches need another). */
+int gbta_batch_set_stream(gbta_batch* bt, void* stream);
+int gbta_batch_set_order(gbta_batch* bt, int policy);
+int gbta_batch_set_wait_limit_ms(gbta_batch* bt, double ms);
+/* Bind the instances' device blocks: arrays (host) of n device pointers in the
+ * Serinv layout; R, T may be NULL (or hold NULL) for a[k] = 0; rhs may be NULL when
+ * the solve phase is not used.  The pointers must stay valid for every later run and
+ * every replay of a captured graph. */
+int gbta_batch_bind(gbta_batch* bt, double* const* D, double* const* L, double* const* R, double* const* T,
+                    double* const* rhs);
+/* Enqueue the phases (GBTA_PHASE_* bits) of every instance on the batch stream, in
+ * the order factor, logdet, solve, selected inversion.  No host synchronisation. */
+int gbta_batch_run_async(gbta_batch* bt, int phases, double* logdet_out);
+/* The same, captured once into a CUDA graph (re-captured when phases or logdet_out
+ * change) and launched: one graph launch per call. */
+int gbta_batch_graph_launch(gbta_batch* bt, int phases, double* logdet_out);
+/* Kernels one replay of the captured graph launches. */
+long long gbta_batch_graph_kernels(const gbta_batch* bt);
+/* Wait for the stream.  Returns 0, GBTA_ERR_TIMEOUT, or the pivot row (> 0) of the
+ * first instance that is not positive definite; info[k] (host, may be NULL) receives
+ * every instance's pivot row (0 = fine). */
+int gbta_batch_status(gbta_batch* bt, int* info);
+
 #ifdef __cplusplus
 }
 #endif

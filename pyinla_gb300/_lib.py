@@ -22,6 +22,14 @@ GBTA_ERR_ALLOC = -5
 GBTA_METHOD_FP64 = 0
 GBTA_METHOD_OZAKI = 1
 GBTA_MAX_VARIATES = 8        # include/pyinla_gb300.h
+GBTA_PHASE_FACTOR = 1
+GBTA_PHASE_LOGDET = 2
+GBTA_PHASE_SOLVE = 4
+GBTA_PHASE_SELINV = 8
+GBTA_PHASE_ALL = 15
+GBTA_BATCH_ORDER_PROPORTIONAL = 0
+GBTA_BATCH_ORDER_ROUND_ROBIN = 1
+GBTA_BATCH_ORDER_SEQUENTIAL = 2
 
 _lib = None
 _lock = threading.Lock()
@@ -69,6 +77,17 @@ SIGNATURES = {
                                     _vp, _vp, _vp, _vp, ctypes.c_double, _vp, _vp, _vp, _vp]),
     "gbta_contract_kron": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                     _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gbta_batch_create": (_c_int, [_c_int, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
+    "gbta_batch_destroy": (_c_int, [_vp]),
+    "gbta_batch_workspace_bytes": (ctypes.c_size_t, [_vp]),
+    "gbta_batch_set_stream": (_c_int, [_vp, _vp]),
+    "gbta_batch_set_order": (_c_int, [_vp, _c_int]),
+    "gbta_batch_set_wait_limit_ms": (_c_int, [_vp, ctypes.c_double]),
+    "gbta_batch_bind": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "gbta_batch_run_async": (_c_int, [_vp, _c_int, _vp]),
+    "gbta_batch_graph_launch": (_c_int, [_vp, _c_int, _vp]),
+    "gbta_batch_graph_kernels": (_c_ll, [_vp]),
+    "gbta_batch_status": (_c_int, [_vp, _vp]),
 }
 
 

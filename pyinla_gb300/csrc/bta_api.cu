@@ -70,6 +70,40 @@ struct gbta_solver {
   long long trace_n = 0;          // records of the last traced launch
 };
 
+namespace gbta {
+
+// Task lists in a topological order of the dataflow DAGs (each task only waits for
+// tasks earlier in the list, so the ticket dispenser cannot deadlock).
+std::vector<int4> factor_task_list(const Geom& g) {
+  std::vector<int4> t;
+  for (int i = 0; i < g.nt; ++i)
+    for (int c = 0; c < g.B; ++c) {
+      t.push_back(make_int4(FT_DIAG, i, c, c));
+      for (int r = c + 1; r < g.B; ++r) t.push_back(make_int4(FT_OFFD, i, r, c));
+      if (i < g.nt - 1)
+        for (int r = 0; r < g.B; ++r) t.push_back(make_int4(FT_LOW, i, r, c));
+      if (g.a > 0) t.push_back(make_int4(FT_ARW, i, 0, c));
+    }
+  if (g.a > 0) t.push_back(make_int4(FT_TIP, 0, 0, 0));
+  return t;
+}
+
+std::vector<int4> selinv_task_list(const Geom& g) {
+  std::vector<int4> t;
+  if (g.a > 0) t.push_back(make_int4(ST_TIP, 0, 0, 0));
+  for (int i = g.nt - 1; i >= 0; --i)
+    for (int c = g.B - 1; c >= 0; --c) {
+      if (g.a > 0) t.push_back(make_int4(ST_OFF, i, 2 * g.B, c));
+      if (i < g.nt - 1)
+        for (int r = 0; r < g.B; ++r) t.push_back(make_int4(ST_OFF, i, g.B + r, c));
+      for (int r = c + 1; r < g.B; ++r) t.push_back(make_int4(ST_OFF, i, r, c));
+      t.push_back(make_int4(ST_DIAG, i, c, c));
+    }
+  return t;
+}
+
+}  // namespace gbta
+
 namespace {
 
 int grid_of(const gbta_solver* s, int ntasks) {
@@ -99,34 +133,6 @@ gbta::LaunchCtl next_launch(gbta_solver* s, int ntasks) {
 int reset_ticket(gbta_solver* s) {
   GBTA_CUDA(cudaMemsetAsync(s->d_ctrl, 0, 2 * sizeof(int), s->stream));
   return GBTA_OK;
-}
-
-std::vector<int4> factor_tasks(const gbta::Geom& g) {
-  std::vector<int4> t;
-  for (int i = 0; i < g.nt; ++i)
-    for (int c = 0; c < g.B; ++c) {
-      t.push_back(make_int4(gbta::FT_DIAG, i, c, c));
-      for (int r = c + 1; r < g.B; ++r) t.push_back(make_int4(gbta::FT_OFFD, i, r, c));
-      if (i < g.nt - 1)
-        for (int r = 0; r < g.B; ++r) t.push_back(make_int4(gbta::FT_LOW, i, r, c));
-      if (g.a > 0) t.push_back(make_int4(gbta::FT_ARW, i, 0, c));
-    }
-  if (g.a > 0) t.push_back(make_int4(gbta::FT_TIP, 0, 0, 0));
-  return t;
-}
-
-std::vector<int4> selinv_tasks(const gbta::Geom& g) {
-  std::vector<int4> t;
-  if (g.a > 0) t.push_back(make_int4(gbta::ST_TIP, 0, 0, 0));
-  for (int i = g.nt - 1; i >= 0; --i)
-    for (int c = g.B - 1; c >= 0; --c) {
-      if (g.a > 0) t.push_back(make_int4(gbta::ST_OFF, i, 2 * g.B, c));
-      if (i < g.nt - 1)
-        for (int r = 0; r < g.B; ++r) t.push_back(make_int4(gbta::ST_OFF, i, g.B + r, c));
-      for (int r = c + 1; r < g.B; ++r) t.push_back(make_int4(gbta::ST_OFF, i, r, c));
-      t.push_back(make_int4(gbta::ST_DIAG, i, c, c));
-    }
-  return t;
 }
 
 int check_solver(const gbta_solver* s) {
@@ -189,7 +195,7 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   CREATE_CUDA(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
   s->stream = s->own_stream;
 
-  const std::vector<int4> ft = factor_tasks(s->g), st = selinv_tasks(s->g);
+  const std::vector<int4> ft = gbta::factor_task_list(s->g), st = gbta::selinv_task_list(s->g);
   s->n_ftasks = (int)ft.size();
   s->n_stasks = (int)st.size();
   const size_t ntile = (size_t)nt * s->g.B;

@@ -1,0 +1,497 @@
+// Per-task bodies of the BTA factorization, shared by the single-instance kernels
+// (bta_factor.cu, bta_factor_oz.cu) and the multi-instance kernel (bta_batch.cu).
+//
+// BTA Cholesky factorization (Serinv pobtaf / pobtf) as one persistent dataflow kernel.
+//
+// Replaces the sequential block recurrence that the reference runs through Serinv
+// (src/pyinla/solvers/structured_solver.py:83-93):
+//   D_i <- chol(D_i); L_i <- L_i D_i^{-T}; R_i <- R_i D_i^{-T};
+//   D_{i+1} -= L_i L_i^T; R_{i+1} -= R_i L_i^T; T -= R_i R_i^T; T <- chol(T)
+// by a left-looking tile Cholesky of the banded tile matrix.  One task finalises one
+// TS x TS tile of D_i (lower), L_i or R_i: it subtracts the products of already
+// final tiles to its left (including the previous block column, which is the
+// Schur update D_{i+1} -= L_i L_i^T / R_{i+1} -= R_i L_i^T), then factors (diagonal
+// tile) or solves against the diagonal tile of its column.  Tiles of the next
+// block start as soon as the panels they need are final, so consecutive diagonal
+// blocks overlap instead of running one after the other.
+//
+// Two ways to compute the tile products of the left-looking loop (FactorArgs::method):
+//  * FP64: FP64 FMAs on staged FP64 tiles (factor_fp64_task);
+//  * OZAKI: the tiles' digit planes (written by the tasks that finalised them) go
+//    through mma.sync with exact fp32 accumulation, folded into FP64 every OZ_CHUNK
+//    steps (factor_oz_task, see bta_ozaki.cuh).
+// Both share the task DAG, the ordering and the FP64 epilogues: tile factorizations
+// (POTRF), triangular solves (TRSM) and the arrow-tip partials.
+#pragma once
+
+#include "bta_ozaki.cuh"
+
+namespace gbta {
+
+// Arguments of one factorization instance (both product methods).
+struct FactorArgs {
+  double* D;
+  double* L;
+  double* R;
+  double* T;
+  Geom g;
+  int use_arrow;
+  int method;           // GBTA_METHOD_FP64 / GBTA_METHOD_OZAKI
+  const int4* tasks;
+  int ntasks;
+  double* tip_part;     // [nt*B] tiles of R_i(c) R_i(c)^T (a x a used)
+  __half* digits;       // Ozaki: [nflags][OZ_TILE] digit planes of the final tiles
+  const int* erow;      // Ozaki: [nt*b + a] row exponents
+  int* info;            // where a failed pivot is recorded (null: the control block)
+  Ctl c;
+};
+
+static __device__ __forceinline__ const double* Dblk(const FactorArgs& p, int i) {
+  return p.D + (size_t)i * p.g.b * p.g.b;
+}
+static __device__ __forceinline__ const double* Lblk(const FactorArgs& p, int i) {
+  return p.L + (size_t)i * p.g.b * p.g.b;
+}
+static __device__ __forceinline__ const double* Rblk(const FactorArgs& p, int i) {
+  return p.R + (size_t)i * p.g.a * p.g.b;
+}
+
+// Tile (r, c) of a b x b block / column tile c of an a x b arrow block.
+static __device__ __forceinline__ Tile btile(const double* blk, const Geom& g, int r, int c) {
+  return make_tile(blk, g.b, r * TS, c * TS, g.b, g.b);
+}
+static __device__ __forceinline__ Tile atile(const double* blk, const Geom& g, int c) {
+  return make_tile(blk, g.b, 0, c * TS, g.a, g.b);
+}
+
+// Stage the diagonal factor tile D_i(c, c) (identity padded) after waiting for it.
+static __device__ bool load_diag_factor(const FactorArgs& p, int i, int c, double* F, int* s_ok) {
+  if (!cta_wait(p.c, p.c.flags + p.g.fD(i, c, c), nullptr, s_ok)) return false;
+  tile_load(F, btile(Dblk(p, i), p.g, c, c));
+  __syncthreads();
+  tile_pad_identity(F, p.g.vrows(c));
+  __syncthreads();
+  return true;
+}
+
+// Shared memory of the FP64 factor task: 4 tiles (K-loop double buffer; the target X
+// and the diagonal factor F alias its first two, used only before / after the loop),
+// TS pivots, and the wait flag.
+constexpr size_t FP64F_SMEM = 4 * TILE_SMEM * sizeof(double) + TS * sizeof(double);
+
+// Task t of a FP64-product factorization instance.  `raw` is FP64F_SMEM bytes of
+// shared memory.  Returns false when the launch is aborted.
+static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int t, unsigned char* raw, int* s_okp) {
+  double* sm = reinterpret_cast<double*>(raw);
+  double* vec = sm + 4 * TILE_SMEM;     // pivots' 1/sqrt, or reciprocals of a factor tile's diagonal
+  double* bufs = sm;
+  double* X = sm;
+  double* F = sm + TILE_SMEM;
+  int& s_ok = *s_okp;
+  const Geom& g = p.g;
+  const Ctl& c = p.c;
+  int* info_slot = p.info ? p.info : c.ctrl + CTRL_INFO;
+  {
+    const unsigned long long t_task0 = c.trace ? gtimer() : 0ull;
+    const int4 tk = p.tasks[t];
+    const int type = tk.x, i = tk.y, r = tk.z, col = tk.w;
+    if (!p.use_arrow && (type == FT_ARW || type == FT_TIP)) return true;
+
+    Acc acc;
+    if (type == FT_TIP) {
+      // T -= sum_{i,c} R_i(c) R_i(c)^T in a fixed order, then chol(T) (a <= TS).
+      tile_load(X, make_tile(p.T, g.a, 0, 0, g.a, g.a));
+      __syncthreads();
+      acc_from_smem(acc, X);
+      bool ok = true;
+      for (int k = 0; k < g.nt * g.B && ok; ++k) {
+        ok = cta_wait(c, c.flags + g.fR(k / g.B, k % g.B), nullptr, &s_ok);
+        if (!ok) break;
+        const double* P = p.tip_part + (size_t)k * TS * TS;
+#pragma unroll
+        for (int ii = 0; ii < 2; ++ii)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc.v[ii][q] -= __ldcg(P + acc_row(ii) * TS + acc_col(q));
+      }
+      if (!ok) return false;
+      acc_to_smem(acc, X);
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < TS * TS; idx += NT) {   // zero padding, identity diagonal
+        const int rr = idx / TS, cc = idx % TS;
+        if (rr >= g.a || cc >= g.a) X[rr * LDS + cc] = (rr == cc) ? 1.0 : 0.0;
+      }
+      const int info = smem_potrf(X, vec);
+      if (info) {
+        if (threadIdx.x == 0) {
+          atomicCAS(info_slot, 0, g.nt * g.b + info);
+          raise_abort(c);
+        }
+        return false;
+      }
+      tile_store(p.T, g.a, g.a, g.a, X);
+      cta_publish(c, c.flags + g.fT());
+      trace_task(c, t, type, t_task0);
+      return true;
+    }
+
+    // ---- K-loop: subtract products of final tiles left of the target.
+    // Target row operand source for within-block (k < col) and previous-block terms.
+    const double* tgt_blk;
+    Tile tgt;
+    int* tgt_flag;
+    if (type == FT_DIAG || type == FT_OFFD) {
+      tgt_blk = Dblk(p, i);
+      tgt = btile(tgt_blk, g, r, col);
+      tgt_flag = c.flags + g.fD(i, r, col);
+    } else if (type == FT_LOW) {
+      tgt_blk = Lblk(p, i);
+      tgt = btile(tgt_blk, g, r, col);
+      tgt_flag = c.flags + g.fL(i, r, col);
+    } else {   // FT_ARW
+      tgt_blk = Rblk(p, i);
+      tgt = atile(tgt_blk, g, col);
+      tgt_flag = c.flags + g.fR(i, col);
+    }
+    tile_load(X, tgt);
+    __syncthreads();
+    acc_from_smem(acc, X);
+    __syncthreads();
+
+    const bool prev = (i > 0) && (type != FT_LOW);
+    const int nprev = prev ? g.B : 0;
+    const int nsteps = nprev + col;
+    auto step_of = [&](int s) -> Step {
+      Step st;
+      st.ta = false;
+      st.tb = true;
+      if (s < nprev) {   // previous block column: Schur terms with L_{i-1}
+        const int k = s;
+        if (type == FT_ARW) {
+          st.a = atile(Rblk(p, i - 1), g, k);
+          st.fa = c.flags + g.fR(i - 1, k);
+        } else {
+          st.a = btile(Lblk(p, i - 1), g, r, k);
+          st.fa = c.flags + g.fL(i - 1, r, k);
+        }
+        st.b = btile(Lblk(p, i - 1), g, col, k);
+        st.fb = c.flags + g.fL(i - 1, col, k);
+      } else {           // within the block column: tiles k < col of the same row
+        const int k = s - nprev;
+        if (type == FT_ARW) {
+          st.a = atile(Rblk(p, i), g, k);
+          st.fa = c.flags + g.fR(i, k);
+        } else if (type == FT_LOW) {
+          st.a = btile(Lblk(p, i), g, r, k);
+          st.fa = c.flags + g.fL(i, r, k);
+        } else {
+          st.a = btile(Dblk(p, i), g, r, k);
+          st.fa = c.flags + g.fD(i, r, k);
+        }
+        st.b = btile(Dblk(p, i), g, col, k);
+        st.fb = c.flags + g.fD(i, col, k);
+        if (st.fa == st.fb) st.fb = nullptr;
+      }
+      return st;
+    };
+    if (!kloop<true>(acc, nsteps, step_of, c, bufs, &s_ok)) return false;
+    acc_to_smem(acc, X);
+    __syncthreads();
+
+    if (type == FT_DIAG) {
+      tile_pad_identity(X, g.vrows(col));
+      const int info = smem_potrf(X, vec);
+      if (info) {
+        if (threadIdx.x == 0) {
+          atomicCAS(info_slot, 0, i * g.b + col * TS + info);
+          raise_abort(c);
+        }
+        return false;
+      }
+      tile_store(const_cast<double*>(tgt.p), g.b, tgt.rows, tgt.cols, X);
+      cta_publish(c, tgt_flag);
+      trace_task(c, t, type, t_task0);
+      return true;
+    }
+
+    // Off-diagonal targets: X <- X * D_i(col,col)^{-T}.
+    if (!load_diag_factor(p, i, col, F, &s_ok)) return false;
+    tile_diag_recip(F, vec);
+    smem_trsm_rlt(X, F, vec);
+    tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
+    if (type == FT_OFFD) {
+      // The factor's strict upper triangle is zero: clear the mirrored tile.
+      const Tile up = btile(Dblk(p, i), g, col, r);
+      tile_store_zero(const_cast<double*>(up.p), g.b, up.rows, up.cols);
+    }
+    if (type == FT_ARW) {
+      // Partial tip update P = X X^T, consumed in order by the tip task.
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < TS * TS; idx += NT) F[(idx % TS) * LDS + idx / TS] = X[(idx / TS) * LDS + idx % TS];
+      __syncthreads();
+      Acc pacc;
+      acc_zero(pacc);
+      tile_mma<false>(pacc, X, F);
+      double* P = p.tip_part + (size_t)(i * g.B + col) * TS * TS;
+#pragma unroll
+      for (int ii = 0; ii < 2; ++ii)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) P[acc_row(ii) * TS + acc_col(q)] = pacc.v[ii][q];
+    }
+    cta_publish(c, tgt_flag);
+    trace_task(c, t, type, t_task0);
+  }
+  return true;
+}
+
+// dynamic shared memory layout
+constexpr int OZF_STAGE_HALVES = 2 * OZ_OPER;   // A and B operand of one stage
+constexpr size_t OZF_SMEM = 2 * OZF_STAGE_HALVES * sizeof(__half) + 2 * TILE_SMEM * sizeof(double) +
+                            TS * sizeof(double) + 2 * TS * sizeof(int);
+
+// Shared-memory views of one CTA (carved from the dynamic buffer by oz_factor_smem).
+struct OzFactorSmem {
+  __half* stages;
+  double* X;
+  double* F;
+  double* vec;
+  int* erow_t;   // exponents of the target's rows
+  int* ecol_t;   // exponents of the target's columns
+  int* s_ok;
+  int* s_ready;
+};
+
+static __device__ __forceinline__ OzFactorSmem oz_factor_smem(unsigned char* raw, int* s_ok, int* s_ready) {
+  OzFactorSmem m;
+  m.stages = reinterpret_cast<__half*>(raw);
+  m.X = reinterpret_cast<double*>(raw + 2 * OZF_STAGE_HALVES * sizeof(__half));
+  m.F = m.X + TILE_SMEM;
+  m.vec = m.F + TILE_SMEM;
+  m.erow_t = reinterpret_cast<int*>(m.vec + TS);
+  m.ecol_t = m.erow_t + TS;
+  m.s_ok = s_ok;
+  m.s_ready = s_ready;
+  return m;
+}
+
+// Task t of the instance described by p.  Returns false when the launch is aborted
+// (a failed pivot or a wait that ran out).
+static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t, const OzFactorSmem& sm) {
+  __half* stages = sm.stages;
+  double* X = sm.X;
+  double* F = sm.F;
+  double* vec = sm.vec;
+  int* erow_t = sm.erow_t;
+  int* ecol_t = sm.ecol_t;
+  int& s_ok = *sm.s_ok;
+  int& s_ready = *sm.s_ready;
+  const Geom& g = p.g;
+  const Ctl& c = p.c;
+  int* info_slot = p.info ? p.info : c.ctrl + CTRL_INFO;
+  {
+    const unsigned long long t_task0 = c.trace ? gtimer() : 0ull;
+    const int4 tk = p.tasks[t];
+    const int type = tk.x, i = tk.y, r = tk.z, col = tk.w;
+    if (!p.use_arrow && (type == FT_ARW || type == FT_TIP)) return true;
+    const size_t bb = (size_t)g.b * g.b, ab = (size_t)g.a * g.b;
+
+    if (type == FT_TIP) {
+      // T -= sum_{i,c} R_i(c) R_i(c)^T in a fixed order, then chol(T) (a <= TS).
+      Acc acc;
+      tile_load(X, make_tile(p.T, g.a, 0, 0, g.a, g.a));
+      __syncthreads();
+      acc_from_smem(acc, X);
+      bool ok = true;
+      for (int k = 0; k < g.nt * g.B && ok; ++k) {
+        ok = cta_wait(c, c.flags + g.fR(k / g.B, k % g.B), nullptr, &s_ok);
+        if (!ok) break;
+        const double* P = p.tip_part + (size_t)k * TS * TS;
+#pragma unroll
+        for (int ii = 0; ii < 2; ++ii)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc.v[ii][q] -= __ldcg(P + acc_row(ii) * TS + acc_col(q));
+      }
+      if (!ok) return false;
+      acc_to_smem(acc, X);
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < TS * TS; idx += NT) {
+        const int rr = idx / TS, cc = idx % TS;
+        if (rr >= g.a || cc >= g.a) X[rr * LDS + cc] = (rr == cc) ? 1.0 : 0.0;
+      }
+      const int info = smem_potrf(X, vec);
+      if (info) {
+        if (threadIdx.x == 0) {
+          atomicCAS(info_slot, 0, g.nt * g.b + info);
+          raise_abort(c);
+        }
+        return false;
+      }
+      tile_store(p.T, g.a, g.a, g.a, X);
+      cta_publish(c, c.flags + g.fT());
+      trace_task(c, t, type, t_task0);
+      return true;
+    }
+
+    // ---- target tile, its flag / digit slot, and the global rows of its rows
+    Tile tgt;
+    int tgt_slot;
+    long long row_base;
+    if (type == FT_DIAG || type == FT_OFFD) {
+      tgt = make_tile(p.D + i * bb, g.b, r * TS, col * TS, g.b, g.b);
+      tgt_slot = g.fD(i, r, col);
+      row_base = (long long)i * g.b + r * TS;
+    } else if (type == FT_LOW) {
+      tgt = make_tile(p.L + i * bb, g.b, r * TS, col * TS, g.b, g.b);
+      tgt_slot = g.fL(i, r, col);
+      row_base = (long long)(i + 1) * g.b + r * TS;
+    } else {
+      tgt = make_tile(p.R + i * ab, g.b, 0, col * TS, g.a, g.b);
+      tgt_slot = g.fR(i, col);
+      row_base = (long long)g.nt * g.b;
+    }
+    const long long col_base = (long long)i * g.b + col * TS;   // rows of the diagonal tile (i, col)
+    if (threadIdx.x < TS) {
+      erow_t[threadIdx.x] = (threadIdx.x < tgt.rows) ? p.erow[row_base + threadIdx.x] : 0;
+      ecol_t[threadIdx.x] = (threadIdx.x < tgt.cols) ? p.erow[col_base + threadIdx.x] : 0;
+    }
+    tile_load(X, tgt);
+    __syncthreads();
+    OzAcc acc;
+    int esum[2][4];
+#pragma unroll
+    for (int n = 0; n < 2; ++n)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        acc.v[n][j] = X[oz_row(n, j) * LDS + oz_col(n, j)];
+        esum[n][j] = erow_t[oz_row(n, j)] + ecol_t[oz_col(n, j)];
+      }
+    oz_clear_partials(acc);
+
+    // ---- product loop over the final tiles left of the target (previous block
+    //      column first, then columns k < col of this block)
+    const bool prev = (i > 0) && (type != FT_LOW);
+    const int nprev = prev ? g.B : 0;
+    const int nsteps = nprev + col;
+    auto slots = [&](int s, int& sa, int& sb) {
+      if (s < nprev) {
+        const int k = s;
+        sa = (type == FT_ARW) ? g.fR(i - 1, k) : g.fL(i - 1, r, k);
+        sb = g.fL(i - 1, col, k);
+      } else {
+        const int k = s - nprev;
+        sa = (type == FT_ARW) ? g.fR(i, k) : (type == FT_LOW) ? g.fL(i, r, k) : g.fD(i, r, k);
+        sb = g.fD(i, col, k);
+      }
+    };
+    bool ok = true;
+    if (nsteps > 0) {
+      auto flags_of = [&](int s, const int*& f0, const int*& f1) {
+        int sa, sb;
+        slots(s, sa, sb);
+        f0 = c.flags + sa;
+        f1 = (sa == sb) ? nullptr : c.flags + sb;
+      };
+      int sa, sb;
+      slots(0, sa, sb);
+      ok = cta_wait(c, c.flags + sa, sa == sb ? nullptr : c.flags + sb, &s_ok);
+      if (ok) {
+        if (threadIdx.x == 0) s_ready = 1;
+        oz_load_async(stages, p.digits + (size_t)sa * OZ_TILE);
+        oz_load_async(stages + OZ_OPER, p.digits + (size_t)sb * OZ_TILE);
+        cp_async_commit();
+      }
+      for (int s = 0; s < nsteps && ok; ++s) {
+        __half* cur = stages + (s & 1) * OZF_STAGE_HALVES;
+        __half* nxt = stages + ((s + 1) & 1) * OZF_STAGE_HALVES;
+        cp_async_wait_all();
+        __syncthreads();   // stage s is in shared memory; stage s-1 buffers are free
+        const bool more = s + 1 < nsteps;
+        bool issued = false;
+        int na = 0, nb = 0;
+        if (more) {
+          if (s_ready <= s + 1) {   // uniform: read after the barrier
+            scan_ready(c, nsteps, flags_of, &s_ready);
+            __syncthreads();
+          }
+          if (s_ready > s + 1) {
+            slots(s + 1, na, nb);
+            oz_load_async(nxt, p.digits + (size_t)na * OZ_TILE);
+            oz_load_async(nxt + OZ_OPER, p.digits + (size_t)nb * OZ_TILE);
+            cp_async_commit();
+            issued = true;
+          }
+        }
+        oz_step(acc, cur, cur + OZ_OPER);
+        if ((s + 1) % OZ_CHUNK == 0 || !more) oz_fold_sub(acc, esum);
+        if (more && !issued) {
+          slots(s + 1, na, nb);
+          if (!(ok = cta_wait(c, c.flags + na, na == nb ? nullptr : c.flags + nb, &s_ok))) break;
+          if (threadIdx.x == 0) s_ready = s + 2;
+          oz_load_async(nxt, p.digits + (size_t)na * OZ_TILE);
+          oz_load_async(nxt + OZ_OPER, p.digits + (size_t)nb * OZ_TILE);
+          cp_async_commit();
+        }
+      }
+    }
+    if (!ok) {
+      cp_async_wait_all();
+      return false;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int n = 0; n < 2; ++n)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) X[oz_row(n, j) * LDS + oz_col(n, j)] = acc.v[n][j];
+    __syncthreads();
+
+    if (type == FT_DIAG) {
+      tile_pad_identity(X, g.vrows(col));
+      const int info = smem_potrf(X, vec);
+      if (info) {
+        if (threadIdx.x == 0) {
+          atomicCAS(info_slot, 0, i * g.b + col * TS + info);
+          raise_abort(c);
+        }
+        return false;
+      }
+      tile_store(const_cast<double*>(tgt.p), g.b, tgt.rows, tgt.cols, X);
+      oz_store_digits(p.digits + (size_t)tgt_slot * OZ_TILE, X, tgt.rows, tgt.cols, erow_t);
+      cta_publish(c, c.flags + tgt_slot);
+      trace_task(c, t, type, t_task0);
+      return true;
+    }
+
+    // Off-diagonal targets: X <- X * D_i(col,col)^{-T}.
+    if (!cta_wait(c, c.flags + g.fD(i, col, col), nullptr, &s_ok)) return false;
+    tile_load(F, make_tile(p.D + i * bb, g.b, col * TS, col * TS, g.b, g.b));
+    __syncthreads();
+    tile_pad_identity(F, g.vrows(col));
+    __syncthreads();
+    tile_diag_recip(F, vec);
+    smem_trsm_rlt(X, F, vec);
+    tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
+    oz_store_digits(p.digits + (size_t)tgt_slot * OZ_TILE, X, tgt.rows, tgt.cols, erow_t);
+    if (type == FT_OFFD) {
+      const Tile up = make_tile(p.D + i * bb, g.b, col * TS, r * TS, g.b, g.b);
+      tile_store_zero(const_cast<double*>(up.p), g.b, up.rows, up.cols);
+    }
+    if (type == FT_ARW) {
+      // tip partial P = X X^T in FP64 (consumed in order by the tip task)
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < TS * TS; idx += NT) F[(idx % TS) * LDS + idx / TS] = X[(idx / TS) * LDS + idx % TS];
+      __syncthreads();
+      Acc pacc;
+      acc_zero(pacc);
+      tile_mma<false>(pacc, X, F);
+      double* P = p.tip_part + (size_t)(i * g.B + col) * TS * TS;
+#pragma unroll
+      for (int ii = 0; ii < 2; ++ii)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) P[acc_row(ii) * TS + acc_col(q)] = pacc.v[ii][q];
+    }
+    cta_publish(c, c.flags + tgt_slot);
+    trace_task(c, t, type, t_task0);
+  }
+  return true;
+}
+
+}  // namespace gbta

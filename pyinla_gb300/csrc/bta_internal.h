@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace gbta {
 
 constexpr int TS = 32;  // tile edge (FP64 elements)
@@ -38,6 +40,10 @@ struct LaunchCtl {
   long long* trace = nullptr;   // per-task trace records, or null
 };
 
+// Task lists of the factorization and selected-inversion DAGs (bta_api.cu).
+std::vector<int4> factor_task_list(const Geom& g);
+std::vector<int4> selinv_task_list(const Geom& g);
+
 // Host-side count of kernel launches issued by this library (see gbta_kernel_launches).
 void count_launches(int n);
 
@@ -52,7 +58,15 @@ void launch_factor_oz(const Geom& g, double* D, double* L, double* R, double* T,
                       const int4* tasks, int ntasks, double* tip_part, __half* digits, int* erow,
                       const LaunchCtl& lc);
 
+// Row exponents of the input matrix (before a tensor-core factorization).
+void launch_row_exponents(const Geom& g, const double* D, const double* T, int use_arrow, int* erow,
+                          cudaStream_t stream);
+
 size_t selinv_oz_digit_bytes(const Geom& g);
+// Column exponents and transposed digit planes of the factor (before a tensor-core
+// selected inversion).
+void launch_selinv_oz_prepare(const Geom& g, const double* D, const double* L, const double* R, int use_arrow,
+                              __half* fdig, int* ecol, cudaStream_t stream);
 void launch_selinv_oz(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                       double* SD, double* SL, double* SR, double* ST, int use_arrow, const int4* tasks,
                       int ntasks, __half* fdig, int* ecol, const LaunchCtl& lc);

@@ -33,7 +33,7 @@ namespace gbta {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[GBTA_NOALLOC_SCRATCH_BYTES];
 
 // Writes the factorization task list in the order the regular path builds it on the
-// host (bta_api.cu: factor_tasks): per block i, per column c: DIAG, OFFD (r > c),
+// host (bta_api.cu: factor_task_list): per block i, per column c: DIAG, OFFD (r > c),
 // LOW (i < nt-1), ARW (a > 0); then TIP (a > 0).  One thread per (i, c).
 __global__ void k_gen_factor_tasks(Geom g, int4* tasks) {
   const int ic = blockIdx.x * blockDim.x + threadIdx.x;

@@ -1,313 +1,16 @@
-// BTA triangular sweeps (Serinv pobtas / pobts) as one persistent dataflow kernel.
-//
-// Replaces the block forward / backward substitutions the reference runs through
-// Serinv (src/pyinla/solvers/structured_solver.py:112-140): trans = 0 solves
-// L y = b, trans = 1 solves L^T x = y, in place on the right-hand side.  One task
-// produces one 32-row tile g of the solution.  The tiles form a chain (tile g needs
-// tile g-1 in the forward sweep, g+1 in the backward sweep), so each task does all
-// of its work that does not depend on that neighbour before waiting for it:
-//   * invert its diagonal factor tile, Linv = F^{-1}, and form M = Linv P
-//     (backward: Linv^T P^T) with P the block coupling it to the neighbour tile;
-//   * subtract the products of every other solution tile it depends on, then
-//     u = Linv s (backward: Linv^T s);
-// leaving only  y_g = u - M y_neighbour  (one 32 x 32 matrix-vector product spread
-// over the whole CTA) between the neighbour's publication and its own.  The forward
-// sweep also leaves the arrow contribution R_i(:,r) y(i,r) of each tile in a partial
-// buffer that the arrow task sums in a fixed order.
-#include "bta_common.cuh"
+// Single-instance BTA triangular-sweep kernel (Serinv pobtas / pobts); the task body
+// is solve_task in bta_solve_task.cuh.
+#include "bta_solve_task.cuh"
 
 namespace gbta {
 
-constexpr int NC = SOLVE_NC;   // right-hand-side columns per launch
-
-struct SolveArgs {
-  const double* D;
-  const double* L;
-  const double* R;
-  const double* T;
-  double* B;        // right-hand sides (row-major, row stride ldb), columns [0, nc)
-  int ldb;
-  int nc;
-  Geom g;
-  int use_arrow;
-  int trans;
-  double* part;     // [nt*B][TS*NC] arrow partials
-  Ctl c;
-};
-
-__device__ __forceinline__ int vflag(const Geom& g, int i, int r) { return i * g.B + r; }
-
-// Vectors are TS x NC, stored [row][col] in shared memory (V[row*NC + col]).
-// res[q] = sum_m M[row][m] v[m][q] for q < nc, with M[row][m] = Ms[row*LDS + m]
-// (MT = false) or Ms[m*LDS + row] (MT = true).  Thread t owns row t/4 and the
-// k-range [8*(t%4), +8); the four partial sums of a row are combined with shuffles,
-// so every thread of the row returns the full dot products.
-template <bool MT>
-__device__ __forceinline__ void cta_gemv(const double* Ms, const double* V, int nc, double (&res)[NC]) {
-  const int row = threadIdx.x >> 2, part = threadIdx.x & 3;
-#pragma unroll
-  for (int q = 0; q < NC; ++q) {
-    double s = 0.0;
-    if (q < nc) {
-#pragma unroll
-      for (int k = 0; k < TS / 4; ++k) {
-        const int m = part * (TS / 4) + k;
-        const double mv = MT ? Ms[m * LDS + row] : Ms[row * LDS + m];
-        s = fma(mv, V[m * NC + q], s);
-      }
-    }
-    s += __shfl_xor_sync(0xffffffffu, s, 1);
-    s += __shfl_xor_sync(0xffffffffu, s, 2);
-    res[q] = s;
-  }
-}
-
-// Load the solution tile starting at global row `row0` (rows valid) into V.
-__device__ __forceinline__ void vec_load(double* V, const SolveArgs& p, int row0, int rows) {
-  const int row = threadIdx.x / NC, col = threadIdx.x % NC;
-  V[row * NC + col] = (row < rows && col < p.nc) ? __ldcg(p.B + (size_t)(row0 + row) * p.ldb + col) : 0.0;
-}
-
-// Dependency of a sweep step: the matrix tile (row-major; used as is in the forward
-// sweep, transposed in the backward sweep), the solution rows it multiplies, its flag.
-struct DepTile {
-  Tile t;
-  int vrow0, vrows;
-  const int* flag;
-};
-
 __global__ void __launch_bounds__(NT, 1) k_solve(SolveArgs p) {
-  __shared__ double Fs[TILE_SMEM];   // diagonal factor tile
-  __shared__ double Ws[TILE_SMEM];   // Linv = F^{-1}
-  __shared__ double Ms[TILE_SMEM];   // M = Linv P (forward) or Linv^T P^T (backward)
-  __shared__ double Ts[TILE_SMEM];   // staged dependency tile
-  __shared__ double Vs[TS * NC];     // staged solution tile
-  __shared__ double Ss[TS * NC];     // accumulated right-hand side
-  __shared__ double rd[TS];
+  __shared__ __align__(16) unsigned char raw[SOLVE_SMEM];
   __shared__ int s_ok, s_t;
-  const Geom& g = p.g;
-  const Ctl& c = p.c;
-  const int ntile = g.nt * g.B;
-  const int ntasks = ntile + (p.use_arrow ? 1 : 0);
-  const size_t bb = (size_t)g.b * g.b, ab = (size_t)g.a * g.b;
-  const int arrow_row0 = g.nt * g.b;
-  const bool fwd = p.trans == 0;
-
   while (true) {
-    const int t = cta_ticket(c, &s_t);
-    if (t < 0 || t >= ntasks) break;
-    const unsigned long long t_task0 = c.trace ? gtimer() : 0ull;
-    bool is_arrow;
-    int gi;
-    if (fwd) {
-      is_arrow = t == ntile;
-      gi = t;
-    } else {
-      is_arrow = p.use_arrow && t == 0;
-      gi = ntile - 1 - (t - (p.use_arrow ? 1 : 0));
-    }
-    const int srow = threadIdx.x / NC, scol = threadIdx.x % NC;
-
-    if (is_arrow) {
-      // forward: s = b_a - ordered sum of the partials, y_a = T^{-1} s;
-      // backward: x_a = T^{-T} y_a
-      tile_load(Fs, make_tile(p.T, g.a, 0, 0, g.a, g.a));
-      __syncthreads();
-      tile_pad_identity(Fs, g.a);
-      for (int idx = threadIdx.x; idx < TS * TS; idx += NT) Ws[(idx / TS) * LDS + idx % TS] = (idx / TS == idx % TS);
-      __syncthreads();
-      tile_diag_recip(Fs, rd);
-      smem_trsm_rln(Ws, Fs, rd);   // Ws = T^{-1}
-      double s = (srow < g.a && scol < p.nc) ? __ldcg(p.B + (size_t)(arrow_row0 + srow) * p.ldb + scol) : 0.0;
-      if (fwd) {
-        bool ok = true;
-        for (int k = 0; k < ntile; ++k) {
-          if (!(ok = cta_wait(c, c.flags + k, nullptr, &s_ok))) break;
-          s -= __ldcg(p.part + (size_t)k * TS * NC + threadIdx.x);
-        }
-        if (!ok) break;
-      }
-      Ss[threadIdx.x] = s;
-      __syncthreads();
-      double res[NC];
-      if (fwd)
-        cta_gemv<false>(Ws, Ss, p.nc, res);
-      else
-        cta_gemv<true>(Ws, Ss, p.nc, res);
-      if ((threadIdx.x & 3) == 0) {
-        const int row = threadIdx.x >> 2;
-        for (int q = 0; q < p.nc; ++q)
-          if (row < g.a) p.B[(size_t)(arrow_row0 + row) * p.ldb + q] = res[q];
-      }
-      cta_publish(c, c.flags + ntile);
-      trace_task(c, t, 1, t_task0);
-      continue;
-    }
-
-    const int i = gi / g.B, r = gi % g.B;
-    const int rows = g.vrows(r);
-    const int row0 = i * g.b + r * TS;
-    // ---- independent of other tasks: Linv of the diagonal tile and M
-    tile_load(Fs, make_tile(p.D + i * bb, g.b, r * TS, r * TS, g.b, g.b));
-    __syncthreads();
-    tile_pad_identity(Fs, rows);
-    for (int idx = threadIdx.x; idx < TS * TS; idx += NT) Ws[(idx / TS) * LDS + idx % TS] = (idx / TS == idx % TS);
-    __syncthreads();
-    tile_diag_recip(Fs, rd);
-    smem_trsm_rln(Ws, Fs, rd);   // Ws = F^{-1}
-    bool has_nb = false;
-    DepTile nb;
-    if (fwd) {
-      if (r > 0) {
-        has_nb = true;
-        nb.t = make_tile(p.D + i * bb, g.b, r * TS, (r - 1) * TS, g.b, g.b);
-        nb.vrow0 = i * g.b + (r - 1) * TS;
-        nb.vrows = g.vrows(r - 1);
-        nb.flag = c.flags + vflag(g, i, r - 1);
-      } else if (i > 0) {
-        has_nb = true;
-        nb.t = make_tile(p.L + (i - 1) * bb, g.b, 0, (g.B - 1) * TS, g.b, g.b);
-        nb.vrow0 = (i - 1) * g.b + (g.B - 1) * TS;
-        nb.vrows = g.vrows(g.B - 1);
-        nb.flag = c.flags + vflag(g, i - 1, g.B - 1);
-      }
-    } else {
-      if (r < g.B - 1) {
-        has_nb = true;
-        nb.t = make_tile(p.D + i * bb, g.b, (r + 1) * TS, r * TS, g.b, g.b);
-        nb.vrow0 = i * g.b + (r + 1) * TS;
-        nb.vrows = g.vrows(r + 1);
-        nb.flag = c.flags + vflag(g, i, r + 1);
-      } else if (i < g.nt - 1) {
-        has_nb = true;
-        nb.t = make_tile(p.L + i * bb, g.b, 0, r * TS, g.b, g.b);
-        nb.vrow0 = (i + 1) * g.b;
-        nb.vrows = g.vrows(0);
-        nb.flag = c.flags + vflag(g, i + 1, 0);
-      }
-    }
-    if (has_nb) {
-      // forward M = F^{-1} P, backward M = F^{-T} P^T: M[row][m] multiplies the
-      // neighbour's solution element m.
-      tile_load(Ts, nb.t);
-      __syncthreads();
-      for (int idx = threadIdx.x; idx < TS * TS; idx += NT) {
-        const int rr = idx / TS, cc = idx % TS;
-        double sacc = 0.0;
-        if (fwd) {
-#pragma unroll 8
-          for (int m = 0; m < TS; ++m) sacc = fma(Ws[rr * LDS + m], Ts[m * LDS + cc], sacc);
-        } else {
-#pragma unroll 8
-          for (int m = 0; m < TS; ++m) sacc = fma(Ws[m * LDS + rr], Ts[cc * LDS + m], sacc);
-        }
-        Ms[rr * LDS + cc] = sacc;
-      }
-    }
-    // ---- the other dependencies (all solved before the neighbour): s -= A_k v_k
-    Ss[threadIdx.x] = (srow < rows && scol < p.nc) ? __ldcg(p.B + (size_t)(row0 + srow) * p.ldb + scol) : 0.0;
-    __syncthreads();
-    int ndep, nfirst;
-    if (fwd) {
-      // L_{i-1}(r, k) y(i-1, k) for k < B, D_i(r, k) y(i, k) for k < r, minus the neighbour
-      nfirst = (i > 0) ? ((r == 0) ? g.B - 1 : g.B) : 0;
-      ndep = nfirst + (r > 0 ? r - 1 : 0);
-    } else {
-      // arrow, L_i(k, r)^T x(i+1, k) for k < B, D_i(k, r)^T x(i, k) for k > r, minus the neighbour
-      nfirst = (i < g.nt - 1) ? ((r == g.B - 1) ? g.B - 1 : g.B) : 0;
-      ndep = (p.use_arrow ? 1 : 0) + nfirst + (r < g.B - 1 ? g.B - 2 - r : 0);
-    }
-    bool ok = true;
-    for (int st = 0; st < ndep && ok; ++st) {
-      DepTile d;
-      if (fwd) {
-        if (st < nfirst) {
-          d.t = make_tile(p.L + (i - 1) * bb, g.b, r * TS, st * TS, g.b, g.b);
-          d.vrow0 = (i - 1) * g.b + st * TS;
-          d.vrows = g.vrows(st);
-          d.flag = c.flags + vflag(g, i - 1, st);
-        } else {
-          const int k = st - nfirst;   // k < r - 1
-          d.t = make_tile(p.D + i * bb, g.b, r * TS, k * TS, g.b, g.b);
-          d.vrow0 = i * g.b + k * TS;
-          d.vrows = g.vrows(k);
-          d.flag = c.flags + vflag(g, i, k);
-        }
-      } else {
-        int s2 = st;
-        if (p.use_arrow && s2 == 0) {
-          d.t = make_tile(p.R + i * ab, g.b, 0, r * TS, g.a, g.b);
-          d.vrow0 = arrow_row0;
-          d.vrows = g.a;
-          d.flag = c.flags + ntile;
-        } else {
-          if (p.use_arrow) --s2;
-          if (s2 < nfirst) {
-            const int k = g.B - 1 - s2;   // L_i rows B-1 down to (r == B-1 ? 1 : 0)
-            d.t = make_tile(p.L + i * bb, g.b, k * TS, r * TS, g.b, g.b);
-            d.vrow0 = (i + 1) * g.b + k * TS;
-            d.vrows = g.vrows(k);
-            d.flag = c.flags + vflag(g, i + 1, k);
-          } else {
-            const int k = g.B - 1 - (s2 - nfirst);   // D_i rows B-1 down to r+2
-            d.t = make_tile(p.D + i * bb, g.b, k * TS, r * TS, g.b, g.b);
-            d.vrow0 = i * g.b + k * TS;
-            d.vrows = g.vrows(k);
-            d.flag = c.flags + vflag(g, i, k);
-          }
-        }
-      }
-      tile_load(Ts, d.t);   // the matrix tile does not depend on other tasks
-      if (!(ok = cta_wait(c, d.flag, nullptr, &s_ok))) break;
-      vec_load(Vs, p, d.vrow0, d.vrows);
-      __syncthreads();
-      double res[NC];
-      if (fwd)
-        cta_gemv<false>(Ts, Vs, p.nc, res);
-      else
-        cta_gemv<true>(Ts, Vs, p.nc, res);
-      if ((threadIdx.x & 3) == 0)
-        for (int q = 0; q < p.nc; ++q) Ss[(threadIdx.x >> 2) * NC + q] -= res[q];
-      __syncthreads();
-    }
-    if (!ok) break;
-    // u = Linv s (forward) or Linv^T s (backward)
-    double u[NC];
-    if (fwd)
-      cta_gemv<false>(Ws, Ss, p.nc, u);
-    else
-      cta_gemv<true>(Ws, Ss, p.nc, u);
-    // ---- the neighbour: y = u - M v_nb
-    if (has_nb) {
-      if (!cta_wait(c, nb.flag, nullptr, &s_ok)) break;
-      vec_load(Vs, p, nb.vrow0, nb.vrows);
-      __syncthreads();
-      double res[NC];
-      cta_gemv<false>(Ms, Vs, p.nc, res);
-#pragma unroll
-      for (int q = 0; q < NC; ++q) u[q] -= res[q];
-    }
-    __syncthreads();
-    if ((threadIdx.x & 3) == 0) {
-      const int row = threadIdx.x >> 2;
-      for (int q = 0; q < NC; ++q) {
-        Ss[row * NC + q] = (q < p.nc && row < rows) ? u[q] : 0.0;
-        if (q < p.nc && row < rows) p.B[(size_t)(row0 + row) * p.ldb + q] = u[q];
-      }
-    }
-    if (fwd && p.use_arrow) {
-      // arrow partial R_i(:, r) y(i, r) (rows >= a of the staged tile are zero)
-      tile_load(Ts, make_tile(p.R + i * ab, g.b, 0, r * TS, g.a, g.b));
-      __syncthreads();
-      double res[NC];
-      cta_gemv<false>(Ts, Ss, p.nc, res);
-      if ((threadIdx.x & 3) == 0) {
-        const int row = threadIdx.x >> 2;
-        for (int q = 0; q < NC; ++q) p.part[(size_t)gi * TS * NC + row * NC + q] = (q < p.nc) ? res[q] : 0.0;
-      }
-    }
-    cta_publish(c, c.flags + vflag(g, i, r));
-    trace_task(c, t, 0, t_task0);
+    const int t = cta_ticket(p.c, &s_t);
+    if (t < 0 || t >= p.ntasks) break;
+    if (!solve_task(p, t, raw, &s_ok)) break;
   }
 }
 
@@ -326,6 +29,7 @@ void launch_solve(const Geom& g, const double* D, const double* L, const double*
   p.use_arrow = use_arrow;
   p.trans = trans;
   p.part = arrow_part;
+  p.ntasks = g.nt * g.B + (use_arrow ? 1 : 0);
   p.c.ctrl = lc.ctrl;
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;
