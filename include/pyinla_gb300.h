@@ -102,6 +102,11 @@ int gbta_set_wait_limit_ms(gbta_solver* s, double ms);
 int gbta_set_method(gbta_solver* s, int method);
 int gbta_get_method(const gbta_solver* s);
 
+/* Persistent CTAs per SM of the dataflow launches (0, the default: as many as the
+ * kernel's registers and shared memory allow; GBTA_CTAS_PER_SM in the environment
+ * sets the initial value).  No reference counterpart (a launch-shape setting). */
+int gbta_set_ctas_per_sm(gbta_solver* s, int n);
+
 /* Task tracing (off by default).  When enabled, every dataflow kernel launched by
  * the solver records one entry per task: [ticket, (task type << 16) | SM id,
  * start ns, end ns] (GPU global timer).  gbta_get_trace copies the records of the
@@ -251,6 +256,8 @@ size_t gbta_batch_workspace_bytes(const gbta_batch* bt);
 /* Work goes to `stream` (NULL = CUDA default stream; graph launches need another). */
 int gbta_batch_set_stream(gbta_batch* bt, void* stream);
 int gbta_batch_set_order(gbta_batch* bt, int policy);
+/* Persistent CTAs per SM of the batch's launches (0, the default: as many as fit). */
+int gbta_batch_set_ctas_per_sm(gbta_batch* bt, int n);
 int gbta_batch_set_wait_limit_ms(gbta_batch* bt, double ms);
 /* Bind the instances' device blocks: arrays (host) of n device pointers in the
  * Serinv layout; R, T may be NULL (or hold NULL) for a[k] = 0; rhs may be NULL when

@@ -54,6 +54,7 @@ SIGNATURES = {
     "gbta_set_wait_limit_ms": (_c_int, [_vp, ctypes.c_double]),
     "gbta_set_method": (_c_int, [_vp, _c_int]),
     "gbta_get_method": (_c_int, [_vp]),
+    "gbta_set_ctas_per_sm": (_c_int, [_vp, _c_int]),
     "gbta_set_trace": (_c_int, [_vp, _c_int]),
     "gbta_get_trace": (_c_ll, [_vp, _vp, _c_ll]),
     "gbta_workspace_bytes": (ctypes.c_size_t, [_vp]),
@@ -82,6 +83,7 @@ SIGNATURES = {
     "gbta_batch_workspace_bytes": (ctypes.c_size_t, [_vp]),
     "gbta_batch_set_stream": (_c_int, [_vp, _vp]),
     "gbta_batch_set_order": (_c_int, [_vp, _c_int]),
+    "gbta_batch_set_ctas_per_sm": (_c_int, [_vp, _c_int]),
     "gbta_batch_set_wait_limit_ms": (_c_int, [_vp, ctypes.c_double]),
     "gbta_batch_bind": (_c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "gbta_batch_run_async": (_c_int, [_vp, _c_int, _vp]),

@@ -74,6 +74,7 @@ class BtaBatch:
             self.ptr, _ptr_array([t.data_ptr() for t in self.D]), _ptr_array([t.data_ptr() for t in self.L]),
             _ptr_array([t.data_ptr() for t in self.R]), _ptr_array([t.data_ptr() for t in self.T]),
             _ptr_array([t.data_ptr() for t in self.rhs])))
+        self.ctas_per_sm = 0
         self.set_order(order)
 
     # ------------------------------------------------------------------ settings
@@ -82,6 +83,11 @@ class BtaBatch:
             raise ValueError(f"unknown order {order!r}; one of {sorted(ORDERS)}")
         _lib.check(self.lib.gbta_batch_set_order(self.ptr, ORDERS[order]))
         self.order = order
+
+    def set_ctas_per_sm(self, n: int) -> None:
+        """Persistent CTAs per SM of the batch's launches (0: as many as fit)."""
+        _lib.check(self.lib.gbta_batch_set_ctas_per_sm(self.ptr, int(n)))
+        self.ctas_per_sm = int(n)
 
     def set_wait_limit_ms(self, ms: float) -> None:
         _lib.check(self.lib.gbta_batch_set_wait_limit_ms(self.ptr, float(ms)))

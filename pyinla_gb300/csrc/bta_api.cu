@@ -42,7 +42,7 @@ struct gbta_solver {
   gbta::Geom g;
   int device = 0;
   int nsm = 0;
-  int ctas_per_sm = 1;
+  int ctas_per_sm = 0;   // persistent CTAs per SM (0: as many as fit)
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   unsigned long long wait_ns = 20ull * 1000 * 1000 * 1000;
@@ -106,12 +106,6 @@ std::vector<int4> selinv_task_list(const Geom& g) {
 
 namespace {
 
-int grid_of(const gbta_solver* s, int ntasks) {
-  int g = s->nsm * s->ctas_per_sm;
-  if (ntasks < g) g = ntasks;
-  return g < 1 ? 1 : g;
-}
-
 gbta::LaunchCtl next_launch(gbta_solver* s, int ntasks) {
   gbta::LaunchCtl lc;
   s->epoch += 1;
@@ -119,7 +113,10 @@ gbta::LaunchCtl next_launch(gbta_solver* s, int ntasks) {
   lc.flags = s->d_flags;
   lc.epoch = s->epoch;
   lc.wait_ns = s->wait_ns;
-  lc.grid = grid_of(s, ntasks);
+  lc.grid = 0;
+  lc.nsm = s->nsm;
+  lc.ctas_per_sm = s->ctas_per_sm;
+  lc.ntasks = ntasks;
   lc.stream = s->stream;
   if (s->d_trace && ntasks <= s->trace_cap) {
     lc.trace = s->d_trace;
@@ -190,7 +187,7 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   CREATE_CUDA(cudaDeviceGetAttribute(&s->nsm, cudaDevAttrMultiProcessorCount, s->device));
   if (const char* v = std::getenv("GBTA_CTAS_PER_SM")) {
     const int k = std::atoi(v);
-    if (k >= 1 && k <= 8) s->ctas_per_sm = k;
+    if (k >= 0 && k <= 8) s->ctas_per_sm = k;
   }
   CREATE_CUDA(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
   s->stream = s->own_stream;
@@ -254,6 +251,13 @@ int gbta_set_method(gbta_solver* s, int method) {
 }
 
 int gbta_get_method(const gbta_solver* s) { return s ? s->method : -1; }
+
+int gbta_set_ctas_per_sm(gbta_solver* s, int n) {
+  if (int r = check_solver(s)) return r;
+  if (n < 0 || n > 8) return fail(GBTA_ERR_ARG, "ctas_per_sm must be in [0, 8]");
+  s->ctas_per_sm = n;
+  return GBTA_OK;
+}
 
 int gbta_set_trace(gbta_solver* s, int enable) {
   if (int r = check_solver(s)) return r;

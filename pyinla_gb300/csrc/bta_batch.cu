@@ -150,6 +150,7 @@ struct gbta_batch {
   cudaStream_t stream = nullptr;
   unsigned long long wait_ns = 20ull * 1000 * 1000 * 1000;
   int policy = GBTA_BATCH_ORDER_PROPORTIONAL;
+  int ctas_per_sm = 0;   // persistent CTAs per SM (0: as many as fit)
   int* d_ctrl = nullptr;
   int* d_info = nullptr;
   int* d_flags = nullptr;
@@ -299,10 +300,13 @@ int reset_ticket(gbta_batch* bt) {
   return GBTA_OK;
 }
 
-int grid_of(const gbta_batch* bt, int ntasks) {
-  int g = bt->nsm;
-  if (ntasks < g) g = ntasks;
-  return g < 1 ? 1 : g;
+int grid_of(const gbta_batch* bt, const void* kernel, size_t smem, int ntasks) {
+  gbta::LaunchCtl lc;
+  lc.grid = 1;
+  lc.nsm = bt->nsm;
+  lc.ctas_per_sm = bt->ctas_per_sm;
+  lc.ntasks = ntasks;
+  return gbta::launch_grid(kernel, gbta::NT, smem, lc);
 }
 
 int run_async(gbta_batch* bt, int phases, double* logdet_out) {
@@ -321,7 +325,8 @@ int run_async(gbta_batch* bt, int phases, double* logdet_out) {
   if (phases & GBTA_PHASE_FACTOR) {
     for (const BatchInst& q : bt->inst)
       if (q.method == GBTA_METHOD_OZAKI) gbta::launch_row_exponents(q.g, q.D, q.T, q.g.a > 0, q.erow, st);
-    gbta::k_factor_batch<<<grid_of(bt, bt->n_forder), gbta::NT, gbta::BATCH_FACTOR_SMEM, st>>>(
+    gbta::k_factor_batch<<<grid_of(bt, (const void*)gbta::k_factor_batch, gbta::BATCH_FACTOR_SMEM, bt->n_forder), gbta::NT,
+                            gbta::BATCH_FACTOR_SMEM, st>>>(
         bt->d_fargs, bt->d_forder, bt->n_forder, c);
     gbta::count_launches(1);
     BATCH_CUDA(cudaGetLastError());
@@ -336,7 +341,7 @@ int run_async(gbta_batch* bt, int phases, double* logdet_out) {
   if (phases & GBTA_PHASE_SOLVE) {
     for (int dir = 0; dir < 2; ++dir) {
       if (int r = reset_ticket(bt)) return r;
-      gbta::k_solve_batch<<<grid_of(bt, bt->n_vorder), gbta::NT, 0, st>>>(bt->d_vargs + dir * bt->n, bt->d_vorder,
+      gbta::k_solve_batch<<<grid_of(bt, (const void*)gbta::k_solve_batch, 0, bt->n_vorder), gbta::NT, 0, st>>>(bt->d_vargs + dir * bt->n, bt->d_vorder,
                                                                             bt->n_vorder, c);
       gbta::count_launches(1);
       BATCH_CUDA(cudaGetLastError());
@@ -347,7 +352,8 @@ int run_async(gbta_batch* bt, int phases, double* logdet_out) {
       if (q.method == GBTA_METHOD_OZAKI)
         gbta::launch_selinv_oz_prepare(q.g, q.D, q.L, q.R, q.g.a > 0, q.digits, q.erow, st);
     if (int r = reset_ticket(bt)) return r;
-    gbta::k_selinv_batch<<<grid_of(bt, bt->n_sorder), gbta::NT, gbta::BATCH_SELINV_SMEM, st>>>(
+    gbta::k_selinv_batch<<<grid_of(bt, (const void*)gbta::k_selinv_batch, gbta::BATCH_SELINV_SMEM, bt->n_sorder), gbta::NT,
+                            gbta::BATCH_SELINV_SMEM, st>>>(
         bt->d_sargs, bt->d_sorder, bt->n_sorder, c);
     gbta::count_launches(1);
     for (const BatchInst& q : bt->inst) {
@@ -516,6 +522,14 @@ int gbta_batch_set_order(gbta_batch* bt, int policy) {
   drop_graph(bt);
   bt->policy = policy;
   return upload_orders(bt);
+}
+
+int gbta_batch_set_ctas_per_sm(gbta_batch* bt, int n) {
+  if (int r = check_batch(bt)) return r;
+  if (n < 0 || n > 8) return bfail(GBTA_ERR_ARG, "batch: ctas_per_sm must be in [0, 8]");
+  if (n != bt->ctas_per_sm) drop_graph(bt);
+  bt->ctas_per_sm = n;
+  return GBTA_OK;
 }
 
 int gbta_batch_set_wait_limit_ms(gbta_batch* bt, double ms) {

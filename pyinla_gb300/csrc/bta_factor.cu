@@ -36,7 +36,7 @@ void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, in
   p.c.epoch = lc.epoch;
   p.c.wait_ns = lc.wait_ns;
   p.c.trace = lc.trace;
-  k_factor<<<lc.grid, NT, 0, lc.stream>>>(p);
+  k_factor<<<launch_grid((const void*)k_factor, NT, 0, lc), NT, 0, lc.stream>>>(p);
   count_launches(1);
 }
 

@@ -70,7 +70,7 @@ void launch_factor_oz(const Geom& g, double* D, double* L, double* R, double* T,
   p.c.epoch = lc.epoch;
   p.c.wait_ns = lc.wait_ns;
   p.c.trace = lc.trace;
-  k_factor_oz<<<lc.grid, NT, OZF_SMEM, lc.stream>>>(p);
+  k_factor_oz<<<launch_grid((const void*)k_factor_oz, NT, OZF_SMEM, lc), NT, OZF_SMEM, lc.stream>>>(p);
   count_launches(1);
 }
 

@@ -35,10 +35,18 @@ struct LaunchCtl {
   int* flags;
   int epoch;
   unsigned long long wait_ns;
-  int grid;
+  int grid;                     // persistent CTAs when nsm == 0
   cudaStream_t stream;
   long long* trace = nullptr;   // per-task trace records, or null
+  int nsm = 0;                  // > 0: size the grid from the kernel's occupancy (launch_grid)
+  int ctas_per_sm = 0;          // CTAs per SM (0: as many as fit)
+  int ntasks = 0;               // never more CTAs than tasks
 };
+
+// Persistent grid of a kernel with `threads` threads and `smem` bytes of dynamic
+// shared memory: lc.grid when lc.nsm == 0, else nsm x (ctas_per_sm, capped by the
+// kernel's occupancy; all that fit when 0), at most ntasks.
+int launch_grid(const void* kernel, int threads, size_t smem, const LaunchCtl& lc);
 
 // Task lists of the factorization and selected-inversion DAGs (bta_api.cu).
 std::vector<int4> factor_task_list(const Geom& g);

@@ -16,6 +16,16 @@ std::atomic<long long> g_launches{0};
 
 void count_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
+int launch_grid(const void* kernel, int threads, size_t smem, const LaunchCtl& lc) {
+  if (lc.nsm <= 0) return lc.grid;
+  int occ = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem) != cudaSuccess || occ < 1) occ = 1;
+  const int per = lc.ctas_per_sm > 0 ? (lc.ctas_per_sm < occ ? lc.ctas_per_sm : occ) : occ;
+  long long g = (long long)lc.nsm * per;
+  if (lc.ntasks > 0 && g > lc.ntasks) g = lc.ntasks;
+  return g < 1 ? 1 : (int)g;
+}
+
 __global__ void __launch_bounds__(256) k_dfma_peak(double* out, int iters, double a, double b) {
   double x0 = threadIdx.x * 1e-9, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
          x7 = x0 + 7;

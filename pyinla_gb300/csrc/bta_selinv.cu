@@ -63,7 +63,7 @@ void launch_selinv(const Geom& g, const double* D, const double* L, const double
   p.c.epoch = lc.epoch;
   p.c.wait_ns = lc.wait_ns;
   p.c.trace = lc.trace;
-  k_selinv<<<lc.grid, NT, 0, lc.stream>>>(p);
+  k_selinv<<<launch_grid((const void*)k_selinv, NT, 0, lc), NT, 0, lc.stream>>>(p);
   count_launches(1);
 }
 

@@ -131,7 +131,7 @@ void launch_selinv_oz(const Geom& g, const double* D, const double* L, const dou
   p.c.epoch = lc.epoch;
   p.c.wait_ns = lc.wait_ns;
   p.c.trace = lc.trace;
-  k_selinv_oz<<<lc.grid, NT, OZS_SMEM, lc.stream>>>(p);
+  k_selinv_oz<<<launch_grid((const void*)k_selinv_oz, NT, OZS_SMEM, lc), NT, OZS_SMEM, lc.stream>>>(p);
   count_launches(1);
 }
 

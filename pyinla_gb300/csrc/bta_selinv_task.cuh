@@ -314,7 +314,9 @@ static __device__ __forceinline__ void oz_slice_to_smem(__half* As, const double
 }
 
 constexpr int OZS_STAGE = 2 * OZ_OPER;   // halves per stage (A, B)
-constexpr size_t OZS_SMEM = 2 * OZS_STAGE * sizeof(__half) + 3 * TILE_SMEM * sizeof(double) + TS * sizeof(double) +
+// X and F follow the two stages; W (used only by the epilogue and the tip task, when
+// no stage is in flight) reuses the first stage, so that two CTAs fit on one SM.
+constexpr size_t OZS_SMEM = 2 * OZS_STAGE * sizeof(__half) + 2 * TILE_SMEM * sizeof(double) + TS * sizeof(double) +
                             TS * sizeof(int) + 4 * sizeof(double);
 
 // Task t of a tensor-core selected-inversion instance.  `raw` is OZS_SMEM bytes of
@@ -324,8 +326,8 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
   __half* stages = reinterpret_cast<__half*>(raw);
   double* X = reinterpret_cast<double*>(raw + 2 * OZS_STAGE * sizeof(__half));
   double* F = X + TILE_SMEM;
-  double* W = F + TILE_SMEM;
-  double* rd = W + TILE_SMEM;
+  double* W = reinterpret_cast<double*>(raw);   // aliases stage 0 (free in the epilogue)
+  double* rd = F + TILE_SMEM;
   int* ecol_t = reinterpret_cast<int*>(rd + TS);
   double* red4 = reinterpret_cast<double*>(ecol_t + TS);
   int& s_ok = *s_okp;

@@ -35,7 +35,7 @@ void launch_solve(const Geom& g, const double* D, const double* L, const double*
   p.c.epoch = lc.epoch;
   p.c.wait_ns = lc.wait_ns;
   p.c.trace = lc.trace;
-  k_solve<<<lc.grid, NT, 0, lc.stream>>>(p);
+  k_solve<<<launch_grid((const void*)k_solve, NT, 0, lc), NT, 0, lc.stream>>>(p);
   count_launches(1);
 }
 

@@ -60,6 +60,10 @@ class BtaHandle:
         factorization computes its tile products."""
         _lib.check(self.lib.gbta_set_method(self.ptr, int(method)))
 
+    def set_ctas_per_sm(self, n: int) -> None:
+        """Persistent CTAs per SM of the dataflow launches (0: as many as fit)."""
+        _lib.check(self.lib.gbta_set_ctas_per_sm(self.ptr, int(n)))
+
     def method(self) -> int:
         return int(self.lib.gbta_get_method(self.ptr))
 

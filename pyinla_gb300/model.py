@@ -57,6 +57,18 @@ class CoefficientDerivatives:
         self.dtau_y = dt.reshape(dt.shape[0], -1)
 
 
+@dataclass
+class SeparablePart:
+    """One block c * T_AR1(rho) (x) Q_s of a separable prior, Q_s = sum_j w_j S_j over the
+    spec's base spatial matrices; derivatives are with respect to theta."""
+    c: float
+    dlogc: np.ndarray        # (d,)
+    rho: float
+    drho: np.ndarray         # (d,)
+    w: np.ndarray            # (J,)
+    dw: np.ndarray           # (d, J)
+
+
 def union_pattern(mats: list[sps.csr_matrix]):
     """Union CSR pattern of same-shape sparse matrices and each matrix's values on it."""
     n = mats[0].shape[0]
@@ -122,6 +134,12 @@ class KronSpec:
     def lik_theta_indices(self) -> list[int]:
         """Index in theta of theta_y,v = log tau_y,v for each variate v."""
         raise NotImplementedError
+
+    def separable_prior(self, theta):
+        """For priors that are, up to a mixing of unit determinant, a block diagonal of
+        separable blocks c_k T_AR1(rho_k) (x) Q_s,k: (base spatial matrices S_j, list of
+        SeparablePart).  None when the prior has no such structure."""
+        return None
 
     def obs_variates(self) -> np.ndarray:
         v = getattr(self, "obs_variate", None)
@@ -242,6 +260,23 @@ class KronGaussianModel:
         self._contract_out = torch.empty(4 * self.K * nt + 2 * self.nv * (nt + 1), dtype=f64, device=dev)
         self.h = BtaHandle.get(b, nt, a)
         self.last = {}
+        # separable priors: logdet and tr(Q_prior^-1 dQ_prior) from the ns x ns spatial
+        # factors (see _separable_prior_terms); "selinv" forces the prior's selected inverse
+        self.prior_trace = "separable"
+        sep = spec.separable_prior(spec.theta0) if hasattr(spec, "theta0") else None
+        self._sep_base = None
+        if sep is not None:
+            base, _ = sep
+            rp, cl, uv = union_pattern(base)
+            self._sep_base = base
+            self._sep_rowptr = torch.from_numpy(rp).to(dev)
+            self._sep_col = torch.from_numpy(cl).to(dev)
+            self._sep_uval = torch.from_numpy(np.ascontiguousarray(uv)).to(dev)
+            self._sep_vw = torch.zeros(2 * len(base), dtype=torch.int32, device=dev)
+            self._sep_D = torch.empty((1, self.ns, self.ns), dtype=f64, device=dev)
+            self._sep_coef = torch.empty(len(base), dtype=f64, device=dev)
+            self._sep_out = torch.empty(4 * len(base) + 4, dtype=f64, device=dev)
+            self._sep_h = BtaHandle.get(self.ns, 1, 0)
 
     def coefficients(self, theta):
         return self.spec.coefficients(theta)
@@ -321,6 +356,54 @@ class KronGaussianModel:
         _lib.check(code)
         return float(out.value)
 
+    def _spatial_logdet_and_traces(self, w: np.ndarray):
+        """logdet Q_s and tr(Q_s^-1 S_j) for Q_s = sum_j w_j S_j (ns x ns), on the device:
+        Kronecker assembly with one time block, factorization, logdet, selected
+        inversion (the full inverse of a single block) and the trace contractions."""
+        h, lib = self._sep_h, self._sep_h.lib
+        h.set_stream(current_stream_ptr())
+        J = len(self._sep_base)
+        self._sep_coef.copy_(self.torch.from_numpy(np.asarray(w, dtype=np.float64)))
+        _lib.check(lib.gbta_assemble_kron(
+            h.ptr, self.ns, 1, J, self._sep_rowptr.data_ptr(), self._sep_col.data_ptr(), self._sep_uval.data_ptr(),
+            self._sep_vw.data_ptr(), self._sep_coef.data_ptr(), None, None, None, None, None, None, None, None, 0.0,
+            self._sep_D.data_ptr(), None, None, None))
+        _lib.check(lib.gbta_pobtf(h.ptr, self._sep_D.data_ptr(), None))
+        out = ctypes.c_double(0.0)
+        _lib.check(lib.gbta_logdet(h.ptr, self._sep_D.data_ptr(), None, 0, ctypes.byref(out)))
+        _lib.check(lib.gbta_pobtsi(h.ptr, self._sep_D.data_ptr(), None))
+        _lib.check(lib.gbta_contract_kron(
+            h.ptr, self.ns, 1, J, self._sep_rowptr.data_ptr(), self._sep_col.data_ptr(), self._sep_uval.data_ptr(),
+            self._sep_vw.data_ptr(), None, None, None, None, None, None, self._sep_D.data_ptr(), None, None, None,
+            None, self._sep_out.data_ptr()))
+        tr = self._sep_out.cpu().numpy()[:J].copy()
+        return float(out.value), tr
+
+    def _separable_prior_terms(self, theta):
+        """logdet_bt Q_prior and its theta-gradient for a separable prior:
+        Q_re = (W^T (x) I) blockdiag_k(c_k T_k (x) Q_s,k) (W (x) I) with |det W| = 1 gives
+            logdet = sum_k nt ns log c_k + ns logdet T_k + nt logdet Q_s,k,
+            d logdet = sum_k nt ns dlog c_k + ns dlogdet T_k + nt sum_j dw_kj tr(Q_s,k^-1 S_j),
+        with the stationary AR1 logdet T(rho) = -(nt-1) log(1 - rho^2).  Equal to the
+        BTA factorization's logdet of the time-major prior and to its adjoint trace
+        tr(Q_prior^-1 dQ_prior), at the cost of one ns x ns factor per block."""
+        _, parts = self.spec.separable_prior(theta)
+        nt, ns = self.nt, self.ns
+        d = np.asarray(theta).size
+        logdet = 0.0
+        grad = np.zeros(d)
+        cache = {}
+        for part in parts:
+            key = tuple(np.asarray(part.w, dtype=np.float64).tolist())
+            if key not in cache:
+                cache[key] = self._spatial_logdet_and_traces(part.w)
+            ld_s, tr_s = cache[key]
+            r = part.rho
+            logdet += nt * ns * np.log(part.c) - ns * (nt - 1) * np.log1p(-r * r) + nt * ld_s
+            dlogdet_t = 2.0 * r * (nt - 1) / (1.0 - r * r)
+            grad += nt * ns * part.dlogc + ns * dlogdet_t * part.drho + nt * (part.dw @ tr_s)
+        return logdet, grad
+
     def _split(self, out: np.ndarray):
         K, nt = self.K, self.nt
         KN = K * nt
@@ -380,16 +463,22 @@ class KronGaussianModel:
         cc, dd, qc, qd, lc, lq = self._split(self._contract(
             self.Dc, self.Lc if self.nt > 1 else None, self.Rc if has_arrow else None,
             self.Tc if has_arrow else None, self.mu))
-        # prior selected inverse (bt)
-        _lib.check(lib.gbta_pobtsi(h.ptr, self.Dp.data_ptr(), self.Lp.data_ptr()))
-        pc, pd, _, _, _, _ = self._split(self._contract(self.Dp, self.Lp if self.nt > 1 else None, None, None, None))
+        # prior trace tr(Q_prior^-1 dQ_prior): from the spatial factors for a separable
+        # prior, else from the prior's selected inverse (bt)
+        tr_prior = None
+        if self._sep_base is not None and self.prior_trace == "separable":
+            _, tr_prior = self._separable_prior_terms(theta)
+        else:
+            _lib.check(lib.gbta_pobtsi(h.ptr, self.Dp.data_ptr(), self.Lp.data_ptr()))
+            pc, pd, _, _, _, _ = self._split(self._contract(self.Dp, self.Lp if self.nt > 1 else None, None, None,
+                                                            None))
         mAty = (self._Aty_v @ self.mu).cpu().numpy()      # mu^T A_v^T y_v per variate
         d = dc.dalpha.shape[0]
         grad = np.zeros(d)
         for k in range(d):
             da, db, dt = dc.dalpha[k], dc.dbeta[k], dc.dtau_y[k]
             tr_c = float(np.sum(da * cc) + 2.0 * np.sum(db * dd) + dt @ lc)
-            tr_p = float(np.sum(da * pc) + 2.0 * np.sum(db * pd))
+            tr_p = float(tr_prior[k]) if tr_prior is not None else float(np.sum(da * pc) + 2.0 * np.sum(db * pd))
             mqm = float(np.sum(da * qc) + 2.0 * np.sum(db * qd) + dt @ lq)
             mdb = float(dt @ mAty)                         # mu^T d(b), b = sum_v tau_y,v A_v^T y_v
             grad[k] = -0.5 * tr_p + 0.5 * tr_c - mdb + 0.5 * mqm
@@ -463,6 +552,17 @@ class SeparableSpdeAr1(KronSpec):
     def lik_theta_indices(self) -> list[int]:
         return [3]
 
+    def separable_prior(self, theta):
+        kappa, r_t, rho, tau, _ = self.unpack(theta)
+        d = 4
+        dlogc = np.zeros(d)
+        dlogc[2] = 1.0
+        drho = np.zeros(d)
+        drho[1] = rho / r_t
+        dw = np.zeros((d, 3))
+        dw[0] = spde.spde_weights_dlogkappa(kappa)
+        return self.terms, [SeparablePart(c=tau, dlogc=dlogc, rho=rho, drho=drho, w=spde.spde_weights(kappa), dw=dw)]
+
 
 def default_theta(rho: float = 0.9, kappa: float = None, tau: float = 1.0, tau_y: float = 4.0, ns: int = 1024):
     """theta = (log kappa, log r_t, log tau, log tau_y) for the benchmark model; kappa
@@ -527,6 +627,7 @@ class CoregionalSpdeAr1(KronSpec):
         self.theta0 = np.asarray(theta0, dtype=np.float64).reshape(3 * self.nv)
         self.prior_prec = float(prior_prec)
         base = spde.spde_terms(mesh)
+        self.base_terms = base
         self.terms, self.term_vw, self._term_jpq = [], [], []
         for j, S in enumerate(base):
             for p in range(self.nv):
@@ -601,6 +702,21 @@ class CoregionalSpdeAr1(KronSpec):
 
     def lik_theta_indices(self) -> list[int]:
         return [3 * k + 2 for k in range(self.nv)]
+
+    def separable_prior(self, theta):
+        """Q_re = P (V^T (x) I) blockdiag_k(sigma_k^-2 Qu_k) (V (x) I) P^T with V unit lower
+        triangular and P the time-major permutation: separable blocks, unit mixing."""
+        kappa, r_t, rho, _ = self._unpack(theta)
+        d = 3 * self.nv
+        parts = []
+        for k in range(self.nv):
+            drho = np.zeros(d)
+            drho[3 * k + 1] = rho[k] / r_t[k]
+            dw = np.zeros((d, 3))
+            dw[3 * k] = spde.spde_weights_dlogkappa(kappa[k])
+            parts.append(SeparablePart(c=float(self.sigma[k] ** -2.0), dlogc=np.zeros(d), rho=float(rho[k]), drho=drho,
+                                       w=spde.spde_weights(kappa[k]), dw=dw))
+        return self.base_terms, parts
 
     @classmethod
     def synthetic(cls, n_side: int, nt: int, nb_per: int, nv: int, n_obs: int, seed: int, m_side: int = 0,

@@ -152,3 +152,24 @@ def test_coregional_objective_and_gradient(built, nv):
                            spec.lik_theta_indices(), spec.log_prior_grad(theta), spec.obs_variates())
     assert relerr(g, gd) < 1e-8, (g, gd)
     check_fd(m, theta, g)
+
+
+@pytest.mark.parametrize("kind", ["separable", "coreg2", "coreg3"])
+def test_separable_prior_logdet_and_trace(built, kind):
+    """The spatial-factor logdet and prior trace of a separable prior equal the BTA
+    factorization's logdet and the selected-inverse trace."""
+    if kind == "separable":
+        spec = SeparableSpdeAr1.synthetic(6, 5, 2, 400, seed=21)
+        theta = spec.theta0 + np.array([0.2, -0.1, 0.3, 0.1])
+    else:
+        nv = 2 if kind == "coreg2" else 3
+        spec = CoregionalSpdeAr1.synthetic(4, 4, 2, nv, 900, seed=23, m_side=5)
+        theta = spec.theta0 + 0.1 * np.cos(np.arange(3 * nv))
+    m = KronGaussianModel(spec)
+    m.evaluate(theta)
+    ld_sep, tr_sep = m._separable_prior_terms(theta)
+    assert abs(ld_sep - m.last["logdet_prior"]) <= 1e-10 * abs(m.last["logdet_prior"])
+    _, g_sep = m.evaluate(theta, gradient=True)
+    m.prior_trace = "selinv"
+    _, g_sel = m.evaluate(theta, gradient=True)
+    assert relerr(g_sep, g_sel) < 1e-9, (g_sep, g_sel)
