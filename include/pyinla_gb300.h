@@ -108,9 +108,11 @@ int gbta_get_method(const gbta_solver* s);
 int gbta_set_ctas_per_sm(gbta_solver* s, int n);
 
 /* Task tracing (off by default).  When enabled, every dataflow kernel launched by
- * the solver records one entry per task: [ticket, (task type << 16) | SM id,
- * start ns, end ns] (GPU global timer).  gbta_get_trace copies the records of the
- * last traced launch to host memory and returns how many were copied. */
+ * the solver records one entry of 8 int64 per task: [ticket, (task type << 16) | SM
+ * id, start ns, end ns, m0, m1, m2, m3] (GPU global timer; m0..m3 are intermediate
+ * marks of the task's phases, 0 where a kernel sets none).  gbta_get_trace copies the
+ * records (out: 8 * max_records int64) of the last traced launch to host memory and
+ * returns how many were copied. */
 int gbta_set_trace(gbta_solver* s, int enable);
 long long gbta_get_trace(gbta_solver* s, long long* out, long long max_records);
 

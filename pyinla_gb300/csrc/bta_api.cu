@@ -267,7 +267,8 @@ int gbta_set_trace(gbta_solver* s, int enable) {
   s->trace_cap = s->trace_n = 0;
   if (enable) {
     const long long cap = s->n_ftasks > s->n_stasks ? s->n_ftasks : s->n_stasks;
-    GBTA_CUDA(cudaMalloc(&s->d_trace, (size_t)cap * 4 * sizeof(long long)));
+    GBTA_CUDA(cudaMalloc(&s->d_trace, (size_t)cap * 8 * sizeof(long long)));
+    GBTA_CUDA(cudaMemset(s->d_trace, 0, (size_t)cap * 8 * sizeof(long long)));
     s->trace_cap = cap;
   }
   return GBTA_OK;
@@ -277,7 +278,7 @@ long long gbta_get_trace(gbta_solver* s, long long* out, long long max_records) 
   if (!s || !s->d_trace || !out) return 0;
   const long long n = s->trace_n < max_records ? s->trace_n : max_records;
   if (cudaStreamSynchronize(s->stream) != cudaSuccess) return 0;
-  if (cudaMemcpy(out, s->d_trace, (size_t)n * 4 * sizeof(long long), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+  if (cudaMemcpy(out, s->d_trace, (size_t)n * 8 * sizeof(long long), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
   return n;
 }
 

@@ -35,7 +35,7 @@ struct Ctl {
   int* flags;
   int epoch;
   unsigned long long wait_ns;
-  long long* trace;   // optional: 4 int64 per task (see trace_task), or null
+  long long* trace;   // optional: TRACE_WORDS int64 per task (see trace_task), or null
 };
 
 __device__ __forceinline__ int ld_acquire(const int* p) {
@@ -60,16 +60,25 @@ __device__ __forceinline__ unsigned smid() {
   asm volatile("mov.u32 %0, %%smid;" : "=r"(r));
   return r;
 }
-// Task trace record (thread 0): [ticket, (type << 16) | sm, t_start, t_end] in
-// globaltimer nanoseconds; written only when tracing is enabled.
+// Task trace record (thread 0): [ticket, (type << 16) | sm, t_start, t_end, m0..m3] in
+// globaltimer nanoseconds, m0..m3 optional intermediate marks (0 when unused);
+// written only when tracing is enabled.
+constexpr int TRACE_WORDS = 8;
 __device__ __forceinline__ void trace_task(const Ctl& c, int ticket, int type, unsigned long long t0) {
   if (c.trace && threadIdx.x == 0) {
-    long long* r = c.trace + 4ll * ticket;
+    long long* r = c.trace + (long long)TRACE_WORDS * ticket;
     r[0] = ticket;
     r[1] = ((long long)type << 16) | smid();
     r[2] = (long long)t0;
     r[3] = (long long)gtimer();
   }
+}
+__device__ __forceinline__ void trace_clear_marks(const Ctl& c, int ticket) {
+  if (c.trace && threadIdx.x == 0)
+    for (int k = 4; k < TRACE_WORDS; ++k) c.trace[(long long)TRACE_WORDS * ticket + k] = 0;
+}
+__device__ __forceinline__ void trace_mark(const Ctl& c, int ticket, int k) {
+  if (c.trace && threadIdx.x == 0) c.trace[(long long)TRACE_WORDS * ticket + 4 + k] = (long long)gtimer();
 }
 
 __device__ __forceinline__ void raise_abort(const Ctl& c) { atomicExch(c.ctrl + CTRL_ABORT, 1); }
@@ -377,123 +386,157 @@ static __device__ bool kloop(Acc& acc, int nsteps, StepFn step_of, const Ctl& c,
 // Small dense kernels on shared tiles (whole CTA).
 // ---------------------------------------------------------------------------
 
-// Scalar FP64 helpers.  On GB300 one warp-wide FP64 instruction occupies an SM
-// sub-partition's FP64 unit for ~64 cycles, so the sequential per-column work of the
-// small tile kernels is kept to a few FP64 instructions: reciprocals and inverse
-// square roots are Newton-Raphson refinements (y <- y (2 - x y), resp.
-// y <- y (3 - x y^2) / 2, each doubling the correct bits) of the hardware
-// approximations rcp.approx / rsqrt.approx, computed once per tile or per pivot.
-__device__ __forceinline__ double nr_recip(double x) {
+// Scalar FP64 helpers.  On GB300 a warp-wide FP64 instruction occupies its SM
+// sub-partition's FP64 unit for ~64-76 cycles, whether it is dependent, independent or
+// even predicated off, so the sequential work of the tile routines below is counted in
+// FP64 instructions.  Reciprocals and inverse square roots start from the hardware
+// approximations rcp.approx / rsqrt.approx (~20 correct bits) and take ONE third-order
+// correction (a truncated binomial series, i.e. a third-order Householder step), which
+// leaves a truncation error of order e^3 ~ 2^-57:
+//   1/d:       e = 1 - d y,    y <- y (1 + e + e^2)
+//   1/sqrt(d): e = 1 - d y^2,  y <- y (1 + e/2 + 3 e^2 / 8)
+__device__ __forceinline__ double rcp3(double d) {
   double y;
-  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-  double e = fma(-x, y, 1.0);
-  y = fma(y, e, y);
-  e = fma(-x, y, 1.0);
-  y = fma(y, e, y);
-  e = fma(-x, y, 1.0);
-  return fma(y, e, y);
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(d));
+  const double e = fma(-d, y, 1.0);
+  const double p = 1.0 + e;
+  const double ye = y * e;
+  return fma(ye, p, y);
 }
-__device__ __forceinline__ double nr_rsqrt(double x) {
+__device__ __forceinline__ double rsqrt3(double d) {
   double y;
-  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-  const double h = 0.5 * x;
-  double r = fma(-h * y, y, 0.5);
-  y = fma(y, r, y);
-  r = fma(-h * y, y, 0.5);
-  y = fma(y, r, y);
-  r = fma(-h * y, y, 0.5);
-  return fma(y, r, y);
-}
-
-// sqrt(x) and 1/sqrt(x) together by Goldschmidt's iteration (R. E. Goldschmidt,
-// "Applications of division by convergence", MIT thesis, 1964): from y0 ~ 1/sqrt(x)
-// (rsqrt.approx, ~20 correct bits), g = x y0, h = y0/2 and r = 1/2 - g h,
-// g <- g + g r, h <- h + h r doubles the correct bits per step; g and h update in
-// parallel, so two steps are a chain of five FP64 operations instead of the eleven
-// of three dependent Newton steps.
-__device__ __forceinline__ void gs_sqrt_rsqrt(double x, double& sq, double& rs) {
-  double y;
-  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-  double g = x * y, h = 0.5 * y;
-  double r = fma(-g, h, 0.5);
-  g = fma(g, r, g);
-  h = fma(h, r, h);
-  r = fma(-g, h, 0.5);
-  g = fma(g, r, g);
-  h = fma(h, r, h);
-  sq = g;
-  rs = 2.0 * h;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(d));
+  const double dy = d * y;
+  const double e = fma(-dy, y, 1.0);
+  const double p = fma(e, 0.375, 0.5);
+  const double ye = y * e;
+  return fma(ye, p, y);
 }
 
 // rd[j] = 1 / F[j][j] for the TS diagonal entries (one lane each).  Caller syncs.
 __device__ __forceinline__ void tile_diag_recip(const double* F, double* rd) {
-  if (threadIdx.x < TS) rd[threadIdx.x] = nr_recip(F[threadIdx.x * LDS + threadIdx.x]);
+  if (threadIdx.x < TS) rd[threadIdx.x] = rcp3(F[threadIdx.x * LDS + threadIdx.x]);
+}
+
+// ---- register-resident tile factorization and triangular solves ------------------
+// Thread (lane r, warp g) holds row r of the tile at the eight columns c = g + 4q
+// (q = 0..7) in registers, so every FP64 instruction has 32 useful lanes.  Columns
+// are processed in order; the warp owning the current column finalises it and
+// publishes it through a shared double buffer (one barrier per column), and every
+// warp then updates its later columns with one FMA per element.  The loops over
+// columns and register slots are fully unrolled: the conditions "column c = g + 4q
+// is after column j" are written as a compile-time part plus a runtime part that
+// only the one boundary slot needs, because an FP64 instruction issued under a false
+// predicate still costs a full pipe slot.
+__device__ __forceinline__ bool col_after(int q, int j, int g) {   // g + 4q > j
+  return 4 * q > j || (4 * q + 3 > j && g > j - 4 * q);
+}
+__device__ __forceinline__ bool col_before(int q, int j, int g) {  // g + 4q < j
+  return 4 * q + 3 < j || (4 * q < j && g < j - 4 * q);
 }
 
 // In-place lower Cholesky of S (TS x TS; entries past n must already be identity).
-// Returns 0, or the 1-based column of the first non-positive (or NaN) pivot.
-// One barrier per column: step j updates the trailing matrix with the unscaled
-// column j and 1/d_j; the columns are scaled by 1/sqrt(d_j) in a final pass (column
-// j is not modified after step j).  The strict upper triangle is zeroed on success.
-// `ybuf` is a TS-double shared scratch.
-static __device__ int smem_potrf(double* S, double* ybuf) {
+// Returns 0, or the 1-based column of the first non-positive (or NaN) pivot (the
+// tile then holds NaNs).  The strict upper triangle is zeroed.  One-column lookahead:
+// the warp owning column j+1 updates that column first and computes its pivot
+// (l_kk = d y, l_rk = a_rk y with y = 1/sqrt(d)) before its other updates of step j.
+static __device__ int smem_potrf(double* S) {
+  __shared__ double xs[2 * TS];
+  __shared__ int s_info;
+  const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+  __syncthreads();
+  double acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = S[r * LDS + g + 4 * q];
+  if (g == 0) {
+    const double d = __shfl_sync(0xffffffffu, acc[0], 0);
+    const double y = rsqrt3(d);
+    acc[0] = (r > 0) ? acc[0] * y : (r == 0 ? d * y : 0.0);
+    xs[r] = acc[0];
+    if (r == 0) s_info = (d > 0.0) ? 0 : 1;
+  }
+  __syncthreads();
+#pragma unroll
   for (int j = 0; j < TS; ++j) {
+    const double* xb = xs + (j & 1) * TS;
+    const double lr = xb[r];
+    if (j + 1 < TS && g == ((j + 1) & 3)) {
+      const int qn = (j + 1) >> 2;
+      const double a = fma(-lr, xb[j + 1], acc[qn]);
+      const double d = __shfl_sync(0xffffffffu, a, j + 1);
+      const double y = rsqrt3(d);
+      const double l = (r > j + 1) ? a * y : (r == j + 1 ? d * y : 0.0);
+      acc[qn] = l;
+      xs[((j + 1) & 1) * TS + r] = l;
+      if (r == 0 && !(d > 0.0) && s_info == 0) s_info = j + 2;
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (col_after(q, j + 1, g)) acc[q] = fma(-lr, xb[g + 4 * q], acc[q]);
     __syncthreads();
-    const double d = S[j * LDS + j];
-    if (!(d > 0.0)) {
-      __syncthreads();
-      return j + 1;
-    }
-    double sq, y;
-    gs_sqrt_rsqrt(d, sq, y);
-    const double inv = y * y;
-    if (threadIdx.x == 0) ybuf[j] = y;
-    const int m = TS - 1 - j;
-    for (int idx = threadIdx.x; idx < m * m; idx += NT) {
-      const int rr = j + 1 + idx / m, kk = j + 1 + idx % m;
-      if (kk <= rr) S[rr * LDS + kk] = fma(-S[rr * LDS + j] * inv, S[kk * LDS + j], S[rr * LDS + kk]);
-    }
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int c = g + 4 * q;
+    S[r * LDS + c] = (c > r) ? 0.0 : acc[q];
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < TS * TS; idx += NT) {
-    const int r = idx / TS, c = idx % TS;
-    S[r * LDS + c] = (c > r) ? 0.0 : S[r * LDS + c] * ybuf[c];
-  }
-  __syncthreads();
-  return 0;
+  return s_info;
 }
 
-// X <- X * F^{-T} with F lower triangular; rd = 1/diag(F) (tile_diag_recip, synced).
-// One barrier per column: column j stays unscaled until a final pass, updates use
-// X[r][j] * rd[j].
+// X <- X * F^{-T} with F lower triangular; rd = 1/diag(F) (tile_diag_recip).  Row r
+// solves x_r F^T = X_r by forward substitution over the columns.
 static __device__ void smem_trsm_rlt(double* X, const double* F, const double* rd) {
-  for (int j = 0; j < TS - 1; ++j) {
-    __syncthreads();
-    const double rj = rd[j];
-    const int m = TS - 1 - j;
-    for (int idx = threadIdx.x; idx < TS * m; idx += NT) {
-      const int r = idx / m, col = j + 1 + idx % m;
-      X[r * LDS + col] = fma(-X[r * LDS + j] * rj, F[col * LDS + j], X[r * LDS + col]);
-    }
-  }
+  __shared__ double xs[2 * TS];
+  const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
   __syncthreads();
-  for (int idx = threadIdx.x; idx < TS * TS; idx += NT) X[(idx / TS) * LDS + idx % TS] *= rd[idx % TS];
+  double acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = X[r * LDS + g + 4 * q];
+#pragma unroll
+  for (int j = 0; j < TS; ++j) {
+    double* xb = xs + (j & 1) * TS;
+    if (g == (j & 3)) {
+      const double x = acc[j >> 2] * rd[j];
+      acc[j >> 2] = x;
+      xb[r] = x;
+    }
+    __syncthreads();
+    const double xr = xb[r];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (col_after(q, j, g)) acc[q] = fma(-xr, F[(g + 4 * q) * LDS + j], acc[q]);
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) X[r * LDS + g + 4 * q] = acc[q];
   __syncthreads();
 }
 
-// X <- X * F^{-1} with F lower triangular (solve X F = X, backward column sweep);
-// rd = 1/diag(F).  Same one-barrier-per-column scheme.
+// X <- X * F^{-1} with F lower triangular; rd = 1/diag(F).  Row r solves x_r F = X_r
+// by backward substitution over the columns.
 static __device__ void smem_trsm_rln(double* X, const double* F, const double* rd) {
-  for (int j = TS - 1; j > 0; --j) {
-    __syncthreads();
-    const double rj = rd[j];
-    for (int idx = threadIdx.x; idx < TS * j; idx += NT) {
-      const int r = idx / j, col = idx % j;
-      X[r * LDS + col] = fma(-X[r * LDS + j] * rj, F[j * LDS + col], X[r * LDS + col]);
-    }
-  }
+  __shared__ double xs[2 * TS];
+  const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
   __syncthreads();
-  for (int idx = threadIdx.x; idx < TS * TS; idx += NT) X[(idx / TS) * LDS + idx % TS] *= rd[idx % TS];
+  double acc[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) acc[q] = X[r * LDS + g + 4 * q];
+#pragma unroll
+  for (int j = TS - 1; j >= 0; --j) {
+    double* xb = xs + (j & 1) * TS;
+    if (g == (j & 3)) {
+      const double x = acc[j >> 2] * rd[j];
+      acc[j >> 2] = x;
+      xb[r] = x;
+    }
+    __syncthreads();
+    const double xr = xb[r];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (col_before(q, j, g)) acc[q] = fma(-xr, F[j * LDS + g + 4 * q], acc[q]);
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) X[r * LDS + g + 4 * q] = acc[q];
   __syncthreads();
 }
 

@@ -120,7 +120,7 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
         const int rr = idx / TS, cc = idx % TS;
         if (rr >= g.a || cc >= g.a) X[rr * LDS + cc] = (rr == cc) ? 1.0 : 0.0;
       }
-      const int info = smem_potrf(X, vec);
+      const int info = smem_potrf(X);
       if (info) {
         if (threadIdx.x == 0) {
           atomicCAS(info_slot, 0, g.nt * g.b + info);
@@ -199,7 +199,7 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
 
     if (type == FT_DIAG) {
       tile_pad_identity(X, g.vrows(col));
-      const int info = smem_potrf(X, vec);
+      const int info = smem_potrf(X);
       if (info) {
         if (threadIdx.x == 0) {
           atomicCAS(info_slot, 0, i * g.b + col * TS + info);
@@ -317,7 +317,7 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
         const int rr = idx / TS, cc = idx % TS;
         if (rr >= g.a || cc >= g.a) X[rr * LDS + cc] = (rr == cc) ? 1.0 : 0.0;
       }
-      const int info = smem_potrf(X, vec);
+      const int info = smem_potrf(X);
       if (info) {
         if (threadIdx.x == 0) {
           atomicCAS(info_slot, 0, g.nt * g.b + info);
@@ -437,6 +437,8 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
       return false;
     }
     __syncthreads();
+    trace_clear_marks(c, t);
+    trace_mark(c, t, 0);   // product loop done
 #pragma unroll
     for (int n = 0; n < 2; ++n)
 #pragma unroll
@@ -445,7 +447,7 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
 
     if (type == FT_DIAG) {
       tile_pad_identity(X, g.vrows(col));
-      const int info = smem_potrf(X, vec);
+      const int info = smem_potrf(X);
       if (info) {
         if (threadIdx.x == 0) {
           atomicCAS(info_slot, 0, i * g.b + col * TS + info);
@@ -453,8 +455,10 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
         }
         return false;
       }
+      trace_mark(c, t, 1);   // tile factored
       tile_store(const_cast<double*>(tgt.p), g.b, tgt.rows, tgt.cols, X);
       oz_store_digits(p.digits + (size_t)tgt_slot * OZ_TILE, X, tgt.rows, tgt.cols, erow_t);
+      trace_mark(c, t, 2);   // tile and digits written
       cta_publish(c, c.flags + tgt_slot);
       trace_task(c, t, type, t_task0);
       return true;
@@ -462,14 +466,17 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
 
     // Off-diagonal targets: X <- X * D_i(col,col)^{-T}.
     if (!cta_wait(c, c.flags + g.fD(i, col, col), nullptr, &s_ok)) return false;
+    trace_mark(c, t, 1);   // diagonal factor tile ready
     tile_load(F, make_tile(p.D + i * bb, g.b, col * TS, col * TS, g.b, g.b));
     __syncthreads();
     tile_pad_identity(F, g.vrows(col));
     __syncthreads();
     tile_diag_recip(F, vec);
     smem_trsm_rlt(X, F, vec);
+    trace_mark(c, t, 2);   // triangular solve done
     tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
     oz_store_digits(p.digits + (size_t)tgt_slot * OZ_TILE, X, tgt.rows, tgt.cols, erow_t);
+    trace_mark(c, t, 3);   // tile and digits written
     if (type == FT_OFFD) {
       const Tile up = make_tile(p.D + i * bb, g.b, col * TS, r * TS, g.b, g.b);
       tile_store_zero(const_cast<double*>(up.p), g.b, up.rows, up.cols);
