@@ -437,11 +437,14 @@ __device__ __forceinline__ bool col_before(int q, int j, int g) {  // g + 4q < j
 
 // In-place lower Cholesky of S (TS x TS; entries past n must already be identity).
 // Returns 0, or the 1-based column of the first non-positive (or NaN) pivot (the
-// tile then holds NaNs).  The strict upper triangle is zeroed.  One-column lookahead:
-// the warp owning column j+1 updates that column first and computes its pivot
-// (l_kk = d y, l_rk = a_rk y with y = 1/sqrt(d)) before its other updates of step j.
+// tile then holds NaNs).  The strict upper triangle is zeroed.
+// Step j publishes pivot column j+1 (l_kk = d y, l_rk = a_rk y, y = 1/sqrt(d)); only
+// the warp owning column j+1 works on the critical path in that step (update of
+// column j+1 with pivot j, then its pivot); it applies pivot j to its other columns
+// one step later, together with pivot j+1.  Pivot columns rotate through three
+// shared slots.
 static __device__ int smem_potrf(double* S) {
-  __shared__ double xs[2 * TS];
+  __shared__ double xs[3 * TS];
   __shared__ int s_info;
   const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
   __syncthreads();
@@ -458,21 +461,29 @@ static __device__ int smem_potrf(double* S) {
   __syncthreads();
 #pragma unroll
   for (int j = 0; j < TS; ++j) {
-    const double* xb = xs + (j & 1) * TS;
-    const double lr = xb[r];
+    const double* xj = xs + (j % 3) * TS;
     if (j + 1 < TS && g == ((j + 1) & 3)) {
       const int qn = (j + 1) >> 2;
-      const double a = fma(-lr, xb[j + 1], acc[qn]);
+      const double a = fma(-xj[r], xj[j + 1], acc[qn]);
       const double d = __shfl_sync(0xffffffffu, a, j + 1);
       const double y = rsqrt3(d);
       const double l = (r > j + 1) ? a * y : (r == j + 1 ? d * y : 0.0);
       acc[qn] = l;
-      xs[((j + 1) & 1) * TS + r] = l;
+      xs[((j + 1) % 3) * TS + r] = l;
       if (r == 0 && !(d > 0.0) && s_info == 0) s_info = j + 2;
-    }
+    } else {
+      const double lr = xj[r];
 #pragma unroll
-    for (int q = 0; q < 8; ++q)
-      if (col_after(q, j + 1, g)) acc[q] = fma(-lr, xb[g + 4 * q], acc[q]);
+      for (int q = 0; q < 8; ++q)
+        if (col_after(q, j + 1, g)) acc[q] = fma(-lr, xj[g + 4 * q], acc[q]);
+      if (j >= 1 && g == (j & 3)) {   // owner of the previous step: its deferred pivot j-1
+        const double* xp = xs + ((j + 2) % 3) * TS;
+        const double lp = xp[r];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (col_after(q, j + 1, g)) acc[q] = fma(-lp, xp[g + 4 * q], acc[q]);
+      }
+    }
     __syncthreads();
   }
 #pragma unroll

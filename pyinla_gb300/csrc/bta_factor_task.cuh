@@ -456,9 +456,9 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
         return false;
       }
       trace_mark(c, t, 1);   // tile factored
+      // (diagonal tiles are never operands of the product loops: no digit planes)
       tile_store(const_cast<double*>(tgt.p), g.b, tgt.rows, tgt.cols, X);
-      oz_store_digits(p.digits + (size_t)tgt_slot * OZ_TILE, X, tgt.rows, tgt.cols, erow_t);
-      trace_mark(c, t, 2);   // tile and digits written
+      trace_mark(c, t, 2);   // tile written
       cta_publish(c, c.flags + tgt_slot);
       trace_task(c, t, type, t_task0);
       return true;
@@ -477,10 +477,6 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
     tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
     oz_store_digits(p.digits + (size_t)tgt_slot * OZ_TILE, X, tgt.rows, tgt.cols, erow_t);
     trace_mark(c, t, 3);   // tile and digits written
-    if (type == FT_OFFD) {
-      const Tile up = make_tile(p.D + i * bb, g.b, col * TS, r * TS, g.b, g.b);
-      tile_store_zero(const_cast<double*>(up.p), g.b, up.rows, up.cols);
-    }
     if (type == FT_ARW) {
       // tip partial P = X X^T in FP64 (consumed in order by the tip task)
       __syncthreads();
@@ -496,6 +492,12 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
         for (int q = 0; q < 4; ++q) P[acc_row(ii) * TS + acc_col(q)] = pacc.v[ii][q];
     }
     cta_publish(c, c.flags + tgt_slot);
+    if (type == FT_OFFD) {
+      // The factor's strict upper triangle is zero: clear the mirrored tile (read by
+      // no task of the factorization, so after the publication).
+      const Tile up = make_tile(p.D + i * bb, g.b, col * TS, r * TS, g.b, g.b);
+      tile_store_zero(const_cast<double*>(up.p), g.b, up.rows, up.cols);
+    }
     trace_task(c, t, type, t_task0);
   }
   return true;
