@@ -58,6 +58,7 @@ struct gbta_solver {
   double* d_arrow_part = nullptr;
   double* d_ld = nullptr;   // logdet partials [nt + 1] + result [1]
   double* d_sig = nullptr;  // selected-inversion output blocks (lazy)
+  double* d_selws = nullptr;  // selected-inversion pre-pass: diagonal inverses (lazy)
   size_t sig_elems = 0;
   int* h_ctrl = nullptr;    // pinned
   size_t ws_bytes = 0;
@@ -228,6 +229,7 @@ int gbta_destroy(gbta_solver* s) {
   cudaFree(s->d_arrow_part);
   cudaFree(s->d_ld);
   cudaFree(s->d_sig);
+  cudaFree(s->d_selws);
   cudaFree(s->d_trace);
   cudaFree(s->d_digits);
   cudaFree(s->d_erow);
@@ -290,7 +292,9 @@ int gbta_set_wait_limit_ms(gbta_solver* s, double ms) {
 }
 
 size_t gbta_workspace_bytes(const gbta_solver* s) {
-  return s ? s->ws_bytes + s->sig_elems * sizeof(double) + s->digit_bytes : 0;
+  return s ? s->ws_bytes + s->sig_elems * sizeof(double) + s->digit_bytes +
+                 (s->d_selws ? gbta::selinv_prepare_bytes(s->g) : 0)
+           : 0;
 }
 
 int gbta_status(gbta_solver* s) {
@@ -419,19 +423,25 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
     GBTA_CUDA(cudaMalloc(&s->d_sig, need * sizeof(double)));
     s->sig_elems = need;
   }
+  if (!s->d_selws) {
+    GBTA_CUDA(cudaStreamSynchronize(s->stream));
+    GBTA_CUDA(cudaMalloc(&s->d_selws, gbta::selinv_prepare_bytes(g)));
+  }
+  const double* cinv = s->d_selws + (size_t)g.nt * g.B * gbta::TS * gbta::TS;
   double* SD = s->d_sig;
   double* SL = SD + g.nt * bb;
   double* SR = SL + (g.nt - 1) * bb;
   double* ST = SR + (size_t)g.nt * g.a * g.b;
   if (s->method == GBTA_METHOD_OZAKI)
     if (int r = ensure_digits(s)) return r;
+  gbta::launch_selinv_prepare(g, D, L, R, use_arrow, s->d_selws, s->stream);
   if (int r = reset_ticket(s)) return r;
   const gbta::LaunchCtl lc = next_launch(s, s->n_stasks);
   if (s->method == GBTA_METHOD_OZAKI)
     gbta::launch_selinv_oz(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks,
-                           (__half*)s->d_digits, s->d_erow, lc);
+                           (__half*)s->d_digits, s->d_erow, cinv, lc);
   else
-    gbta::launch_selinv(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks, lc);
+    gbta::launch_selinv(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks, cinv, lc);
   GBTA_CUDA(cudaGetLastError());
   gbta::launch_selinv_writeback(g, SD, SL, SR, ST, D, L, R, T, use_arrow, s->stream);
   GBTA_CUDA(cudaGetLastError());

@@ -131,6 +131,7 @@ struct BatchInst {
   double* arrow_part = nullptr;
   double* ld = nullptr;       // logdet partials [nt + 1]
   double* sig = nullptr;      // Sigma workspace
+  double* selws = nullptr;    // selected-inversion pre-pass (diagonal inverses)
   __half* digits = nullptr;   // Ozaki only
   int* erow = nullptr;        // Ozaki only
   // bound caller buffers
@@ -271,6 +272,7 @@ int build_args(gbta_batch* bt) {
     s.ntasks = q.n_stasks;
     s.fdig = q.digits;
     s.ecol = q.erow;
+    s.cinv = q.selws + (size_t)g.nt * g.B * gbta::TS * gbta::TS;
     s.c = batch_ctl(bt, flags, EP_SELINV);
     for (int dir = 0; dir < 2; ++dir) {
       gbta::SolveArgs& v = va[dir * n + k];
@@ -349,6 +351,8 @@ int run_async(gbta_batch* bt, int phases, double* logdet_out) {
   }
   if (phases & GBTA_PHASE_SELINV) {
     for (const BatchInst& q : bt->inst)
+      gbta::launch_selinv_prepare(q.g, q.D, q.L, q.R, q.g.a > 0, q.selws, st);
+    for (const BatchInst& q : bt->inst)
       if (q.method == GBTA_METHOD_OZAKI)
         gbta::launch_selinv_oz_prepare(q.g, q.D, q.L, q.R, q.g.a > 0, q.digits, q.erow, st);
     if (int r = reset_ticket(bt)) return r;
@@ -406,7 +410,7 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
   // ---- plan the pool
   size_t off = 0, flags_total = 0;
   std::vector<std::vector<int4>> ft(n), st(n);
-  std::vector<size_t> o_ft(n), o_st(n), o_tip(n), o_arw(n), o_ld(n), o_sig(n), o_dig(n), o_erow(n);
+  std::vector<size_t> o_ft(n), o_st(n), o_tip(n), o_arw(n), o_ld(n), o_sig(n), o_sel(n), o_dig(n), o_erow(n);
   for (int k = 0; k < n; ++k) {
     BatchInst& q = bt->inst[k];
     q.g = gbta::Geom{b[k], nt[k], a[k], (b[k] + gbta::TS - 1) / gbta::TS};
@@ -432,6 +436,8 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
     off = align_up(off + (g.nt + 2) * sizeof(double));
     o_sig[k] = off;
     off = align_up(off + (g.nt * bb + (g.nt - 1) * bb + (size_t)g.nt * g.a * g.b + (size_t)g.a * g.a) * sizeof(double));
+    o_sel[k] = off;
+    off = align_up(off + gbta::selinv_prepare_bytes(g));
     o_dig[k] = o_erow[k] = 0;
     if (q.method == GBTA_METHOD_OZAKI) {
       o_dig[k] = off;
@@ -460,6 +466,7 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
     q.arrow_part = reinterpret_cast<double*>(base + o_arw[k]);
     q.ld = reinterpret_cast<double*>(base + o_ld[k]);
     q.sig = reinterpret_cast<double*>(base + o_sig[k]);
+    q.selws = reinterpret_cast<double*>(base + o_sel[k]);
     if (q.method == GBTA_METHOD_OZAKI) {
       q.digits = reinterpret_cast<__half*>(base + o_dig[k]);
       q.erow = reinterpret_cast<int*>(base + o_erow[k]);

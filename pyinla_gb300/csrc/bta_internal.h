@@ -77,7 +77,7 @@ void launch_selinv_oz_prepare(const Geom& g, const double* D, const double* L, c
                               __half* fdig, int* ecol, cudaStream_t stream);
 void launch_selinv_oz(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                       double* SD, double* SL, double* SR, double* ST, int use_arrow, const int4* tasks,
-                      int ntasks, __half* fdig, int* ecol, const LaunchCtl& lc);
+                      int ntasks, __half* fdig, int* ecol, const double* cinv, const LaunchCtl& lc);
 
 void launch_solve(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                   double* Bv, int ldb, int nc, int trans, int use_arrow, double* arrow_part,
@@ -85,7 +85,15 @@ void launch_solve(const Geom& g, const double* D, const double* L, const double*
 
 void launch_selinv(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                    double* SD, double* SL, double* SR, double* ST, int use_arrow, const int4* tasks,
-                   int ntasks, const LaunchCtl& lc);
+                   int ntasks, const double* cinv, const LaunchCtl& lc);
+
+// Selected-inversion pre-pass over the factor (both product methods): replaces every
+// off-diagonal pattern tile F(l,c) by G = F(l,c) F(c,c)^{-1} (in place) and writes
+// C_c = F(c,c)^{-T} F(c,c)^{-1} per diagonal tile into the second half of `ws`
+// (selinv_prepare_bytes; the first half holds F(c,c)^{-1}).
+size_t selinv_prepare_bytes(const Geom& g);
+void launch_selinv_prepare(const Geom& g, const double* D, double* L, double* R, int use_arrow, double* ws,
+                           cudaStream_t stream);
 
 void launch_selinv_writeback(const Geom& g, const double* SD, const double* SL, const double* SR,
                              const double* ST, double* D, double* L, double* R, double* T, int use_arrow,

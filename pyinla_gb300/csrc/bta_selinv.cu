@@ -16,6 +16,124 @@ __global__ void __launch_bounds__(NT, 1) k_selinv(SelinvArgs p) {
   }
 }
 
+// ---- pre-pass: G tiles and the diagonal inverses ------------------------------------
+// "column c is not after column k" for the register layout of smem_potrf (c = g + 4q).
+__device__ __forceinline__ bool col_upto(int q, int k, int g) { return !col_after(q, k, g); }
+
+// X <- X W with W lower triangular (rows of X: lane, columns: warp + 4 q).
+static __device__ void smem_gemm_lower_right(double* X, const double* W) {
+  const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+  __syncthreads();
+  double out[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) out[q] = 0.0;
+#pragma unroll
+  for (int k = 0; k < TS; ++k) {
+    const double xv = X[r * LDS + k];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (col_upto(q, k, g)) out[q] = fma(xv, W[k * LDS + g + 4 * q], out[q]);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < 8; ++q) X[r * LDS + g + 4 * q] = out[q];
+  __syncthreads();
+}
+
+// C <- W^T W with W lower triangular.
+static __device__ void smem_gram_lower(double* C, const double* W) {
+  const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+  __syncthreads();
+  double out[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) out[q] = 0.0;
+#pragma unroll
+  for (int k = 0; k < TS; ++k) {
+    const double wr = W[k * LDS + r];   // W(k, r): zero for k < r
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      if (col_upto(q, k, g)) out[q] = fma(wr, W[k * LDS + g + 4 * q], out[q]);
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) C[r * LDS + g + 4 * q] = out[q];
+  __syncthreads();
+}
+
+// One CTA per diagonal factor tile F = D_i(c, c): finv = F^{-1}, cinv = F^{-T} F^{-1}
+// (identity-padded past the block edge).
+__global__ void __launch_bounds__(NT) k_diag_inverses(const double* D, Geom g, double* finv, double* cinv) {
+  __shared__ double F[TILE_SMEM], W[TILE_SMEM], rd[TS];
+  const int ic = blockIdx.x;
+  const int i = ic / g.B, c = ic % g.B;
+  const size_t bb = (size_t)g.b * g.b;
+  tile_load(F, make_tile(D + i * bb, g.b, c * TS, c * TS, g.b, g.b));
+  for (int idx = threadIdx.x; idx < TS * TS; idx += NT) W[(idx / TS) * LDS + idx % TS] = (idx / TS == idx % TS);
+  __syncthreads();
+  tile_pad_identity(F, g.vrows(c));
+  __syncthreads();
+  tile_diag_recip(F, rd);
+  smem_trsm_rln(W, F, rd);   // W = F^{-1}
+  tile_store(finv + (size_t)ic * TS * TS, TS, TS, TS, W);
+  smem_gram_lower(F, W);
+  tile_store(cinv + (size_t)ic * TS * TS, TS, TS, TS, F);
+}
+
+// One CTA per off-diagonal pattern tile F(l, c) of block column i (the slots of D_i
+// below the diagonal, L_i and R_i): G = F(l, c) F(c, c)^{-1}, in place.
+__global__ void __launch_bounds__(NT) k_g_tiles(double* D, double* L, double* R, Geom g, int use_arrow,
+                                                const double* finv) {
+  __shared__ double X[TILE_SMEM], W[TILE_SMEM];
+  const int slot = blockIdx.x;
+  const int B = g.B;
+  const size_t bb = (size_t)g.b * g.b, ab = (size_t)g.a * g.b;
+  int i, c;
+  double* base;
+  int row0, rows;
+  if (slot < g.nt * B * B) {
+    i = slot / (B * B);
+    const int r = (slot / B) % B;
+    c = slot % B;
+    if (r <= c) return;
+    base = D + i * bb;
+    row0 = r * TS;
+    rows = g.b;
+  } else if (slot < (2 * g.nt - 1) * B * B) {
+    const int s2 = slot - g.nt * B * B;
+    i = s2 / (B * B);
+    const int r = (s2 / B) % B;
+    c = s2 % B;
+    base = L + i * bb;
+    row0 = r * TS;
+    rows = g.b;
+  } else if (slot < (2 * g.nt - 1) * B * B + g.nt * B) {
+    if (!use_arrow) return;
+    const int s3 = slot - (2 * g.nt - 1) * B * B;
+    i = s3 / B;
+    c = s3 % B;
+    base = R + i * ab;
+    row0 = 0;
+    rows = g.a;
+  } else {
+    return;
+  }
+  const Tile t = make_tile(base, g.b, row0, c * TS, rows, g.b);
+  tile_load(X, t);
+  tile_load(W, make_tile(finv + (size_t)(i * B + c) * TS * TS, TS, 0, 0, TS, TS));
+  smem_gemm_lower_right(X, W);
+  tile_store(const_cast<double*>(t.p), g.b, t.rows, t.cols, X);
+}
+
+size_t selinv_prepare_bytes(const Geom& g) { return 2 * (size_t)g.nt * g.B * TS * TS * sizeof(double); }
+
+void launch_selinv_prepare(const Geom& g, const double* D, double* L, double* R, int use_arrow, double* ws,
+                           cudaStream_t stream) {
+  double* finv = ws;
+  double* cinv = ws + (size_t)g.nt * g.B * TS * TS;
+  k_diag_inverses<<<g.nt * g.B, NT, 0, stream>>>(D, g, finv, cinv);
+  k_g_tiles<<<g.nflags(), NT, 0, stream>>>(const_cast<double*>(D), L, R, g, use_arrow, finv);
+  count_launches(2);
+}
+
 // Copy Sigma back into the caller's buffers; D_i and T become full symmetric.
 __global__ void k_writeback(const double* SD, const double* SL, const double* SR, const double* ST, double* D,
                             double* L, double* R, double* T, Geom g, int use_arrow) {
@@ -41,7 +159,7 @@ __global__ void k_writeback(const double* SD, const double* SL, const double* SR
 
 void launch_selinv(const Geom& g, const double* D, const double* L, const double* R, const double* T, double* SD,
                    double* SL, double* SR, double* ST, int use_arrow, const int4* tasks, int ntasks,
-                   const LaunchCtl& lc) {
+                   const double* cinv, const LaunchCtl& lc) {
   SelinvArgs p;
   p.D = D;
   p.L = L;
@@ -58,6 +176,7 @@ void launch_selinv(const Geom& g, const double* D, const double* L, const double
   p.ntasks = ntasks;
   p.fdig = nullptr;
   p.ecol = nullptr;
+  p.cinv = cinv;
   p.c.ctrl = lc.ctrl;
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;

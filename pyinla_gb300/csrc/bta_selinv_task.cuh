@@ -8,6 +8,11 @@
 // tile column k and its below-diagonal pattern P_k:
 //   Sigma(j,k) = -( sum_{l in P_k} Sigma(j,l) F(l,k) ) F(k,k)^{-1}      (j in P_k)
 //   Sigma(k,k) =  ( F(k,k)^{-T} - sum_{l in P_k} Sigma(l,k)^T F(l,k) ) F(k,k)^{-1}
+// The factor is fixed during the inversion, so a pre-pass (launch_selinv_prepare)
+// forms, off the critical path, G(l,k) = F(l,k) F(k,k)^{-1} in place of every pattern
+// tile and C_k = F(k,k)^{-T} F(k,k)^{-1} per diagonal tile; then
+//   Sigma(j,k) = -sum_l Sigma(j,l) G(l,k),   Sigma(k,k) = C_k - sum_l Sigma(l,k)^T G(l,k)
+// and no task ends in a triangular solve.
 // P_k of tile column c of block i is: tiles of D_i below c, all tiles of L_i (block
 // row i+1) and the arrow tile.  Every Sigma(j,l) needed lies in a later column, so
 // tasks run column by column from the tip backwards; a task of column k starts its
@@ -48,8 +53,9 @@ struct SelinvArgs {
   int method;           // GBTA_METHOD_FP64 / GBTA_METHOD_OZAKI
   const int4* tasks;
   int ntasks;
-  const __half* fdig;   // Ozaki: transposed factor digits per flag slot
-  const int* ecol;      // Ozaki: per global column (nt*b) exponent of the factor column pattern
+  const __half* fdig;   // Ozaki: transposed digits of the G tiles per flag slot
+  const int* ecol;      // Ozaki: per global column (nt*b) exponent of the G column pattern
+  const double* cinv;   // [nt*B][TS*TS]: F_cc^{-T} F_cc^{-1} of every diagonal factor tile
   Ctl c;
 };
 
@@ -175,6 +181,24 @@ static __device__ void diag_finish(double* X, double* W, const double* F, const 
   __syncthreads();
 }
 
+// X <- C + X, symmetrised (C = F^{-T} F^{-1} of the diagonal factor tile, X = -Z).
+static __device__ void diag_from_cinv(double* X, const double* C) {
+  double v[PER_THREAD];
+#pragma unroll
+  for (int k = 0; k < PER_THREAD; ++k) {
+    const int idx = threadIdx.x + k * NT;
+    const int r = idx / TS, cc = idx % TS;
+    v[k] = 0.5 * ((C[r * LDS + cc] + X[r * LDS + cc]) + (C[cc * LDS + r] + X[cc * LDS + r]));
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < PER_THREAD; ++k) {
+    const int idx = threadIdx.x + k * NT;
+    X[(idx / TS) * LDS + idx % TS] = v[k];
+  }
+  __syncthreads();
+}
+
 // Shared memory of the FP64 selected-inversion task: 4 tiles (K-loop double buffer;
 // X, F, W alias its first three) and the TS reciprocals of the diagonal factor tile.
 constexpr size_t FP64S_SMEM = 4 * TILE_SMEM * sizeof(double) + TS * sizeof(double);
@@ -217,7 +241,7 @@ static __device__ __forceinline__ bool selinv_fp64_task(const SelinvArgs& p, int
     Acc acc;
     acc_zero(acc);
     if (type == ST_OFF) {
-      // Y = sum_l Sigma(j,l) F(l,col); Sigma(j,col) = -Y F(col,col)^{-1}
+      // Sigma(j,col) = -sum_l Sigma(j,l) G(l,col)
       auto step_of = [&](int s) -> Step {
         const int l = pat_code(p, i, col, s);
         const SigTile st_ = sig_tile(p, i, j, l);
@@ -230,21 +254,15 @@ static __device__ __forceinline__ bool selinv_fp64_task(const SelinvArgs& p, int
         st.fb = nullptr;
         return st;
       };
-      if (!kloop<true>(acc, np, step_of, c, bufs, &s_ok)) return false;   // acc = -Y
+      if (!kloop<true>(acc, np, step_of, c, bufs, &s_ok)) return false;   // acc = -Y = Sigma(j,col)
       acc_to_smem(acc, X);
       __syncthreads();
-      tile_load(F, fac_tile(p, i, col, col));
-      __syncthreads();
-      tile_pad_identity(F, g.vrows(col));
-      __syncthreads();
-      tile_diag_recip(F, rd);
-      smem_trsm_rln(X, F, rd);
       const SigTile d = sig_dest(p, i, j, col);
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
       cta_publish(c, const_cast<int*>(d.flag));
       trace_task(c, t, type, t_task0);
     } else {   // ST_DIAG
-      // Z = sum_l Sigma(l,col)^T F(l,col)
+      // Z = sum_l Sigma(l,col)^T G(l,col); Sigma(col,col) = F^{-T} F^{-1} - Z
       auto step_of = [&](int s) -> Step {
         const int l = pat_code(p, i, col, s);
         const SigTile st_ = sig_dest(p, i, l, col);
@@ -257,16 +275,11 @@ static __device__ __forceinline__ bool selinv_fp64_task(const SelinvArgs& p, int
         st.fb = nullptr;
         return st;
       };
-      if (!kloop<false>(acc, np, step_of, c, bufs, &s_ok)) return false;
+      if (!kloop<true>(acc, np, step_of, c, bufs, &s_ok)) return false;   // acc = -Z
       acc_to_smem(acc, X);
+      tile_load(F, make_tile(p.cinv + (size_t)(i * g.B + col) * TS * TS, TS, 0, 0, TS, TS));
       __syncthreads();
-      tile_load(F, fac_tile(p, i, col, col));
-      __syncthreads();
-      tile_pad_identity(F, g.vrows(col));
-      __syncthreads();
-      tile_diag_recip(F, rd);
-      __syncthreads();
-      diag_finish(X, W, F, rd);
+      diag_from_cinv(X, F);
       const SigTile d = sig_dest(p, i, col, col);
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
       cta_publish(c, const_cast<int*>(d.flag));
@@ -457,27 +470,20 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       return false;
     }
     __syncthreads();
-    // ST_OFF: X = -Y ; ST_DIAG: X = Z = -acc.v
+    // acc.v = -(sum of the products): ST_OFF: Sigma(j,col); ST_DIAG: -Z
 #pragma unroll
     for (int n = 0; n < 2; ++n)
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
-        X[oz_row(n, q) * LDS + oz_col(n, q)] = (type == ST_OFF) ? acc.v[n][q] : -acc.v[n][q];
-    __syncthreads();
-    const size_t bb = (size_t)g.b * g.b;
-    tile_load(F, make_tile(p.D + i * bb, g.b, col * TS, col * TS, g.b, g.b));
-    __syncthreads();
-    tile_pad_identity(F, g.vrows(col));
-    __syncthreads();
-    tile_diag_recip(F, rd);
+      for (int q = 0; q < 4; ++q) X[oz_row(n, q) * LDS + oz_col(n, q)] = acc.v[n][q];
     if (type == ST_OFF) {
-      smem_trsm_rln(X, F, rd);
+      __syncthreads();
       const SigTile d = sig_dest(p, i, j, col);
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
       cta_publish(c, const_cast<int*>(d.flag));
     } else {
+      tile_load(F, make_tile(p.cinv + (size_t)(i * g.B + col) * TS * TS, TS, 0, 0, TS, TS));
       __syncthreads();
-      diag_finish(X, W, F, rd);
+      diag_from_cinv(X, F);
       const SigTile d = sig_dest(p, i, col, col);
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
       cta_publish(c, const_cast<int*>(d.flag));
