@@ -68,22 +68,40 @@ __device__ __forceinline__ void oz_digits(double x, int E, int (&d)[OZ_S]) {
   for (int s = 0; s < OZ_S; ++s) d[s] = sgn * (int)((F >> (54 - OZ_W * (s + 1))) & 63);
 }
 
+// Two signed digits (|d| <= 63) as an exact fp16 pair without conversion instructions:
+// the fp16 bit pattern 0x6400 + n is the integer 1024 + n for 0 <= n < 1024, so
+// (0x6400 + 64 + d) - 1088 = d exactly (1088 = 0x6440), one half2 subtraction for both.
+__device__ __forceinline__ unsigned oz_digit_pair(int d0, int d1) {
+  const unsigned bits = (unsigned)(0x6440 + d0) | ((unsigned)(0x6440 + d1) << 16);
+  const __half h1088 = __ushort_as_half((unsigned short)0x6440);
+  const __half2 h = __hsub2(*reinterpret_cast<const __half2*>(&bits), __halves2half2(h1088, h1088));
+  return *reinterpret_cast<const unsigned*>(&h);
+}
+
 // Write the digit planes of the valid part of a shared FP64 tile X (rows x cols)
-// to dst ([plane][row][col] halves), rows scaled by E[row] (global exponents).
+// to dst ([plane][row][col] halves), rows scaled by E[row] (global exponents).  Each
+// thread converts pairs of adjacent columns and stores them as one 32-bit word.
 __device__ __forceinline__ void oz_store_digits(__half* dst, const double* X, int rows, int cols, const int* E) {
 #pragma unroll
-  for (int k = 0; k < PER_THREAD; ++k) {
-    const int idx = threadIdx.x + k * NT;
-    const int r = idx / TS, c = idx % TS;
-    int d[OZ_S];
+  for (int q = 0; q < PER_THREAD / 2; ++q) {
+    const int p = threadIdx.x + q * NT;
+    const int r = p / (TS / 2), c = 2 * (p % (TS / 2));
+    int d0[OZ_S], d1[OZ_S];
     if (r < rows && c < cols) {
-      oz_digits(X[r * LDS + c], E[r], d);
+      oz_digits(X[r * LDS + c], E[r], d0);
     } else {
 #pragma unroll
-      for (int s = 0; s < OZ_S; ++s) d[s] = 0;
+      for (int s = 0; s < OZ_S; ++s) d0[s] = 0;
     }
+    if (r < rows && c + 1 < cols) {
+      oz_digits(X[r * LDS + c + 1], E[r], d1);
+    } else {
 #pragma unroll
-    for (int s = 0; s < OZ_S; ++s) dst[s * TS * TS + idx] = __int2half_rn(d[s]);
+      for (int s = 0; s < OZ_S; ++s) d1[s] = 0;
+    }
+    unsigned* w = reinterpret_cast<unsigned*>(dst + r * TS + c);
+#pragma unroll
+    for (int s = 0; s < OZ_S; ++s) w[s * (TS * TS / 2)] = oz_digit_pair(d0[s], d1[s]);
   }
 }
 

@@ -64,19 +64,28 @@ __global__ void __launch_bounds__(NT) k_fac_digits_t(const double* D, const doub
     return;
   }
   __half* dst = dig + (size_t)slot * OZ_TILE;
+  // pairs of rows (m, m+1) of one column jj: adjacent in the transposed layout
 #pragma unroll
-  for (int k = 0; k < PER_THREAD; ++k) {
-    const int idx = threadIdx.x + k * NT;
-    const int m = idx / TS, jj = idx % TS;   // element (m, jj) of the tile
-    int d[OZ_S];
+  for (int q = 0; q < PER_THREAD / 2; ++q) {
+    const int p = threadIdx.x + q * NT;
+    const int jj = p % TS, m = 2 * (p / TS);
+    const int e = (jj < t.cols) ? ecol[(size_t)i * g.b + c * TS + jj] : 0;
+    int d0[OZ_S], d1[OZ_S];
     if (m < t.rows && jj < t.cols) {
-      oz_digits(t.p[(size_t)m * t.ld + jj], ecol[(size_t)i * g.b + c * TS + jj], d);
+      oz_digits(t.p[(size_t)m * t.ld + jj], e, d0);
     } else {
 #pragma unroll
-      for (int s = 0; s < OZ_S; ++s) d[s] = 0;
+      for (int s = 0; s < OZ_S; ++s) d0[s] = 0;
     }
+    if (m + 1 < t.rows && jj < t.cols) {
+      oz_digits(t.p[(size_t)(m + 1) * t.ld + jj], e, d1);
+    } else {
 #pragma unroll
-    for (int s = 0; s < OZ_S; ++s) dst[s * TS * TS + jj * TS + m] = __int2half_rn(d[s]);
+      for (int s = 0; s < OZ_S; ++s) d1[s] = 0;
+    }
+    unsigned* w = reinterpret_cast<unsigned*>(dst + jj * TS + m);
+#pragma unroll
+    for (int s = 0; s < OZ_S; ++s) w[s * (TS * TS / 2)] = oz_digit_pair(d0[s], d1[s]);
   }
 }
 

@@ -297,32 +297,71 @@ static __device__ __forceinline__ int fac_slot(const Geom& g, int i, int l, int 
   return g.fD(i, l, c);
 }
 // ---- consumer-side slicing of a staged FP64 tile ------------------------------------
-// CTA max |v| of the register-staged tile (all threads return it).
-static __device__ __forceinline__ double cta_absmax(const double (&v)[PER_THREAD], double* red4) {
-  double m = 0.0;
+// The left-operand tile is staged in registers as element pairs that are adjacent in
+// the k dimension of the A operand, so that each digit plane gets one 32-bit shared
+// store per pair:
+//   not transposed (A(m, k) = X(m, k)):  pair (X(r, c), X(r, c+1)), c even;
+//   transposed     (A(m, k) = X(k, m)):  pair (X(r, c), X(r+1, c)), r even.
+// Pair p = threadIdx.x + q * NT (q = 0..3); a warp reads whole 256-byte rows.
+static __device__ __forceinline__ void pair_coords(int p, bool trans, int& r, int& c) {
+  if (trans) {
+    c = p % TS;
+    r = 2 * (p / TS);
+  } else {
+    r = p / (TS / 2);
+    c = 2 * (p % (TS / 2));
+  }
+}
+static __device__ __forceinline__ void tile_ldg_pairs(double (&v)[PER_THREAD], const Tile& t, bool trans) {
 #pragma unroll
-  for (int k = 0; k < PER_THREAD; ++k) m = fmax(m, fabs(v[k]));
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) red4[threadIdx.x >> 5] = m;
-  __syncthreads();
-  m = fmax(fmax(red4[0], red4[1]), fmax(red4[2], red4[3]));
-  __syncthreads();
-  return m;
+  for (int q = 0; q < PER_THREAD / 2; ++q) {
+    int r, c;
+    pair_coords(threadIdx.x + q * NT, trans, r, c);
+    const int r1 = trans ? r + 1 : r, c1 = trans ? c : c + 1;
+    v[2 * q] = (r < t.rows && c < t.cols) ? __ldcg(t.p + (size_t)r * t.ld + c) : 0.0;
+    v[2 * q + 1] = (r1 < t.rows && c1 < t.cols) ? __ldcg(t.p + (size_t)r1 * t.ld + c1) : 0.0;
+  }
 }
 
-// Write the digit planes of the register-staged tile relative to 2^E into the shared
-// A operand ([plane][row][k], padded rows); trans: element (r, c) is A(c, r).
-static __device__ __forceinline__ void oz_slice_to_smem(__half* As, const double (&v)[PER_THREAD], int E, bool trans) {
+// CTA max |v| of the register-staged tile (all threads return it): an integer max of
+// the sign-cleared bit patterns (ordered like the magnitudes), so that no FP64
+// instruction is spent on it.
+static __device__ __forceinline__ double cta_absmax(const double (&v)[PER_THREAD], double* red4) {
+  unsigned long long m = 0;
 #pragma unroll
   for (int k = 0; k < PER_THREAD; ++k) {
-    const int idx = threadIdx.x + k * NT;
-    const int r = idx / TS, c = idx % TS;
-    const int row = trans ? c : r, kk = trans ? r : c;
-    int d[OZ_S];
-    oz_digits(v[k], E, d);
+    const unsigned long long a = (unsigned long long)__double_as_longlong(v[k]) & 0x7fffffffffffffffull;
+    m = a > m ? a : m;
+  }
 #pragma unroll
-    for (int s = 0; s < OZ_S; ++s) As[s * OZ_PLANE + row * OZ_LD + kk] = __int2half_rn(d[s]);
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, m, o);
+    m = x > m ? x : m;
+  }
+  unsigned long long* red = reinterpret_cast<unsigned long long*>(red4);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  unsigned long long r = red[0];
+#pragma unroll
+  for (int w = 1; w < NT / 32; ++w) r = red[w] > r ? red[w] : r;
+  __syncthreads();
+  return __longlong_as_double((long long)r);
+}
+
+// Write the digit planes of the register-staged pairs relative to 2^E into the shared
+// A operand ([plane][row][k], padded rows).
+static __device__ __forceinline__ void oz_slice_to_smem(__half* As, const double (&v)[PER_THREAD], int E, bool trans) {
+#pragma unroll
+  for (int q = 0; q < PER_THREAD / 2; ++q) {
+    int r, c;
+    pair_coords(threadIdx.x + q * NT, trans, r, c);
+    const int row = trans ? c : r, kk = trans ? r : c;
+    int d0[OZ_S], d1[OZ_S];
+    oz_digits(v[2 * q], E, d0);
+    oz_digits(v[2 * q + 1], E, d1);
+    unsigned* dst = reinterpret_cast<unsigned*>(As + row * OZ_LD + kk);
+#pragma unroll
+    for (int s = 0; s < OZ_S; ++s) dst[s * (OZ_PLANE / 2)] = oz_digit_pair(d0[s], d1[s]);
   }
 }
 
@@ -412,7 +451,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       ok = cta_wait(c, lt.flag, nullptr, &s_ok);
       if (ok) {
         if (threadIdx.x == 0) s_ready = 1;
-        tile_ldg(vreg, lt.t);
+        tile_ldg_pairs(vreg, lt.t, lt.trans);
         oz_load_async(stages + OZ_OPER, right_of(0));
         cp_async_commit();
         const double mx = cta_absmax(vreg, red4);
@@ -435,7 +474,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
             __syncthreads();
           }
           if (s_ready > s + 1) {
-            tile_ldg(vreg, nt_.t);
+            tile_ldg_pairs(vreg, nt_.t, nt_.trans);
             oz_load_async(nxt + OZ_OPER, right_of(s + 1));
             cp_async_commit();
             have = true;
@@ -447,7 +486,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
           if (!have) {
             if (!(ok = cta_wait(c, nt_.flag, nullptr, &s_ok))) break;
             if (threadIdx.x == 0) s_ready = s + 2;
-            tile_ldg(vreg, nt_.t);
+            tile_ldg_pairs(vreg, nt_.t, nt_.trans);
             oz_load_async(nxt + OZ_OPER, right_of(s + 1));
             cp_async_commit();
           }
