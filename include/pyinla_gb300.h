@@ -73,6 +73,12 @@ long long gbta_kernel_launches(void);
  * SM (`iters` FMA rounds per thread); the roofline denominator of the FP64 kernels. */
 int gbta_probe_fp64_peak(int iters, double* tflops);
 
+/* Clock cycles per call of the 32 x 32 tile routines, each timed alone on one CTA:
+ * cycles[0] tile reload (included in the others), [1] tile Cholesky, [2] reciprocals
+ * + X F^{-T}, [3] reciprocals + X F^{-1}, [4] digit planes, [5] tile store.  No
+ * reference counterpart (a measurement aid). */
+int gbta_probe_tiles(int iters, long long* cycles);
+
 /* Text of the last error raised on the calling thread ("" if none). */
 const char* gbta_last_error(void);
 

@@ -1,0 +1,75 @@
+// Cycle counts of the 32 x 32 tile routines on the critical paths of the factorization
+// and the selected inversion, each timed alone on one CTA of 128 threads (clock64 over
+// `iters` repetitions, every repetition reloading the tile from global memory, whose
+// cost is reported separately): tile Cholesky, reciprocals + X F^{-T}, reciprocals +
+// X F^{-1}, digit planes of a tile, and a tile store.  The tile is a diagonally
+// dominant SPD matrix built in the kernel.
+#include <cuda_runtime.h>
+
+#include "../../include/pyinla_gb300.h"
+#include "bta_ozaki.cuh"
+
+namespace gbta {
+
+__global__ void __launch_bounds__(NT) k_probe_tiles(double* scratch, __half* dig, long long* cyc, int iters) {
+  __shared__ double X[TILE_SMEM], F[TILE_SMEM], rd[TS];
+  __shared__ int E[TS];
+  double* A = scratch;              // SPD tile (TS x TS, row-major)
+  double* Bm = scratch + TS * TS;   // general tile
+  for (int idx = threadIdx.x; idx < TS * TS; idx += NT) {
+    const int r = idx / TS, c = idx % TS;
+    const int lo = r < c ? r : c, hi = r < c ? c : r;
+    const double h = (double)((lo * 131 + hi * 71) % 97) / 97.0 - 0.5;   // symmetric pattern
+    A[idx] = (r == c) ? 2.0 + h : h / TS;
+    Bm[idx] = (double)((r * 37 + c * 11) % 89) / 89.0 - 0.5;
+  }
+  if (threadIdx.x < TS) E[threadIdx.x] = 2;
+  __syncthreads();
+  const Tile ta = make_tile(A, TS, 0, 0, TS, TS), tb = make_tile(Bm, TS, 0, 0, TS, TS);
+  long long t0, t1;
+#define GBTA_TIMED(slot, body)                                    \
+  __syncthreads();                                                \
+  t0 = clock64();                                                 \
+  for (int it = 0; it < iters; ++it) {                            \
+    body                                                          \
+  }                                                               \
+  t1 = clock64();                                                 \
+  if (threadIdx.x == 0) cyc[slot] = (t1 - t0) / iters;
+  GBTA_TIMED(0, tile_load(X, ta); __syncthreads();)
+  GBTA_TIMED(1, tile_load(X, ta); __syncthreads(); smem_potrf(X);)
+  tile_load(F, ta);
+  __syncthreads();
+  smem_potrf(F);
+  GBTA_TIMED(2, tile_load(X, tb); __syncthreads(); tile_diag_recip(F, rd); smem_trsm_rlt(X, F, rd);)
+  GBTA_TIMED(3, tile_load(X, tb); __syncthreads(); tile_diag_recip(F, rd); smem_trsm_rln(X, F, rd);)
+  GBTA_TIMED(4, tile_load(X, tb); __syncthreads(); oz_store_digits(dig, X, TS, TS, E); __syncthreads();)
+  GBTA_TIMED(5, tile_load(X, tb); __syncthreads(); tile_store(scratch + 2 * TS * TS, TS, TS, TS, X); __syncthreads();)
+#undef GBTA_TIMED
+}
+
+}  // namespace gbta
+
+extern "C" int gbta_set_error(int code, const char* msg);
+
+extern "C" int gbta_probe_tiles(int iters, long long* cycles) {
+  if (!cycles || iters < 1) return gbta_set_error(GBTA_ERR_ARG, "probe: need iters >= 1 and an output");
+  double* scratch = nullptr;
+  __half* dig = nullptr;
+  long long* cyc = nullptr;
+  if (cudaMalloc(&scratch, 3 * gbta::TS * gbta::TS * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&dig, gbta::OZ_TILE * sizeof(__half)) != cudaSuccess ||
+      cudaMalloc(&cyc, 6 * sizeof(long long)) != cudaSuccess) {
+    cudaFree(scratch);
+    cudaFree(dig);
+    return gbta_set_error(GBTA_ERR_ALLOC, "probe: cudaMalloc failed");
+  }
+  gbta::k_probe_tiles<<<1, gbta::NT>>>(scratch, dig, cyc, iters);
+  gbta::count_launches(1);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(cycles, cyc, 6 * sizeof(long long), cudaMemcpyDeviceToHost);
+  cudaFree(scratch);
+  cudaFree(dig);
+  cudaFree(cyc);
+  if (e != cudaSuccess) return gbta_set_error(GBTA_ERR_CUDA, cudaGetErrorString(e));
+  return GBTA_OK;
+}

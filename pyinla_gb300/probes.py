@@ -1,0 +1,40 @@
+"""Measurement probes of the GPU at hand: ``python -m pyinla_gb300.probes``.
+
+Prints the chip's FP64 FMA rate (the roofline denominator of the FP64 kernels) and
+the cycle counts of the 32 x 32 tile routines that sit on the dataflow critical
+paths (see gbta_probe_tiles in include/pyinla_gb300.h).
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+
+import numpy as np
+
+from . import _lib
+
+
+def fp64_peak_tflops(iters: int = 4000) -> float:
+    lib = _lib.load()
+    out = ctypes.c_double(0.0)
+    _lib.check(lib.gbta_probe_fp64_peak(int(iters), ctypes.byref(out)))
+    return float(out.value)
+
+
+def tile_cycles(iters: int = 200) -> dict:
+    lib = _lib.load()
+    cyc = np.zeros(6, dtype=np.int64)
+    _lib.check(lib.gbta_probe_tiles(int(iters), cyc.ctypes.data))
+    names = ["reload", "potrf", "recip+trsm_rlt", "recip+trsm_rln", "digit_planes", "store"]
+    return {n: int(c) for n, c in zip(names, cyc)}
+
+
+def main() -> None:
+    from . import build
+
+    build.build()
+    print(json.dumps({"fp64_dfma_tflops": fp64_peak_tflops(), "tile_cycles": tile_cycles()}))
+
+
+if __name__ == "__main__":
+    main()
