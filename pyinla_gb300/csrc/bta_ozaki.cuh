@@ -105,6 +105,13 @@ __device__ __forceinline__ void oz_store_digits(__half* dst, const double* X, in
   }
 }
 
+// ilogb of a finite nonzero double given by its magnitude bits (integer instructions
+// only; subnormals through the leading-zero count).
+__device__ __forceinline__ int ilogb_bits(unsigned long long a) {
+  const int e = (int)(a >> 52);
+  return e ? e - 1023 : -1011 - __clzll((long long)a);
+}
+
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
 }
@@ -197,11 +204,11 @@ __device__ __forceinline__ void oz_fold_sub(OzAcc& acc, const int (&esum)[2][4])
         I[d] = __float2int_rn(acc.p[d][n][j]);
         acc.p[d][n][j] = 0.f;
       }
-      // diagonals 2..5, 6..9 and 10..11 in three exact 64-bit integers
+      // diagonals 2..5 and 6..11 in two exact 64-bit integers (|I| < 2^24, so the low
+      // word stays below 2^55), then two conversions and one FMA
       const long long hi = (((long long)I[0] * 64 + I[1]) * 64 + I[2]) * 64 + I[3];
-      const long long mid = (((long long)I[4] * 64 + I[5]) * 64 + I[6]) * 64 + I[7];
-      const long long lo = (long long)I[8] * 64 + I[9];
-      const double vv = fma((double)mid, 0x1p-24, fma((double)lo, 0x1p-36, (double)hi));
+      const long long lo = (((((long long)I[4] * 64 + I[5]) * 64 + I[6]) * 64 + I[7]) * 64 + I[8]) * 64 + I[9];
+      const double vv = fma((double)lo, 0x1p-36, (double)hi);
       const double sc = __longlong_as_double((long long)(1023 + esum[n][j] - 30) << 52);
       acc.v[n][j] = fma(-vv, sc, acc.v[n][j]);
     }

@@ -323,10 +323,12 @@ static __device__ __forceinline__ void tile_ldg_pairs(double (&v)[PER_THREAD], c
   }
 }
 
-// CTA max |v| of the register-staged tile (all threads return it): an integer max of
+// Exponent for slicing the register-staged tile: ilogb(max |v|) + 1 over the CTA, or
+// NO_EXP for an all-zero tile (all threads return it).  The max is an integer max of
 // the sign-cleared bit patterns (ordered like the magnitudes), so that no FP64
 // instruction is spent on it.
-static __device__ __forceinline__ double cta_absmax(const double (&v)[PER_THREAD], double* red4) {
+constexpr int NO_EXP = -100000;
+static __device__ __forceinline__ int cta_tile_exponent(const double (&v)[PER_THREAD], double* red4) {
   unsigned long long m = 0;
 #pragma unroll
   for (int k = 0; k < PER_THREAD; ++k) {
@@ -345,7 +347,7 @@ static __device__ __forceinline__ double cta_absmax(const double (&v)[PER_THREAD
 #pragma unroll
   for (int w = 1; w < NT / 32; ++w) r = red[w] > r ? red[w] : r;
   __syncthreads();
-  return __longlong_as_double((long long)r);
+  return r ? ilogb_bits(r) + 1 : NO_EXP;
 }
 
 // Write the digit planes of the register-staged pairs relative to 2^E into the shared
@@ -419,7 +421,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
     for (int n = 0; n < 2; ++n)
 #pragma unroll
       for (int q = 0; q < 4; ++q) acc.v[n][q] = 0.0;
-    int E = -100000;   // running exponent of the left operand (unset)
+    int E = NO_EXP;   // running exponent of the left operand (unset)
     int esum[2][4];
     auto set_esum = [&]() {
 #pragma unroll
@@ -454,8 +456,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         tile_ldg_pairs(vreg, lt.t, lt.trans);
         oz_load_async(stages + OZ_OPER, right_of(0));
         cp_async_commit();
-        const double mx = cta_absmax(vreg, red4);
-        if (mx > 0.0) E = ilogb(mx) + 1;
+        E = cta_tile_exponent(vreg, red4);
         set_esum();
         oz_slice_to_smem(stages, vreg, E, lt.trans);
       }
@@ -490,16 +491,15 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
             oz_load_async(nxt + OZ_OPER, right_of(s + 1));
             cp_async_commit();
           }
-          const double mx = cta_absmax(vreg, red4);
-          const int En = mx > 0.0 ? ilogb(mx) + 1 : -100000;
+          const int En = cta_tile_exponent(vreg, red4);
           if (En > E || since_fold == OZ_CHUNK) {
-            if (E > -100000) oz_fold_sub(acc, esum);
+            if (E > NO_EXP) oz_fold_sub(acc, esum);
             since_fold = 0;
             if (En > E) E = En;
             set_esum();
           }
           oz_slice_to_smem(nxt, vreg, E, nt_.trans);
-        } else if (E > -100000) {
+        } else if (E > NO_EXP) {
           oz_fold_sub(acc, esum);   // acc.v = -(sum)
         }
       }
