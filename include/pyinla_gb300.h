@@ -79,6 +79,13 @@ int gbta_probe_fp64_peak(int iters, double* tflops);
  * reference counterpart (a measurement aid). */
 int gbta_probe_tiles(int iters, long long* cycles);
 
+/* Clock cycles of the primitives those routines are built from, on one CTA:
+ * cycles[0] dependent DFMA (one warp), [1] independent DFMA per warp instruction (one
+ * warp), [2] the same with four warps, [3] DFMA under a warp-uniform false predicate,
+ * [4] dependent rsqrt.approx.f64 + DADD, [5] dependent 64-bit shuffle, [6] dependent
+ * shared load, [7] bar.sync of four warps.  No reference counterpart. */
+int gbta_probe_latencies(long long* cycles);
+
 /* Text of the last error raised on the calling thread ("" if none). */
 const char* gbta_last_error(void);
 

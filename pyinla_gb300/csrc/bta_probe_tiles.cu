@@ -73,3 +73,106 @@ extern "C" int gbta_probe_tiles(int iters, long long* cycles) {
   if (e != cudaSuccess) return gbta_set_error(GBTA_ERR_CUDA, cudaGetErrorString(e));
   return GBTA_OK;
 }
+
+// Latencies of the primitives the tile routines are built from, on one CTA of 128
+// threads (clock64 over 256 repetitions): [0] dependent DFMA chain (one warp), [1]
+// independent DFMAs per warp instruction (one warp, eight chains), [2] independent
+// DFMAs per warp instruction (four warps, one per sub-partition), [3] a DFMA issued
+// under a warp-uniform false predicate, [4] dependent rsqrt.approx.f64 + DADD, [5]
+// dependent 64-bit shuffle, [6] dependent shared-memory load, [7] bar.sync (4 warps).
+namespace gbta {
+__global__ void __launch_bounds__(NT) k_probe_latency(double* out, long long* cyc, double seed) {
+  __shared__ double sm[NT];
+  sm[threadIdx.x] = seed + threadIdx.x;
+  __syncthreads();
+  double a = seed + threadIdx.x * 1e-3;
+  const double b = 1.0000001, c = 1e-9;
+  const int N = 256;
+  long long t0, t1;
+  if (threadIdx.x < 32) {
+    t0 = clock64();
+#pragma unroll 16
+    for (int i = 0; i < N; ++i) a = fma(a, b, c);
+    t1 = clock64();
+    if (threadIdx.x == 0) cyc[0] = (t1 - t0) / N;
+  }
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = a + k;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    t0 = clock64();
+    for (int i = 0; i < N / 8; ++i) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) x[k] = fma(x[k], b, c);
+    }
+    t1 = clock64();
+    if (threadIdx.x == 0) cyc[1] = (t1 - t0) / N;
+  }
+  __syncthreads();
+  t0 = clock64();
+  for (int i = 0; i < N / 8; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], b, c);
+  }
+  t1 = clock64();
+  if (threadIdx.x == 0) cyc[2] = (t1 - t0) / N;
+  __syncthreads();
+  t0 = clock64();
+  for (int i = 0; i < N / 8; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      if ((int)seed > 1000 + k) x[k] = fma(x[k], b, c);
+  }
+  t1 = clock64();
+  if (threadIdx.x == 0) cyc[3] = (t1 - t0) / N;
+  double y = a;
+  __syncthreads();
+  t0 = clock64();
+  for (int i = 0; i < N; ++i) {
+    asm volatile("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(y));
+    y = y + 1.0;
+  }
+  t1 = clock64();
+  if (threadIdx.x == 0) cyc[4] = (t1 - t0) / N;
+  double s = a;
+  __syncthreads();
+  t0 = clock64();
+  for (int i = 0; i < N; ++i) s = __shfl_sync(0xffffffffu, s, (threadIdx.x + 1) & 31);
+  t1 = clock64();
+  if (threadIdx.x == 0) cyc[5] = (t1 - t0) / N;
+  int idx = threadIdx.x & 7;
+  __syncthreads();
+  t0 = clock64();
+  for (int i = 0; i < N; ++i) idx = (int)sm[idx] & 7;
+  t1 = clock64();
+  if (threadIdx.x == 0) cyc[6] = (t1 - t0) / N;
+  __syncthreads();
+  t0 = clock64();
+  for (int i = 0; i < N; ++i) __syncthreads();
+  t1 = clock64();
+  if (threadIdx.x == 0) cyc[7] = (t1 - t0) / N;
+  double tot = a + y + s + idx;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) tot += x[k];
+  out[threadIdx.x] = tot;
+}
+}  // namespace gbta
+
+extern "C" int gbta_probe_latencies(long long* cycles) {
+  if (!cycles) return gbta_set_error(GBTA_ERR_ARG, "probe: output required");
+  double* out = nullptr;
+  long long* cyc = nullptr;
+  if (cudaMalloc(&out, gbta::NT * sizeof(double)) != cudaSuccess || cudaMalloc(&cyc, 8 * sizeof(long long)) != cudaSuccess) {
+    cudaFree(out);
+    return gbta_set_error(GBTA_ERR_ALLOC, "probe: cudaMalloc failed");
+  }
+  gbta::k_probe_latency<<<1, gbta::NT>>>(out, cyc, 0.5);
+  gbta::count_launches(1);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(cycles, cyc, 8 * sizeof(long long), cudaMemcpyDeviceToHost);
+  cudaFree(out);
+  cudaFree(cyc);
+  if (e != cudaSuccess) return gbta_set_error(GBTA_ERR_CUDA, cudaGetErrorString(e));
+  return GBTA_OK;
+}

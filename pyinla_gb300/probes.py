@@ -1,8 +1,9 @@
 """Measurement probes of the GPU at hand: ``python -m pyinla_gb300.probes``.
 
-Prints the chip's FP64 FMA rate (the roofline denominator of the FP64 kernels) and
-the cycle counts of the 32 x 32 tile routines that sit on the dataflow critical
-paths (see gbta_probe_tiles in include/pyinla_gb300.h).
+Prints the chip's FP64 FMA rate (the roofline denominator of the FP64 kernels), the
+cycle counts of the 32 x 32 tile routines that sit on the dataflow critical paths
+and of the primitives they are built from (gbta_probe_tiles, gbta_probe_latencies in
+include/pyinla_gb300.h).
 """
 from __future__ import annotations
 
@@ -29,11 +30,21 @@ def tile_cycles(iters: int = 200) -> dict:
     return {n: int(c) for n, c in zip(names, cyc)}
 
 
+def primitive_cycles() -> dict:
+    lib = _lib.load()
+    cyc = np.zeros(8, dtype=np.int64)
+    _lib.check(lib.gbta_probe_latencies(cyc.ctypes.data))
+    names = ["dfma_dependent_1warp", "dfma_independent_1warp", "dfma_independent_4warps", "dfma_predicated_off",
+             "rsqrt_approx_f64_plus_dadd", "shfl_f64", "lds_dependent", "bar_sync_4warps"]
+    return {n: int(c) for n, c in zip(names, cyc)}
+
+
 def main() -> None:
     from . import build
 
     build.build()
-    print(json.dumps({"fp64_dfma_tflops": fp64_peak_tflops(), "tile_cycles": tile_cycles()}))
+    print(json.dumps({"fp64_dfma_tflops": fp64_peak_tflops(), "tile_cycles": tile_cycles(),
+                      "primitive_cycles": primitive_cycles()}))
 
 
 if __name__ == "__main__":
