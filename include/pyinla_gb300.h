@@ -86,6 +86,11 @@ int gbta_probe_tiles(int iters, long long* cycles);
  * shared load, [7] bar.sync of four warps.  No reference counterpart. */
 int gbta_probe_latencies(long long* cycles);
 
+/* Chip-wide TFLOP/s of the candidate paths for FP64 tile products: tflops[0] DMMA
+ * (mma.m8n8k4.f64), [1] HMMA (mma.m16n8k16 f16 -> f32), [2] FFMA.  No reference
+ * counterpart (a measurement aid). */
+int gbta_probe_tensor_rates(int iters, double* tflops);
+
 /* Text of the last error raised on the calling thread ("" if none). */
 const char* gbta_last_error(void);
 

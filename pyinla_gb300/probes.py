@@ -39,11 +39,18 @@ def primitive_cycles() -> dict:
     return {n: int(c) for n, c in zip(names, cyc)}
 
 
+def tensor_rates(iters: int = 2000) -> dict:
+    lib = _lib.load()
+    out = np.zeros(3, dtype=np.float64)
+    _lib.check(lib.gbta_probe_tensor_rates(int(iters), out.ctypes.data))
+    return {"dmma_f64_tflops": float(out[0]), "hmma_f16_f32_tflops": float(out[1]), "ffma_tflops": float(out[2])}
+
+
 def main() -> None:
     from . import build
 
     build.build()
-    print(json.dumps({"fp64_dfma_tflops": fp64_peak_tflops(), "tile_cycles": tile_cycles(),
+    print(json.dumps({"fp64_dfma_tflops": fp64_peak_tflops(), **tensor_rates(), "tile_cycles": tile_cycles(),
                       "primitive_cycles": primitive_cycles()}))
 
 
