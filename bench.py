@@ -53,6 +53,32 @@ def bta_flops(nt: int, b: int, a: int) -> tuple[float, float]:
     return float(ff), float(fs)
 
 
+# Tile steps of the digit-plane products and the fp16 tensor work of one step: four
+# warps x two k16 slices x 53 digit-plane pairs x two n8 halves of mma.m16n8k16
+# (4096 flops each) = 53 times the 2 * 32^3 FP64 flops of the tile product.
+OZ_STEP_TENSOR_FLOPS = 4 * 2 * 53 * 2 * 4096
+
+
+def oz_tile_steps(nt: int, b: int, a: int) -> tuple[int, int]:
+    """Product steps of the tensor-core factorization and selected inversion (their
+    task DAGs): factor tile (r, c) of block i sums over c earlier tiles, plus the B
+    tiles of the previous block column except for L tiles; selected-inversion column
+    (i, c) has |P| = arrow + B (block i+1, i < nt-1) + (B-1-c) pattern rows, and each
+    of its |P| off-diagonal tasks and its diagonal task sums over all of them."""
+    B = (b + 31) // 32
+    fsteps = 0
+    ssteps = 0
+    for i in range(nt):
+        nprev = B if i > 0 else 0
+        for c in range(B):
+            fsteps += (nprev + c) * (1 + (B - 1 - c) + (1 if a else 0))    # DIAG, OFFD, ARW
+            if i < nt - 1:
+                fsteps += c * B                                          # LOW
+            npat = (1 if a else 0) + (B if i < nt - 1 else 0) + (B - 1 - c)
+            ssteps += npat * (npat + 1)
+    return fsteps, ssteps
+
+
 # ----------------------------------------------------------------------------- clocks
 class ClockSampler:
     """nvidia-smi clock / throttle samples during the timed region (read-only queries)."""
@@ -261,6 +287,21 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         except (ValueError, OSError):
             traffic = None
 
+    # the same launch seen from the tensor pipe: fp16 mma work of its digit-plane
+    # products against the measured bf16 tensor peak of this machine (a kernel timed
+    # inside back-to-back seconds-long steps: the sustained figure)
+    fsteps, ssteps = oz_tile_steps(nt, b, a)
+    tflops = (ssteps if dominant == "sel" else fsteps) * OZ_STEP_TENSOR_FLOPS
+    tachieved = tflops / (avg[dominant] * 1e-3) / 1e12
+    try:
+        mp = json.loads((REPO / "MEASURED_PEAKS.json").read_text())
+        tpeak, tsrc = float(mp["bf16_tflops_sustained"]), "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
+    except (OSError, ValueError, KeyError):
+        tpeak, tsrc = 1700.0, "fallback sustained bf16 figure (MEASURED_PEAKS.json absent)"
+    tensor_pipe = {"achieved": tachieved, "peak": tpeak, "unit": "TFLOP/s", "frac": tachieved / tpeak,
+                   "peak_source": tsrc,
+                   "work": "fp16 mma.sync work of the digit-plane tile products (53x their FP64 flops)"}
+
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -274,8 +315,10 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
                      "frac": achieved / peak_tf if peak_tf else None, "traffic": traffic,
                      "kernel": "k_selinv" if dominant == "sel" else "k_factor",
-                     "peak_source": "measured FP64 DFMA rate of this GPU (gbta_probe_fp64_peak); "
-                                    "GB300 has no faster FP64 tensor path"},
+                     "peak_source": "measured FP64 DFMA rate of this GPU (gbta_probe_fp64_peak; the "
+                                    "pool's MEASURED_PEAKS.json carries no FP64 figure); GB300's FP64 "
+                                    "tensor (DMMA) path measures below it"},
+        "tensor_pipe": tensor_pipe,
         "frac_of_peak_step": value / world / peak_tf if peak_tf else None,
         "gpu_launches": int(launches),
         "clocks": clk,
