@@ -246,6 +246,27 @@ int gbta_contract_kron(gbta_solver* s, int ns, int nv, int nterms, const int* up
                        const double* lik_R, const double* lik_T, const int* arrow_variate, const double* SD,
                        const double* SL, const double* SR, const double* ST, const double* mu, double* out);
 
+/* ---- marginal variances from a selected inverse --------------------------- */
+/* Latent marginal variances out[nt*b + a] = diag(Sigma) in latent order, from the
+ * diagonal blocks SD and the tip ST of a selected inverse (gbta_pobtasi output).
+ * Replaces PyINLA.get_marginal_variances_latent_parameters
+ * (src/pyinla/core/pyinla.py:940-964: _structured_to_spmatrix on the identity's
+ * pattern, structured_solver.py:470-538, then extract_diagonal,
+ * src/pyinla/utils/spmatrix_utils.py:46-63).  Asynchronous on the solver's stream. */
+int gbta_sigma_diagonal(gbta_solver* s, const double* SD, const double* ST, double* out);
+
+/* Observation marginal variances out[r] = (A Sigma A^T)_rr for the nrows rows of the
+ * CSR observation matrix A (device arrays: A_rowptr[nrows + 1], A_col, A_val; columns
+ * in latent order), read from the Sigma blocks SD, SL, SR, ST.  Replaces
+ * PyINLA.get_marginal_variances_observations (src/pyinla/core/pyinla.py:966-1018: Sigma
+ * on the pattern of Q_cond, then the diagonal of the dense product a @ Sigma @ a.T).
+ * Pairs of columns farther apart than neighbouring time blocks are outside the BTA
+ * pattern and contribute 0; a row with a column outside [0, nt*b + a) gets NaN.
+ * Deterministic.  Asynchronous on the solver's stream. */
+int gbta_obs_variances(gbta_solver* s, long long nrows, const long long* A_rowptr, const int* A_col,
+                       const double* A_val, const double* SD, const double* SL, const double* SR,
+                       const double* ST, double* out);
+
 /* ---- many instances in one persistent launch per phase -------------------- */
 /* A batch holds n independent BTA instances of arbitrary geometry (b[k], nt[k], a[k];
  * a[k] = 0: block tridiagonal) -- the Q(theta) of a gradient's central-difference

@@ -452,6 +452,29 @@ class KronGaussianModel:
             return f
         return f, self._adjoint_gradient(theta, coef, quad)
 
+    def marginal_variances(self, theta):
+        """(diag(Sigma), diag(A Sigma A^T)) at theta, Sigma = Q_cond^-1: the two outputs of
+        the reference's run() (pyinla.py:303-311; get_marginal_variances_latent_parameters
+        and get_marginal_variances_observations, pyinla.py:940-1018).  For a Gaussian
+        likelihood Q_cond does not depend on x*, so theta alone fixes them."""
+        from .marginals import DeviceCSR, latent_variances, observation_variances
+        theta = np.asarray(theta, dtype=np.float64)
+        h = self.h
+        h.set_stream(current_stream_ptr())
+        ptrs = self._upload_coef(self.coefficients(theta))
+        self._assemble(ptrs, self.Dc, self.Lc, self.Rc, self.Tc, with_lik=True)
+        has_arrow = self.nb > 0
+        R, T = (self.Rc.data_ptr(), self.Tc.data_ptr()) if has_arrow else (None, None)
+        _lib.check(h.lib.gbta_pobtaf(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T))
+        _lib.check(h.lib.gbta_pobtasi(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T))
+        if getattr(self, "_A_dev", None) is None:
+            self._A_dev = DeviceCSR(self.spec.A)
+        SL = self.Lc if self.nt > 1 else None
+        SR, ST = (self.Rc, self.Tc) if has_arrow else (None, None)
+        lat = latent_variances(h, self.Dc, ST)
+        obs = observation_variances(h, self._A_dev, self.Dc, SL, SR, ST)
+        return lat.cpu().numpy(), obs.cpu().numpy()
+
     def _adjoint_gradient(self, theta, coef: Coefficients, quad: float) -> np.ndarray:
         h = self.h
         lib = h.lib
