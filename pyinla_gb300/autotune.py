@@ -5,7 +5,7 @@ Two choices are made by measurement on the GPU at hand and cached per device:
 * the product method of every instance shape (block size b, arrow a): FP64 FMAs or
   tensor-core digit planes (``GBTA_METHOD_FP64`` / ``GBTA_METHOD_OZAKI``).  The tile
   edge is fixed at 32 by the kernels' layout; what differs between the methods is the
-  shape of the product work per tile step (one FP64 32x32x32 update, or 53 integer
+  shape of the product work per tile step (one FP64 32x32x32 update, or 43 integer
   m16n8k16 products over digit planes) and the data it stages.  Each candidate
   factorizes and inverts a synthetic SPD instance of that (b, a) with ``nt_probe``
   blocks; the faster wins;

@@ -8,17 +8,22 @@
 // integer matrix multiplication unit", IJHPCA 2024):
 //
 //  * every element x of row g is written in fixed point relative to a per-row
-//    exponent E_g with |x| < 2^E_g:  x ~ sign(x) * sum_{s=1..9} d_s 2^(E_g - 6 s),
-//    d_s in [0, 63] (54 bits, rounded to nearest: error <= 2^(E_g - 55)).  The signed digits are
-//    exact in fp16 and are stored once per tile, as 9 "digit planes";
-//  * sum_k x_ik y_jk = sum_{s,t} 2^(E_i + E_j - 6(s+t)) sum_k d_s,ik g_t,jk.  Each
-//    inner sum is an integer matrix product computed by mma.sync; the 53 pairs with
-//    s + t <= 11 are kept (the dropped ones weigh below 2^(E_i+E_j-60) per term in
-//    total, under FP64 rounding of the result) and pairs of equal s + t share one
-//    fp32 accumulator;
-//  * every partial sum is an integer below 9 * 63^2 * 32 * OZ_CHUNK < 2^24, so the
-//    fp32 accumulation is exact; every OZ_CHUNK tile steps the nine diagonals are
-//    combined exactly in 64-bit integers and folded into the FP64 accumulator.
+//    exponent E_g with |x| < 2^E_g: N = round(x 2^(55 - E_g)) (|N| <= 2^55, error
+//    <= 2^(E_g - 56)) in balanced base 128, x ~ sum_{s=0..7} d_s 2^(E_g - 6 - 7 s)
+//    with d_1..d_7 in [-64, 63] and d_0 in [-64, 64].  The digits are exact in fp16
+//    and are stored once per tile, as 8 "digit planes";
+//  * sum_k x_ik y_jk = sum_{s,t} 2^(E_i + E_j - 12 - 7(s+t)) sum_k d_s,ik g_t,jk.  Each
+//    inner sum is an integer matrix product computed by mma.sync; the 43 pairs with
+//    s + t <= 8 are kept (the dropped ones weigh below 2^(E_i+E_j-55) in total for a
+//    32-term tile product, under FP64 rounding of the result) and pairs of equal
+//    s + t share one fp32 accumulator;
+//  * every partial sum is an integer of magnitude below 8 * 64^2 * 32 * OZ_CHUNK < 2^24,
+//    so the fp32 accumulation is exact; every OZ_CHUNK tile steps the nine diagonals
+//    are combined exactly in 64-bit integers and folded into the FP64 accumulator.
+//
+// Balanced digits (rather than magnitude digits with the sign applied) carry 7 bits
+// each at the same product magnitude (|d| <= 64), so 8 planes and 43 pairs give what
+// 9 planes and 53 pairs of 6-bit magnitude digits gave, with a smaller error.
 //
 // For the Cholesky factor the per-row exponents come from the matrix itself: a row of
 // L satisfies sum_j L_gj^2 = Q_gg, so E_g = ilogb(sqrt(Q_gg)) + 2 bounds every element
@@ -31,17 +36,19 @@
 
 namespace gbta {
 
-constexpr int OZ_S = 9;                       // digit planes per tile
-constexpr int OZ_W = 6;                       // bits per digit
-constexpr int OZ_ND = 10;                     // diagonals s + t = 2 .. 11
-constexpr int OZ_CHUNK = 12;                  // tile steps per exact fp32 accumulation
+constexpr int OZ_S = 8;                       // digit planes per tile
+constexpr int OZ_W = 7;                       // bits per digit
+constexpr int OZ_ND = 9;                      // diagonals s + t = 0 .. 8
+constexpr int OZ_CHUNK = 15;                  // tile steps per exact fp32 accumulation
+constexpr int OZ_ZERO = 64;                   // biased field of the digit 0 (field = d + 64)
 constexpr int OZ_LD = 40;                     // shared row stride of a plane (halves): conflict-free ldmatrix
 constexpr int OZ_PLANE = TS * OZ_LD;          // halves per plane in shared memory
 constexpr int OZ_OPER = OZ_S * OZ_PLANE;      // halves per operand tile in shared memory
 constexpr int OZ_TILE = OZ_S * TS * TS;       // halves per tile in the global digit buffer
-constexpr int OZ_CHUNKS16 = OZ_S * TS * 4;    // 16-byte pieces per tile (9 * 32 rows * 64 B)
+constexpr int OZ_CHUNKS16 = OZ_S * TS * 4;    // 16-byte pieces per tile (8 * 32 rows * 64 B)
 
-static_assert(9 * 63 * 63 * TS * OZ_CHUNK < (1 << 24), "fp32 accumulation must stay exact");
+// At most 8 pairs share a diagonal; |d| <= 64.
+static_assert(8 * 64 * 64 * TS * OZ_CHUNK < (1 << 24), "fp32 accumulation must stay exact");
 
 // Row exponent: E = ilogb(sqrt(q)) + 2 (q > 0), so |x| <= sqrt(q) < 2^(E-1).
 __device__ __forceinline__ int oz_row_exponent(double q) {
@@ -49,30 +56,43 @@ __device__ __forceinline__ int oz_row_exponent(double q) {
   return ilogb(sqrt(q)) + 2;
 }
 
-// The nine signed digits of x relative to 2^E (sign applied to every digit).
-__device__ __forceinline__ void oz_digits(double x, int E, int (&d)[OZ_S]) {
+// The eight balanced digits of x relative to 2^E, as biased fields f_s = d_s + 64
+// (f_0 in [0, 128], the others in [0, 127]).  N + sum_s 64 * 128^(7-s) is non-negative
+// and its 7-bit fields are the biased digits, so the balanced decomposition costs
+// shifts and masks only (no carries to propagate).
+__device__ __forceinline__ void oz_digits(double x, int E, int (&f)[OZ_S]) {
   const long long bits = __double_as_longlong(x);
   const int ex = (int)((bits >> 52) & 0x7ff);
-  unsigned long long F = 0;
+  long long N = 0;
   if (ex != 0x7ff && (bits & 0x7fffffffffffffffll) != 0) {
     const unsigned long long m = (bits & 0xfffffffffffffull) | (ex ? (1ull << 52) : 0ull);
-    const int sh = (ex ? ex : 1) - 1075 + 54 - E;   // F = round(|x| 2^(54 - E)) = round(m 2^sh)
+    const int sh = (ex ? ex : 1) - 1075 + 55 - E;   // |N| = round(|x| 2^(55 - E)) = round(m 2^sh)
+    unsigned long long F = 0;
     if (sh >= 0)
-      F = (sh <= 1) ? (m << sh) : ~0ull;
+      F = (sh <= 2) ? (m << sh) : ~0ull;
     else if (sh > -54)
       F = (m + (1ull << (-sh - 1))) >> (-sh);         // round half up on the magnitude
-    if (F >= (1ull << 54)) F = (1ull << 54) - 1;     // only reachable for out-of-bound input
+    if (F > (1ull << 55)) F = 1ull << 55;             // only reachable for out-of-bound input
+    N = bits < 0 ? -(long long)F : (long long)F;
   }
-  const int sgn = bits < 0 ? -1 : 1;
+  constexpr unsigned long long BIAS = 0x0081020408102040ull;   // sum_{s=0..7} 64 * 128^s
+  const unsigned long long P = (unsigned long long)N + BIAS;
+  f[0] = (int)(P >> 49);
 #pragma unroll
-  for (int s = 0; s < OZ_S; ++s) d[s] = sgn * (int)((F >> (54 - OZ_W * (s + 1))) & 63);
+  for (int s = 1; s < OZ_S; ++s) f[s] = (int)((P >> (OZ_W * (OZ_S - 1 - s))) & 127);
 }
 
-// Two signed digits (|d| <= 63) as an exact fp16 pair without conversion instructions:
-// the fp16 bit pattern 0x6400 + n is the integer 1024 + n for 0 <= n < 1024, so
-// (0x6400 + 64 + d) - 1088 = d exactly (1088 = 0x6440), one half2 subtraction for both.
-__device__ __forceinline__ unsigned oz_digit_pair(int d0, int d1) {
-  const unsigned bits = (unsigned)(0x6440 + d0) | ((unsigned)(0x6440 + d1) << 16);
+__device__ __forceinline__ void oz_zero_digits(int (&f)[OZ_S]) {
+#pragma unroll
+  for (int s = 0; s < OZ_S; ++s) f[s] = OZ_ZERO;
+}
+
+// Two digits given by their biased fields (0 <= f <= 128) as an exact fp16 pair
+// without conversion instructions: the fp16 bit pattern 0x6400 + f is the integer
+// 1024 + f, so (0x6400 + f) - 1088 = f - 64 = d exactly (1088 = 0x6440), one half2
+// subtraction for both.
+__device__ __forceinline__ unsigned oz_digit_pair(int f0, int f1) {
+  const unsigned bits = (unsigned)(0x6400 + f0) | ((unsigned)(0x6400 + f1) << 16);
   const __half h1088 = __ushort_as_half((unsigned short)0x6440);
   const __half2 h = __hsub2(*reinterpret_cast<const __half2*>(&bits), __halves2half2(h1088, h1088));
   return *reinterpret_cast<const unsigned*>(&h);
@@ -87,18 +107,14 @@ __device__ __forceinline__ void oz_store_digits(__half* dst, const double* X, in
     const int p = threadIdx.x + q * NT;
     const int r = p / (TS / 2), c = 2 * (p % (TS / 2));
     int d0[OZ_S], d1[OZ_S];
-    if (r < rows && c < cols) {
+    if (r < rows && c < cols)
       oz_digits(X[r * LDS + c], E[r], d0);
-    } else {
-#pragma unroll
-      for (int s = 0; s < OZ_S; ++s) d0[s] = 0;
-    }
-    if (r < rows && c + 1 < cols) {
+    else
+      oz_zero_digits(d0);
+    if (r < rows && c + 1 < cols)
       oz_digits(X[r * LDS + c + 1], E[r], d1);
-    } else {
-#pragma unroll
-      for (int s = 0; s < OZ_S; ++s) d1[s] = 0;
-    }
+    else
+      oz_zero_digits(d1);
     unsigned* w = reinterpret_cast<unsigned*>(dst + r * TS + c);
 #pragma unroll
     for (int s = 0; s < OZ_S; ++s) w[s * (TS * TS / 2)] = oz_digit_pair(d0[s], d1[s]);
@@ -167,7 +183,7 @@ __device__ __forceinline__ void oz_clear_partials(OzAcc& a) {
       for (int j = 0; j < 4; ++j) a.p[d][n][j] = 0.f;
 }
 
-// One tile step: p[s+t] += d_s(A) * d_t(B)^T for the 53 pairs s + t <= 11.
+// One tile step: p[s+t] += d_s(A) * d_t(B)^T for the 43 pairs s + t <= 8.
 __device__ __forceinline__ void oz_step(OzAcc& acc, const __half* As, const __half* Bs) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int m0 = (w >> 1) * 16, n0 = (w & 1) * 16;
@@ -190,8 +206,8 @@ __device__ __forceinline__ void oz_step(OzAcc& acc, const __half* As, const __ha
   }
 }
 
-// Fold the exact partial sums into the FP64 accumulator: v -= sum_D p_D 2^(Ei+Ej-6D)
-// (D = 2..11).
+// Fold the exact partial sums into the FP64 accumulator:
+// v -= sum_D p_D 2^(Ei+Ej-12-7D) (D = 0..8).
 // `esum[n][j]` = E_i + E_j of the thread's elements.  Clears the partials.
 __device__ __forceinline__ void oz_fold_sub(OzAcc& acc, const int (&esum)[2][4]) {
 #pragma unroll
@@ -204,12 +220,13 @@ __device__ __forceinline__ void oz_fold_sub(OzAcc& acc, const int (&esum)[2][4])
         I[d] = __float2int_rn(acc.p[d][n][j]);
         acc.p[d][n][j] = 0.f;
       }
-      // diagonals 2..5 and 6..11 in two exact 64-bit integers (|I| < 2^24, so the low
-      // word stays below 2^55), then two conversions and one FMA
-      const long long hi = (((long long)I[0] * 64 + I[1]) * 64 + I[2]) * 64 + I[3];
-      const long long lo = (((((long long)I[4] * 64 + I[5]) * 64 + I[6]) * 64 + I[7]) * 64 + I[8]) * 64 + I[9];
-      const double vv = fma((double)lo, 0x1p-36, (double)hi);
-      const double sc = __longlong_as_double((long long)(1023 + esum[n][j] - 30) << 52);
+      // diagonals 0..3 and 4..8 in two exact 64-bit integers (|I| < 2^24, so the high
+      // word stays below 2^46 and the low one below 2^53: both convert exactly), then
+      // two conversions and one FMA; diagonal 3 has weight 2^(Ei+Ej-33)
+      const long long hi = (((long long)I[0] * 128 + I[1]) * 128 + I[2]) * 128 + I[3];
+      const long long lo = ((((long long)I[4] * 128 + I[5]) * 128 + I[6]) * 128 + I[7]) * 128 + I[8];
+      const double vv = fma((double)lo, 0x1p-35, (double)hi);
+      const double sc = __longlong_as_double((long long)(1023 + esum[n][j] - 33) << 52);
       acc.v[n][j] = fma(-vv, sc, acc.v[n][j]);
     }
 }

@@ -71,18 +71,14 @@ __global__ void __launch_bounds__(NT) k_fac_digits_t(const double* D, const doub
     const int jj = p % TS, m = 2 * (p / TS);
     const int e = (jj < t.cols) ? ecol[(size_t)i * g.b + c * TS + jj] : 0;
     int d0[OZ_S], d1[OZ_S];
-    if (m < t.rows && jj < t.cols) {
+    if (m < t.rows && jj < t.cols)
       oz_digits(t.p[(size_t)m * t.ld + jj], e, d0);
-    } else {
-#pragma unroll
-      for (int s = 0; s < OZ_S; ++s) d0[s] = 0;
-    }
-    if (m + 1 < t.rows && jj < t.cols) {
+    else
+      oz_zero_digits(d0);
+    if (m + 1 < t.rows && jj < t.cols)
       oz_digits(t.p[(size_t)(m + 1) * t.ld + jj], e, d1);
-    } else {
-#pragma unroll
-      for (int s = 0; s < OZ_S; ++s) d1[s] = 0;
-    }
+    else
+      oz_zero_digits(d1);
     unsigned* w = reinterpret_cast<unsigned*>(dst + jj * TS + m);
 #pragma unroll
     for (int s = 0; s < OZ_S; ++s) w[s * (TS * TS / 2)] = oz_digit_pair(d0[s], d1[s]);
