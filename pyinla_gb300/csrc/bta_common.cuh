@@ -80,6 +80,9 @@ __device__ __forceinline__ void trace_clear_marks(const Ctl& c, int ticket) {
 __device__ __forceinline__ void trace_mark(const Ctl& c, int ticket, int k) {
   if (c.trace && threadIdx.x == 0) c.trace[(long long)TRACE_WORDS * ticket + 4 + k] = (long long)gtimer();
 }
+__device__ __forceinline__ void trace_put(const Ctl& c, int ticket, int k, long long v) {
+  if (c.trace && threadIdx.x == 0) c.trace[(long long)TRACE_WORDS * ticket + 4 + k] = v;
+}
 
 __device__ __forceinline__ void raise_abort(const Ctl& c) { atomicExch(c.ctrl + CTRL_ABORT, 1); }
 

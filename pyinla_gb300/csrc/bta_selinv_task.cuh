@@ -444,6 +444,10 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
     bool ok = true;
     double vreg[PER_THREAD];
     int since_fold = 0;
+    // trace marks: m0 first operand ready, m1 end of the last blocking wait in the
+    // product loop, m2 ns spent in those waits, m3 product steps
+    unsigned long long waited = 0;
+    trace_clear_marks(c, t);
     auto flags_of = [&](int s, const int*& f0, const int*& f1) {
       f0 = left_of(s).flag;
       f1 = nullptr;
@@ -451,6 +455,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
     if (np > 0) {
       SigTile lt = left_of(0);
       ok = cta_wait(c, lt.flag, nullptr, &s_ok);
+      trace_mark(c, t, 0);
       if (ok) {
         if (threadIdx.x == 0) s_ready = 1;
         tile_ldg_pairs(vreg, lt.t, lt.trans);
@@ -485,7 +490,12 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         ++since_fold;
         if (more) {
           if (!have) {
+            const unsigned long long w0 = c.trace ? gtimer() : 0ull;
             if (!(ok = cta_wait(c, nt_.flag, nullptr, &s_ok))) break;
+            if (c.trace) {
+              waited += gtimer() - w0;
+              trace_mark(c, t, 1);
+            }
             if (threadIdx.x == 0) s_ready = s + 2;
             tile_ldg_pairs(vreg, nt_.t, nt_.trans);
             oz_load_async(nxt + OZ_OPER, right_of(s + 1));
@@ -508,6 +518,8 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       cp_async_wait_all();
       return false;
     }
+    trace_put(c, t, 2, (long long)waited);
+    trace_put(c, t, 3, np);
     __syncthreads();
     // acc.v = -(sum of the products): ST_OFF: Sigma(j,col); ST_DIAG: -Z
 #pragma unroll
