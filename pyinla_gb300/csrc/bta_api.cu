@@ -64,6 +64,8 @@ struct gbta_solver {
   size_t ws_bytes = 0;
   int method = GBTA_METHOD_OZAKI;  // how tile products are computed in the factorization
   void* d_digits = nullptr;         // Ozaki digit planes (lazy)
+  void* d_sdig = nullptr;           // Ozaki digit planes of the Sigma tiles (lazy)
+  int* d_sexp = nullptr;            // and their exponents
   int* d_erow = nullptr;            // Ozaki row exponents (lazy)
   size_t digit_bytes = 0;
   long long* d_trace = nullptr;   // task trace of the last launch (when enabled)
@@ -232,6 +234,8 @@ int gbta_destroy(gbta_solver* s) {
   cudaFree(s->d_selws);
   cudaFree(s->d_trace);
   cudaFree(s->d_digits);
+  cudaFree(s->d_sdig);
+  cudaFree(s->d_sexp);
   cudaFree(s->d_erow);
   if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
@@ -432,14 +436,22 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
   double* SL = SD + g.nt * bb;
   double* SR = SL + (g.nt - 1) * bb;
   double* ST = SR + (size_t)g.nt * g.a * g.b;
-  if (s->method == GBTA_METHOD_OZAKI)
+  if (s->method == GBTA_METHOD_OZAKI) {
     if (int r = ensure_digits(s)) return r;
+    if (!s->d_sdig) {
+      GBTA_CUDA(cudaStreamSynchronize(s->stream));
+      const size_t bytes = gbta::selinv_oz_digit_bytes(g), ebytes = (size_t)g.nflags() * sizeof(int);
+      GBTA_CUDA(cudaMalloc(&s->d_sdig, bytes));
+      GBTA_CUDA(cudaMalloc(&s->d_sexp, ebytes));
+      s->digit_bytes += bytes + ebytes;
+    }
+  }
   gbta::launch_selinv_prepare(g, D, L, R, use_arrow, s->d_selws, s->stream);
   if (int r = reset_ticket(s)) return r;
   const gbta::LaunchCtl lc = next_launch(s, s->n_stasks);
   if (s->method == GBTA_METHOD_OZAKI)
     gbta::launch_selinv_oz(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks,
-                           (__half*)s->d_digits, s->d_erow, cinv, lc);
+                           (__half*)s->d_digits, s->d_erow, cinv, (__half*)s->d_sdig, s->d_sexp, lc);
   else
     gbta::launch_selinv(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks, cinv, lc);
   GBTA_CUDA(cudaGetLastError());

@@ -75,9 +75,12 @@ size_t selinv_oz_digit_bytes(const Geom& g);
 // selected inversion).
 void launch_selinv_oz_prepare(const Geom& g, const double* D, const double* L, const double* R, int use_arrow,
                               __half* fdig, int* ecol, cudaStream_t stream);
+// sdig / sexp: digit planes (selinv_oz_digit_bytes) and exponents (nflags ints) of
+// the Sigma tiles, written by the tasks that produce them.
 void launch_selinv_oz(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                       double* SD, double* SL, double* SR, double* ST, int use_arrow, const int4* tasks,
-                      int ntasks, __half* fdig, int* ecol, const double* cinv, const LaunchCtl& lc);
+                      int ntasks, __half* fdig, int* ecol, const double* cinv, __half* sdig, int* sexp,
+                      const LaunchCtl& lc);
 
 void launch_solve(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                   double* Bv, int ldb, int nc, int trans, int use_arrow, double* arrow_part,

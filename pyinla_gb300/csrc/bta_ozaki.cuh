@@ -99,26 +99,36 @@ __device__ __forceinline__ unsigned oz_digit_pair(int f0, int f1) {
 }
 
 // Write the digit planes of the valid part of a shared FP64 tile X (rows x cols)
-// to dst ([plane][row][col] halves), rows scaled by E[row] (global exponents).  Each
-// thread converts pairs of adjacent columns and stores them as one 32-bit word.
-__device__ __forceinline__ void oz_store_digits(__half* dst, const double* X, int rows, int cols, const int* E) {
+// to dst ([plane][row][col] halves), row r relative to 2^Eof(r).  Each thread converts
+// pairs of adjacent columns and stores them as one 32-bit word; the rest is zero.
+template <class EOf>
+__device__ __forceinline__ void oz_store_digits_e(__half* dst, const double* X, int rows, int cols, EOf Eof) {
 #pragma unroll
   for (int q = 0; q < PER_THREAD / 2; ++q) {
     const int p = threadIdx.x + q * NT;
     const int r = p / (TS / 2), c = 2 * (p % (TS / 2));
     int d0[OZ_S], d1[OZ_S];
     if (r < rows && c < cols)
-      oz_digits(X[r * LDS + c], E[r], d0);
+      oz_digits(X[r * LDS + c], Eof(r), d0);
     else
       oz_zero_digits(d0);
     if (r < rows && c + 1 < cols)
-      oz_digits(X[r * LDS + c + 1], E[r], d1);
+      oz_digits(X[r * LDS + c + 1], Eof(r), d1);
     else
       oz_zero_digits(d1);
     unsigned* w = reinterpret_cast<unsigned*>(dst + r * TS + c);
 #pragma unroll
     for (int s = 0; s < OZ_S; ++s) w[s * (TS * TS / 2)] = oz_digit_pair(d0[s], d1[s]);
   }
+}
+
+// Rows relative to per-row exponents E[row].
+__device__ __forceinline__ void oz_store_digits(__half* dst, const double* X, int rows, int cols, const int* E) {
+  oz_store_digits_e(dst, X, rows, cols, [E](int r) { return E[r]; });
+}
+// All rows relative to one exponent E.
+__device__ __forceinline__ void oz_store_digits_uniform(__half* dst, const double* X, int rows, int cols, int E) {
+  oz_store_digits_e(dst, X, rows, cols, [E](int) { return E; });
 }
 
 // ilogb of a finite nonzero double given by its magnitude bits (integer instructions
@@ -145,8 +155,27 @@ __device__ __forceinline__ void oz_load_async(__half* sdst, const __half* gsrc) 
   }
 }
 
+// Stage a tile's digit planes shifted down by q planes: shared plane s holds global
+// plane s - q (zero for s < q; global planes past the last are dropped).  Reading a
+// tile sliced against 2^E_t in the frame of a larger exponent E = E_t + 7q.
+__device__ __forceinline__ void oz_load_async_shift(__half* sdst, const __half* gsrc, int q) {
+  for (int idx = threadIdx.x; idx < OZ_CHUNKS16; idx += NT) {
+    const int s = idx / (TS * 4), row = (idx / 4) % TS, part = idx % 4;
+    __half* d = sdst + s * OZ_PLANE + row * OZ_LD + part * 8;
+    if (s < q)
+      *reinterpret_cast<uint4*>(d) = make_uint4(0u, 0u, 0u, 0u);
+    else
+      cp_async16(d, gsrc + (s - q) * TS * TS + row * TS + part * 8);
+  }
+}
+
 __device__ __forceinline__ void ldsm_x4(unsigned (&r)[4], const __half* p) {
   asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(smem_u32(p)));
+}
+__device__ __forceinline__ void ldsm_x4_trans(unsigned (&r)[4], const __half* p) {
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                : "r"(smem_u32(p)));
 }
@@ -183,17 +212,26 @@ __device__ __forceinline__ void oz_clear_partials(OzAcc& a) {
       for (int j = 0; j < 4; ++j) a.p[d][n][j] = 0.f;
 }
 
-// One tile step: p[s+t] += d_s(A) * d_t(B)^T for the 43 pairs s + t <= 8.
-__device__ __forceinline__ void oz_step(OzAcc& acc, const __half* As, const __half* Bs) {
+// One tile step: p[s+t] += d_s(A) * d_t(B)^T for the 43 pairs s + t <= 8.  The A
+// planes hold A(m, k) at [m][k], or, with TA, at [k][m] (read with ldmatrix.trans).
+template <bool TA>
+__device__ __forceinline__ void oz_step_t(OzAcc& acc, const __half* As, const __half* Bs) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int m0 = (w >> 1) * 16, n0 = (w & 1) * 16;
   const int ar = m0 + (lane & 7) + ((lane >> 3) & 1) * 8, ac = (lane >> 4) * 8;
+  // transposed A: lane supplies row k = (lane >> 4) * 8 + (lane & 7) at column m
+  const int tr = (lane >> 4) * 8 + (lane & 7), tc = m0 + ((lane >> 3) & 1) * 8;
   const int br = n0 + (lane & 7) + (lane >> 4) * 8, bc = ((lane >> 3) & 1) * 8;
 #pragma unroll
   for (int kk = 0; kk < TS; kk += 16) {
     unsigned a[OZ_S][4], b[OZ_S][4];
+    if (TA) {
 #pragma unroll
-    for (int s = 0; s < OZ_S; ++s) ldsm_x4(a[s], As + s * OZ_PLANE + ar * OZ_LD + kk + ac);
+      for (int s = 0; s < OZ_S; ++s) ldsm_x4_trans(a[s], As + s * OZ_PLANE + (kk + tr) * OZ_LD + tc);
+    } else {
+#pragma unroll
+      for (int s = 0; s < OZ_S; ++s) ldsm_x4(a[s], As + s * OZ_PLANE + ar * OZ_LD + kk + ac);
+    }
 #pragma unroll
     for (int s = 0; s < OZ_S; ++s) ldsm_x4(b[s], Bs + s * OZ_PLANE + br * OZ_LD + kk + bc);
 #pragma unroll
@@ -204,6 +242,10 @@ __device__ __forceinline__ void oz_step(OzAcc& acc, const __half* As, const __ha
         mma16816(acc.p[s + t][1], a[s], b[t][2], b[t][3]);
       }
   }
+}
+
+__device__ __forceinline__ void oz_step(OzAcc& acc, const __half* As, const __half* Bs) {
+  oz_step_t<false>(acc, As, Bs);
 }
 
 // Fold the exact partial sums into the FP64 accumulator:

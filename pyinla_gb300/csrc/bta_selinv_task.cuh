@@ -28,10 +28,11 @@
 //    the right operand F(l,c) is fixed during the inversion, so every factor tile is
 //    sliced once (k_fac_digits_t) relative to per-column exponents
 //    (k_fac_col_exponents: max over the column's pattern) and stored transposed for
-//    the ldmatrix layout; the left operand Sigma tiles are sliced while staged,
-//    relative to the task's running exponent E (the largest tile exponent seen so far
-//    in the task); when a tile raises E, the exact partial sums are first folded into
-//    FP64 with the old E.  Tile inverses and triangular solves stay in FP64.
+//    the ldmatrix layout; every Sigma tile is sliced once, by the task that produces
+//    it, against its own exponent (a multiple of 7), and its consumers stage those
+//    planes shifted to the task's running exponent E (the largest tile exponent seen
+//    so far in the task); when a tile raises E, the exact partial sums are first
+//    folded into FP64 with the old E.  Tile inverses and triangular solves stay in FP64.
 #pragma once
 
 #include "bta_ozaki.cuh"
@@ -56,6 +57,8 @@ struct SelinvArgs {
   const __half* fdig;   // Ozaki: transposed digits of the G tiles per flag slot
   const int* ecol;      // Ozaki: per global column (nt*b) exponent of the G column pattern
   const double* cinv;   // [nt*B][TS*TS]: F_cc^{-T} F_cc^{-1} of every diagonal factor tile
+  __half* sdig;         // Ozaki: digit planes of every Sigma tile per flag slot
+  int* sexp;            // Ozaki: their exponents (multiples of 7, or NO_EXP)
   Ctl c;
 };
 
@@ -296,44 +299,22 @@ static __device__ __forceinline__ int fac_slot(const Geom& g, int i, int l, int 
   if (l >= B) return g.fL(i, l - B, c);
   return g.fD(i, l, c);
 }
-// ---- consumer-side slicing of a staged FP64 tile ------------------------------------
-// The left-operand tile is staged in registers as element pairs that are adjacent in
-// the k dimension of the A operand, so that each digit plane gets one 32-bit shared
-// store per pair:
-//   not transposed (A(m, k) = X(m, k)):  pair (X(r, c), X(r, c+1)), c even;
-//   transposed     (A(m, k) = X(k, m)):  pair (X(r, c), X(r+1, c)), r even.
-// Pair p = threadIdx.x + q * NT (q = 0..3); a warp reads whole 256-byte rows.
-static __device__ __forceinline__ void pair_coords(int p, bool trans, int& r, int& c) {
-  if (trans) {
-    c = p % TS;
-    r = 2 * (p / TS);
-  } else {
-    r = p / (TS / 2);
-    c = 2 * (p % (TS / 2));
-  }
-}
-static __device__ __forceinline__ void tile_ldg_pairs(double (&v)[PER_THREAD], const Tile& t, bool trans) {
-#pragma unroll
-  for (int q = 0; q < PER_THREAD / 2; ++q) {
-    int r, c;
-    pair_coords(threadIdx.x + q * NT, trans, r, c);
-    const int r1 = trans ? r + 1 : r, c1 = trans ? c : c + 1;
-    v[2 * q] = (r < t.rows && c < t.cols) ? __ldcg(t.p + (size_t)r * t.ld + c) : 0.0;
-    v[2 * q + 1] = (r1 < t.rows && c1 < t.cols) ? __ldcg(t.p + (size_t)r1 * t.ld + c1) : 0.0;
-  }
-}
-
-// Exponent for slicing the register-staged tile: ilogb(max |v|) + 1 over the CTA, or
-// NO_EXP for an all-zero tile (all threads return it).  The max is an integer max of
-// the sign-cleared bit patterns (ordered like the magnitudes), so that no FP64
-// instruction is spent on it.
+// Exponent value of an all-zero tile.
 constexpr int NO_EXP = -100000;
-static __device__ __forceinline__ int cta_tile_exponent(const double (&v)[PER_THREAD], double* red4) {
+
+// Exponent of the valid part of a shared tile for its Sigma digit planes: the smallest
+// multiple of 7 with |x| < 2^E (so that tiles of one product loop differ by whole
+// planes), or NO_EXP for an all-zero tile.  Integer max of the magnitude bits.
+static __device__ __forceinline__ int smem_tile_exponent7(const double* X, int rows, int cols, double* red4) {
   unsigned long long m = 0;
 #pragma unroll
   for (int k = 0; k < PER_THREAD; ++k) {
-    const unsigned long long a = (unsigned long long)__double_as_longlong(v[k]) & 0x7fffffffffffffffull;
-    m = a > m ? a : m;
+    const int idx = threadIdx.x + k * NT;
+    const int r = idx / TS, cc = idx % TS;
+    if (r < rows && cc < cols) {
+      const unsigned long long a = (unsigned long long)__double_as_longlong(X[r * LDS + cc]) & 0x7fffffffffffffffull;
+      m = a > m ? a : m;
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -341,46 +322,55 @@ static __device__ __forceinline__ int cta_tile_exponent(const double (&v)[PER_TH
     m = x > m ? x : m;
   }
   unsigned long long* red = reinterpret_cast<unsigned long long*>(red4);
+  __syncthreads();
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
   __syncthreads();
   unsigned long long r = red[0];
 #pragma unroll
   for (int w = 1; w < NT / 32; ++w) r = red[w] > r ? red[w] : r;
   __syncthreads();
-  return r ? ilogb_bits(r) + 1 : NO_EXP;
+  if (!r) return NO_EXP;
+  const int e = ilogb_bits(r) + 1;   // |x| < 2^e
+  return e >= 0 ? 7 * ((e + 6) / 7) : -7 * ((-e) / 7);
 }
 
-// Write the digit planes of the register-staged pairs relative to 2^E into the shared
-// A operand ([plane][row][k], padded rows).
-static __device__ __forceinline__ void oz_slice_to_smem(__half* As, const double (&v)[PER_THREAD], int E, bool trans) {
-#pragma unroll
-  for (int q = 0; q < PER_THREAD / 2; ++q) {
-    int r, c;
-    pair_coords(threadIdx.x + q * NT, trans, r, c);
-    const int row = trans ? c : r, kk = trans ? r : c;
-    int d0[OZ_S], d1[OZ_S];
-    oz_digits(v[2 * q], E, d0);
-    oz_digits(v[2 * q + 1], E, d1);
-    unsigned* dst = reinterpret_cast<unsigned*>(As + row * OZ_LD + kk);
-#pragma unroll
-    for (int s = 0; s < OZ_S; ++s) dst[s * (OZ_PLANE / 2)] = oz_digit_pair(d0[s], d1[s]);
-  }
+// Digit planes and exponent of a finished Sigma tile (shared X, rows x cols valid),
+// written to its flag slot before the tile is published.
+static __device__ __forceinline__ void sig_store_digits(const SelinvArgs& p, int slot, const double* X, int rows,
+                                                        int cols, double* red4) {
+  const int E = smem_tile_exponent7(X, rows, cols, red4);
+  oz_store_digits_uniform(p.sdig + (size_t)slot * OZ_TILE, X, rows, cols, E == NO_EXP ? 0 : E);
+  if (threadIdx.x == 0) p.sexp[slot] = E;
 }
 
-constexpr int OZS_STAGE = 2 * OZ_OPER;   // halves per stage (A, B)
-// X and F follow the two stages; W (used only by the epilogue and the tip task, when
-// no stage is in flight) reuses the first stage, so that two CTAs fit on one SM.
+// Plane shift of a left operand with exponent En in the frame of the running
+// exponent E >= En (both multiples of 7, or NO_EXP): OZ_S drops the whole tile.
+static __device__ __forceinline__ int sig_shift(int E, int En) {
+  if (En == NO_EXP) return E == NO_EXP ? 0 : OZ_S;
+  const int q = (E - En) / 7;
+  return q < OZ_S ? q : OZ_S;
+}
+
+// OZS_STAGE: halves per stage (A, B digit planes).  X and F follow the two stages; W
+// (used only by the tip task, when no stage is in flight) reuses the first stage.
+constexpr int OZS_STAGE = 2 * OZ_OPER;
 constexpr size_t OZS_SMEM = 2 * OZS_STAGE * sizeof(__half) + 2 * TILE_SMEM * sizeof(double) + TS * sizeof(double) +
                             TS * sizeof(int) + 4 * sizeof(double);
 
 // Task t of a tensor-core selected-inversion instance.  `raw` is OZS_SMEM bytes of
 // (16-byte aligned) shared memory.  Returns false when the launch is aborted.
+//
+// Both operands arrive as digit planes: the right one (G) sliced by the pre-pass, the
+// left one (a Sigma tile) sliced once by the task that produced it, against its own
+// exponent E_t (a multiple of 7).  The product loop keeps a running exponent E (the
+// largest E_t so far) and stages each left tile shifted down by (E - E_t) / 7 planes;
+// a tile that raises E first folds the exact partial sums with the old E.
 static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t, unsigned char* raw, int* s_okp,
                                                       int* s_readyp) {
   __half* stages = reinterpret_cast<__half*>(raw);
   double* X = reinterpret_cast<double*>(raw + 2 * OZS_STAGE * sizeof(__half));
   double* F = X + TILE_SMEM;
-  double* W = reinterpret_cast<double*>(raw);   // aliases stage 0 (free in the epilogue)
+  double* W = reinterpret_cast<double*>(raw);   // aliases stage 0 (free in the tip task)
   double* rd = F + TILE_SMEM;
   int* ecol_t = reinterpret_cast<int*>(rd + TS);
   double* red4 = reinterpret_cast<double*>(ecol_t + TS);
@@ -404,6 +394,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       __syncthreads();
       diag_finish(X, W, F, rd);
       tile_store(p.ST, g.a, g.a, g.a, X);
+      sig_store_digits(p, g.fT(), X, g.a, g.a, red4);
       cta_publish(c, c.flags + g.fT());
       trace_task(c, t, type, t_task0);
       return true;
@@ -429,7 +420,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
 #pragma unroll
         for (int q = 0; q < 4; ++q) esum[n][q] = E + ecol_t[oz_col(n, q)];
     };
-    // step s: left tile (FP64) and right digits
+    // step s: left tile (Sigma digits) and right digits (G)
     auto left_of = [&](int s) -> SigTile {
       const int l = pat_code(p, i, col, s);
       if (type == ST_OFF) return sig_tile(p, i, j, l);
@@ -440,9 +431,16 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
     auto right_of = [&](int s) -> const __half* {
       return p.fdig + (size_t)fac_slot(g, i, pat_code(p, i, col, s), col) * OZ_TILE;
     };
+    // stage step s's operands into `dst` with the left tile shifted by q planes
+    auto stage = [&](__half* dst, const SigTile& lt, int q, int s) {
+      const int slot = (int)(lt.flag - c.flags);
+      oz_load_async_shift(dst, p.sdig + (size_t)slot * OZ_TILE, q);
+      oz_load_async(dst + OZ_OPER, right_of(s));
+      cp_async_commit();
+    };
+    auto exp_of = [&](const SigTile& lt) -> int { return __ldcg(p.sexp + (lt.flag - c.flags)); };
 
     bool ok = true;
-    double vreg[PER_THREAD];
     int since_fold = 0;
     // trace marks: m0 first operand ready, m1 end of the last blocking wait in the
     // product loop, m2 ns spent in those waits, m3 product steps
@@ -456,14 +454,12 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       SigTile lt = left_of(0);
       ok = cta_wait(c, lt.flag, nullptr, &s_ok);
       trace_mark(c, t, 0);
+      bool tcur = lt.trans;
       if (ok) {
         if (threadIdx.x == 0) s_ready = 1;
-        tile_ldg_pairs(vreg, lt.t, lt.trans);
-        oz_load_async(stages + OZ_OPER, right_of(0));
-        cp_async_commit();
-        E = cta_tile_exponent(vreg, red4);
+        E = exp_of(lt);
         set_esum();
-        oz_slice_to_smem(stages, vreg, E, lt.trans);
+        stage(stages, lt, 0, 0);
       }
       for (int s = 0; s < np && ok; ++s) {
         __half* cur = stages + (s & 1) * OZS_STAGE;
@@ -473,6 +469,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         const bool more = s + 1 < np;
         bool have = false;
         SigTile nt_;
+        int En = NO_EXP;
         if (more) {
           nt_ = left_of(s + 1);
           if (s_ready <= s + 1) {   // uniform: read after the barrier
@@ -480,13 +477,15 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
             __syncthreads();
           }
           if (s_ready > s + 1) {
-            tile_ldg_pairs(vreg, nt_.t, nt_.trans);
-            oz_load_async(nxt + OZ_OPER, right_of(s + 1));
-            cp_async_commit();
+            En = exp_of(nt_);
+            stage(nxt, nt_, En > E ? 0 : sig_shift(E, En), s + 1);
             have = true;
           }
         }
-        oz_step(acc, cur, cur + OZ_OPER);
+        if (tcur)
+          oz_step_t<true>(acc, cur, cur + OZ_OPER);
+        else
+          oz_step_t<false>(acc, cur, cur + OZ_OPER);
         ++since_fold;
         if (more) {
           if (!have) {
@@ -497,18 +496,18 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
               trace_mark(c, t, 1);
             }
             if (threadIdx.x == 0) s_ready = s + 2;
-            tile_ldg_pairs(vreg, nt_.t, nt_.trans);
-            oz_load_async(nxt + OZ_OPER, right_of(s + 1));
-            cp_async_commit();
+            En = exp_of(nt_);
           }
-          const int En = cta_tile_exponent(vreg, red4);
-          if (En > E || since_fold == OZ_CHUNK) {
+          if ((En > E && En != NO_EXP) || since_fold == OZ_CHUNK) {
             if (E > NO_EXP) oz_fold_sub(acc, esum);
             since_fold = 0;
-            if (En > E) E = En;
-            set_esum();
+            if (En > E && En != NO_EXP) {
+              E = En;
+              set_esum();
+            }
           }
-          oz_slice_to_smem(nxt, vreg, E, nt_.trans);
+          if (!have) stage(nxt, nt_, sig_shift(E, En), s + 1);
+          tcur = nt_.trans;
         } else if (E > NO_EXP) {
           oz_fold_sub(acc, esum);   // acc.v = -(sum)
         }
@@ -530,6 +529,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       __syncthreads();
       const SigTile d = sig_dest(p, i, j, col);
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
+      sig_store_digits(p, (int)(d.flag - c.flags), X, d.t.rows, d.t.cols, red4);
       cta_publish(c, const_cast<int*>(d.flag));
     } else {
       tile_load(F, make_tile(p.cinv + (size_t)(i * g.B + col) * TS * TS, TS, 0, 0, TS, TS));
@@ -537,6 +537,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       diag_from_cinv(X, F);
       const SigTile d = sig_dest(p, i, col, col);
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
+      sig_store_digits(p, (int)(d.flag - c.flags), X, d.t.rows, d.t.cols, red4);
       cta_publish(c, const_cast<int*>(d.flag));
     }
     trace_task(c, t, type, t_task0);
