@@ -438,82 +438,57 @@ __device__ __forceinline__ bool col_before(int q, int j, int g) {  // g + 4q < j
   return 4 * q + 3 < j || (4 * q < j && g < j - 4 * q);
 }
 
-// ---- column dataflow inside a CTA ----------------------------------------------------
-// The column-sequential routines below publish each finished column into their own
-// shared tile and count the published columns in a shared word; a warp waits (acquire,
-// bounded) only for the column it needs next instead of a CTA barrier per column, so
-// that the owner of the next column starts its critical work as soon as the previous
-// column is out while the other warps are still applying older columns.
-__device__ __forceinline__ unsigned smem_addr(const void* p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ int lds_acquire(const int* p) {
-  int v;
-  asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(smem_addr(p)) : "memory");
-  return v;
-}
-__device__ __forceinline__ void sts_release(int* p, int v) {
-  asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(p)), "r"(v) : "memory");
-}
-constexpr int COL_SPIN_LIMIT = 1 << 24;   // a producer warp of the same CTA never stalls this long
-// Wait until *cnt >= target (every lane polls).  False when the limit ran out.
-__device__ __forceinline__ bool col_wait(const int* cnt, int target) {
-  for (int it = 0; it < COL_SPIN_LIMIT; ++it)
-    if (lds_acquire(cnt) >= target) return true;
-  return false;
-}
-// Publish: the warp's shared writes of the column, then the count (release).
-__device__ __forceinline__ void col_publish(int* cnt, int value) {
-  __syncwarp();
-  if ((threadIdx.x & 31) == 0) sts_release(cnt, value);
-}
-
 // In-place lower Cholesky of S (TS x TS; entries past n must already be identity).
 // Returns 0, or the 1-based column of the first non-positive (or NaN) pivot (the
-// tile then holds NaNs); TS + 1 if a column wait ran out (cannot happen while the
-// CTA's warps run).  The strict upper triangle is zeroed.
-// Column j+1 is finished by its owner warp as soon as column j is published (update
-// with column j, pivot l_kk = d y, l_rk = a_rk y, y = 1/sqrt(d)) and written into
-// S[., j+1]; every warp applies column j to its later columns in column order.
+// tile then holds NaNs).  The strict upper triangle is zeroed.
+// Step j publishes pivot column j+1 (l_kk = d y, l_rk = a_rk y, y = 1/sqrt(d)); only
+// the warp owning column j+1 works on the critical path in that step (update of
+// column j+1 with pivot j, then its pivot); it applies pivot j to its other columns
+// one step later, together with pivot j+1.  Pivot columns rotate through three
+// shared slots.
 static __device__ int smem_potrf(double* S) {
-  __shared__ int s_info, s_done;
+  __shared__ double xs[3 * TS];
+  __shared__ int s_info;
   const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
   __syncthreads();
   double acc[8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) acc[q] = S[r * LDS + g + 4 * q];
-  if (threadIdx.x == 0) s_done = 0;
-  __syncthreads();
-  bool ok = true;
   if (g == 0) {
     const double d = __shfl_sync(0xffffffffu, acc[0], 0);
     const double y = rsqrt3(d);
     acc[0] = (r > 0) ? acc[0] * y : (r == 0 ? d * y : 0.0);
-    S[r * LDS] = acc[0];
+    xs[r] = acc[0];
     if (r == 0) s_info = (d > 0.0) ? 0 : 1;
-    col_publish(&s_done, 1);
   }
+  __syncthreads();
 #pragma unroll
   for (int j = 0; j < TS; ++j) {
-    ok = ok && col_wait(&s_done, j + 1);
-    const double lr = S[r * LDS + j];
+    const double* xj = xs + (j % 3) * TS;
     if (j + 1 < TS && g == ((j + 1) & 3)) {
       const int qn = (j + 1) >> 2;
-      const double a = fma(-lr, S[(j + 1) * LDS + j], acc[qn]);
+      const double a = fma(-xj[r], xj[j + 1], acc[qn]);
       const double d = __shfl_sync(0xffffffffu, a, j + 1);
       const double y = rsqrt3(d);
       const double l = (r > j + 1) ? a * y : (r == j + 1 ? d * y : 0.0);
       acc[qn] = l;
-      S[r * LDS + j + 1] = l;
+      xs[((j + 1) % 3) * TS + r] = l;
       if (r == 0 && !(d > 0.0) && s_info == 0) s_info = j + 2;
-      col_publish(&s_done, j + 2);
-    }
+    } else {
+      const double lr = xj[r];
 #pragma unroll
-    for (int q = 0; q < 8; ++q)
-      if (col_after(q, j + 1, g)) acc[q] = fma(-lr, S[(g + 4 * q) * LDS + j], acc[q]);
+      for (int q = 0; q < 8; ++q)
+        if (col_after(q, j + 1, g)) acc[q] = fma(-lr, xj[g + 4 * q], acc[q]);
+      if (j >= 1 && g == (j & 3)) {   // owner of the previous step: its deferred pivot j-1
+        const double* xp = xs + ((j + 2) % 3) * TS;
+        const double lp = xp[r];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (col_after(q, j + 1, g)) acc[q] = fma(-lp, xp[g + 4 * q], acc[q]);
+      }
+    }
+    __syncthreads();
   }
-  if (!ok && r == 0) atomicCAS(&s_info, 0, TS + 1);
-  __syncthreads();
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const int c = g + 4 * q;
@@ -524,42 +499,30 @@ static __device__ int smem_potrf(double* S) {
 }
 
 // X <- X * F^{-T} with F lower triangular; rd = 1/diag(F) (tile_diag_recip).  Row r
-// solves x_r F^T = X_r by forward substitution over the columns: the owner of column
-// j+1 applies column j to it and finishes it as soon as column j is published (into
-// X[., j]); every warp applies column j to its other later columns in column order.
+// solves x_r F^T = X_r by forward substitution over the columns.
 static __device__ void smem_trsm_rlt(double* X, const double* F, const double* rd) {
-  __shared__ int s_done;
+  __shared__ double xs[2 * TS];
   const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
   __syncthreads();
   double acc[8];
 #pragma unroll
   for (int q = 0; q < 8; ++q) acc[q] = X[r * LDS + g + 4 * q];
-  if (threadIdx.x == 0) s_done = 0;
-  __syncthreads();
-  if (g == 0) {
-    acc[0] *= rd[0];
-    X[r * LDS] = acc[0];
-    col_publish(&s_done, 1);
-  }
-  bool ok = true;
 #pragma unroll
   for (int j = 0; j < TS; ++j) {
-    ok = ok && col_wait(&s_done, j + 1);
-    const double xr = X[r * LDS + j];
-    if (j + 1 < TS && g == ((j + 1) & 3)) {
-      const int qn = (j + 1) >> 2;
-      const double x = fma(-xr, F[(j + 1) * LDS + j], acc[qn]) * rd[j + 1];
-      acc[qn] = x;
-      X[r * LDS + j + 1] = x;
-      col_publish(&s_done, j + 2);
+    double* xb = xs + (j & 1) * TS;
+    if (g == (j & 3)) {
+      const double x = acc[j >> 2] * rd[j];
+      acc[j >> 2] = x;
+      xb[r] = x;
     }
+    __syncthreads();
+    const double xr = xb[r];
 #pragma unroll
     for (int q = 0; q < 8; ++q)
-      if (col_after(q, j + 1, g)) acc[q] = fma(-xr, F[(g + 4 * q) * LDS + j], acc[q]);
+      if (col_after(q, j, g)) acc[q] = fma(-xr, F[(g + 4 * q) * LDS + j], acc[q]);
   }
-  __syncthreads();
 #pragma unroll
-  for (int q = 0; q < 8; ++q) X[r * LDS + g + 4 * q] = ok ? acc[q] : __longlong_as_double(0x7ff8000000000000ll);
+  for (int q = 0; q < 8; ++q) X[r * LDS + g + 4 * q] = acc[q];
   __syncthreads();
 }
 
