@@ -442,9 +442,6 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
 
     bool ok = true;
     int since_fold = 0;
-    // exponent of a later step loaded one step ahead (its flag already seen), so that
-    // the load's latency hides under the current step's products
-    int pf_step = -1, pf_exp = NO_EXP;
     // trace marks: m0 first operand ready, m1 end of the last blocking wait in the
     // product loop, m2 ns spent in those waits, m3 product steps
     unsigned long long waited = 0;
@@ -480,13 +477,9 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
             __syncthreads();
           }
           if (s_ready > s + 1) {
-            En = (pf_step == s + 1) ? pf_exp : exp_of(nt_);
+            En = exp_of(nt_);
             stage(nxt, nt_, En > E ? 0 : sig_shift(E, En), s + 1);
             have = true;
-            if (s + 2 < np && s_ready > s + 2) {
-              pf_exp = exp_of(left_of(s + 2));
-              pf_step = s + 2;
-            }
           }
         }
         if (tcur)
