@@ -75,7 +75,8 @@ int gbta_probe_fp64_peak(int iters, double* tflops);
 
 /* Clock cycles per call of the 32 x 32 tile routines, each timed alone on one CTA:
  * cycles[0] tile reload (included in the others), [1] tile Cholesky, [2] reciprocals
- * + X F^{-T}, [3] reciprocals + X F^{-1}, [4] digit planes, [5] tile store.  No
+ * + X F^{-T}, [3] reciprocals + X F^{-1}, [4] digit planes, [5] tile store, [6]
+ * reciprocals + row scaling + X F^{-T} on 8 rows (cycles holds 7 values).  No
  * reference counterpart (a measurement aid). */
 int gbta_probe_tiles(int iters, long long* cycles);
 

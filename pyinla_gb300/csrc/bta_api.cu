@@ -56,6 +56,7 @@ struct gbta_solver {
   int n_stasks = 0;
   double* d_tip_part = nullptr;
   double* d_arrow_part = nullptr;
+  int* d_faux = nullptr;      // feeder flags [nt*B] and row-group counters [nt*B]
   double* d_ld = nullptr;   // logdet partials [nt + 1] + result [1]
   double* d_sig = nullptr;  // selected-inversion output blocks (lazy)
   double* d_selws = nullptr;  // selected-inversion pre-pass: diagonal inverses (lazy)
@@ -77,14 +78,22 @@ namespace gbta {
 
 // Task lists in a topological order of the dataflow DAGs (each task only waits for
 // tasks earlier in the list, so the ticket dispenser cannot deadlock).
+// Per block i, per column c: the feeder's products (they do not need the diagonal tile,
+// so they come first), the diagonal tile, the feeder's row groups (triangular solves
+// split over FEED_ROWS-row tasks, so that the solve on the critical path of the
+// factorization runs on several SMs), the other tiles of the column; then the tip.
 std::vector<int4> factor_task_list(const Geom& g) {
   std::vector<int4> t;
   for (int i = 0; i < g.nt; ++i)
     for (int c = 0; c < g.B; ++c) {
+      const int fk = g.feeder_kind(i, c);
+      if (fk == 1) t.push_back(make_int4(FT_OFFD | FT_PRE, i, c + 1, c));
+      if (fk == 2) t.push_back(make_int4(FT_LOW | FT_PRE, i, 0, c));
       t.push_back(make_int4(FT_DIAG, i, c, c));
-      for (int r = c + 1; r < g.B; ++r) t.push_back(make_int4(FT_OFFD, i, r, c));
+      for (int q = 0; q < g.feeder_quarters(i, c); ++q) t.push_back(make_int4(FT_FEEDQ, i, q, c));
+      for (int r = c + 1 + (fk == 1 ? 1 : 0); r < g.B; ++r) t.push_back(make_int4(FT_OFFD, i, r, c));
       if (i < g.nt - 1)
-        for (int r = 0; r < g.B; ++r) t.push_back(make_int4(FT_LOW, i, r, c));
+        for (int r = (fk == 2 ? 1 : 0); r < g.B; ++r) t.push_back(make_int4(FT_LOW, i, r, c));
       if (g.a > 0) t.push_back(make_int4(FT_ARW, i, 0, c));
     }
   if (g.a > 0) t.push_back(make_int4(FT_TIP, 0, 0, 0));
@@ -205,6 +214,8 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   CREATE_CUDA(cudaMalloc(&s->d_stasks, st.size() * sizeof(int4)));
   CREATE_CUDA(cudaMalloc(&s->d_tip_part, ntile * gbta::TS * gbta::TS * sizeof(double)));
   CREATE_CUDA(cudaMalloc(&s->d_arrow_part, ntile * gbta::TS * gbta::SOLVE_NC * sizeof(double)));
+  CREATE_CUDA(cudaMalloc(&s->d_faux, 2 * ntile * sizeof(int)));
+  CREATE_CUDA(cudaMemsetAsync(s->d_faux, 0, 2 * ntile * sizeof(int), s->stream));
   CREATE_CUDA(cudaMalloc(&s->d_ld, (nt + 2) * sizeof(double)));
   CREATE_CUDA(cudaMallocHost(&s->h_ctrl, CTRL_INTS * sizeof(int)));
   CREATE_CUDA(cudaMemsetAsync(s->d_ctrl, 0, CTRL_INTS * sizeof(int), s->stream));
@@ -214,7 +225,8 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   CREATE_CUDA(cudaStreamSynchronize(s->stream));
 #undef CREATE_CUDA
   s->ws_bytes = CTRL_INTS * sizeof(int) + (size_t)nflags * sizeof(int) + (ft.size() + st.size()) * sizeof(int4) +
-                ntile * gbta::TS * (gbta::TS + gbta::SOLVE_NC) * sizeof(double) + (nt + 2) * sizeof(double);
+                ntile * gbta::TS * (gbta::TS + gbta::SOLVE_NC) * sizeof(double) + (nt + 2) * sizeof(double) +
+                2 * ntile * sizeof(int);
   *out = s;
   g_last_error.clear();
   return GBTA_OK;
@@ -229,6 +241,7 @@ int gbta_destroy(gbta_solver* s) {
   cudaFree(s->d_stasks);
   cudaFree(s->d_tip_part);
   cudaFree(s->d_arrow_part);
+  cudaFree(s->d_faux);
   cudaFree(s->d_ld);
   cudaFree(s->d_sig);
   cudaFree(s->d_selws);
@@ -339,12 +352,14 @@ static int factor_async(gbta_solver* s, double* D, double* L, double* R, double*
   if (s->method == GBTA_METHOD_OZAKI)
     if (int r = ensure_digits(s)) return r;
   if (int r = reset_ticket(s)) return r;
+  const size_t ntile = (size_t)s->g.nt * s->g.B;
+  GBTA_CUDA(cudaMemsetAsync(s->d_faux + ntile, 0, ntile * sizeof(int), s->stream));   // row-group counters
   const gbta::LaunchCtl lc = next_launch(s, s->n_ftasks);
   if (s->method == GBTA_METHOD_OZAKI)
     gbta::launch_factor_oz(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part,
-                           (__half*)s->d_digits, s->d_erow, lc);
+                           (__half*)s->d_digits, s->d_erow, lc, s->d_faux);
   else
-    gbta::launch_factor(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part, lc);
+    gbta::launch_factor(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part, lc, s->d_faux);
   GBTA_CUDA(cudaGetLastError());
   return GBTA_OK;
 }

@@ -123,6 +123,7 @@ struct BatchInst {
   gbta::Geom g;
   int method = GBTA_METHOD_OZAKI;
   size_t flags_off = 0;     // in ints, into the flag pool
+  size_t faux_off = 0;      // in ints, into the feeder pool (flags [nt*B], counters [nt*B])
   int n_ftasks = 0, n_stasks = 0, n_vtasks = 0;
   // device workspace (inside the pool)
   int4* ftasks = nullptr;
@@ -158,6 +159,8 @@ struct gbta_batch {
   int* d_info = nullptr;
   int* d_flags = nullptr;
   size_t nflags_total = 0;
+  int* d_faux = nullptr;    // feeder flags and row-group counters of every instance
+  size_t nfaux_total = 0;
   void* pool = nullptr;
   size_t pool_bytes = 0;
   int* h_ctrl = nullptr;   // pinned
@@ -256,6 +259,8 @@ int build_args(gbta_batch* bt) {
     f.digits = q.digits;
     f.erow = q.erow;
     f.info = bt->d_info + k;
+    f.feed_pre = bt->d_faux + q.faux_off;
+    f.feed_cnt = f.feed_pre + (size_t)g.nt * g.B;
     f.c = batch_ctl(bt, flags, EP_FACTOR);
     gbta::SelinvArgs& s = sa[k];
     const size_t bb = (size_t)g.b * g.b;
@@ -327,6 +332,7 @@ int run_async(gbta_batch* bt, int phases, double* logdet_out) {
   BATCH_CUDA(cudaMemsetAsync(bt->d_ctrl, 0, CTRL_INTS * sizeof(int), st));
   BATCH_CUDA(cudaMemsetAsync(bt->d_info, 0, bt->n * sizeof(int), st));
   BATCH_CUDA(cudaMemsetAsync(bt->d_flags, 0, bt->nflags_total * sizeof(int), st));
+  BATCH_CUDA(cudaMemsetAsync(bt->d_faux, 0, bt->nfaux_total * sizeof(int), st));
   const gbta::Ctl c = batch_ctl(bt, nullptr, 0);
   if (phases & GBTA_PHASE_FACTOR) {
     for (const BatchInst& q : bt->inst)
@@ -427,6 +433,8 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
     q.n_stasks = (int)st[k].size();
     q.n_vtasks = g.nt * g.B + (g.a > 0 ? 1 : 0);
     q.flags_off = flags_total;
+    q.faux_off = bt->nfaux_total;
+    bt->nfaux_total += 2 * (size_t)g.nt * g.B;
     flags_total += (size_t)g.nflags();
     const size_t ntile = (size_t)g.nt * g.B, bb = (size_t)g.b * g.b;
     o_ft[k] = off;
@@ -459,6 +467,7 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
   bt->nflags_total = flags_total;
   CREATE_CUDA(cudaMalloc(&bt->pool, off));
   CREATE_CUDA(cudaMalloc(&bt->d_flags, flags_total * sizeof(int)));
+  CREATE_CUDA(cudaMalloc(&bt->d_faux, bt->nfaux_total * sizeof(int)));
   CREATE_CUDA(cudaMalloc(&bt->d_ctrl, CTRL_INTS * sizeof(int)));
   CREATE_CUDA(cudaMalloc(&bt->d_info, n * sizeof(int)));
   CREATE_CUDA(cudaMallocHost(&bt->h_ctrl, CTRL_INTS * sizeof(int)));
@@ -504,6 +513,7 @@ int gbta_batch_destroy(gbta_batch* bt) {
   drop_graph(bt);
   cudaFree(bt->pool);
   cudaFree(bt->d_flags);
+  cudaFree(bt->d_faux);
   cudaFree(bt->d_ctrl);
   cudaFree(bt->d_info);
   cudaFree(bt->d_fargs);
@@ -520,7 +530,7 @@ int gbta_batch_destroy(gbta_batch* bt) {
 }
 
 size_t gbta_batch_workspace_bytes(const gbta_batch* bt) {
-  return bt ? bt->pool_bytes + bt->nflags_total * sizeof(int) : 0;
+  return bt ? bt->pool_bytes + (bt->nflags_total + bt->nfaux_total) * sizeof(int) : 0;
 }
 
 int gbta_batch_set_stream(gbta_batch* bt, void* stream) {

@@ -526,6 +526,45 @@ static __device__ void smem_trsm_rlt(double* X, const double* F, const double* r
   __syncthreads();
 }
 
+// Rows row0 .. row0 + 7 of X <- X * F^{-T} (F lower triangular, identity padded).
+// Warp w solves rows row0 + 2w and row0 + 2w + 1: lane l holds columns (l & 15) and
+// (l & 15) + 16 of row row0 + 2w + (l >> 4).  Column j is finished on the lane that
+// holds it and broadcast to its row's 16 lanes with one shuffle, so the sweep needs no
+// barrier; the later columns are updated with one FMA each.  With FS (a copy of F
+// whose row j is scaled by 1/F_jj, see tile_scale_rows_by_recip) and X's columns
+// pre-scaled the same way, no multiplication is left on the column chain.
+static __device__ void smem_trsm_rlt_rows8(double* X, const double* FS, const double* rd, int row0) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int row = row0 + 2 * w + (lane >> 4), cg = lane & 15, base = lane & 16;
+  __syncthreads();
+  double a0 = X[row * LDS + cg] * rd[cg], a1 = X[row * LDS + cg + 16] * rd[cg + 16];
+#pragma unroll
+  for (int j = 0; j < TS; ++j) {
+    const double xj = __shfl_sync(0xffffffffu, j < 16 ? a0 : a1, base | (j & 15));
+    if (j < 15) {
+      const double f0 = FS[cg * LDS + j];
+      if (cg > j) a0 = fma(-xj, f0, a0);
+    }
+    const double f1 = FS[(cg + 16) * LDS + j];
+    if (j < 16 || cg + 16 > j) a1 = fma(-xj, f1, a1);
+  }
+  __syncthreads();
+  X[row * LDS + cg] = a0;
+  X[row * LDS + cg + 16] = a1;
+  __syncthreads();
+}
+
+// FS <- F with row j scaled by rd[j] = 1/F_jj (the strict lower part is what the
+// row solves read).  Caller syncs before and after.
+__device__ __forceinline__ void tile_scale_rows_by_recip(double* FS, const double* F, const double* rd) {
+#pragma unroll
+  for (int k = 0; k < PER_THREAD; ++k) {
+    const int idx = threadIdx.x + k * NT;
+    const int r = idx / TS, c = idx % TS;
+    FS[r * LDS + c] = F[r * LDS + c] * rd[r];
+  }
+}
+
 // X <- X * F^{-1} with F lower triangular; rd = 1/diag(F).  Row r solves x_r F = X_r
 // by backward substitution over the columns.
 static __device__ void smem_trsm_rln(double* X, const double* F, const double* rd) {

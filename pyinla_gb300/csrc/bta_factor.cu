@@ -16,7 +16,7 @@ __global__ void __launch_bounds__(NT, 1) k_factor(FactorArgs p) {
 }
 
 void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow, const int4* tasks,
-                   int ntasks, double* tip_part, const LaunchCtl& lc) {
+                   int ntasks, double* tip_part, const LaunchCtl& lc, int* feed_aux) {
   FactorArgs p;
   p.D = D;
   p.L = L;
@@ -31,6 +31,8 @@ void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, in
   p.digits = nullptr;
   p.erow = nullptr;
   p.info = nullptr;
+  p.feed_pre = feed_aux;
+  p.feed_cnt = feed_aux ? feed_aux + (size_t)g.nt * g.B : nullptr;
   p.c.ctrl = lc.ctrl;
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;

@@ -44,7 +44,8 @@ void launch_row_exponents(const Geom& g, const double* D, const double* T, int u
 size_t factor_oz_digit_bytes(const Geom& g) { return (size_t)g.nflags() * OZ_TILE * sizeof(__half); }
 
 void launch_factor_oz(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow, const int4* tasks,
-                      int ntasks, double* tip_part, __half* digits, int* erow, const LaunchCtl& lc) {
+                      int ntasks, double* tip_part, __half* digits, int* erow, const LaunchCtl& lc,
+                      int* feed_aux) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_factor_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZF_SMEM);
@@ -65,6 +66,8 @@ void launch_factor_oz(const Geom& g, double* D, double* L, double* R, double* T,
   p.method = GBTA_METHOD_OZAKI;
   p.erow = erow;
   p.info = nullptr;
+  p.feed_pre = feed_aux;
+  p.feed_cnt = feed_aux ? feed_aux + (size_t)g.nt * g.B : nullptr;
   p.c.ctrl = lc.ctrl;
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;

@@ -43,6 +43,8 @@ struct FactorArgs {
   __half* digits;       // Ozaki: [nflags][OZ_TILE] digit planes of the final tiles
   const int* erow;      // Ozaki: [nt*b + a] row exponents
   int* info;            // where a failed pivot is recorded (null: the control block)
+  int* feed_pre;        // [nt*B] flag: the feeder of diagonal tile (i, c) has its products
+  int* feed_cnt;        // [nt*B] row groups of that feeder solved so far (zero at launch)
   Ctl c;
 };
 
@@ -62,6 +64,74 @@ static __device__ __forceinline__ Tile btile(const double* blk, const Geom& g, i
 }
 static __device__ __forceinline__ Tile atile(const double* blk, const Geom& g, int c) {
   return make_tile(blk, g.b, 0, c * TS, g.a, g.b);
+}
+
+// The feeder tile of diagonal tile (i, c) (Geom::feeder_kind), its flag slot and the
+// global row of its first row.
+static __device__ __forceinline__ Tile feeder_tile(const FactorArgs& p, int i, int c, int& slot, long long& row0) {
+  const Geom& g = p.g;
+  if (g.feeder_kind(i, c) == 1) {
+    slot = g.fD(i, c + 1, c);
+    row0 = (long long)i * g.b + (c + 1) * TS;
+    return btile(Dblk(p, i), g, c + 1, c);
+  }
+  slot = g.fL(i, 0, c);
+  row0 = (long long)(i + 1) * g.b;
+  return btile(Lblk(p, i), g, 0, c);
+}
+
+// FT_FEEDQ task: rows FEED_ROWS q .. of the feeder of diagonal tile (i, col) <- their
+// products (left there by the FT_PRE task) times D_i(col, col)^{-T}, plus their digit
+// planes (tensor-core method).  The task that completes the last row group publishes
+// the tile.  X, F, FS: shared tiles; rd: TS doubles; erow_t: TS ints (digits only).
+static __device__ bool factor_feed_rows(const FactorArgs& p, int t, int i, int q, int col, double* X, double* F,
+                                        double* FS, double* rd, int* erow_t, int* s_ok, unsigned long long t_task0) {
+  const Geom& g = p.g;
+  const Ctl& c = p.c;
+  int slot;
+  long long grow0;
+  const Tile ft = feeder_tile(p, i, col, slot, grow0);
+  const int gc = i * g.B + col, row0 = q * FEED_ROWS;
+  if (!cta_wait(c, p.feed_pre + gc, c.flags + g.fD(i, col, col), s_ok)) return false;
+  tile_load(F, btile(Dblk(p, i), g, col, col));
+  for (int idx = threadIdx.x; idx < FEED_ROWS * TS; idx += NT) {
+    const int rr = row0 + idx / TS, cc = idx % TS;
+    X[rr * LDS + cc] = (rr < ft.rows && cc < ft.cols) ? __ldcg(ft.p + (size_t)rr * ft.ld + cc) : 0.0;
+  }
+  const bool digits = p.method == GBTA_METHOD_OZAKI && p.digits;
+  if (digits && threadIdx.x < TS) erow_t[threadIdx.x] = threadIdx.x < ft.rows ? p.erow[grow0 + threadIdx.x] : 0;
+  __syncthreads();
+  tile_pad_identity(F, g.vrows(col));
+  __syncthreads();
+  tile_diag_recip(F, rd);
+  __syncthreads();
+  tile_scale_rows_by_recip(FS, F, rd);
+  smem_trsm_rlt_rows8(X, FS, rd, row0);
+  for (int idx = threadIdx.x; idx < FEED_ROWS * TS; idx += NT) {
+    const int rr = row0 + idx / TS, cc = idx % TS;
+    if (rr < ft.rows && cc < ft.cols) const_cast<double*>(ft.p)[(size_t)rr * ft.ld + cc] = X[rr * LDS + cc];
+  }
+  if (digits) {
+    __half* dst = p.digits + (size_t)slot * OZ_TILE;
+    oz_store_digits_rows(dst, X, row0, ft.rows, ft.cols, erow_t);
+    if (q == g.feeder_quarters(i, col) - 1)   // rows past the last group: zero digits
+      for (int idx = threadIdx.x; idx < OZ_S * (TS - row0 - FEED_ROWS) * TS / 2; idx += NT) {
+        const int per = (TS - row0 - FEED_ROWS) * TS / 2;
+        const int sp = idx / per, w = idx % per;
+        reinterpret_cast<unsigned*>(dst + sp * TS * TS + (row0 + FEED_ROWS) * TS)[w] = 0u;
+      }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const int done = atomicAdd(p.feed_cnt + gc, 1) + 1;
+    if (done == g.feeder_quarters(i, col)) {
+      __threadfence();
+      st_release(c.flags + slot, c.epoch);
+    }
+  }
+  trace_task(c, t, FT_FEEDQ, t_task0);
+  return true;
 }
 
 // Stage the diagonal factor tile D_i(c, c) (identity padded) after waiting for it.
@@ -94,8 +164,10 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
   {
     const unsigned long long t_task0 = c.trace ? gtimer() : 0ull;
     const int4 tk = p.tasks[t];
-    const int type = tk.x, i = tk.y, r = tk.z, col = tk.w;
+    const int type = tk.x & 7, i = tk.y, r = tk.z, col = tk.w;
+    const bool pre_only = (tk.x & FT_PRE) != 0;
     if (!p.use_arrow && (type == FT_ARW || type == FT_TIP)) return true;
+    if (type == FT_FEEDQ) return factor_feed_rows(p, t, i, r, col, X, F, sm + 2 * TILE_SMEM, vec, nullptr, &s_ok, t_task0);
 
     Acc acc;
     if (type == FT_TIP) {
@@ -197,6 +269,17 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
     acc_to_smem(acc, X);
     __syncthreads();
 
+    if (pre_only) {   // feeder products: the FT_FEEDQ tasks finish the tile
+      tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
+      cta_publish(c, p.feed_pre + i * g.B + col);
+      if (type == FT_OFFD) {
+        const Tile up = btile(Dblk(p, i), g, col, r);
+        tile_store_zero(const_cast<double*>(up.p), g.b, up.rows, up.cols);
+      }
+      trace_task(c, t, type, t_task0);
+      return true;
+    }
+
     if (type == FT_DIAG) {
       tile_pad_identity(X, g.vrows(col));
       const int info = smem_potrf(X);
@@ -290,8 +373,11 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
   {
     const unsigned long long t_task0 = c.trace ? gtimer() : 0ull;
     const int4 tk = p.tasks[t];
-    const int type = tk.x, i = tk.y, r = tk.z, col = tk.w;
+    const int type = tk.x & 7, i = tk.y, r = tk.z, col = tk.w;
+    const bool pre_only = (tk.x & FT_PRE) != 0;
     if (!p.use_arrow && (type == FT_ARW || type == FT_TIP)) return true;
+    if (type == FT_FEEDQ)
+      return factor_feed_rows(p, t, i, r, col, X, F, reinterpret_cast<double*>(stages), vec, erow_t, &s_ok, t_task0);
     const size_t bb = (size_t)g.b * g.b, ab = (size_t)g.a * g.b;
 
     if (type == FT_TIP) {
@@ -444,6 +530,17 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
 #pragma unroll
       for (int j = 0; j < 4; ++j) X[oz_row(n, j) * LDS + oz_col(n, j)] = acc.v[n][j];
     __syncthreads();
+
+    if (pre_only) {   // feeder products: the FT_FEEDQ tasks finish the tile and its digits
+      tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
+      cta_publish(c, p.feed_pre + i * g.B + col);
+      if (type == FT_OFFD) {
+        const Tile up = make_tile(p.D + i * bb, g.b, col * TS, r * TS, g.b, g.b);
+        tile_store_zero(const_cast<double*>(up.p), g.b, up.rows, up.cols);
+      }
+      trace_task(c, t, type, t_task0);
+      return true;
+    }
 
     if (type == FT_DIAG) {
       tile_pad_identity(X, g.vrows(col));

@@ -11,8 +11,12 @@ namespace gbta {
 
 constexpr int TS = 32;  // tile edge (FP64 elements)
 
-// Task codes of the factorization DAG.
-enum FactorTask { FT_DIAG = 0, FT_OFFD = 1, FT_LOW = 2, FT_ARW = 3, FT_TIP = 4 };
+// Task codes of the factorization DAG.  FT_PRE is a flag on an FT_OFFD / FT_LOW task:
+// the task only forms the tile's products and leaves the triangular solve to the
+// FT_FEEDQ tasks of its rows (the feeder tile of a diagonal tile, see Geom).
+enum FactorTask { FT_DIAG = 0, FT_OFFD = 1, FT_LOW = 2, FT_ARW = 3, FT_TIP = 4, FT_FEEDQ = 5 };
+constexpr int FT_PRE = 8;
+constexpr int FEED_ROWS = 8;   // rows of a feeder tile solved by one FT_FEEDQ task
 // Task codes of the selected-inversion DAG.
 enum SelinvTask { ST_TIP = 0, ST_OFF = 1, ST_DIAG = 2 };
 
@@ -27,6 +31,15 @@ struct Geom {
   __host__ __device__ int vrows(int r) const {   // valid rows of block-tile r
     const int v = b - r * TS;
     return v < TS ? v : TS;
+  }
+  // The feeder of diagonal tile (i, c): the tile right below it in the next global tile
+  // row, whose solve against (i, c) and product with itself are the last steps before
+  // the next diagonal tile can be factored.  0: none (last tile column of the matrix),
+  // 1: D_i(c + 1, c), 2: L_i(0, c) (c = B - 1, i < nt - 1).
+  __host__ __device__ int feeder_kind(int i, int c) const { return c + 1 < B ? 1 : (i < nt - 1 ? 2 : 0); }
+  __host__ __device__ int feeder_rows(int i, int c) const { return feeder_kind(i, c) == 1 ? vrows(c + 1) : vrows(0); }
+  __host__ __device__ int feeder_quarters(int i, int c) const {
+    return feeder_kind(i, c) ? (feeder_rows(i, c) + FEED_ROWS - 1) / FEED_ROWS : 0;
   }
 };
 
@@ -55,8 +68,11 @@ std::vector<int4> selinv_task_list(const Geom& g);
 // Host-side count of kernel launches issued by this library (see gbta_kernel_launches).
 void count_launches(int n);
 
+// feed_aux: 2 * nt * B ints (feeder "products done" flags, then per-feeder counters of
+// solved row groups, which must be zero at launch), or null when the task list has
+// no FT_PRE / FT_FEEDQ tasks.
 void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow,
-                   const int4* tasks, int ntasks, double* tip_part, const LaunchCtl& lc);
+                   const int4* tasks, int ntasks, double* tip_part, const LaunchCtl& lc, int* feed_aux = nullptr);
 
 constexpr int SOLVE_NC = 4;   // right-hand-side columns per solve launch
 
@@ -64,7 +80,7 @@ constexpr int SOLVE_NC = 4;   // right-hand-side columns per solve launch
 size_t factor_oz_digit_bytes(const Geom& g);
 void launch_factor_oz(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow,
                       const int4* tasks, int ntasks, double* tip_part, __half* digits, int* erow,
-                      const LaunchCtl& lc);
+                      const LaunchCtl& lc, int* feed_aux = nullptr);
 
 // Row exponents of the input matrix (before a tensor-core factorization).
 void launch_row_exponents(const Geom& g, const double* D, const double* T, int use_arrow, int* erow,

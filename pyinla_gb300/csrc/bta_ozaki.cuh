@@ -122,6 +122,26 @@ __device__ __forceinline__ void oz_store_digits_e(__half* dst, const double* X, 
   }
 }
 
+// Digit planes of rows row0 .. row0 + FEED_ROWS - 1 of a shared tile (valid part rows x
+// cols, row r relative to 2^E[r]); one column pair per thread.
+__device__ __forceinline__ void oz_store_digits_rows(__half* dst, const double* X, int row0, int rows, int cols,
+                                                     const int* E) {
+  static_assert(FEED_ROWS * TS / 2 == NT, "one column pair of the row group per thread");
+  const int r = row0 + threadIdx.x / (TS / 2), c = 2 * (threadIdx.x % (TS / 2));
+  int d0[OZ_S], d1[OZ_S];
+  if (r < rows && c < cols)
+    oz_digits(X[r * LDS + c], E[r], d0);
+  else
+    oz_zero_digits(d0);
+  if (r < rows && c + 1 < cols)
+    oz_digits(X[r * LDS + c + 1], E[r], d1);
+  else
+    oz_zero_digits(d1);
+  unsigned* w = reinterpret_cast<unsigned*>(dst + r * TS + c);
+#pragma unroll
+  for (int s = 0; s < OZ_S; ++s) w[s * (TS * TS / 2)] = oz_digit_pair(d0[s], d1[s]);
+}
+
 // Rows relative to per-row exponents E[row].
 __device__ __forceinline__ void oz_store_digits(__half* dst, const double* X, int rows, int cols, const int* E) {
   oz_store_digits_e(dst, X, rows, cols, [E](int r) { return E[r]; });

@@ -2,7 +2,8 @@
 // and the selected inversion, each timed alone on one CTA of 128 threads (clock64 over
 // `iters` repetitions, every repetition reloading the tile from global memory, whose
 // cost is reported separately): tile Cholesky, reciprocals + X F^{-T}, reciprocals +
-// X F^{-1}, digit planes of a tile, and a tile store.  The tile is a diagonally
+// X F^{-1}, digit planes of a tile, a tile store, and reciprocals + row scaling + the
+// 8-row X F^{-T} of one quarter of a tile.  The tile is a diagonally
 // dominant SPD matrix built in the kernel.
 #include <cuda_runtime.h>
 
@@ -12,7 +13,7 @@
 namespace gbta {
 
 __global__ void __launch_bounds__(NT) k_probe_tiles(double* scratch, __half* dig, long long* cyc, int iters) {
-  __shared__ double X[TILE_SMEM], F[TILE_SMEM], rd[TS];
+  __shared__ double X[TILE_SMEM], F[TILE_SMEM], FS[TILE_SMEM], rd[TS];
   __shared__ int E[TS];
   double* A = scratch;              // SPD tile (TS x TS, row-major)
   double* Bm = scratch + TS * TS;   // general tile
@@ -44,6 +45,8 @@ __global__ void __launch_bounds__(NT) k_probe_tiles(double* scratch, __half* dig
   GBTA_TIMED(3, tile_load(X, tb); __syncthreads(); tile_diag_recip(F, rd); smem_trsm_rln(X, F, rd);)
   GBTA_TIMED(4, tile_load(X, tb); __syncthreads(); oz_store_digits(dig, X, TS, TS, E); __syncthreads();)
   GBTA_TIMED(5, tile_load(X, tb); __syncthreads(); tile_store(scratch + 2 * TS * TS, TS, TS, TS, X); __syncthreads();)
+  GBTA_TIMED(6, tile_load(X, tb); __syncthreads(); tile_diag_recip(F, rd); __syncthreads();
+             tile_scale_rows_by_recip(FS, F, rd); smem_trsm_rlt_rows8(X, FS, rd, 0);)
 #undef GBTA_TIMED
 }
 
@@ -58,7 +61,7 @@ extern "C" int gbta_probe_tiles(int iters, long long* cycles) {
   long long* cyc = nullptr;
   if (cudaMalloc(&scratch, 3 * gbta::TS * gbta::TS * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&dig, gbta::OZ_TILE * sizeof(__half)) != cudaSuccess ||
-      cudaMalloc(&cyc, 6 * sizeof(long long)) != cudaSuccess) {
+      cudaMalloc(&cyc, 7 * sizeof(long long)) != cudaSuccess) {
     cudaFree(scratch);
     cudaFree(dig);
     return gbta_set_error(GBTA_ERR_ALLOC, "probe: cudaMalloc failed");
@@ -66,7 +69,7 @@ extern "C" int gbta_probe_tiles(int iters, long long* cycles) {
   gbta::k_probe_tiles<<<1, gbta::NT>>>(scratch, dig, cyc, iters);
   gbta::count_launches(1);
   cudaError_t e = cudaDeviceSynchronize();
-  if (e == cudaSuccess) e = cudaMemcpy(cycles, cyc, 6 * sizeof(long long), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(cycles, cyc, 7 * sizeof(long long), cudaMemcpyDeviceToHost);
   cudaFree(scratch);
   cudaFree(dig);
   cudaFree(cyc);

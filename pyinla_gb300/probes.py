@@ -24,9 +24,10 @@ def fp64_peak_tflops(iters: int = 4000) -> float:
 
 def tile_cycles(iters: int = 200) -> dict:
     lib = _lib.load()
-    cyc = np.zeros(6, dtype=np.int64)
+    cyc = np.zeros(7, dtype=np.int64)
     _lib.check(lib.gbta_probe_tiles(int(iters), cyc.ctypes.data))
-    names = ["reload", "potrf", "recip+trsm_rlt", "recip+trsm_rln", "digit_planes", "store"]
+    names = ["reload", "potrf", "recip+trsm_rlt", "recip+trsm_rln", "digit_planes", "store",
+             "recip+scale+trsm_rlt_8rows"]
     return {n: int(c) for n, c in zip(names, cyc)}
 
 
