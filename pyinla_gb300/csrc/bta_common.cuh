@@ -496,24 +496,13 @@ static __device__ int smem_potrf(double* S) {
   __syncthreads();
   bool ok = true;
   if (w == 0) {
-    double lp = 0.0;          // l_{r, j-1}
-    double vn = S[r * LDS];   // column j as read ahead (valid when fn != 0)
-    int fn = 1;
+    double lp = 0.0;   // l_{r, j-1}
 #pragma unroll
     for (int j = 0; j < TS; ++j) {
-      double v = vn;
-      if (!fn) {   // the read-ahead came too early: wait for the column, read it again
-        ok = col_wait(&s_col[j], 1) && ok;
-        v = S[r * LDS + j];
-      }
+      if (j >= 2) ok = col_wait(&s_col[j], 1) && ok;
+      double v = S[r * LDS + j];
       if (j >= 1) v = fma(-lp, __shfl_sync(0xffffffffu, lp, j), v);
       const double d = __shfl_sync(0xffffffffu, v, j);
-      // read column j + 1 ahead: the flag probe and the load (ordered after it by the
-      // acquire) overlap with this column's pivot chain
-      if (j + 1 < TS) {
-        fn = (j + 1 < 2) ? 1 : lds_acquire(&s_col[j + 1]);
-        vn = S[r * LDS + j + 1];
-      }
       const double y = rsqrt3(d);
       double l = ((r == j) ? d : v) * y;
       l = (r < j) ? 0.0 : l;
