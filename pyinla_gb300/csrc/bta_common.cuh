@@ -438,103 +438,62 @@ __device__ __forceinline__ bool col_before(int q, int j, int g) {  // g + 4q < j
   return 4 * q + 3 < j || (4 * q < j && g < j - 4 * q);
 }
 
-// ---- column dataflow inside a CTA ----------------------------------------------------
-__device__ __forceinline__ unsigned smem_addr(const void* p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ int lds_acquire(const int* p) {
-  int v;
-  asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(smem_addr(p)) : "memory");
-  return v;
-}
-__device__ __forceinline__ void sts_release(int* p, int v) {
-  asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(p)), "r"(v) : "memory");
-}
-constexpr int COL_SPIN_LIMIT = 1 << 24;   // a producer warp of the same CTA never stalls this long
-// Wait until *cnt >= target (every lane polls).  False when the limit ran out.
-__device__ __forceinline__ bool col_wait(const int* cnt, int target) {
-  for (int it = 0; it < COL_SPIN_LIMIT; ++it)
-    if (lds_acquire(cnt) >= target) return true;
-  return false;
-}
-// Publish: the warp's shared writes, then the word (release).
-__device__ __forceinline__ void col_publish(int* word, int value) {
-  __syncwarp();
-  if ((threadIdx.x & 31) == 0) sts_release(word, value);
-}
-
 // In-place lower Cholesky of S (TS x TS; entries past n must already be identity).
 // Returns 0, or the 1-based column of the first non-positive (or NaN) pivot (the
-// tile then holds NaNs); TS + 1 if a wait inside the routine ran out (cannot happen
-// while the CTA's warps run).  The strict upper triangle is zeroed.
-//
-// Warp 0 is the pivot warp: for column j it takes the column with the updates of
-// pivots 0 .. j-2 already applied, applies pivot j-1 itself (kept in registers),
-// computes l_jj = d y and l_rj = a_rj y (y = 1/sqrt(d)) and publishes column j in place.
-// Warps 1..3 hold columns 2..31 (column c in warp 1 + (c - 2) % 3, lane = row) and
-// apply every published pivot k to their columns c >= k + 2, column k + 2 first, which
-// they then publish for the pivot warp.  The pivot warp's FP64 unit thus only runs the
-// column chain (one FMA, the third-order rsqrt refinement, one scale per column), and
-// no CTA barrier sits inside the sweep.
+// tile then holds NaNs).  The strict upper triangle is zeroed.
+// Step j publishes pivot column j+1 (l_kk = d y, l_rk = a_rk y, y = 1/sqrt(d)); only
+// the warp owning column j+1 works on the critical path in that step (update of
+// column j+1 with pivot j, then its pivot); it applies pivot j to its other columns
+// one step later, together with pivot j+1.  Pivot columns rotate through three
+// shared slots.
 static __device__ int smem_potrf(double* S) {
-  __shared__ int s_info, s_piv, s_fail;
-  __shared__ int s_col[TS];   // 1: column c holds the updates of pivots 0 .. c-2
-  const int r = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __shared__ double xs[3 * TS];
+  __shared__ int s_info;
+  const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
   __syncthreads();
-  if (threadIdx.x < TS) s_col[threadIdx.x] = 0;
-  if (threadIdx.x == 0) {
-    s_piv = 0;
-    s_info = 0;
-    s_fail = 0;
-  }
-  constexpr int NH = (TS - 2) / 3;   // columns per helper warp
-  double acc[NH];
-  if (w > 0) {
+  double acc[8];
 #pragma unroll
-    for (int m = 0; m < NH; ++m) acc[m] = S[r * LDS + w + 1 + 3 * m];
+  for (int q = 0; q < 8; ++q) acc[q] = S[r * LDS + g + 4 * q];
+  if (g == 0) {
+    const double d = __shfl_sync(0xffffffffu, acc[0], 0);
+    const double y = rsqrt3(d);
+    acc[0] = (r > 0) ? acc[0] * y : (r == 0 ? d * y : 0.0);
+    xs[r] = acc[0];
+    if (r == 0) s_info = (d > 0.0) ? 0 : 1;
   }
   __syncthreads();
-  bool ok = true;
-  if (w == 0) {
-    double lp = 0.0;   // l_{r, j-1}
 #pragma unroll
-    for (int j = 0; j < TS; ++j) {
-      if (j >= 2) ok = col_wait(&s_col[j], 1) && ok;
-      double v = S[r * LDS + j];
-      if (j >= 1) v = fma(-lp, __shfl_sync(0xffffffffu, lp, j), v);
-      const double d = __shfl_sync(0xffffffffu, v, j);
+  for (int j = 0; j < TS; ++j) {
+    const double* xj = xs + (j % 3) * TS;
+    if (j + 1 < TS && g == ((j + 1) & 3)) {
+      const int qn = (j + 1) >> 2;
+      const double a = fma(-xj[r], xj[j + 1], acc[qn]);
+      const double d = __shfl_sync(0xffffffffu, a, j + 1);
       const double y = rsqrt3(d);
-      double l = ((r == j) ? d : v) * y;
-      l = (r < j) ? 0.0 : l;
-      S[r * LDS + j] = l;
-      if (r == 0 && !(d > 0.0) && s_info == 0) s_info = j + 1;
-      col_publish(&s_piv, j + 1);
-      lp = l;
-    }
-  } else {
+      const double l = (r > j + 1) ? a * y : (r == j + 1 ? d * y : 0.0);
+      acc[qn] = l;
+      xs[((j + 1) % 3) * TS + r] = l;
+      if (r == 0 && !(d > 0.0) && s_info == 0) s_info = j + 2;
+    } else {
+      const double lr = xj[r];
 #pragma unroll
-    for (int k = 0; k < TS - 2; ++k) {
-      ok = col_wait(&s_piv, k + 1) && ok;
-      const double lr = S[r * LDS + k];
-      // column k + 2 (owned by warp 1 + k % 3): finish and publish it first
+      for (int q = 0; q < 8; ++q)
+        if (col_after(q, j + 1, g)) acc[q] = fma(-lr, xj[g + 4 * q], acc[q]);
+      if (j >= 1 && g == (j & 3)) {   // owner of the previous step: its deferred pivot j-1
+        const double* xp = xs + ((j + 2) % 3) * TS;
+        const double lp = xp[r];
 #pragma unroll
-      for (int m = 0; m < NH; ++m)
-        if (3 * m + 1 <= k + 1 && 3 * m + 3 >= k + 1 && w + 1 + 3 * m == k + 2) {
-          acc[m] = fma(-lr, S[(k + 2) * LDS + k], acc[m]);
-          S[r * LDS + k + 2] = acc[m];
-          col_publish(&s_col[k + 2], 1);
-        }
-      // then the other later columns (c = w + 1 + 3m > k + 2)
-#pragma unroll
-      for (int m = 0; m < NH; ++m) {
-        const bool later = (3 * m > k) || (3 * m > k - 2 && w > k + 1 - 3 * m);
-        if (later) acc[m] = fma(-lr, S[(w + 1 + 3 * m) * LDS + k], acc[m]);
+        for (int q = 0; q < 8; ++q)
+          if (col_after(q, j + 1, g)) acc[q] = fma(-lp, xp[g + 4 * q], acc[q]);
       }
     }
+    __syncthreads();
   }
-  if (!ok) atomicExch(&s_fail, 1);
-  __syncthreads();
-  if (threadIdx.x == 0 && s_fail) s_info = TS + 1;
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int c = g + 4 * q;
+    S[r * LDS + c] = (c > r) ? 0.0 : acc[q];
+  }
   __syncthreads();
   return s_info;
 }
