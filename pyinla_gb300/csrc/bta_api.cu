@@ -66,7 +66,6 @@ struct gbta_solver {
   int method = GBTA_METHOD_OZAKI;  // how tile products are computed in the factorization
   void* d_digits = nullptr;         // Ozaki digit planes (lazy)
   void* d_sdig = nullptr;           // Ozaki digit planes of the Sigma tiles (lazy)
-  int* d_sexp = nullptr;            // and their exponents
   int* d_erow = nullptr;            // Ozaki row exponents (lazy)
   size_t digit_bytes = 0;
   long long* d_trace = nullptr;   // task trace of the last launch (when enabled)
@@ -121,9 +120,14 @@ namespace {
 gbta::LaunchCtl next_launch(gbta_solver* s, int ntasks) {
   gbta::LaunchCtl lc;
   s->epoch += 1;
+  if (s->epoch >= (1 << (31 - gbta::EPOCH_SHIFT)) - 1) {   // wrap: clear every epoch-stamped word
+    cudaMemsetAsync(s->d_flags, 0, (size_t)s->g.nflags() * sizeof(int), s->stream);
+    cudaMemsetAsync(s->d_faux, 0, (size_t)s->g.nt * s->g.B * sizeof(int), s->stream);
+    s->epoch = 1;
+  }
   lc.ctrl = s->d_ctrl;
   lc.flags = s->d_flags;
-  lc.epoch = s->epoch;
+  lc.epoch = s->epoch << gbta::EPOCH_SHIFT;
   lc.wait_ns = s->wait_ns;
   lc.grid = 0;
   lc.nsm = s->nsm;
@@ -248,7 +252,6 @@ int gbta_destroy(gbta_solver* s) {
   cudaFree(s->d_trace);
   cudaFree(s->d_digits);
   cudaFree(s->d_sdig);
-  cudaFree(s->d_sexp);
   cudaFree(s->d_erow);
   if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
@@ -455,10 +458,9 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
     if (int r = ensure_digits(s)) return r;
     if (!s->d_sdig) {
       GBTA_CUDA(cudaStreamSynchronize(s->stream));
-      const size_t bytes = gbta::selinv_oz_digit_bytes(g), ebytes = (size_t)g.nflags() * sizeof(int);
+      const size_t bytes = gbta::selinv_oz_digit_bytes(g);
       GBTA_CUDA(cudaMalloc(&s->d_sdig, bytes));
-      GBTA_CUDA(cudaMalloc(&s->d_sexp, ebytes));
-      s->digit_bytes += bytes + ebytes;
+      s->digit_bytes += bytes;
     }
   }
   gbta::launch_selinv_prepare(g, D, L, R, use_arrow, s->d_selws, s->stream);
@@ -466,7 +468,7 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
   const gbta::LaunchCtl lc = next_launch(s, s->n_stasks);
   if (s->method == GBTA_METHOD_OZAKI)
     gbta::launch_selinv_oz(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks,
-                           (__half*)s->d_digits, s->d_erow, cinv, (__half*)s->d_sdig, s->d_sexp, lc);
+                           (__half*)s->d_digits, s->d_erow, cinv, (__half*)s->d_sdig, lc);
   else
     gbta::launch_selinv(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks, cinv, lc);
   GBTA_CUDA(cudaGetLastError());

@@ -136,7 +136,6 @@ struct BatchInst {
   __half* digits = nullptr;   // Ozaki only
   int* erow = nullptr;        // Ozaki only
   __half* sdig = nullptr;     // Ozaki only: digit planes of the Sigma tiles
-  int* sexp = nullptr;        // Ozaki only: their exponents
   // bound caller buffers
   double *D = nullptr, *L = nullptr, *R = nullptr, *T = nullptr, *rhs = nullptr;
 };
@@ -226,7 +225,7 @@ gbta::Ctl batch_ctl(const gbta_batch* bt, int* flags, int epoch) {
   gbta::Ctl c;
   c.ctrl = bt->d_ctrl;
   c.flags = flags;
-  c.epoch = epoch;
+  c.epoch = epoch << gbta::EPOCH_SHIFT;
   c.wait_ns = bt->wait_ns;
   c.trace = nullptr;
   return c;
@@ -280,7 +279,6 @@ int build_args(gbta_batch* bt) {
     s.fdig = q.digits;
     s.ecol = q.erow;
     s.sdig = q.sdig;
-    s.sexp = q.sexp;
     s.cinv = q.selws + (size_t)g.nt * g.B * gbta::TS * gbta::TS;
     s.c = batch_ctl(bt, flags, EP_SELINV);
     for (int dir = 0; dir < 2; ++dir) {
@@ -421,7 +419,7 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
   size_t off = 0, flags_total = 0;
   std::vector<std::vector<int4>> ft(n), st(n);
   std::vector<size_t> o_ft(n), o_st(n), o_tip(n), o_arw(n), o_ld(n), o_sig(n), o_sel(n), o_dig(n), o_erow(n),
-      o_sdig(n), o_sexp(n);
+      o_sdig(n);
   for (int k = 0; k < n; ++k) {
     BatchInst& q = bt->inst[k];
     q.g = gbta::Geom{b[k], nt[k], a[k], (b[k] + gbta::TS - 1) / gbta::TS};
@@ -451,7 +449,7 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
     off = align_up(off + (g.nt * bb + (g.nt - 1) * bb + (size_t)g.nt * g.a * g.b + (size_t)g.a * g.a) * sizeof(double));
     o_sel[k] = off;
     off = align_up(off + gbta::selinv_prepare_bytes(g));
-    o_dig[k] = o_erow[k] = o_sdig[k] = o_sexp[k] = 0;
+    o_dig[k] = o_erow[k] = o_sdig[k] = 0;
     if (q.method == GBTA_METHOD_OZAKI) {
       o_dig[k] = off;
       off = align_up(off + gbta::factor_oz_digit_bytes(g));
@@ -459,8 +457,6 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
       off = align_up(off + ((size_t)g.nt * g.b + g.a) * sizeof(int));
       o_sdig[k] = off;
       off = align_up(off + gbta::selinv_oz_digit_bytes(g));
-      o_sexp[k] = off;
-      off = align_up(off + (size_t)g.nflags() * sizeof(int));
     }
   }
   bt->pool_bytes = off;
@@ -489,7 +485,6 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
       q.digits = reinterpret_cast<__half*>(base + o_dig[k]);
       q.erow = reinterpret_cast<int*>(base + o_erow[k]);
       q.sdig = reinterpret_cast<__half*>(base + o_sdig[k]);
-      q.sexp = reinterpret_cast<int*>(base + o_sexp[k]);
     }
     CREATE_CUDA(cudaMemcpy(q.ftasks, ft[k].data(), ft[k].size() * sizeof(int4), cudaMemcpyHostToDevice));
     CREATE_CUDA(cudaMemcpy(q.stasks, st[k].data(), st[k].size() * sizeof(int4), cudaMemcpyHostToDevice));

@@ -94,11 +94,19 @@ __device__ __forceinline__ void raise_abort(const Ctl& c) { atomicExch(c.ctrl + 
 // short sleep.
 constexpr unsigned long long SPIN_NS = 200000;
 
-static __device__ bool spin_ready(const Ctl& c, const int* flag) {
-  if (ld_acquire(flag) >= c.epoch) return true;
+static __device__ bool spin_ready(const Ctl& c, const int* flag, int* seen = nullptr) {
+  int v = ld_acquire(flag);
+  if (v >= c.epoch) {
+    if (seen) *seen = v;
+    return true;
+  }
   const unsigned long long t0 = gtimer();
   for (unsigned it = 1;; ++it) {
-    if (ld_acquire(flag) >= c.epoch) return true;
+    v = ld_acquire(flag);
+    if (v >= c.epoch) {
+      if (seen) *seen = v;
+      return true;
+    }
     if ((it & 63) == 0) {
       if (ld_relaxed(c.ctrl + CTRL_ABORT)) return false;
       const unsigned long long dt = gtimer() - t0;
@@ -127,6 +135,25 @@ static __device__ bool cta_wait(const Ctl& c, const int* f0, const int* f1, int*
   return ok;
 }
 
+// CTA-wide wait on one flag that also returns the flag word seen (epoch + payload) to
+// every thread through *s_val.  Contains __syncthreads().
+static __device__ bool cta_wait_val(const Ctl& c, const int* f, int* s_ok, int* s_val) {
+  if (threadIdx.x == 0) *s_ok = spin_ready(c, f, s_val) ? 1 : 0;
+  __syncthreads();
+  const bool ok = *s_ok != 0;
+  __syncthreads();
+  return ok;
+}
+
+// Publish a tile with a payload in its flag word (see EPOCH_SHIFT).
+__device__ __forceinline__ void cta_publish_val(const Ctl& c, int* flag, int payload) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    st_release(flag, c.epoch + payload);
+  }
+}
+
 // Readiness scan for pipelined product loops.  Thread 0 advances *s_ready (the
 // number of leading steps whose operand flags are all set) by checking up to
 // SCAN_AHEAD further steps with independent relaxed loads and a single acquire fence,
@@ -141,14 +168,19 @@ __device__ __forceinline__ int ld_relaxed_gpu(const int* p) {
 }
 __device__ __forceinline__ void fence_acquire_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
+// With `ring` (SCAN_RING ints), the first flag word of every step found ready is kept
+// at ring[step % SCAN_RING] (read while step - *s_ready < SCAN_RING - SCAN_AHEAD).
+constexpr int SCAN_RING = 2 * SCAN_AHEAD;
 template <class FlagsOf>
-__device__ __forceinline__ void scan_ready(const Ctl& c, int nsteps, FlagsOf flags_of, int* s_ready) {
+__device__ __forceinline__ void scan_ready(const Ctl& c, int nsteps, FlagsOf flags_of, int* s_ready,
+                                           int* ring = nullptr) {
   if (threadIdx.x == 0) {
     const int r0 = *s_ready;
-    int v[SCAN_AHEAD];
+    int v[SCAN_AHEAD], w0[SCAN_AHEAD];
 #pragma unroll
     for (int k = 0; k < SCAN_AHEAD; ++k) {
       v[k] = 1;
+      w0[k] = c.epoch;
       if (r0 + k < nsteps) {
         const int* f0;
         const int* f1;
@@ -156,13 +188,17 @@ __device__ __forceinline__ void scan_ready(const Ctl& c, int nsteps, FlagsOf fla
         const int a = f0 ? ld_relaxed_gpu(f0) : c.epoch;
         const int b = f1 ? ld_relaxed_gpu(f1) : c.epoch;
         v[k] = (a >= c.epoch) && (b >= c.epoch);
+        w0[k] = a;
       }
     }
     fence_acquire_gpu();
     int r = r0;
 #pragma unroll
     for (int k = 0; k < SCAN_AHEAD; ++k)
-      if (r == r0 + k && r < nsteps && v[k]) ++r;
+      if (r == r0 + k && r < nsteps && v[k]) {
+        if (ring) ring[r % SCAN_RING] = w0[k];
+        ++r;
+      }
     *s_ready = r;
   }
 }

@@ -11,6 +11,12 @@ namespace gbta {
 
 constexpr int TS = 32;  // tile edge (FP64 elements)
 
+// Launch epochs are multiples of 2^EPOCH_SHIFT: a ready flag holds epoch + payload,
+// payload < 2^EPOCH_SHIFT (the selected inversion stores each Sigma tile's exponent
+// there), and "ready" is flag >= epoch.  Epoch-stamped words are cleared before the
+// epoch counter would pass 2^(31 - EPOCH_SHIFT).
+constexpr int EPOCH_SHIFT = 9;
+
 // Task codes of the factorization DAG.  FT_PRE is a flag on an FT_OFFD / FT_LOW task:
 // the task only forms the tile's products and leaves the triangular solve to the
 // FT_FEEDQ tasks of its rows (the feeder tile of a diagonal tile, see Geom).
@@ -91,11 +97,11 @@ size_t selinv_oz_digit_bytes(const Geom& g);
 // selected inversion).
 void launch_selinv_oz_prepare(const Geom& g, const double* D, const double* L, const double* R, int use_arrow,
                               __half* fdig, int* ecol, cudaStream_t stream);
-// sdig / sexp: digit planes (selinv_oz_digit_bytes) and exponents (nflags ints) of
-// the Sigma tiles, written by the tasks that produce them.
+// sdig: digit planes (selinv_oz_digit_bytes) of the Sigma tiles, written by the tasks
+// that produce them (their exponents travel in the tiles' flag words).
 void launch_selinv_oz(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                       double* SD, double* SL, double* SR, double* ST, int use_arrow, const int4* tasks,
-                      int ntasks, __half* fdig, int* ecol, const double* cinv, __half* sdig, int* sexp,
+                      int ntasks, __half* fdig, int* ecol, const double* cinv, __half* sdig,
                       const LaunchCtl& lc);
 
 void launch_solve(const Geom& g, const double* D, const double* L, const double* R, const double* T,

@@ -136,7 +136,7 @@ extern "C" int gbta_pobtaf_noalloc(int b, int nt, int a, double* D, double* L, d
   gbta::LaunchCtl lc;
   lc.ctrl = ctrl;
   lc.flags = flags;
-  lc.epoch = 1;
+  lc.epoch = 1 << gbta::EPOCH_SHIFT;
   lc.wait_ns = 20ull * 1000 * 1000 * 1000;
   lc.grid = (int)(ntasks < nsm ? ntasks : nsm);
   lc.stream = st;

@@ -108,7 +108,7 @@ size_t selinv_oz_digit_bytes(const Geom& g) { return (size_t)g.nflags() * OZ_TIL
 
 void launch_selinv_oz(const Geom& g, const double* D, const double* L, const double* R, const double* T, double* SD,
                       double* SL, double* SR, double* ST, int use_arrow, const int4* tasks, int ntasks, __half* fdig,
-                      int* ecol, const double* cinv, __half* sdig, int* sexp, const LaunchCtl& lc) {
+                      int* ecol, const double* cinv, __half* sdig, const LaunchCtl& lc) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_selinv_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZS_SMEM);
@@ -133,7 +133,6 @@ void launch_selinv_oz(const Geom& g, const double* D, const double* L, const dou
   p.ecol = ecol;
   p.cinv = cinv;
   p.sdig = sdig;
-  p.sexp = sexp;
   p.c.ctrl = lc.ctrl;
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;

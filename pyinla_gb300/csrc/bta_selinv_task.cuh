@@ -57,8 +57,8 @@ struct SelinvArgs {
   const __half* fdig;   // Ozaki: transposed digits of the G tiles per flag slot
   const int* ecol;      // Ozaki: per global column (nt*b) exponent of the G column pattern
   const double* cinv;   // [nt*B][TS*TS]: F_cc^{-T} F_cc^{-1} of every diagonal factor tile
-  __half* sdig;         // Ozaki: digit planes of every Sigma tile per flag slot
-  int* sexp;            // Ozaki: their exponents (multiples of 7, or NO_EXP)
+  __half* sdig;         // Ozaki: digit planes of every Sigma tile per flag slot (their
+                        // exponents ride in the tiles' flag words, see sig_exp_code)
   Ctl c;
 };
 
@@ -334,13 +334,21 @@ static __device__ __forceinline__ int smem_tile_exponent7(const double* X, int r
   return e >= 0 ? 7 * ((e + 6) / 7) : -7 * ((-e) / 7);
 }
 
-// Digit planes and exponent of a finished Sigma tile (shared X, rows x cols valid),
-// written to its flag slot before the tile is published.
-static __device__ __forceinline__ void sig_store_digits(const SelinvArgs& p, int slot, const double* X, int rows,
-                                                        int cols, double* red4) {
+// A Sigma tile's exponent (a multiple of 7 in [-1071, 1029], or NO_EXP) as the payload
+// of its flag word (below 2^EPOCH_SHIFT), and back.
+static __device__ __forceinline__ int sig_exp_code(int E) { return E == NO_EXP ? 0 : E / 7 + 256; }
+static __device__ __forceinline__ int sig_exp_decode(int flag_word, int epoch) {
+  const int code = flag_word - epoch;
+  return code ? (code - 256) * 7 : NO_EXP;
+}
+
+// Digit planes of a finished Sigma tile (shared X, rows x cols valid), written to its
+// slot before the tile is published; returns the flag payload of its exponent.
+static __device__ __forceinline__ int sig_store_digits(const SelinvArgs& p, int slot, const double* X, int rows,
+                                                       int cols, double* red4) {
   const int E = smem_tile_exponent7(X, rows, cols, red4);
   oz_store_digits_uniform(p.sdig + (size_t)slot * OZ_TILE, X, rows, cols, E == NO_EXP ? 0 : E);
-  if (threadIdx.x == 0) p.sexp[slot] = E;
+  return sig_exp_code(E);
 }
 
 // Plane shift of a left operand with exponent En in the frame of the running
@@ -355,7 +363,7 @@ static __device__ __forceinline__ int sig_shift(int E, int En) {
 // (used only by the tip task, when no stage is in flight) reuses the first stage.
 constexpr int OZS_STAGE = 2 * OZ_OPER;
 constexpr size_t OZS_SMEM = 2 * OZS_STAGE * sizeof(__half) + 2 * TILE_SMEM * sizeof(double) + TS * sizeof(double) +
-                            TS * sizeof(int) + 4 * sizeof(double);
+                            TS * sizeof(int) + 4 * sizeof(double) + (SCAN_RING + 1) * sizeof(int);
 
 // Task t of a tensor-core selected-inversion instance.  `raw` is OZS_SMEM bytes of
 // (16-byte aligned) shared memory.  Returns false when the launch is aborted.
@@ -374,6 +382,8 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
   double* rd = F + TILE_SMEM;
   int* ecol_t = reinterpret_cast<int*>(rd + TS);
   double* red4 = reinterpret_cast<double*>(ecol_t + TS);
+  int* ring = reinterpret_cast<int*>(red4 + 4);   // flag words of the steps found ready
+  int* s_val = ring + SCAN_RING;                  // flag word of the last blocking wait
   int& s_ok = *s_okp;
   int& s_ready = *s_readyp;
   const Geom& g = p.g;
@@ -394,8 +404,8 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       __syncthreads();
       diag_finish(X, W, F, rd);
       tile_store(p.ST, g.a, g.a, g.a, X);
-      sig_store_digits(p, g.fT(), X, g.a, g.a, red4);
-      cta_publish(c, c.flags + g.fT());
+      const int code = sig_store_digits(p, g.fT(), X, g.a, g.a, red4);
+      cta_publish_val(c, c.flags + g.fT(), code);
       trace_task(c, t, type, t_task0);
       return true;
     }
@@ -438,7 +448,6 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       oz_load_async(dst + OZ_OPER, right_of(s));
       cp_async_commit();
     };
-    auto exp_of = [&](const SigTile& lt) -> int { return __ldcg(p.sexp + (lt.flag - c.flags)); };
 
     bool ok = true;
     int since_fold = 0;
@@ -452,12 +461,12 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
     };
     if (np > 0) {
       SigTile lt = left_of(0);
-      ok = cta_wait(c, lt.flag, nullptr, &s_ok);
+      ok = cta_wait_val(c, lt.flag, &s_ok, s_val);
       trace_mark(c, t, 0);
       bool tcur = lt.trans;
       if (ok) {
         if (threadIdx.x == 0) s_ready = 1;
-        E = exp_of(lt);
+        E = sig_exp_decode(*s_val, c.epoch);
         set_esum();
         stage(stages, lt, 0, 0);
       }
@@ -473,11 +482,11 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         if (more) {
           nt_ = left_of(s + 1);
           if (s_ready <= s + 1) {   // uniform: read after the barrier
-            scan_ready(c, np, flags_of, &s_ready);
+            scan_ready(c, np, flags_of, &s_ready, ring);
             __syncthreads();
           }
           if (s_ready > s + 1) {
-            En = exp_of(nt_);
+            En = sig_exp_decode(ring[(s + 1) % SCAN_RING], c.epoch);
             stage(nxt, nt_, En > E ? 0 : sig_shift(E, En), s + 1);
             have = true;
           }
@@ -490,13 +499,13 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         if (more) {
           if (!have) {
             const unsigned long long w0 = c.trace ? gtimer() : 0ull;
-            if (!(ok = cta_wait(c, nt_.flag, nullptr, &s_ok))) break;
+            if (!(ok = cta_wait_val(c, nt_.flag, &s_ok, s_val))) break;
             if (c.trace) {
               waited += gtimer() - w0;
               trace_mark(c, t, 1);
             }
             if (threadIdx.x == 0) s_ready = s + 2;
-            En = exp_of(nt_);
+            En = sig_exp_decode(*s_val, c.epoch);
           }
           if ((En > E && En != NO_EXP) || since_fold == OZ_CHUNK) {
             if (E > NO_EXP) oz_fold_sub(acc, esum);
@@ -529,16 +538,16 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       __syncthreads();
       const SigTile d = sig_dest(p, i, j, col);
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
-      sig_store_digits(p, (int)(d.flag - c.flags), X, d.t.rows, d.t.cols, red4);
-      cta_publish(c, const_cast<int*>(d.flag));
+      const int code = sig_store_digits(p, (int)(d.flag - c.flags), X, d.t.rows, d.t.cols, red4);
+      cta_publish_val(c, const_cast<int*>(d.flag), code);
     } else {
       tile_load(F, make_tile(p.cinv + (size_t)(i * g.B + col) * TS * TS, TS, 0, 0, TS, TS));
       __syncthreads();
       diag_from_cinv(X, F);
       const SigTile d = sig_dest(p, i, col, col);
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
-      sig_store_digits(p, (int)(d.flag - c.flags), X, d.t.rows, d.t.cols, red4);
-      cta_publish(c, const_cast<int*>(d.flag));
+      const int code = sig_store_digits(p, (int)(d.flag - c.flags), X, d.t.rows, d.t.cols, red4);
+      cta_publish_val(c, const_cast<int*>(d.flag), code);
     }
     trace_task(c, t, type, t_task0);
   }
