@@ -76,7 +76,10 @@ int gbta_probe_fp64_peak(int iters, double* tflops);
 /* Clock cycles per call of the 32 x 32 tile routines, each timed alone on one CTA:
  * cycles[0] tile reload (included in the others), [1] tile Cholesky, [2] reciprocals
  * + X F^{-T}, [3] reciprocals + X F^{-1}, [4] digit planes, [5] tile store, [6]
- * reciprocals + row scaling + X F^{-T} on 8 rows (cycles holds 7 values).  No
+ * reciprocals + row scaling + X F^{-T} on 8 rows, [7] one tensor-core tile step (43
+ * digit-plane pairs of 32 x 32 x 32, operands in shared memory), [8] staging both
+ * operands' digit planes (2 x 16 KB) from global into shared memory (cycles holds 9
+ * values).  No
  * reference counterpart (a measurement aid). */
 int gbta_probe_tiles(int iters, long long* cycles);
 

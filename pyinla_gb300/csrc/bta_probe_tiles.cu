@@ -3,7 +3,8 @@
 // `iters` repetitions, every repetition reloading the tile from global memory, whose
 // cost is reported separately): tile Cholesky, reciprocals + X F^{-T}, reciprocals +
 // X F^{-1}, digit planes of a tile, a tile store, and reciprocals + row scaling + the
-// 8-row X F^{-T} of one quarter of a tile.  The tile is a diagonally
+// 8-row X F^{-T} of one quarter of a tile, and one tensor-core tile step (43 digit-
+// plane pairs of 32 x 32 x 32, operands already in shared memory).  The tile is a diagonally
 // dominant SPD matrix built in the kernel.
 #include <cuda_runtime.h>
 
@@ -14,6 +15,8 @@ namespace gbta {
 
 __global__ void __launch_bounds__(NT) k_probe_tiles(double* scratch, __half* dig, long long* cyc, int iters) {
   __shared__ double X[TILE_SMEM], F[TILE_SMEM], FS[TILE_SMEM], rd[TS];
+  __shared__ __align__(16) __half ops[2 * OZ_OPER];
+  __shared__ __align__(16) __half ops2[2 * OZ_OPER];
   __shared__ int E[TS];
   double* A = scratch;              // SPD tile (TS x TS, row-major)
   double* Bm = scratch + TS * TS;   // general tile
@@ -47,6 +50,17 @@ __global__ void __launch_bounds__(NT) k_probe_tiles(double* scratch, __half* dig
   GBTA_TIMED(5, tile_load(X, tb); __syncthreads(); tile_store(scratch + 2 * TS * TS, TS, TS, TS, X); __syncthreads();)
   GBTA_TIMED(6, tile_load(X, tb); __syncthreads(); tile_diag_recip(F, rd); __syncthreads();
              tile_scale_rows_by_recip(FS, F, rd); smem_trsm_rlt_rows8(X, FS, rd, 0);)
+  for (int idx = threadIdx.x; idx < 2 * OZ_OPER; idx += NT) ops[idx] = __float2half((float)((idx * 7) % 129 - 64));
+  __syncthreads();
+  OzAcc acc;
+  oz_clear_partials(acc);
+  GBTA_TIMED(7, oz_step(acc, ops, ops + OZ_OPER);)
+  float sink = 0.f;
+#pragma unroll
+  for (int d = 0; d < OZ_ND; ++d) sink += acc.p[d][0][0] + acc.p[d][1][3];
+  if (sink == 12345.f) cyc[9] = 1;   // keeps the products live
+  GBTA_TIMED(8, oz_load_async(ops2, dig); oz_load_async(ops2 + OZ_OPER, dig); cp_async_commit(); cp_async_wait_all();
+             __syncthreads();)
 #undef GBTA_TIMED
 }
 
@@ -61,7 +75,7 @@ extern "C" int gbta_probe_tiles(int iters, long long* cycles) {
   long long* cyc = nullptr;
   if (cudaMalloc(&scratch, 3 * gbta::TS * gbta::TS * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&dig, gbta::OZ_TILE * sizeof(__half)) != cudaSuccess ||
-      cudaMalloc(&cyc, 7 * sizeof(long long)) != cudaSuccess) {
+      cudaMalloc(&cyc, 10 * sizeof(long long)) != cudaSuccess) {
     cudaFree(scratch);
     cudaFree(dig);
     return gbta_set_error(GBTA_ERR_ALLOC, "probe: cudaMalloc failed");
@@ -69,7 +83,7 @@ extern "C" int gbta_probe_tiles(int iters, long long* cycles) {
   gbta::k_probe_tiles<<<1, gbta::NT>>>(scratch, dig, cyc, iters);
   gbta::count_launches(1);
   cudaError_t e = cudaDeviceSynchronize();
-  if (e == cudaSuccess) e = cudaMemcpy(cycles, cyc, 7 * sizeof(long long), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(cycles, cyc, 9 * sizeof(long long), cudaMemcpyDeviceToHost);
   cudaFree(scratch);
   cudaFree(dig);
   cudaFree(cyc);

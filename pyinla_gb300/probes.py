@@ -24,16 +24,16 @@ def fp64_peak_tflops(iters: int = 4000) -> float:
 
 def tile_cycles(iters: int = 200) -> dict:
     lib = _lib.load()
-    cyc = np.zeros(7, dtype=np.int64)
+    cyc = np.zeros(9, dtype=np.int64)
     _lib.check(lib.gbta_probe_tiles(int(iters), cyc.ctypes.data))
     names = ["reload", "potrf", "recip+trsm_rlt", "recip+trsm_rln", "digit_planes", "store",
-             "recip+scale+trsm_rlt_8rows"]
+             "recip+scale+trsm_rlt_8rows", "oz_tile_step", "oz_stage_2x16KB"]
     return {n: int(c) for n, c in zip(names, cyc)}
 
 
 def primitive_cycles() -> dict:
     lib = _lib.load()
-    cyc = np.zeros(8, dtype=np.int64)
+    cyc = np.zeros(9, dtype=np.int64)
     _lib.check(lib.gbta_probe_latencies(cyc.ctypes.data))
     names = ["dfma_dependent_1warp", "dfma_independent_1warp", "dfma_independent_4warps", "dfma_predicated_off",
              "rsqrt_approx_f64_plus_dadd", "shfl_f64", "lds_dependent", "bar_sync_4warps"]
