@@ -154,19 +154,22 @@ __device__ __forceinline__ void cta_publish_val(const Ctl& c, int* flag, int pay
   }
 }
 
-// Readiness scan for pipelined product loops.  Thread 0 advances *s_ready (the
-// number of leading steps whose operand flags are all set) by checking up to
-// SCAN_AHEAD further steps with independent relaxed loads and a single acquire fence,
-// so one memory round trip covers many steps.  `flags_of(s, f0, f1)` returns the
-// step's flags (nullptr = none).  The caller synchronises the CTA afterwards.
+// Readiness scan for pipelined product loops.  Warp 0 advances *s_ready (the number of
+// leading steps whose operand flags are all set) by checking up to SCAN_AHEAD further
+// steps at once: lane 2k loads the first flag of step *s_ready + k and lane 2k+1 its
+// second, each with an acquire load, so one memory round trip covers all of them and
+// no GPU-scope fence is needed (a fence waits for the CTA's own outstanding writes,
+// which costs thousands of cycles in a busy kernel).  `flags_of(s, f0, f1)` returns the
+// step's flags (nullptr = none).  The caller synchronises the CTA afterwards, which
+// extends the acquires to all its threads.
 constexpr int SCAN_AHEAD = 8;
+static_assert(2 * SCAN_AHEAD <= 32, "one lane per flag");
 
 __device__ __forceinline__ int ld_relaxed_gpu(const int* p) {
   int v;
   asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
-__device__ __forceinline__ void fence_acquire_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
 // With `ring` (SCAN_RING ints), the first flag word of every step found ready is kept
 // at ring[step % SCAN_RING] (read while step - *s_ready < SCAN_RING - SCAN_AHEAD).
@@ -174,32 +177,37 @@ constexpr int SCAN_RING = 2 * SCAN_AHEAD;
 template <class FlagsOf>
 __device__ __forceinline__ void scan_ready(const Ctl& c, int nsteps, FlagsOf flags_of, int* s_ready,
                                            int* ring = nullptr) {
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
     const int r0 = *s_ready;
-    int v[SCAN_AHEAD], w0[SCAN_AHEAD];
-#pragma unroll
-    for (int k = 0; k < SCAN_AHEAD; ++k) {
-      v[k] = 1;
-      w0[k] = c.epoch;
+    const int k = lane >> 1;
+    int word = c.epoch;
+    bool ready = true;
+    if (k < SCAN_AHEAD) {
       if (r0 + k < nsteps) {
         const int* f0;
         const int* f1;
         flags_of(r0 + k, f0, f1);
-        const int a = f0 ? ld_relaxed_gpu(f0) : c.epoch;
-        const int b = f1 ? ld_relaxed_gpu(f1) : c.epoch;
-        v[k] = (a >= c.epoch) && (b >= c.epoch);
-        w0[k] = a;
+        const int* f = (lane & 1) ? f1 : f0;
+        if (f) {
+          word = ld_acquire(f);
+          ready = word >= c.epoch;
+        }
+      } else {
+        ready = false;
       }
     }
-    fence_acquire_gpu();
+    const unsigned ok = __ballot_sync(0xffffffffu, ready);
     int r = r0;
 #pragma unroll
-    for (int k = 0; k < SCAN_AHEAD; ++k)
-      if (r == r0 + k && r < nsteps && v[k]) {
-        if (ring) ring[r % SCAN_RING] = w0[k];
+    for (int kk = 0; kk < SCAN_AHEAD; ++kk) {
+      const int w0 = __shfl_sync(0xffffffffu, word, 2 * kk);
+      if (r == r0 + kk && ((ok >> (2 * kk)) & 3u) == 3u) {
+        if (ring && lane == 0) ring[r % SCAN_RING] = w0;
         ++r;
       }
-    *s_ready = r;
+    }
+    if (lane == 0) *s_ready = r;
   }
 }
 
