@@ -46,6 +46,12 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
 __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+// Atomic add with acquire-release semantics at GPU scope; returns the old value.
+__device__ __forceinline__ int atom_add_acq_rel(int* p, int v) {
+  int old;
+  asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
 __device__ __forceinline__ int ld_relaxed(const int* p) {
   return *(volatile const int*)p;
 }
@@ -145,13 +151,12 @@ static __device__ bool cta_wait_val(const Ctl& c, const int* f, int* s_ok, int* 
   return ok;
 }
 
-// Publish a tile with a payload in its flag word (see EPOCH_SHIFT).
+// Publish a tile with a payload in its flag word (see EPOCH_SHIFT).  The barrier
+// orders every thread's writes before thread 0's release store, which is cumulative,
+// so no separate fence is needed.
 __device__ __forceinline__ void cta_publish_val(const Ctl& c, int* flag, int payload) {
   __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    st_release(flag, c.epoch + payload);
-  }
+  if (threadIdx.x == 0) st_release(flag, c.epoch + payload);
 }
 
 // Readiness scan for pipelined product loops.  Warp 0 advances *s_ready (the number of
@@ -227,11 +232,8 @@ static __device__ bool cta_poll(const Ctl& c, const int* f0, const int* f1, int*
 
 // Publish a tile: every thread's stores are ordered before the flag release.
 __device__ __forceinline__ void cta_publish(const Ctl& c, int* flag) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    st_release(flag, c.epoch);
-  }
+  __syncthreads();   // every thread's writes before thread 0's (cumulative) release store
+  if (threadIdx.x == 0) st_release(flag, c.epoch);
 }
 
 // Pull the next ticket (CTA-uniform).

@@ -122,13 +122,9 @@ static __device__ bool factor_feed_rows(const FactorArgs& p, int t, int i, int q
       }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const int done = atomicAdd(p.feed_cnt + gc, 1) + 1;
-    if (done == g.feeder_quarters(i, col)) {
-      __threadfence();
-      st_release(c.flags + slot, c.epoch);
-    }
+  if (threadIdx.x == 0) {   // acq_rel: releases this group's rows, acquires the earlier groups'
+    const int done = atom_add_acq_rel(p.feed_cnt + gc, 1) + 1;
+    if (done == g.feeder_quarters(i, col)) st_release(c.flags + slot, c.epoch);
   }
   trace_task(c, t, FT_FEEDQ, t_task0);
   return true;
