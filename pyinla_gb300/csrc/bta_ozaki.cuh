@@ -41,11 +41,18 @@ constexpr int OZ_W = 7;                       // bits per digit
 constexpr int OZ_ND = 9;                      // diagonals s + t = 0 .. 8
 constexpr int OZ_CHUNK = 15;                  // tile steps per exact fp32 accumulation
 constexpr int OZ_ZERO = 64;                   // biased field of the digit 0 (field = d + 64)
-constexpr int OZ_LD = 40;                     // shared row stride of a plane (halves): conflict-free ldmatrix
-constexpr int OZ_PLANE = TS * OZ_LD;          // halves per plane in shared memory
+constexpr int OZ_PLANE = TS * TS;            // halves per plane (global and shared memory alike)
 constexpr int OZ_OPER = OZ_S * OZ_PLANE;      // halves per operand tile in shared memory
 constexpr int OZ_TILE = OZ_S * TS * TS;       // halves per tile in the global digit buffer
 constexpr int OZ_CHUNKS16 = OZ_S * TS * 4;    // 16-byte pieces per tile (8 * 32 rows * 64 B)
+
+// Half index of element (row, col) of a digit plane.  Planes are stored as 32 rows of
+// 64 bytes in global and shared memory alike (a tile's planes are one contiguous 16 KB
+// block, copied as is); the four 16-byte chunks of row r are permuted by (r >> 1) & 3,
+// so that the eight rows one ldmatrix reads land in distinct shared-memory banks.
+__host__ __device__ constexpr int oz_swz(int row, int col) {
+  return row * TS + ((((col >> 3) ^ (row >> 1)) & 3) << 3) + (col & 7);
+}
 
 // At most 8 pairs share a diagonal; |d| <= 64.
 static_assert(8 * 64 * 64 * TS * OZ_CHUNK < (1 << 24), "fp32 accumulation must stay exact");
@@ -116,9 +123,9 @@ __device__ __forceinline__ void oz_store_digits_e(__half* dst, const double* X, 
       oz_digits(X[r * LDS + c + 1], Eof(r), d1);
     else
       oz_zero_digits(d1);
-    unsigned* w = reinterpret_cast<unsigned*>(dst + r * TS + c);
+    unsigned* w = reinterpret_cast<unsigned*>(dst + oz_swz(r, c));
 #pragma unroll
-    for (int s = 0; s < OZ_S; ++s) w[s * (TS * TS / 2)] = oz_digit_pair(d0[s], d1[s]);
+    for (int s = 0; s < OZ_S; ++s) w[s * (OZ_PLANE / 2)] = oz_digit_pair(d0[s], d1[s]);
   }
 }
 
@@ -137,9 +144,9 @@ __device__ __forceinline__ void oz_store_digits_rows(__half* dst, const double* 
     oz_digits(X[r * LDS + c + 1], E[r], d1);
   else
     oz_zero_digits(d1);
-  unsigned* w = reinterpret_cast<unsigned*>(dst + r * TS + c);
+  unsigned* w = reinterpret_cast<unsigned*>(dst + oz_swz(r, c));
 #pragma unroll
-  for (int s = 0; s < OZ_S; ++s) w[s * (TS * TS / 2)] = oz_digit_pair(d0[s], d1[s]);
+  for (int s = 0; s < OZ_S; ++s) w[s * (OZ_PLANE / 2)] = oz_digit_pair(d0[s], d1[s]);
 }
 
 // Rows relative to per-row exponents E[row].
@@ -169,10 +176,7 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 
 // Stage one tile's digit planes (global, compact rows) into shared memory (padded rows).
 __device__ __forceinline__ void oz_load_async(__half* sdst, const __half* gsrc) {
-  for (int q = threadIdx.x; q < OZ_CHUNKS16; q += NT) {
-    const int s = q / (TS * 4), row = (q / 4) % TS, part = q % 4;
-    cp_async16(sdst + s * OZ_PLANE + row * OZ_LD + part * 8, gsrc + s * TS * TS + row * TS + part * 8);
-  }
+  for (int q = threadIdx.x; q < OZ_CHUNKS16; q += NT) cp_async16(sdst + q * 8, gsrc + q * 8);
 }
 
 // Stage a tile's digit planes shifted down by q planes: shared plane s holds global
@@ -180,12 +184,12 @@ __device__ __forceinline__ void oz_load_async(__half* sdst, const __half* gsrc) 
 // tile sliced against 2^E_t in the frame of a larger exponent E = E_t + 7q.
 __device__ __forceinline__ void oz_load_async_shift(__half* sdst, const __half* gsrc, int q) {
   for (int idx = threadIdx.x; idx < OZ_CHUNKS16; idx += NT) {
-    const int s = idx / (TS * 4), row = (idx / 4) % TS, part = idx % 4;
-    __half* d = sdst + s * OZ_PLANE + row * OZ_LD + part * 8;
+    const int s = idx / (TS * 4);
+    __half* d = sdst + idx * 8;
     if (s < q)
       *reinterpret_cast<uint4*>(d) = make_uint4(0u, 0u, 0u, 0u);
     else
-      cp_async16(d, gsrc + (s - q) * TS * TS + row * TS + part * 8);
+      cp_async16(d, gsrc + idx * 8 - q * OZ_PLANE);
   }
 }
 
@@ -247,13 +251,13 @@ __device__ __forceinline__ void oz_step_t(OzAcc& acc, const __half* As, const __
     unsigned a[OZ_S][4], b[OZ_S][4];
     if (TA) {
 #pragma unroll
-      for (int s = 0; s < OZ_S; ++s) ldsm_x4_trans(a[s], As + s * OZ_PLANE + (kk + tr) * OZ_LD + tc);
+      for (int s = 0; s < OZ_S; ++s) ldsm_x4_trans(a[s], As + s * OZ_PLANE + oz_swz(kk + tr, tc));
     } else {
 #pragma unroll
-      for (int s = 0; s < OZ_S; ++s) ldsm_x4(a[s], As + s * OZ_PLANE + ar * OZ_LD + kk + ac);
+      for (int s = 0; s < OZ_S; ++s) ldsm_x4(a[s], As + s * OZ_PLANE + oz_swz(ar, kk + ac));
     }
 #pragma unroll
-    for (int s = 0; s < OZ_S; ++s) ldsm_x4(b[s], Bs + s * OZ_PLANE + br * OZ_LD + kk + bc);
+    for (int s = 0; s < OZ_S; ++s) ldsm_x4(b[s], Bs + s * OZ_PLANE + oz_swz(br, kk + bc));
 #pragma unroll
     for (int s = 0; s < OZ_S; ++s)
 #pragma unroll

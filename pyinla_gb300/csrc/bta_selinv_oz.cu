@@ -79,9 +79,9 @@ __global__ void __launch_bounds__(NT) k_fac_digits_t(const double* D, const doub
       oz_digits(t.p[(size_t)(m + 1) * t.ld + jj], e, d1);
     else
       oz_zero_digits(d1);
-    unsigned* w = reinterpret_cast<unsigned*>(dst + jj * TS + m);
+    unsigned* w = reinterpret_cast<unsigned*>(dst + oz_swz(jj, m));
 #pragma unroll
-    for (int s = 0; s < OZ_S; ++s) w[s * (TS * TS / 2)] = oz_digit_pair(d0[s], d1[s]);
+    for (int s = 0; s < OZ_S; ++s) w[s * (OZ_PLANE / 2)] = oz_digit_pair(d0[s], d1[s]);
   }
 }
 
