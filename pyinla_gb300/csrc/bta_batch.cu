@@ -36,7 +36,9 @@ __global__ void __launch_bounds__(NT, 1) k_factor_batch(const FactorArgs* __rest
                                                         const int2* __restrict__ order, int ntotal, Ctl c) {
   extern __shared__ __align__(16) unsigned char raw[];
   __shared__ int s_ok, s_t, s_ready;
-  const OzFactorSmem sm = oz_factor_smem(raw, &s_ok, &s_ready);
+  __shared__ OzPipe pipe;
+  oz_pipe_init(&pipe);
+  const OzFactorSmem sm = oz_factor_smem(raw, &s_ok, &s_ready, &pipe);
   while (true) {
     const int t = cta_ticket(c, &s_t);
     if (t < 0 || t >= ntotal) break;
@@ -51,12 +53,14 @@ __global__ void __launch_bounds__(NT, 1) k_selinv_batch(const SelinvArgs* __rest
                                                         const int2* __restrict__ order, int ntotal, Ctl c) {
   extern __shared__ __align__(16) unsigned char raw[];
   __shared__ int s_ok, s_t, s_ready;
+  __shared__ OzPipe pipe;
+  oz_pipe_init(&pipe);
   while (true) {
     const int t = cta_ticket(c, &s_t);
     if (t < 0 || t >= ntotal) break;
     const int2 o = order[t];
     const SelinvArgs& p = inst[o.x];
-    const bool ok = (p.method == GBTA_METHOD_OZAKI) ? selinv_oz_task(p, o.y, raw, &s_ok, &s_ready)
+    const bool ok = (p.method == GBTA_METHOD_OZAKI) ? selinv_oz_task(p, o.y, raw, &s_ok, &s_ready, &pipe)
                                                     : selinv_fp64_task(p, o.y, raw, &s_ok);
     if (!ok) break;
   }

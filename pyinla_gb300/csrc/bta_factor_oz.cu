@@ -25,7 +25,9 @@ __global__ void k_row_exponents(const double* D, const double* T, Geom g, int us
 __global__ void __launch_bounds__(NT, 1) k_factor_oz(FactorArgs p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_ok, s_t, s_ready;
-  const OzFactorSmem sm = oz_factor_smem(smem_raw, &s_ok, &s_ready);
+  __shared__ OzPipe pipe;
+  oz_pipe_init(&pipe);
+  const OzFactorSmem sm = oz_factor_smem(smem_raw, &s_ok, &s_ready, &pipe);
   while (true) {
     const int t = cta_ticket(p.c, &s_t);
     if (t < 0 || t >= p.ntasks) break;

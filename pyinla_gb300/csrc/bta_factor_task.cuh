@@ -337,10 +337,13 @@ struct OzFactorSmem {
   int* ecol_t;   // exponents of the target's columns
   int* s_ok;
   int* s_ready;
+  OzPipe* pipe;   // bulk-copy barriers of the two stage buffers
 };
 
-static __device__ __forceinline__ OzFactorSmem oz_factor_smem(unsigned char* raw, int* s_ok, int* s_ready) {
+static __device__ __forceinline__ OzFactorSmem oz_factor_smem(unsigned char* raw, int* s_ok, int* s_ready,
+                                                              OzPipe* pipe) {
   OzFactorSmem m;
+  m.pipe = pipe;
   m.stages = reinterpret_cast<__half*>(raw);
   m.X = reinterpret_cast<double*>(raw + 2 * OZF_STAGE_HALVES * sizeof(__half));
   m.F = m.X + TILE_SMEM;
@@ -465,6 +468,18 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
       }
     };
     bool ok = true;
+    OzPipe* pp = sm.pipe;
+    unsigned ph = pp->phase;
+    // stage the operand tiles (slots a, b) of a step into stage buffer st (bulk copies)
+    auto stage = [&](int st, int a_slot, int b_slot) {
+      if (threadIdx.x == 0) {
+        __half* dst = stages + st * OZF_STAGE_HALVES;
+        constexpr unsigned tb = (unsigned)(OZ_TILE * sizeof(__half));
+        oz_bulk_expect(pp, st, 2 * tb);
+        oz_bulk_copy(pp, st, dst, p.digits + (size_t)a_slot * OZ_TILE, tb);
+        oz_bulk_copy(pp, st, dst + OZ_OPER, p.digits + (size_t)b_slot * OZ_TILE, tb);
+      }
+    };
     if (nsteps > 0) {
       auto flags_of = [&](int s, const int*& f0, const int*& f1) {
         int sa, sb;
@@ -477,15 +492,23 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
       ok = cta_wait(c, c.flags + sa, sa == sb ? nullptr : c.flags + sb, &s_ok);
       if (ok) {
         if (threadIdx.x == 0) s_ready = 1;
-        oz_load_async(stages, p.digits + (size_t)sa * OZ_TILE);
-        oz_load_async(stages + OZ_OPER, p.digits + (size_t)sb * OZ_TILE);
-        cp_async_commit();
+        stage(0, sa, sb);
       }
       for (int s = 0; s < nsteps && ok; ++s) {
         __half* cur = stages + (s & 1) * OZF_STAGE_HALVES;
-        __half* nxt = stages + ((s + 1) & 1) * OZF_STAGE_HALVES;
-        cp_async_wait_all();
-        __syncthreads();   // stage s is in shared memory; stage s-1 buffers are free
+        const int nst = (s + 1) & 1;
+        {   // stage s has landed; the barrier frees stage s-1's buffers
+          const bool late = !oz_stage_wait(pp, s & 1, ph);
+          if (__syncthreads_or(late)) {
+            if (threadIdx.x == 0) {
+              atomicCAS(c.ctrl + CTRL_ERR, ERR_NONE, ERR_TIMEOUT);
+              raise_abort(c);
+            }
+            oz_stage_wait(pp, s & 1, ph);   // one more bounded wait for the copy before leaving
+            ok = false;
+            break;
+          }
+        }
         const bool more = s + 1 < nsteps;
         bool issued = false;
         int na = 0, nb = 0;
@@ -496,9 +519,7 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
           }
           if (s_ready > s + 1) {
             slots(s + 1, na, nb);
-            oz_load_async(nxt, p.digits + (size_t)na * OZ_TILE);
-            oz_load_async(nxt + OZ_OPER, p.digits + (size_t)nb * OZ_TILE);
-            cp_async_commit();
+            stage(nst, na, nb);
             issued = true;
           }
         }
@@ -508,16 +529,12 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
           slots(s + 1, na, nb);
           if (!(ok = cta_wait(c, c.flags + na, na == nb ? nullptr : c.flags + nb, &s_ok))) break;
           if (threadIdx.x == 0) s_ready = s + 2;
-          oz_load_async(nxt, p.digits + (size_t)na * OZ_TILE);
-          oz_load_async(nxt + OZ_OPER, p.digits + (size_t)nb * OZ_TILE);
-          cp_async_commit();
+          stage(nst, na, nb);
         }
       }
     }
-    if (!ok) {
-      cp_async_wait_all();
-      return false;
-    }
+    if (!ok) return false;   // no copy is in flight here
+    if (threadIdx.x == 0) pp->phase = ph;
     __syncthreads();
     trace_clear_marks(c, t);
     trace_mark(c, t, 0);   // product loop done

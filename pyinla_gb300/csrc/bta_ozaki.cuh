@@ -179,6 +179,57 @@ __device__ __forceinline__ void oz_load_async(__half* sdst, const __half* gsrc) 
   for (int q = threadIdx.x; q < OZ_CHUNKS16; q += NT) cp_async16(sdst + q * 8, gsrc + q * 8);
 }
 
+// ---- bulk staging of digit planes -------------------------------------------------
+// A product loop stages each step's operands (one contiguous 16 KB block per tile, or
+// its leading planes) with cp.async.bulk copies issued by one thread; the copies
+// signal one mbarrier per stage buffer.  OzPipe is the per-CTA state: the two
+// barriers and the parity of the next completion of each (kept across tasks).
+struct OzPipe {
+  unsigned long long bar[2];
+  unsigned phase;   // bit st: parity of the next completion of stage st
+};
+
+__device__ __forceinline__ void oz_pipe_init(OzPipe* pp) {
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&pp->bar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&pp->bar[1])) : "memory");
+    pp->phase = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+}
+
+// Thread 0: expect `bytes` on stage st's barrier (one arrival), then the copies.
+__device__ __forceinline__ void oz_bulk_expect(OzPipe* pp, int st, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&pp->bar[st])), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void oz_bulk_copy(OzPipe* pp, int st, __half* sdst, const __half* gsrc, unsigned bytes) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(sdst)),
+               "l"(gsrc), "r"(bytes), "r"(smem_u32(&pp->bar[st]))
+               : "memory");
+}
+
+// Every thread: wait (bounded) for stage st's next completion; flips the parity bit
+// in `ph`.  False if the limit ran out (the copies of a healthy GPU take microseconds).
+__device__ __forceinline__ bool oz_stage_wait(OzPipe* pp, int st, unsigned& ph) {
+  const unsigned parity = (ph >> st) & 1u;
+  for (int it = 0; it < (1 << 22); ++it) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(&pp->bar[st])), "r"(parity)
+        : "memory");
+    if (done) {
+      ph ^= 1u << st;
+      return true;
+    }
+  }
+  return false;
+}
+
 // Stage a tile's digit planes shifted down by q planes: shared plane s holds global
 // plane s - q (zero for s < q; global planes past the last are dropped).  Reading a
 // tile sliced against 2^E_t in the frame of a larger exponent E = E_t + 7q.

@@ -97,10 +97,12 @@ void launch_selinv_oz_prepare(const Geom& g, const double* D, const double* L, c
 __global__ void __launch_bounds__(NT, 1) k_selinv_oz(SelinvArgs p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_ok, s_t, s_ready;
+  __shared__ OzPipe pipe;
+  oz_pipe_init(&pipe);
   while (true) {
     const int t = cta_ticket(p.c, &s_t);
     if (t < 0 || t >= p.ntasks) break;
-    if (!selinv_oz_task(p, t, smem_raw, &s_ok, &s_ready)) break;
+    if (!selinv_oz_task(p, t, smem_raw, &s_ok, &s_ready, &pipe)) break;
   }
 }
 

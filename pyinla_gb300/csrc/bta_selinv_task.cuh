@@ -374,7 +374,7 @@ constexpr size_t OZS_SMEM = 2 * OZS_STAGE * sizeof(__half) + 2 * TILE_SMEM * siz
 // largest E_t so far) and stages each left tile shifted down by (E - E_t) / 7 planes;
 // a tile that raises E first folds the exact partial sums with the old E.
 static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t, unsigned char* raw, int* s_okp,
-                                                      int* s_readyp) {
+                                                      int* s_readyp, OzPipe* pp) {
   __half* stages = reinterpret_cast<__half*>(raw);
   double* X = reinterpret_cast<double*>(raw + 2 * OZS_STAGE * sizeof(__half));
   double* F = X + TILE_SMEM;
@@ -441,12 +441,34 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
     auto right_of = [&](int s) -> const __half* {
       return p.fdig + (size_t)fac_slot(g, i, pat_code(p, i, col, s), col) * OZ_TILE;
     };
-    // stage step s's operands into `dst` with the left tile shifted by q planes
-    auto stage = [&](__half* dst, const SigTile& lt, int q, int s) {
+    // stage step s's operands into stage buffer st with the left tile shifted by q
+    // planes: bulk copies of its leading OZ_S - q planes and of the right tile, the
+    // q planes below the shift zeroed by the CTA
+    unsigned ph = pp->phase;
+    auto stage = [&](int st, const SigTile& lt, int q, int s) {
+      __half* dst = stages + st * OZS_STAGE;
       const int slot = (int)(lt.flag - c.flags);
-      oz_load_async_shift(dst, p.sdig + (size_t)slot * OZ_TILE, q);
-      oz_load_async(dst + OZ_OPER, right_of(s));
-      cp_async_commit();
+      const unsigned abytes = q < OZ_S ? (unsigned)((OZ_S - q) * OZ_PLANE * sizeof(__half)) : 0u;
+      if (threadIdx.x == 0) {
+        oz_bulk_expect(pp, st, abytes + (unsigned)(OZ_TILE * sizeof(__half)));
+        if (abytes) oz_bulk_copy(pp, st, dst + q * OZ_PLANE, p.sdig + (size_t)slot * OZ_TILE, abytes);
+        oz_bulk_copy(pp, st, dst + OZ_OPER, right_of(s), (unsigned)(OZ_TILE * sizeof(__half)));
+      }
+      for (int idx = threadIdx.x; idx < q * (OZ_PLANE / 8); idx += NT)
+        reinterpret_cast<uint4*>(dst)[idx] = make_uint4(0u, 0u, 0u, 0u);
+    };
+    // wait for stage st; a copy that never lands aborts the launch
+    auto stage_wait = [&](int st) -> bool {
+      const bool late = !oz_stage_wait(pp, st, ph);
+      if (__syncthreads_or(late)) {
+        if (threadIdx.x == 0) {
+          atomicCAS(c.ctrl + CTRL_ERR, ERR_NONE, ERR_TIMEOUT);
+          raise_abort(c);
+        }
+        oz_stage_wait(pp, st, ph);   // give the copy one more bounded wait before leaving
+        return false;
+      }
+      return true;
     };
 
     bool ok = true;
@@ -468,13 +490,12 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         if (threadIdx.x == 0) s_ready = 1;
         E = sig_exp_decode(*s_val, c.epoch);
         set_esum();
-        stage(stages, lt, 0, 0);
+        stage(0, lt, 0, 0);
       }
       for (int s = 0; s < np && ok; ++s) {
         __half* cur = stages + (s & 1) * OZS_STAGE;
-        __half* nxt = stages + ((s + 1) & 1) * OZS_STAGE;
-        cp_async_wait_all();
-        __syncthreads();
+        const int nst = (s + 1) & 1;
+        if (!(ok = stage_wait(s & 1))) break;   // contains the barrier that frees the other stage
         const bool more = s + 1 < np;
         bool have = false;
         SigTile nt_;
@@ -487,7 +508,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
           }
           if (s_ready > s + 1) {
             En = sig_exp_decode(ring[(s + 1) % SCAN_RING], c.epoch);
-            stage(nxt, nt_, En > E ? 0 : sig_shift(E, En), s + 1);
+            stage(nst, nt_, En > E ? 0 : sig_shift(E, En), s + 1);
             have = true;
           }
         }
@@ -515,17 +536,15 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
               set_esum();
             }
           }
-          if (!have) stage(nxt, nt_, sig_shift(E, En), s + 1);
+          if (!have) stage(nst, nt_, sig_shift(E, En), s + 1);
           tcur = nt_.trans;
         } else if (E > NO_EXP) {
           oz_fold_sub(acc, esum);   // acc.v = -(sum)
         }
       }
     }
-    if (!ok) {
-      cp_async_wait_all();
-      return false;
-    }
+    if (!ok) return false;   // no copy is in flight here
+    if (threadIdx.x == 0) pp->phase = ph;
     trace_put(c, t, 2, (long long)waited);
     trace_put(c, t, 3, np);
     __syncthreads();
