@@ -167,7 +167,7 @@ __device__ __forceinline__ void cta_publish_val(const Ctl& c, int* flag, int pay
 // which costs thousands of cycles in a busy kernel).  `flags_of(s, f0, f1)` returns the
 // step's flags (nullptr = none).  The caller synchronises the CTA afterwards, which
 // extends the acquires to all its threads.
-constexpr int SCAN_AHEAD = 8;
+constexpr int SCAN_AHEAD = 16;
 static_assert(2 * SCAN_AHEAD <= 32, "one lane per flag");
 
 __device__ __forceinline__ int ld_relaxed_gpu(const int* p) {
