@@ -51,13 +51,14 @@ extern "C" {
 
 /* How the factorization computes its tile products (gbta_set_method).
  * GBTA_METHOD_FP64: FP64 FMAs on the CUDA cores.
- * GBTA_METHOD_OZAKI (default): error-free splitting of each FP64 tile into nine 6-bit
- * integer digit planes (per-row exponents from the matrix diagonal) multiplied on the
- * tensor cores with exact fp32 accumulation and folded into FP64; the product error is
- * bounded like an FP64 product's (a few units of 2^-53 of the operands' magnitudes).
- * The selected inversion uses the same scheme for its products (factor tiles sliced
- * once per inversion with per-column exponents, Sigma tiles sliced on the fly).  Tile
- * Cholesky factors, tile inverses / triangular solves and the sweeps stay FP64. */
+ * GBTA_METHOD_OZAKI (default): error-free splitting of each FP64 tile into eight
+ * balanced base-128 integer digit planes (per-row exponents from the matrix diagonal)
+ * multiplied on the tensor cores (43 plane pairs) with exact fp32 accumulation and
+ * folded into FP64; the product error is bounded like an FP64 product's (a few units
+ * of 2^-53 of the operands' magnitudes).  The selected inversion uses the same scheme
+ * for its products (factor tiles sliced once per inversion with per-column exponents,
+ * every Sigma tile sliced once by the task that produces it).  Tile Cholesky factors,
+ * tile inverses / triangular solves and the sweeps stay FP64. */
 #define GBTA_METHOD_FP64 0
 #define GBTA_METHOD_OZAKI 1
 
