@@ -362,8 +362,12 @@ static __device__ __forceinline__ int sig_shift(int E, int En) {
 // OZS_STAGE: halves per stage (A, B digit planes).  X and F follow the two stages; W
 // (used only by the tip task, when no stage is in flight) reuses the first stage.
 constexpr int OZS_STAGE = 2 * OZ_OPER;
+// Step descriptors of a task's product loop, computed once per task (larger loops
+// compute the rest on the fly): left tile slot << 1 | transposed, right tile slot.
+constexpr int OZS_DESC = 512;
 constexpr size_t OZS_SMEM = 2 * OZS_STAGE * sizeof(__half) + 2 * TILE_SMEM * sizeof(double) + TS * sizeof(double) +
-                            TS * sizeof(int) + 4 * sizeof(double) + (SCAN_RING + 1) * sizeof(int);
+                            TS * sizeof(int) + 4 * sizeof(double) + (SCAN_RING + 2) * sizeof(int) +
+                            OZS_DESC * sizeof(int2);
 
 // Task t of a tensor-core selected-inversion instance.  `raw` is OZS_SMEM bytes of
 // (16-byte aligned) shared memory.  Returns false when the launch is aborted.
@@ -384,6 +388,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
   double* red4 = reinterpret_cast<double*>(ecol_t + TS);
   int* ring = reinterpret_cast<int*>(red4 + 4);   // flag words of the steps found ready
   int* s_val = ring + SCAN_RING;                  // flag word of the last blocking wait
+  int2* sdesc = reinterpret_cast<int2*>(ring + SCAN_RING + 2);   // step descriptors (8-byte aligned)
   int& s_ok = *s_okp;
   int& s_ready = *s_readyp;
   const Geom& g = p.g;
@@ -430,17 +435,33 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
 #pragma unroll
         for (int q = 0; q < 4; ++q) esum[n][q] = E + ecol_t[oz_col(n, q)];
     };
-    // step s: left tile (Sigma digits) and right digits (G)
-    auto left_of = [&](int s) -> SigTile {
+    // step s: left tile (Sigma digits, its flag slot and orientation) and right tile
+    // (G digits), as a descriptor (left slot << 1 | transposed, right slot)
+    auto compute_desc = [&](int s) -> int2 {
       const int l = pat_code(p, i, col, s);
-      if (type == ST_OFF) return sig_tile(p, i, j, l);
-      SigTile st_ = sig_dest(p, i, l, col);   // Sigma(l, col), used transposed
-      st_.trans = true;
+      int slot;
+      bool tr;
+      if (type == ST_OFF) {
+        const SigTile st_ = sig_tile(p, i, j, l);
+        slot = (int)(st_.flag - c.flags);
+        tr = st_.trans;
+      } else {   // Sigma(l, col), used transposed
+        slot = (int)(sig_dest(p, i, l, col).flag - c.flags);
+        tr = true;
+      }
+      return make_int2((slot << 1) | (tr ? 1 : 0), fac_slot(g, i, l, col));
+    };
+    for (int s = threadIdx.x; s < np && s < OZS_DESC; s += NT) sdesc[s] = compute_desc(s);
+    __syncthreads();
+    auto desc_of = [&](int s) -> int2 { return s < OZS_DESC ? sdesc[s] : compute_desc(s); };
+    auto left_of = [&](int s) -> SigTile {
+      const int2 d = desc_of(s);
+      SigTile st_;
+      st_.flag = c.flags + (d.x >> 1);
+      st_.trans = (d.x & 1) != 0;
       return st_;
     };
-    auto right_of = [&](int s) -> const __half* {
-      return p.fdig + (size_t)fac_slot(g, i, pat_code(p, i, col, s), col) * OZ_TILE;
-    };
+    auto right_of = [&](int s) -> const __half* { return p.fdig + (size_t)desc_of(s).y * OZ_TILE; };
     // stage step s's operands into stage buffer st with the left tile shifted by q
     // planes: bulk copies of its leading OZ_S - q planes and of the right tile, the
     // q planes below the shift zeroed by the CTA
