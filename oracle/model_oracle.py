@@ -152,3 +152,34 @@ def dense_gradient(spatial_terms, term_vw, ns, nv, nt, nb, A, y, tip_prec, coef,
         g[idx] -= 0.5 * yv.size - 0.5 * tau_y[v] * float(yv @ yv)
     g -= log_prior_grad
     return g
+
+
+def hessian_fd(fun, theta, eps):
+    """FD Hessian of f as in PyINLA._evaluate_hessian_f (pyinla.py:767-910): f at theta,
+    theta +- eps_i (diagonal: (f+ - 2 f + f-) / eps^2) and theta +- eps_i +- eps_j (upper
+    triangle: (f++ - f+- - f-+ + f--) / (4 eps^2), mirrored); 1 + 2d + 2d(d-1) evaluations."""
+    theta = np.asarray(theta, dtype=np.float64)
+    d = theta.size
+    E = eps * np.eye(d)
+    f0 = fun(theta)
+    H = np.zeros((d, d))
+    for i in range(d):
+        H[i, i] = (fun(theta + E[i]) - 2.0 * f0 + fun(theta - E[i])) / eps ** 2
+        for j in range(i + 1, d):
+            H[i, j] = (fun(theta + E[i] + E[j]) - fun(theta + E[i] - E[j]) - fun(theta - E[i] + E[j])
+                       + fun(theta - E[i] - E[j])) / (4.0 * eps * eps)
+            H[j, i] = H[i, j]
+    return H
+
+
+def hessian_from_gradient(grad, theta, eps):
+    """Hessian by central differences of an exact gradient (2d gradient evaluations),
+    symmetrised: H[:, k] = (g(theta + eps e_k) - g(theta - eps e_k)) / (2 eps)."""
+    theta = np.asarray(theta, dtype=np.float64)
+    d = theta.size
+    H = np.zeros((d, d))
+    for k in range(d):
+        e = np.zeros(d)
+        e[k] = eps
+        H[:, k] = (np.asarray(grad(theta + e)) - np.asarray(grad(theta - e))) / (2.0 * eps)
+    return 0.5 * (H + H.T)

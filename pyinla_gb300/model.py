@@ -452,6 +452,28 @@ class KronGaussianModel:
             return f
         return f, self._adjoint_gradient(theta, coef, quad)
 
+    def hessian(self, theta, eps: float = 5e-3) -> np.ndarray:
+        """Hessian of f at theta by central differences of the adjoint gradient, symmetrised:
+        2 d gradient evaluations (each a factorization, a solve and a selected inversion)
+        where the reference differences f itself with 1 + 2d + 2d(d-1) evaluations
+        (PyINLA._evaluate_hessian_f, pyinla.py:767-910; default step eps_hessian_f = 5e-3,
+        configs/pyinla_config.py:52)."""
+        theta = np.asarray(theta, dtype=np.float64)
+        d = theta.size
+        H = np.zeros((d, d))
+        for k in range(d):
+            e = np.zeros(d)
+            e[k] = eps
+            _, gp = self.evaluate(theta + e, gradient=True)
+            _, gm = self.evaluate(theta - e, gradient=True)
+            H[:, k] = (gp - gm) / (2.0 * eps)
+        return 0.5 * (H + H.T)
+
+    def covariance_hp(self, theta, eps: float = 5e-3) -> np.ndarray:
+        """Covariance of the hyperparameters, the inverse of the Hessian of f
+        (PyINLA.compute_covariance_hp, pyinla.py:747-765)."""
+        return np.linalg.inv(self.hessian(theta, eps))
+
     def marginal_variances(self, theta):
         """(diag(Sigma), diag(A Sigma A^T)) at theta, Sigma = Q_cond^-1: the two outputs of
         the reference's run() (pyinla.py:303-311; get_marginal_variances_latent_parameters
