@@ -5,7 +5,7 @@
   agree to ~1e-6;
 * against the reference's own FD-of-f Hessian and covariance (fixture of
   tests/golden/make_hessian_golden.py): both are O(eps^2) approximations of the
-  Hessian, so they agree to ~1e-3 at eps = 5e-3.
+  Hessian; at eps = 5e-3 they agree to ~1e-5 here.
 """
 import numpy as np
 import pytest
@@ -44,6 +44,6 @@ def test_hessian_and_covariance(built):
                                  spec.lik_theta_indices(), spec.log_prior_grad(th))
 
     assert relerr(H, mo.hessian_from_gradient(grad, theta, eps)) < 1e-6
-    assert relerr(H, g["hessian"]) < 2e-3
+    assert relerr(H, g["hessian"]) < 1e-4
     assert np.array_equal(H, H.T)
-    assert relerr(m.covariance_hp(theta, eps), g["cov"]) < 5e-2   # an inverse of an FD matrix
+    assert relerr(m.covariance_hp(theta, eps), g["cov"]) < 1e-3
