@@ -378,6 +378,16 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                              "ratio_vs_plain": t_grad / t_plain, "central_fd_ratio": 2 * d + 1,
                              "speedup_vs_fd": (2 * d + 1) * t_plain / t_grad,
                              "gradients_per_s": 1.0 / t_grad, "dim_theta": int(d)}
+        # theta-Hessian: differences of 2d adjoint gradients, against the reference's
+        # differences of f (1 + 2d + 2d(d-1) evaluations, pyinla.py:767-910)
+        t0 = time.perf_counter()
+        model.hessian(theta)
+        torch.cuda.synchronize()
+        t_hess = time.perf_counter() - t0
+        n_fd = 1 + 2 * d + 2 * d * (d - 1)
+        result["hessian"] = {"ms": t_hess * 1e3, "gradient_evaluations": 2 * int(d),
+                             "reference_f_evaluations": int(n_fd),
+                             "speedup_vs_fd_of_f": n_fd * t_plain / t_hess}
 
     # ---- CPU baseline (rank 0, N = 1 only): the oracle on the host cores
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
