@@ -272,6 +272,26 @@ int gbta_obs_variances(gbta_solver* s, long long nrows, const long long* A_rowpt
                        const double* A_val, const double* SD, const double* SL, const double* SR,
                        const double* ST, double* out);
 
+/* ---- inner Newton iteration for non-Gaussian likelihoods ----------------- */
+/* out[e] = sum_{k = seg[e] .. seg[e+1]-1} w[obs[k]] * coef[k] for e < n_out (device
+ * arrays; fixed order, deterministic): the entries of A^T W A that gbta_assemble_kron
+ * takes as its likelihood part (diagonal-block CSR values, then the dense arrow rows,
+ * then the tip), from the per-entry lists of (observation, A_rp A_rq) pairs.  Replaces
+ * the product A^T D A of Model.construct_Q_conditional (src/pyinla/core/model.py:384-423)
+ * for the inner iteration of PyINLA._inner_iteration (src/pyinla/core/pyinla.py:1025-1074).
+ * Asynchronous on the solver's stream. */
+int gbta_weighted_gram(gbta_solver* s, long long n_out, const long long* seg, const int* obs, const double* coef,
+                       const double* w, double* out);
+
+/* y = Q x for the symmetric BTA matrix in the Serinv layout (D full symmetric blocks,
+ * L_t = block (t+1, t), R_t = arrow rows of column block t, T the tip; use_arrow = 0
+ * ignores R, T and the last a entries).  Device pointers, N = nt*b + a.  The product
+ * Q_prior x of the information vector (src/pyinla/core/model.py:425-449) and of the
+ * prior term x^T Q_prior x (src/pyinla/core/pyinla.py:1076-1110).  Fixed summation
+ * order (deterministic).  Asynchronous on the solver's stream. */
+int gbta_bta_symv(gbta_solver* s, const double* D, const double* L, const double* R, const double* T,
+                  int use_arrow, const double* x, double* y);
+
 /* ---- many instances in one persistent launch per phase -------------------- */
 /* A batch holds n independent BTA instances of arbitrary geometry (b[k], nt[k], a[k];
  * a[k] = 0: block tridiagonal) -- the Q(theta) of a gradient's central-difference

@@ -83,6 +83,8 @@ SIGNATURES = {
                                     _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbta_sigma_diagonal": (_c_int, [_vp, _vp, _vp, _vp]),
     "gbta_obs_variances": (_c_int, [_vp, _c_ll, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gbta_weighted_gram": (_c_int, [_vp, _c_ll, _vp, _vp, _vp, _vp, _vp]),
+    "gbta_bta_symv": (_c_int, [_vp, _vp, _vp, _vp, _vp, _c_int, _vp, _vp]),
     "gbta_batch_create": (_c_int, [_c_int, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
     "gbta_batch_destroy": (_c_int, [_vp]),
     "gbta_batch_workspace_bytes": (ctypes.c_size_t, [_vp]),
