@@ -503,7 +503,7 @@ static __device__ int smem_potrf(double* S) {
   if (g == 0) {
     const double d = __shfl_sync(0xffffffffu, acc[0], 0);
     const double y = rsqrt3(d);
-    acc[0] = (r > 0) ? acc[0] * y : (r == 0 ? d * y : 0.0);
+    acc[0] *= y;   // row 0 holds d itself: l_00 = d y, l_r0 = a_r0 y
     xs[r] = acc[0];
     if (r == 0) s_info = (d > 0.0) ? 0 : 1;
   }
@@ -516,7 +516,7 @@ static __device__ int smem_potrf(double* S) {
       const double a = fma(-xj[r], xj[j + 1], acc[qn]);
       const double d = __shfl_sync(0xffffffffu, a, j + 1);
       const double y = rsqrt3(d);
-      const double l = (r > j + 1) ? a * y : (r == j + 1 ? d * y : 0.0);
+      const double l = (r > j) ? a * y : 0.0;   // lane j+1 holds d = a: one multiply for l_kk and l_rk
       acc[qn] = l;
       xs[((j + 1) % 3) * TS + r] = l;
       if (r == 0 && !(d > 0.0) && s_info == 0) s_info = j + 2;
