@@ -92,7 +92,9 @@ static __device__ bool factor_feed_rows(const FactorArgs& p, int t, int i, int q
   long long grow0;
   const Tile ft = feeder_tile(p, i, col, slot, grow0);
   const int gc = i * g.B + col, row0 = q * FEED_ROWS;
+  trace_clear_marks(c, t);
   if (!cta_wait(c, p.feed_pre + gc, c.flags + g.fD(i, col, col), s_ok)) return false;
+  trace_mark(c, t, 0);   // products and diagonal factor tile ready
   tile_load(F, btile(Dblk(p, i), g, col, col));
   for (int idx = threadIdx.x; idx < FEED_ROWS * TS; idx += NT) {
     const int rr = row0 + idx / TS, cc = idx % TS;
@@ -106,7 +108,9 @@ static __device__ bool factor_feed_rows(const FactorArgs& p, int t, int i, int q
   tile_diag_recip(F, rd);
   __syncthreads();
   tile_scale_rows_by_recip(FS, F, rd);
+  trace_mark(c, t, 1);   // operands staged
   smem_trsm_rlt_rows8(X, FS, rd, row0);
+  trace_mark(c, t, 2);   // rows solved
   for (int idx = threadIdx.x; idx < FEED_ROWS * TS; idx += NT) {
     const int rr = row0 + idx / TS, cc = idx % TS;
     if (rr < ft.rows && cc < ft.cols) const_cast<double*>(ft.p)[(size_t)rr * ft.ld + cc] = X[rr * LDS + cc];
@@ -122,6 +126,7 @@ static __device__ bool factor_feed_rows(const FactorArgs& p, int t, int i, int q
       }
   }
   __syncthreads();
+  trace_mark(c, t, 3);   // rows and digits written
   if (threadIdx.x == 0) {   // acq_rel: releases this group's rows, acquires the earlier groups'
     const int done = atom_add_acq_rel(p.feed_cnt + gc, 1) + 1;
     if (done == g.feeder_quarters(i, col)) st_release(c.flags + slot, c.epoch);
@@ -470,6 +475,7 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
     bool ok = true;
     OzPipe* pp = sm.pipe;
     unsigned ph = pp->phase;
+    unsigned long long t_alldeps = 0;   // (trace) when the last operand was known ready
     // stage the operand tiles (slots a, b) of a step into stage buffer st (bulk copies)
     auto stage = [&](int st, int a_slot, int b_slot) {
       if (threadIdx.x == 0) {
@@ -516,6 +522,7 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
           if (s_ready <= s + 1) {   // uniform: read after the barrier
             scan_ready(c, nsteps, flags_of, &s_ready);
             __syncthreads();
+            if (c.trace && s_ready >= nsteps && !t_alldeps) t_alldeps = gtimer();
           }
           if (s_ready > s + 1) {
             slots(s + 1, na, nb);
@@ -529,6 +536,7 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
           slots(s + 1, na, nb);
           if (!(ok = cta_wait(c, c.flags + na, na == nb ? nullptr : c.flags + nb, &s_ok))) break;
           if (threadIdx.x == 0) s_ready = s + 2;
+          if (c.trace && s + 2 >= nsteps) t_alldeps = gtimer();
           stage(nst, na, nb);
         }
       }
@@ -538,6 +546,7 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
     __syncthreads();
     trace_clear_marks(c, t);
     trace_mark(c, t, 0);   // product loop done
+    trace_put(c, t, 3, (long long)t_alldeps);   // last operand ready
 #pragma unroll
     for (int n = 0; n < 2; ++n)
 #pragma unroll
