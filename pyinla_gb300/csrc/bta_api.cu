@@ -56,7 +56,7 @@ struct gbta_solver {
   int n_stasks = 0;
   double* d_tip_part = nullptr;
   double* d_arrow_part = nullptr;
-  int* d_faux = nullptr;      // feeder flags [nt*B] and row-group counters [nt*B]
+  int* d_faux = nullptr;      // feeder "products done" flags [nt*B]
   double* d_ld = nullptr;   // logdet partials [nt + 1] + result [1]
   double* d_sig = nullptr;  // selected-inversion output blocks (lazy)
   double* d_selws = nullptr;  // selected-inversion pre-pass: diagonal inverses (lazy)
@@ -218,8 +218,8 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   CREATE_CUDA(cudaMalloc(&s->d_stasks, st.size() * sizeof(int4)));
   CREATE_CUDA(cudaMalloc(&s->d_tip_part, ntile * gbta::TS * gbta::TS * sizeof(double)));
   CREATE_CUDA(cudaMalloc(&s->d_arrow_part, ntile * gbta::TS * gbta::SOLVE_NC * sizeof(double)));
-  CREATE_CUDA(cudaMalloc(&s->d_faux, 2 * ntile * sizeof(int)));
-  CREATE_CUDA(cudaMemsetAsync(s->d_faux, 0, 2 * ntile * sizeof(int), s->stream));
+  CREATE_CUDA(cudaMalloc(&s->d_faux, ntile * sizeof(int)));
+  CREATE_CUDA(cudaMemsetAsync(s->d_faux, 0, ntile * sizeof(int), s->stream));
   CREATE_CUDA(cudaMalloc(&s->d_ld, (nt + 2) * sizeof(double)));
   CREATE_CUDA(cudaMallocHost(&s->h_ctrl, CTRL_INTS * sizeof(int)));
   CREATE_CUDA(cudaMemsetAsync(s->d_ctrl, 0, CTRL_INTS * sizeof(int), s->stream));
@@ -230,7 +230,7 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
 #undef CREATE_CUDA
   s->ws_bytes = CTRL_INTS * sizeof(int) + (size_t)nflags * sizeof(int) + (ft.size() + st.size()) * sizeof(int4) +
                 ntile * gbta::TS * (gbta::TS + gbta::SOLVE_NC) * sizeof(double) + (nt + 2) * sizeof(double) +
-                2 * ntile * sizeof(int);
+                ntile * sizeof(int);
   *out = s;
   g_last_error.clear();
   return GBTA_OK;
@@ -355,8 +355,7 @@ static int factor_async(gbta_solver* s, double* D, double* L, double* R, double*
   if (s->method == GBTA_METHOD_OZAKI)
     if (int r = ensure_digits(s)) return r;
   if (int r = reset_ticket(s)) return r;
-  const size_t ntile = (size_t)s->g.nt * s->g.B;
-  GBTA_CUDA(cudaMemsetAsync(s->d_faux + ntile, 0, ntile * sizeof(int), s->stream));   // row-group counters
+  gbta::launch_clear_feeders(s->g, s->d_flags, s->stream);
   const gbta::LaunchCtl lc = next_launch(s, s->n_ftasks);
   if (s->method == GBTA_METHOD_OZAKI)
     gbta::launch_factor_oz(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part,

@@ -127,7 +127,7 @@ struct BatchInst {
   gbta::Geom g;
   int method = GBTA_METHOD_OZAKI;
   size_t flags_off = 0;     // in ints, into the flag pool
-  size_t faux_off = 0;      // in ints, into the feeder pool (flags [nt*B], counters [nt*B])
+  size_t faux_off = 0;      // in ints, into the feeder pool (flags [nt*B])
   int n_ftasks = 0, n_stasks = 0, n_vtasks = 0;
   // device workspace (inside the pool)
   int4* ftasks = nullptr;
@@ -162,7 +162,7 @@ struct gbta_batch {
   int* d_info = nullptr;
   int* d_flags = nullptr;
   size_t nflags_total = 0;
-  int* d_faux = nullptr;    // feeder flags and row-group counters of every instance
+  int* d_faux = nullptr;    // feeder "products done" flags of every instance
   size_t nfaux_total = 0;
   void* pool = nullptr;
   size_t pool_bytes = 0;
@@ -263,7 +263,6 @@ int build_args(gbta_batch* bt) {
     f.erow = q.erow;
     f.info = bt->d_info + k;
     f.feed_pre = bt->d_faux + q.faux_off;
-    f.feed_cnt = f.feed_pre + (size_t)g.nt * g.B;
     f.c = batch_ctl(bt, flags, EP_FACTOR);
     gbta::SelinvArgs& s = sa[k];
     const size_t bb = (size_t)g.b * g.b;
@@ -436,7 +435,7 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
     q.n_vtasks = g.nt * g.B + (g.a > 0 ? 1 : 0);
     q.flags_off = flags_total;
     q.faux_off = bt->nfaux_total;
-    bt->nfaux_total += 2 * (size_t)g.nt * g.B;
+    bt->nfaux_total += (size_t)g.nt * g.B;
     flags_total += (size_t)g.nflags();
     const size_t ntile = (size_t)g.nt * g.B, bb = (size_t)g.b * g.b;
     o_ft[k] = off;

@@ -46,6 +46,10 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
 __device__ __forceinline__ void st_release(int* p, int v) {
   asm volatile("st.release.gpu.global.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+// Release-add at GPU scope without a return value (no round trip for the issuer).
+__device__ __forceinline__ void red_add_release(int* p, int v) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 // Atomic add with acquire-release semantics at GPU scope; returns the old value.
 __device__ __forceinline__ int atom_add_acq_rel(int* p, int v) {
   int old;

@@ -15,6 +15,23 @@ __global__ void __launch_bounds__(NT, 1) k_factor(FactorArgs p) {
   }
 }
 
+__global__ void k_clear_feeders(Geom g, int* flags) {
+  const int n = g.nt * g.B;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const int i = k / g.B, c = k - i * g.B;
+    const int fk = g.feeder_kind(i, c);
+    if (fk == 1) flags[g.fD(i, c + 1, c)] = 0;
+    if (fk == 2) flags[g.fL(i, 0, c)] = 0;
+  }
+}
+
+void launch_clear_feeders(const Geom& g, int* flags, cudaStream_t stream) {
+  const int n = g.nt * g.B;
+  const int blocks = (n + 255) / 256;
+  k_clear_feeders<<<blocks < 1216 ? blocks : 1216, 256, 0, stream>>>(g, flags);
+  count_launches(1);
+}
+
 void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow, const int4* tasks,
                    int ntasks, double* tip_part, const LaunchCtl& lc, int* feed_aux) {
   FactorArgs p;
@@ -32,7 +49,6 @@ void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, in
   p.erow = nullptr;
   p.info = nullptr;
   p.feed_pre = feed_aux;
-  p.feed_cnt = feed_aux ? feed_aux + (size_t)g.nt * g.B : nullptr;
   p.c.ctrl = lc.ctrl;
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;

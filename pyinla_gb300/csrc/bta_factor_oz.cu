@@ -69,7 +69,6 @@ void launch_factor_oz(const Geom& g, double* D, double* L, double* R, double* T,
   p.erow = erow;
   p.info = nullptr;
   p.feed_pre = feed_aux;
-  p.feed_cnt = feed_aux ? feed_aux + (size_t)g.nt * g.B : nullptr;
   p.c.ctrl = lc.ctrl;
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;

@@ -44,7 +44,6 @@ struct FactorArgs {
   const int* erow;      // Ozaki: [nt*b + a] row exponents
   int* info;            // where a failed pivot is recorded (null: the control block)
   int* feed_pre;        // [nt*B] flag: the feeder of diagonal tile (i, c) has its products
-  int* feed_cnt;        // [nt*B] row groups of that feeder solved so far (zero at launch)
   Ctl c;
 };
 
@@ -95,10 +94,22 @@ static __device__ bool factor_feed_rows(const FactorArgs& p, int t, int i, int q
   trace_clear_marks(c, t);
   if (!cta_wait(c, p.feed_pre + gc, c.flags + g.fD(i, col, col), s_ok)) return false;
   trace_mark(c, t, 0);   // products and diagonal factor tile ready
-  tile_load(F, btile(Dblk(p, i), g, col, col));
-  for (int idx = threadIdx.x; idx < FEED_ROWS * TS; idx += NT) {
-    const int rr = row0 + idx / TS, cc = idx % TS;
-    X[rr * LDS + cc] = (rr < ft.rows && cc < ft.cols) ? __ldcg(ft.p + (size_t)rr * ft.ld + cc) : 0.0;
+  {   // the diagonal factor tile and this group's rows: all loads issued before any store
+    double fv[PER_THREAD];
+    tile_ldg(fv, btile(Dblk(p, i), g, col, col));
+    constexpr int RPT = FEED_ROWS * TS / NT;
+    double xv[RPT];
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const int idx = threadIdx.x + k * NT, rr = row0 + idx / TS, cc = idx % TS;
+      xv[k] = (rr < ft.rows && cc < ft.cols) ? __ldcg(ft.p + (size_t)rr * ft.ld + cc) : 0.0;
+    }
+    tile_sts(F, fv);
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+      const int idx = threadIdx.x + k * NT;
+      X[(row0 + idx / TS) * LDS + idx % TS] = xv[k];
+    }
   }
   const bool digits = p.method == GBTA_METHOD_OZAKI && p.digits;
   if (digits && threadIdx.x < TS) erow_t[threadIdx.x] = threadIdx.x < ft.rows ? p.erow[grow0 + threadIdx.x] : 0;
@@ -127,9 +138,12 @@ static __device__ bool factor_feed_rows(const FactorArgs& p, int t, int i, int q
   }
   __syncthreads();
   trace_mark(c, t, 3);   // rows and digits written
-  if (threadIdx.x == 0) {   // acq_rel: releases this group's rows, acquires the earlier groups'
-    const int done = atom_add_acq_rel(p.feed_cnt + gc, 1) + 1;
-    if (done == g.feeder_quarters(i, col)) st_release(c.flags + slot, c.epoch);
+  if (threadIdx.x == 0) {
+    // The feeder's flag starts the launch at zero (launch_clear_feeders) and every row
+    // group adds its share of the epoch with a release-add (no round trip): the flag
+    // reads >= epoch exactly when all groups have written their rows.
+    const int nq = g.feeder_quarters(i, col), share = c.epoch / nq;
+    red_add_release(c.flags + slot, q < nq - 1 ? share : c.epoch - (nq - 1) * share);
   }
   trace_task(c, t, FT_FEEDQ, t_task0);
   return true;

@@ -74,11 +74,15 @@ std::vector<int4> selinv_task_list(const Geom& g);
 // Host-side count of kernel launches issued by this library (see gbta_kernel_launches).
 void count_launches(int n);
 
-// feed_aux: 2 * nt * B ints (feeder "products done" flags, then per-feeder counters of
-// solved row groups, which must be zero at launch), or null when the task list has
-// no FT_PRE / FT_FEEDQ tasks.
+// feed_aux: nt * B ints (feeder "products done" flags), or null when the task list has
+// no FT_PRE / FT_FEEDQ tasks.  With FT_FEEDQ tasks the feeder tiles' own ready flags
+// must be zero at launch (launch_clear_feeders, or a cleared flag array).
 void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow,
                    const int4* tasks, int ntasks, double* tip_part, const LaunchCtl& lc, int* feed_aux = nullptr);
+
+// Zero the ready flags of the feeder tiles (Geom::feeder_kind): the FT_FEEDQ tasks of
+// a factorization add shares of the epoch to them.
+void launch_clear_feeders(const Geom& g, int* flags, cudaStream_t stream);
 
 constexpr int SOLVE_NC = 4;   // right-hand-side columns per solve launch
 
