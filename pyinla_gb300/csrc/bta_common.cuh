@@ -488,18 +488,31 @@ __device__ __forceinline__ bool col_before(int q, int j, int g) {  // g + 4q < j
   return 4 * q + 3 < j || (4 * q < j && g < j - 4 * q);
 }
 
+// Named CTA barriers (ids 1 .. 15; id 0 is __syncthreads) for a producer warp that
+// hands shared-memory data to the other warps: the producer arrives (release), the
+// consumers sync (acquire); NT threads take part.
+__device__ __forceinline__ void nbar_arrive(int id) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "n"(NT) : "memory");
+}
+__device__ __forceinline__ void nbar_sync(int id) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(NT) : "memory");
+}
+
 // In-place lower Cholesky of S (TS x TS; entries past n must already be identity).
 // Returns 0, or the 1-based column of the first non-positive (or NaN) pivot (the
 // tile then holds NaNs).  The strict upper triangle is zeroed.
-// Step j publishes pivot column j+1 (l_kk = d y, l_rk = a_rk y, y = 1/sqrt(d)); only
-// the warp owning column j+1 works on the critical path in that step (update of
-// column j+1 with pivot j, then its pivot); it applies pivot j to its other columns
-// one step later, together with pivot j+1.  Pivot columns rotate through three
-// shared slots.
+// Warp g keeps columns g, g+4, ... in registers (lane = row) and produces their pivot
+// columns (l_kk = d y, l_rk = a_rk y, y = 1/sqrt(d)) into S, handing each one to the
+// other warps with a named barrier instead of a CTA-wide barrier per column: warps
+// drift apart by up to four columns, so the FP64 work of the trailing updates spreads
+// over the steps instead of being paced by the slowest warp of every step.  The owner
+// of column j+1 applies pivot j to that column first and produces pivot j+1 at once
+// (look-ahead), then applies pivot j to its other columns.  A warp consumes pivot p
+// before any pivot past p+4 can exist, so eight barrier ids in rotation suffice.
 static __device__ int smem_potrf(double* S) {
-  __shared__ double xs[3 * TS];
   __shared__ int s_info;
   const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_info = TS + 1;
   __syncthreads();
   double acc[8];
 #pragma unroll
@@ -508,44 +521,42 @@ static __device__ int smem_potrf(double* S) {
     const double d = __shfl_sync(0xffffffffu, acc[0], 0);
     const double y = rsqrt3(d);
     acc[0] *= y;   // row 0 holds d itself: l_00 = d y, l_r0 = a_r0 y
-    xs[r] = acc[0];
-    if (r == 0) s_info = (d > 0.0) ? 0 : 1;
+    S[r * LDS] = acc[0];
+    if (r == 0 && !(d > 0.0)) atomicMin(&s_info, 1);
+    nbar_arrive(1);
   }
-  __syncthreads();
 #pragma unroll
   for (int j = 0; j < TS; ++j) {
-    const double* xj = xs + (j % 3) * TS;
+    double lj;   // l_rj
+    if (g == (j & 3)) {
+      lj = acc[j >> 2];
+    } else {
+      nbar_sync(1 + (j & 7));
+      lj = S[r * LDS + j];
+    }
     if (j + 1 < TS && g == ((j + 1) & 3)) {
       const int qn = (j + 1) >> 2;
-      const double a = fma(-xj[r], xj[j + 1], acc[qn]);
+      const double a = fma(-lj, S[(j + 1) * LDS + j], acc[qn]);
       const double d = __shfl_sync(0xffffffffu, a, j + 1);
       const double y = rsqrt3(d);
       const double l = (r > j) ? a * y : 0.0;   // lane j+1 holds d = a: one multiply for l_kk and l_rk
       acc[qn] = l;
-      xs[((j + 1) % 3) * TS + r] = l;
-      if (r == 0 && !(d > 0.0) && s_info == 0) s_info = j + 2;
-    } else {
-      const double lr = xj[r];
+      S[r * LDS + j + 1] = l;
+      if (r == 0 && !(d > 0.0)) atomicMin(&s_info, j + 2);
+      nbar_arrive(1 + ((j + 1) & 7));
 #pragma unroll
       for (int q = 0; q < 8; ++q)
-        if (col_after(q, j + 1, g)) acc[q] = fma(-lr, xj[g + 4 * q], acc[q]);
-      if (j >= 1 && g == (j & 3)) {   // owner of the previous step: its deferred pivot j-1
-        const double* xp = xs + ((j + 2) % 3) * TS;
-        const double lp = xp[r];
+        if (col_after(q, j + 1, g)) acc[q] = fma(-lj, S[(g + 4 * q) * LDS + j], acc[q]);
+    } else {
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
-          if (col_after(q, j + 1, g)) acc[q] = fma(-lp, xp[g + 4 * q], acc[q]);
-      }
+      for (int q = 0; q < 8; ++q)
+        if (col_after(q, j, g)) acc[q] = fma(-lj, S[(g + 4 * q) * LDS + j], acc[q]);
     }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const int c = g + 4 * q;
-    S[r * LDS + c] = (c > r) ? 0.0 : acc[q];
   }
   __syncthreads();
-  return s_info;
+  const int info = s_info;
+  __syncthreads();
+  return info > TS ? 0 : info;
 }
 
 // X <- X * F^{-T} with F lower triangular; rd = 1/diag(F) (tile_diag_recip).  Row r
