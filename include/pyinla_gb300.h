@@ -84,6 +84,16 @@ int gbta_probe_fp64_peak(int iters, double* tflops);
  * reference counterpart (a measurement aid). */
 int gbta_probe_tiles(int iters, long long* cycles);
 
+/* Check of the tcgen05 tile step (digit-plane products on the 5th-generation tensor
+ * cores, accumulators in tensor memory) against the mma.sync tile step on one CTA,
+ * with pseudo-random digits: mismatches[0..6] count differing exact partial sums for
+ * (left orientation, plane shift) = (plain, 0), (transposed, 0), (plain, 2),
+ * (transposed, 3), (plain, 5), (transposed, 7), (plain, 8); [7] FP64 fold results
+ * that differ in any bit; [8] partial sums after two accumulated steps (-1: an MMA
+ * completion wait ran out).  cycles[0] per tcgen05 tile step, [1] per mma.sync tile
+ * step.  No reference counterpart (a measurement and correctness aid). */
+int gbta_probe_umma(int iters, int* mismatches, long long* cycles);
+
 /* Clock cycles of the primitives those routines are built from, on one CTA:
  * cycles[0] dependent DFMA (one warp), [1] independent DFMA per warp instruction (one
  * warp), [2] the same with four warps, [3] DFMA under a warp-uniform false predicate,

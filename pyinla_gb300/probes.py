@@ -2,7 +2,8 @@
 
 Prints the chip's FP64 FMA rate (the roofline denominator of the FP64 kernels), the
 cycle counts of the 32 x 32 tile routines that sit on the dataflow critical paths
-and of the primitives they are built from (gbta_probe_tiles, gbta_probe_latencies in
+and of the primitives they are built from, and the check of the tcgen05 tile step
+against the mma.sync one (gbta_probe_tiles, gbta_probe_latencies, gbta_probe_umma in
 include/pyinla_gb300.h).
 """
 from __future__ import annotations
@@ -31,6 +32,18 @@ def tile_cycles(iters: int = 200) -> dict:
     return {n: int(c) for n, c in zip(names, cyc)}
 
 
+def umma_check(iters: int = 200) -> dict:
+    """tcgen05 tile step against the mma.sync tile step (gbta_probe_umma)."""
+    lib = _lib.load()
+    mis = np.zeros(9, dtype=np.int32)
+    cyc = np.zeros(2, dtype=np.int64)
+    _lib.check(lib.gbta_probe_umma(int(iters), mis.ctypes.data, cyc.ctypes.data))
+    names = ["plain_q0", "trans_q0", "plain_q2", "trans_q3", "plain_q5", "trans_q7", "plain_q8", "fold_bits",
+             "two_steps"]
+    return {"mismatches": {n: int(m) for n, m in zip(names, mis)},
+            "cycles_per_step": {"tcgen05": int(cyc[0]), "mma_sync": int(cyc[1])}}
+
+
 def primitive_cycles() -> dict:
     lib = _lib.load()
     cyc = np.zeros(9, dtype=np.int64)
@@ -52,7 +65,7 @@ def main() -> None:
 
     build.build()
     print(json.dumps({"fp64_dfma_tflops": fp64_peak_tflops(), **tensor_rates(), "tile_cycles": tile_cycles(),
-                      "primitive_cycles": primitive_cycles()}))
+                      "umma_tile_step": umma_check(), "primitive_cycles": primitive_cycles()}))
 
 
 if __name__ == "__main__":
