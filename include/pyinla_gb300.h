@@ -86,13 +86,27 @@ int gbta_probe_tiles(int iters, long long* cycles);
 
 /* Check of the tcgen05 tile step (digit-plane products on the 5th-generation tensor
  * cores, accumulators in tensor memory) against the mma.sync tile step on one CTA,
- * with pseudo-random digits: mismatches[0..6] count differing exact partial sums for
- * (left orientation, plane shift) = (plain, 0), (transposed, 0), (plain, 2),
- * (transposed, 3), (plain, 5), (transposed, 7), (plain, 8); [7] FP64 fold results
- * that differ in any bit; [8] partial sums after two accumulated steps (-1: an MMA
- * completion wait ran out).  cycles[0] per tcgen05 tile step, [1] per mma.sync tile
- * step.  No reference counterpart (a measurement and correctness aid). */
+ * with pseudo-random digits; each entry counts FP64 results (after the exact fold)
+ * that differ in any bit: mismatches[0..6] for (left orientation, plane shift) =
+ * (plain, 0), (transposed, 0), (plain, 2), (transposed, 3), (plain, 5), (transposed,
+ * 7), (plain, 7); [7] transposed with the MN-major offsets in the other descriptor
+ * fields (a layout check: nonzero is expected); [8], [9] two accumulated steps,
+ * transposed and plain (-1: an MMA completion wait ran out).  cycles[0] per tcgen05
+ * tile step, [1] per mma.sync tile step, [2] issuing one tcgen05 tile step (one
+ * thread, no MMA in flight), [3] one fold of the tensor-memory accumulators into FP64
+ * (cycles holds 4 values).  No reference counterpart (a measurement and correctness
+ * aid). */
 int gbta_probe_umma(int iters, int* mismatches, long long* cycles);
+
+/* Residency of CTAs holding tensor memory (a launch-shape check): a probe kernel with
+ * 100 KB of shared memory and 256 tensor-memory columns per CTA, launched with two
+ * CTAs per SM.  out[0] CTAs per SM the occupancy calculator allows for it (it reports
+ * one for every kernel that allocates tensor memory); out[1] SMs that ran two of its
+ * CTAs at the same time; out[2] SMs that received two; out[3] the longest wait of a
+ * CTA for its tensor memory in ns; out[4] CTAs per SM that fit its registers, shared
+ * and tensor memory (the rule launch_grid applies to tensor-memory kernels).  out
+ * holds 5 values.  No reference counterpart. */
+int gbta_probe_tmem_pairs(long long* out);
 
 /* Clock cycles of the primitives those routines are built from, on one CTA:
  * cycles[0] dependent DFMA (one warp), [1] independent DFMA per warp instruction (one
@@ -141,8 +155,9 @@ int gbta_get_method(const gbta_solver* s);
 int gbta_set_ctas_per_sm(gbta_solver* s, int n);
 
 /* Task tracing (off by default).  When enabled, every dataflow kernel launched by
- * the solver records one entry of 8 int64 per task: [ticket, (task type << 16) | SM
- * id, start ns, end ns, m0, m1, m2, m3] (GPU global timer; m0..m3 are intermediate
+ * the solver records one entry of 8 int64 per task: [ticket, (CTA index << 32) |
+ * (task type << 16) | SM id, start ns, end ns, m0, m1, m2, m3] (GPU global timer;
+ * m0..m3 are intermediate
  * marks of the task's phases, 0 where a kernel sets none).  gbta_get_trace copies the
  * records (out: 8 * max_records int64) of the last traced launch to host memory and
  * returns how many were copied. */

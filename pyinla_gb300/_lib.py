@@ -46,6 +46,7 @@ SIGNATURES = {
     "gbta_probe_fp64_peak": (_c_int, [_c_int, _dp]),
     "gbta_probe_tiles": (_c_int, [_c_int, _vp]),
     "gbta_probe_umma": (_c_int, [_c_int, _vp, _vp]),
+    "gbta_probe_tmem_pairs": (_c_int, [_vp]),
     "gbta_probe_latencies": (_c_int, [_vp]),
     "gbta_probe_tensor_rates": (_c_int, [_c_int, _vp]),
     "gbta_last_error": (ctypes.c_char_p, []),

@@ -29,7 +29,7 @@
 namespace gbta {
 
 constexpr size_t BATCH_FACTOR_SMEM = OZF_SMEM > FP64F_SMEM ? OZF_SMEM : FP64F_SMEM;
-constexpr size_t BATCH_SELINV_SMEM = (OZS_SMEM > FP64S_SMEM ? OZS_SMEM : FP64S_SMEM) + 512;   // + alignment
+constexpr size_t BATCH_SELINV_SMEM = OZS_SMEM > FP64S_SMEM ? OZS_SMEM : FP64S_SMEM;
 
 // Ticket k runs task order[k].y of instance order[k].x, with that instance's method.
 __global__ void __launch_bounds__(NT, 1) k_factor_batch(const FactorArgs* __restrict__ inst,
@@ -51,29 +51,19 @@ __global__ void __launch_bounds__(NT, 1) k_factor_batch(const FactorArgs* __rest
 
 __global__ void __launch_bounds__(NT, 1) k_selinv_batch(const SelinvArgs* __restrict__ inst,
                                                         const int2* __restrict__ order, int ntotal, Ctl c) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char raw[];
   __shared__ int s_ok, s_t, s_ready;
   __shared__ OzPipe pipe;
-  __shared__ UmmaState us;
-  unsigned char* raw = smem_align512(smem_raw);
   oz_pipe_init(&pipe);
-  umma_init(&us);
-  umma_zero_planes(reinterpret_cast<__half*>(raw), 2);
   while (true) {
     const int t = cta_ticket(c, &s_t);
     if (t < 0 || t >= ntotal) break;
     const int2 o = order[t];
     const SelinvArgs& p = inst[o.x];
-    bool ok;
-    if (p.method == GBTA_METHOD_OZAKI) {
-      ok = selinv_oz_task(p, o.y, raw, &s_ok, &s_ready, &pipe, &us);
-    } else {
-      ok = selinv_fp64_task(p, o.y, raw, &s_ok);
-      umma_zero_planes(reinterpret_cast<__half*>(raw), 2);   // the FP64 task used the stage buffers
-    }
+    const bool ok = (p.method == GBTA_METHOD_OZAKI) ? selinv_oz_task(p, o.y, raw, &s_ok, &s_ready, &pipe)
+                                                    : selinv_fp64_task(p, o.y, raw, &s_ok);
     if (!ok) break;
   }
-  umma_release(&us);
 }
 
 __global__ void __launch_bounds__(NT, 1) k_solve_batch(const SolveArgs* __restrict__ inst,
@@ -322,13 +312,13 @@ int reset_ticket(gbta_batch* bt) {
   return GBTA_OK;
 }
 
-int grid_of(const gbta_batch* bt, const void* kernel, size_t smem, int ntasks) {
+int grid_of(const gbta_batch* bt, const void* kernel, size_t smem, int ntasks, int tmem_cols = 0) {
   gbta::LaunchCtl lc;
   lc.grid = 1;
   lc.nsm = bt->nsm;
   lc.ctas_per_sm = bt->ctas_per_sm;
   lc.ntasks = ntasks;
-  return gbta::launch_grid(kernel, gbta::NT, smem, lc);
+  return gbta::launch_grid(kernel, gbta::NT, smem, lc, tmem_cols);
 }
 
 int run_async(gbta_batch* bt, int phases, double* logdet_out) {
@@ -510,6 +500,9 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
                                    (int)gbta::BATCH_FACTOR_SMEM));
   CREATE_CUDA(cudaFuncSetAttribute(gbta::k_selinv_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)gbta::BATCH_SELINV_SMEM));
+  // the largest shared-memory carveout, so that two CTAs fit on an SM
+  CREATE_CUDA(cudaFuncSetAttribute(gbta::k_factor_batch, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  CREATE_CUDA(cudaFuncSetAttribute(gbta::k_selinv_batch, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
 #undef CREATE_CUDA
   *out = bt;
   return GBTA_OK;

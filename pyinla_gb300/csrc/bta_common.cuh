@@ -78,7 +78,7 @@ __device__ __forceinline__ void trace_task(const Ctl& c, int ticket, int type, u
   if (c.trace && threadIdx.x == 0) {
     long long* r = c.trace + (long long)TRACE_WORDS * ticket;
     r[0] = ticket;
-    r[1] = ((long long)type << 16) | smid();
+    r[1] = ((long long)blockIdx.x << 32) | ((long long)type << 16) | smid();
     r[2] = (long long)t0;
     r[3] = (long long)gtimer();
   }

@@ -51,6 +51,7 @@ void launch_factor_oz(const Geom& g, double* D, double* L, double* R, double* T,
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_factor_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZF_SMEM);
+    cudaFuncSetAttribute(k_factor_oz, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     attr_set = true;
   }
   launch_row_exponents(g, D, T, use_arrow, erow, lc.stream);

@@ -5,6 +5,7 @@
 // throughput of the whole chip, measured here with independent FMA chains on every SM.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 
 #include "../../include/pyinla_gb300.h"
@@ -16,10 +17,34 @@ std::atomic<long long> g_launches{0};
 
 void count_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
-int launch_grid(const void* kernel, int threads, size_t smem, const LaunchCtl& lc) {
+int resident_ctas(const void* kernel, int threads, size_t smem, int tmem_cols) {
+  cudaFuncAttributes fa;
+  int dev = 0;
+  if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess) return 1;
+  int regs_sm = 0, smem_sm = 0, resv = 0, thr_sm = 0, blk_sm = 0;
+  cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&resv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  cudaDeviceGetAttribute(&thr_sm, cudaDevAttrMaxThreadsPerMultiProcessor, dev);
+  cudaDeviceGetAttribute(&blk_sm, cudaDevAttrMaxBlocksPerMultiprocessor, dev);
+  const long long warps = (threads + 31) / 32;
+  const long long regs_warp = ((long long)fa.numRegs * 32 + 255) / 256 * 256;   // 256-register units
+  const long long smem_cta = (long long)smem + (long long)fa.sharedSizeBytes + resv;
+  long long n = blk_sm;
+  if (regs_warp > 0) n = std::min(n, (long long)regs_sm / (regs_warp * warps));
+  n = std::min(n, (long long)thr_sm / threads);
+  if (smem_cta > 0) n = std::min(n, (long long)smem_sm / smem_cta);
+  if (tmem_cols > 0) n = std::min(n, (long long)(512 / tmem_cols));
+  return n < 1 ? 1 : (int)n;
+}
+
+int launch_grid(const void* kernel, int threads, size_t smem, const LaunchCtl& lc, int tmem_cols) {
   if (lc.nsm <= 0) return lc.grid;
   int occ = 1;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem) != cudaSuccess || occ < 1) occ = 1;
+  if (tmem_cols > 0)
+    occ = resident_ctas(kernel, threads, smem, tmem_cols);
+  else if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem) != cudaSuccess || occ < 1)
+    occ = 1;
   const int per = lc.ctas_per_sm > 0 ? (lc.ctas_per_sm < occ ? lc.ctas_per_sm : occ) : occ;
   long long g = (long long)lc.nsm * per;
   if (lc.ntasks > 0 && g > lc.ntasks) g = lc.ntasks;

@@ -94,23 +94,16 @@ void launch_selinv_oz_prepare(const Geom& g, const double* D, const double* L, c
   count_launches(2);
 }
 
-constexpr size_t OZS_SMEM_LAUNCH = OZS_SMEM + 512;   // + alignment of the stage buffers
-
 __global__ void __launch_bounds__(NT, 1) k_selinv_oz(SelinvArgs p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_ok, s_t, s_ready;
   __shared__ OzPipe pipe;
-  __shared__ UmmaState us;
-  unsigned char* raw = smem_align512(smem_raw);
   oz_pipe_init(&pipe);
-  umma_init(&us);
-  umma_zero_planes(reinterpret_cast<__half*>(raw), 2);
   while (true) {
     const int t = cta_ticket(p.c, &s_t);
     if (t < 0 || t >= p.ntasks) break;
-    if (!selinv_oz_task(p, t, raw, &s_ok, &s_ready, &pipe, &us)) break;
+    if (!selinv_oz_task(p, t, smem_raw, &s_ok, &s_ready, &pipe)) break;
   }
-  umma_release(&us);
 }
 
 size_t selinv_oz_digit_bytes(const Geom& g) { return (size_t)g.nflags() * OZ_TILE * sizeof(__half); }
@@ -120,7 +113,9 @@ void launch_selinv_oz(const Geom& g, const double* D, const double* L, const dou
                       int* ecol, const double* cinv, __half* sdig, const LaunchCtl& lc) {
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_selinv_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZS_SMEM_LAUNCH);
+    cudaFuncSetAttribute(k_selinv_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZS_SMEM);
+    // the largest shared-memory carveout, so that two CTAs fit on an SM
+    cudaFuncSetAttribute(k_selinv_oz, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     attr_set = true;
   }
   launch_selinv_oz_prepare(g, D, L, R, use_arrow, fdig, ecol, lc.stream);
@@ -147,7 +142,7 @@ void launch_selinv_oz(const Geom& g, const double* D, const double* L, const dou
   p.c.epoch = lc.epoch;
   p.c.wait_ns = lc.wait_ns;
   p.c.trace = lc.trace;
-  k_selinv_oz<<<launch_grid((const void*)k_selinv_oz, NT, OZS_SMEM_LAUNCH, lc), NT, OZS_SMEM_LAUNCH, lc.stream>>>(p);
+  k_selinv_oz<<<launch_grid((const void*)k_selinv_oz, NT, OZS_SMEM, lc), NT, OZS_SMEM, lc.stream>>>(p);
   count_launches(1);
 }
 

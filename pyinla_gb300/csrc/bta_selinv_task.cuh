@@ -24,19 +24,18 @@
 //
 // Two ways to compute the product loops (SelinvArgs::method):
 //  * FP64: FP64 FMAs on staged FP64 tiles (selinv_fp64_task);
-//  * OZAKI: digit-plane products on the tcgen05 tensor cores with accumulators in
-//    tensor memory (selinv_oz_task; bta_ozaki.cuh, bta_umma.cuh): the right operand
-//    F(l,c) is fixed during the inversion, so every factor tile is sliced once
-//    (k_fac_digits_t) relative to per-column exponents (k_fac_col_exponents: max over
-//    the column's pattern) and stored transposed (K-major); every Sigma tile is
-//    sliced once, by the task that produces it, against its own exponent (a multiple
-//    of 7), and its consumers read those planes shifted to the task's running
-//    exponent E (the largest tile exponent seen so far in the task); when a tile
-//    raises E, the exact partial sums are first folded into FP64 with the old E.
-//    Tile inverses and triangular solves stay in FP64.
+//  * OZAKI: tensor-core digit-plane products (selinv_oz_task, see bta_ozaki.cuh):
+//    the right operand F(l,c) is fixed during the inversion, so every factor tile is
+//    sliced once (k_fac_digits_t) relative to per-column exponents
+//    (k_fac_col_exponents: max over the column's pattern) and stored transposed for
+//    the ldmatrix layout; every Sigma tile is sliced once, by the task that produces
+//    it, against its own exponent (a multiple of 7), and its consumers stage those
+//    planes shifted to the task's running exponent E (the largest tile exponent seen
+//    so far in the task); when a tile raises E, the exact partial sums are first
+//    folded into FP64 with the old E.  Tile inverses and triangular solves stay in FP64.
 #pragma once
 
-#include "bta_umma.cuh"
+#include "bta_ozaki.cuh"
 
 namespace gbta {
 
@@ -360,18 +359,15 @@ static __device__ __forceinline__ int sig_shift(int E, int En) {
   return q < OZ_S ? q : OZ_S;
 }
 
-// OZS_STAGE: halves per stage (left planes, zero planes, right planes, zero plane; see
-// bta_umma.cuh).  X and F follow the two stages; W (used only by the tip task, when no
-// stage is in flight) reuses the left planes of the first stage; the fold scratch of
-// the product loops reuses X and F.  The caller aligns `raw` to 512 bytes.
-constexpr int OZS_STAGE = UMMA_STAGE_PLANES * OZ_PLANE;
+// OZS_STAGE: halves per stage (A, B digit planes).  X and F follow the two stages; W
+// (used only by the tip task, when no stage is in flight) reuses the first stage.
+constexpr int OZS_STAGE = 2 * OZ_OPER;
 // Step descriptors of a task's product loop, computed once per task (larger loops
 // compute the rest on the fly): left tile slot << 1 | transposed, right tile slot.
 constexpr int OZS_DESC = 512;
 constexpr size_t OZS_SMEM = 2 * OZS_STAGE * sizeof(__half) + 2 * TILE_SMEM * sizeof(double) + TS * sizeof(double) +
                             TS * sizeof(int) + 4 * sizeof(double) + (SCAN_RING + 2) * sizeof(int) +
                             OZS_DESC * sizeof(int2);
-static_assert(2 * TILE_SMEM * sizeof(double) >= OZ_ND * 8 * 32 * sizeof(float), "fold scratch fits in X and F");
 
 // Task t of a tensor-core selected-inversion instance.  `raw` is OZS_SMEM bytes of
 // (16-byte aligned) shared memory.  Returns false when the launch is aborted.
@@ -382,12 +378,11 @@ static_assert(2 * TILE_SMEM * sizeof(double) >= OZ_ND * 8 * 32 * sizeof(float), 
 // largest E_t so far) and stages each left tile shifted down by (E - E_t) / 7 planes;
 // a tile that raises E first folds the exact partial sums with the old E.
 static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t, unsigned char* raw, int* s_okp,
-                                                      int* s_readyp, OzPipe* pp, UmmaState* us) {
+                                                      int* s_readyp, OzPipe* pp) {
   __half* stages = reinterpret_cast<__half*>(raw);
   double* X = reinterpret_cast<double*>(raw + 2 * OZS_STAGE * sizeof(__half));
   double* F = X + TILE_SMEM;
   double* W = reinterpret_cast<double*>(raw);   // aliases stage 0 (free in the tip task)
-  float* xch = reinterpret_cast<float*>(X);       // fold scratch (X, F are free in the loop)
   double* rd = F + TILE_SMEM;
   int* ecol_t = reinterpret_cast<int*>(rd + TS);
   double* red4 = reinterpret_cast<double*>(ecol_t + TS);
@@ -416,7 +411,6 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       tile_store(p.ST, g.a, g.a, g.a, X);
       const int code = sig_store_digits(p, g.fT(), X, g.a, g.a, red4);
       cta_publish_val(c, c.flags + g.fT(), code);
-      fence_async_smem();   // W (stage 0) is refilled by bulk copies later
       trace_task(c, t, type, t_task0);
       return true;
     }
@@ -427,16 +421,20 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       ecol_t[threadIdx.x] = cc < g.b ? p.ecol[(size_t)i * g.b + cc] : 0;
     }
     __syncthreads();
-    double v[8];   // elements (umma_row(e), umma_col()) of the FP64 accumulator
+    OzAcc acc;
+    oz_clear_partials(acc);
 #pragma unroll
-    for (int e = 0; e < 8; ++e) v[e] = 0.0;
+    for (int n = 0; n < 2; ++n)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc.v[n][q] = 0.0;
     int E = NO_EXP;   // running exponent of the left operand (unset)
-    int esum = 0;
-    auto set_esum = [&]() { esum = E + ecol_t[umma_col()]; };
-    unsigned written = 0;        // accumulator groups written since the last fold
-    unsigned fresh = 7;          // thread 0: groups whose next MMA starts a new sum
-    int qs[2] = {0, 0};          // plane shift and orientation of the left tile per stage
-    bool trs[2] = {false, false};
+    int esum[2][4];
+    auto set_esum = [&]() {
+#pragma unroll
+      for (int n = 0; n < 2; ++n)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) esum[n][q] = E + ecol_t[oz_col(n, q)];
+    };
     // step s: left tile (Sigma digits, its flag slot and orientation) and right tile
     // (G digits), as a descriptor (left slot << 1 | transposed, right slot)
     auto compute_desc = [&](int s) -> int2 {
@@ -464,37 +462,21 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       return st_;
     };
     auto right_of = [&](int s) -> const __half* { return p.fdig + (size_t)desc_of(s).y * OZ_TILE; };
-    // stage step s's operands into stage buffer st, the left tile to be read shifted by
-    // q planes: bulk copies of its leading OZ_S - q planes and of the right tile, once
-    // the MMAs that read the buffer two steps earlier have finished
+    // stage step s's operands into stage buffer st with the left tile shifted by q
+    // planes: bulk copies of its leading OZ_S - q planes and of the right tile, the
+    // q planes below the shift zeroed by the CTA
     unsigned ph = pp->phase;
     auto stage = [&](int st, const SigTile& lt, int q, int s) {
       __half* dst = stages + st * OZS_STAGE;
       const int slot = (int)(lt.flag - c.flags);
       const unsigned abytes = q < OZ_S ? (unsigned)((OZ_S - q) * OZ_PLANE * sizeof(__half)) : 0u;
-      qs[st] = q;
-      trs[st] = lt.trans;
       if (threadIdx.x == 0) {
-        if (!umma_drain_stage(us, st)) {
-          atomicCAS(c.ctrl + CTRL_ERR, ERR_NONE, ERR_TIMEOUT);
-          raise_abort(c);
-        }
         oz_bulk_expect(pp, st, abytes + (unsigned)(OZ_TILE * sizeof(__half)));
-        if (abytes) oz_bulk_copy(pp, st, dst, p.sdig + (size_t)slot * OZ_TILE, abytes);
-        oz_bulk_copy(pp, st, dst + UMMA_RIGHT_PLANE * OZ_PLANE, right_of(s), (unsigned)(OZ_TILE * sizeof(__half)));
+        if (abytes) oz_bulk_copy(pp, st, dst + q * OZ_PLANE, p.sdig + (size_t)slot * OZ_TILE, abytes);
+        oz_bulk_copy(pp, st, dst + OZ_OPER, right_of(s), (unsigned)(OZ_TILE * sizeof(__half)));
       }
-    };
-    // all threads: make the issued MMAs complete, then fold the accumulators into v
-    auto fold = [&](int st) {
-      if (threadIdx.x == 0 && !umma_drain_stage(us, st)) {
-        atomicCAS(c.ctrl + CTRL_ERR, ERR_NONE, ERR_TIMEOUT);
-        raise_abort(c);
-      }
-      tmem_fence_before();
-      __syncthreads();
-      umma_fold_sub(us, written, esum, v, xch);
-      written = 0;
-      fresh = 7;
+      for (int idx = threadIdx.x; idx < q * (OZ_PLANE / 8); idx += NT)
+        reinterpret_cast<uint4*>(dst)[idx] = make_uint4(0u, 0u, 0u, 0u);
     };
     // wait for stage st; a copy that never lands aborts the launch
     auto stage_wait = [&](int st) -> bool {
@@ -524,6 +506,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       SigTile lt = left_of(0);
       ok = cta_wait_val(c, lt.flag, &s_ok, s_val);
       trace_mark(c, t, 0);
+      bool tcur = lt.trans;
       if (ok) {
         if (threadIdx.x == 0) s_ready = 1;
         E = sig_exp_decode(*s_val, c.epoch);
@@ -550,8 +533,10 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
             have = true;
           }
         }
-        if (threadIdx.x == 0) umma_oz_step(us, s & 1, cur, qs[s & 1], trs[s & 1], fresh);
-        written |= umma_groups_written(qs[s & 1]);
+        if (tcur)
+          oz_step_t<true>(acc, cur, cur + OZ_OPER);
+        else
+          oz_step_t<false>(acc, cur, cur + OZ_OPER);
         ++since_fold;
         if (more) {
           if (!have) {
@@ -565,7 +550,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
             En = sig_exp_decode(*s_val, c.epoch);
           }
           if ((En > E && En != NO_EXP) || since_fold == OZ_CHUNK) {
-            if (E > NO_EXP) fold(s & 1);
+            if (E > NO_EXP) oz_fold_sub(acc, esum);
             since_fold = 0;
             if (En > E && En != NO_EXP) {
               E = En;
@@ -573,8 +558,9 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
             }
           }
           if (!have) stage(nst, nt_, sig_shift(E, En), s + 1);
+          tcur = nt_.trans;
         } else if (E > NO_EXP) {
-          fold(s & 1);   // v = -(sum)
+          oz_fold_sub(acc, esum);   // acc.v = -(sum)
         }
       }
     }
@@ -583,9 +569,11 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
     trace_put(c, t, 2, (long long)waited);
     trace_put(c, t, 3, np);
     __syncthreads();
-    // v = -(sum of the products): ST_OFF: Sigma(j,col); ST_DIAG: -Z
+    // acc.v = -(sum of the products): ST_OFF: Sigma(j,col); ST_DIAG: -Z
 #pragma unroll
-    for (int e = 0; e < 8; ++e) X[umma_row(e) * LDS + umma_col()] = v[e];
+    for (int n = 0; n < 2; ++n)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) X[oz_row(n, q) * LDS + oz_col(n, q)] = acc.v[n][q];
     if (type == ST_OFF) {
       __syncthreads();
       const SigTile d = sig_dest(p, i, j, col);

@@ -1,60 +1,60 @@
 // Digit-plane products on the 5th-generation tensor cores (tcgen05.mma, kind::f16,
 // fp32 accumulators in tensor memory).
 //
-// One tile step adds P_d(m, n) = sum_{s+t=d} sum_k X_s(m, k) Y_t(n, k) (d = 0 .. 8, the
+// One tile step adds the pair products P_st(m, n) = sum_k X_s(m, k) Y_t(n, k) of the
 // 43 pairs s + t <= 8 of the digit planes X_s of the left tile and Y_t of the right
-// tile) to nine fp32 accumulators, as 32 x 32 x 32 integer products (see
-// bta_ozaki.cuh for the digit scheme and why fp32 accumulation is exact).
+// tile (32 x 32 x 32 integer products; bta_ozaki.cuh has the digit scheme) to fp32
+// accumulators that a fold later combines per diagonal d = s + t.
 //
-// The diagonal sums are formed by the tensor core itself.  For a group of four
-// consecutive diagonals d0 .. d0+3 and one left plane s, the A operand (M = 128 rows)
-// is the right tile's planes t = d0 - s .. d0 - s + 3 stacked (row 32 j + n = row n of
-// plane d0 + j - s), and the B operand (N = 32) is the left plane s: accumulator row
-// 32 j + n, column m then collects P_{d0+j}(m, n) over s.  The planes of a tile are
-// contiguous 2 KB blocks, so the stacked operand is one shared-memory descriptor whose
-// start moves by one plane per s; zero planes before and after the right tile supply
-// t < 0 and t = 8.  Three groups cover the nine diagonals: {0} (s = 0), {1..4}
-// (s = 0..4) and {5..8} (s = 0..7): 14 left planes x 2 K-halves = 28 MMAs of
-// 128 x 32 x 16 per tile step, 96 accumulator columns.
+// An MMA of 128 x N x 16 costs about the same for every N up to 128 and reaches the
+// tensor core's rate only near N = 256, so the pairs are grouped into wide MMAs.  The
+// A operand (M = 128) stacks four right planes (row 32 j + n = row n of plane t0 + j),
+// the B operand stacks left planes along N (column 32 i + m), and the accumulator
+// cell (lane block j, column block i) collects the pairs with s + t = i + j:
+//   * right planes 0..3 x left planes 0..7 (N = 256): pair (s, t) into cell (t, s);
+//   * right planes 4..7 x left planes 0..3 (N = 128, columns 128..255): pair (s, t)
+//     into cell (t - 4, s + 4);
+//   * the remaining pair (4, 4) runs on mma.sync (oz_pair44) into registers.
+// Two K-halves each: 4 MMAs, 256 accumulator columns (two CTAs per SM fit in tensor
+// memory), 48 pairs computed of which 42 are kept (the fold skips cells with
+// i + j > 8).  A cell holds at most two pairs, so UMMA_CHUNK steps keep every cell,
+// and the (4, 4) sums, below 2^24: fp32 accumulation stays exact.
 //
-// A left tile in the frame of a larger exponent is shifted down by q planes (its
-// plane s is global plane s - q): the shift only skips the MMAs with s < q and moves
-// the B descriptor, no data is moved.  A transposed left tile (stored [k][m]) is read
-// as an MN-major operand.
+// A left tile in the frame of a larger exponent is staged shifted down by q planes
+// (global plane s - q in plane s, zeros below).  A transposed left tile (stored
+// [k][m]) is read as an MN-major operand.
 //
 // Layouts: every plane is 32 rows of 64 bytes with the 16-byte chunks of row r
 // permuted by (r >> 1) & 3 (oz_swz), which is the 64-byte swizzle of the tensor core
-// when the plane starts on a 512-byte boundary.
+// when the plane starts on a 512-byte boundary.  A stage buffer holds the left tile's
+// planes followed by the right tile's.
 #pragma once
 
 #include "bta_ozaki.cuh"
 
 namespace gbta {
 
-constexpr int UMMA_TMEM_COLS = 128;   // accumulator columns allocated per CTA (96 used)
-constexpr int UMMA_GROUPS = 3;
-constexpr int UMMA_ZLEAD = 3;         // zero planes before the right tile
-// Planes of one stage buffer: left tile (8), zero planes (3), right tile (8), zero (1).
-constexpr int UMMA_STAGE_PLANES = OZ_S + UMMA_ZLEAD + OZ_S + 1;
-constexpr int UMMA_RIGHT_PLANE = OZ_S + UMMA_ZLEAD;
+constexpr int UMMA_TMEM_COLS = 256;   // accumulator columns per CTA
+constexpr int UMMA_CHUNK = 48;        // tile steps per exact fp32 accumulation
+constexpr int UMMA_NSTAGE = 3;        // stage buffers of a product loop
+constexpr int UMMA_RIGHT_PLANE = OZ_S;
+constexpr int UMMA_ISSUER = 32;       // the thread that issues, commits and awaits the MMAs
+constexpr int UMMA_STAGE_PLANES = 2 * OZ_S;
+static_assert(2 * TS * 64 * 64 * UMMA_CHUNK < (1 << 24), "accumulator cells must stay below 2^24");
+static_assert(8ll * 64 * 64 * TS * UMMA_CHUNK < (1ll << 31), "diagonal sums must fit in 32 bits");
 
-__device__ __forceinline__ int umma_group_d0(int gi) { return gi == 0 ? 0 : (gi == 1 ? 1 : 5); }
-__device__ __forceinline__ int umma_group_smax(int gi) { return gi == 0 ? 0 : (gi == 1 ? 4 : 7); }
-// Accumulator groups written by a step whose left tile is shifted by q planes.
-__device__ __forceinline__ unsigned umma_groups_written(int q) {
-  return (q == 0 ? 1u : 0u) | (q <= 4 ? 2u : 0u) | (q <= 7 ? 4u : 0u);
-}
-
-// Shared-memory matrix descriptor: 64-byte swizzle, 8-row groups 512 bytes apart (both
-// offset fields; only one is used for the K-major and MN-major 32-wide operands here).
-__device__ __forceinline__ unsigned long long umma_sdesc(unsigned saddr) {
-  return (unsigned long long)((saddr >> 4) & 0x3fffu) | ((unsigned long long)(512 >> 4) << 16) |
-         ((unsigned long long)(512 >> 4) << 32) | (1ull << 46) | (4ull << 61);
+// Shared-memory matrix descriptor, 64-byte swizzle: lbo / sbo are the byte offsets of
+// the leading / stride dimension (for a K-major operand the 8-row groups are sbo
+// apart; for an MN-major one the 32-element column blocks are lbo apart and the
+// 8-row K groups sbo apart).
+__device__ __forceinline__ unsigned long long umma_sdesc(unsigned saddr, unsigned lbo = 512, unsigned sbo = 512) {
+  return (unsigned long long)((saddr >> 4) & 0x3fffu) | ((unsigned long long)((lbo >> 4) & 0x3fffu) << 16) |
+         ((unsigned long long)((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46) | (4ull << 61);
 }
 // Instruction descriptor: fp32 accumulator, fp16 A and B, A K-major, B K-major or
-// MN-major, N = 32, M = 128.
-__device__ __forceinline__ unsigned umma_idesc(bool b_mn_major) {
-  return (1u << 4) | ((b_mn_major ? 1u : 0u) << 16) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+// MN-major, M = 128, N = n (a multiple of 16 up to 256).
+__device__ __forceinline__ unsigned umma_idesc(bool b_mn_major, unsigned n = 32) {
+  return (1u << 4) | ((b_mn_major ? 1u : 0u) << 16) | ((n >> 3) << 17) | ((128u >> 4) << 24);
 }
 
 __device__ __forceinline__ void umma_f16(unsigned dtmem, unsigned long long a, unsigned long long b, unsigned idesc,
@@ -74,16 +74,16 @@ __device__ __forceinline__ void tmem_fence_before() { asm volatile("tcgen05.fenc
 __device__ __forceinline__ void tmem_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// Warp-wide: allocate / free UMMA_TMEM_COLS columns (the address goes to *s_addr).
-__device__ __forceinline__ void tmem_alloc(unsigned* s_addr) {
+// Warp-wide: allocate / free ncols columns (a power of two >= 32; the address goes to
+// *s_addr).
+__device__ __forceinline__ void tmem_alloc(unsigned* s_addr, unsigned ncols = UMMA_TMEM_COLS) {
   asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(s_addr)),
-               "n"(UMMA_TMEM_COLS)
+               "r"(ncols)
                : "memory");
   asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 }
-__device__ __forceinline__ void tmem_dealloc(unsigned taddr) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "n"(UMMA_TMEM_COLS)
-               : "memory");
+__device__ __forceinline__ void tmem_dealloc(unsigned taddr, unsigned ncols = UMMA_TMEM_COLS) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
 }
 
 // Warp-wide: 32 consecutive accumulator columns of the warp's 32 lanes.
@@ -133,22 +133,23 @@ __device__ __forceinline__ bool mbar_wait_parity(unsigned long long* bar, unsign
 // address, one MMA-completion barrier per stage buffer, their parities and which of
 // them still has a commit outstanding.
 struct UmmaState {
-  unsigned long long bar[2];
+  unsigned long long bar[UMMA_NSTAGE];
   unsigned tmem;
   unsigned parity;    // bit st: parity of the next completion of bar[st]
   unsigned pending;   // bit st: a commit on bar[st] not yet waited for
 };
 
 // All threads: barriers, accumulator allocation (warp 0).  Contains __syncthreads().
-__device__ __forceinline__ void umma_init(UmmaState* us) {
+__device__ __forceinline__ void umma_init(UmmaState* us, unsigned ncols = UMMA_TMEM_COLS) {
   if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&us->bar[0])) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&us->bar[1])) : "memory");
+    for (int k = 0; k < UMMA_NSTAGE; ++k)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&us->bar[k])) : "memory");
     us->parity = 0;
     us->pending = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (threadIdx.x < 32) tmem_alloc(&us->tmem);
+  __syncwarp();   // the allocation is warp-wide
+  if (threadIdx.x < 32) tmem_alloc(&us->tmem, ncols);
   tmem_fence_before();
   __syncthreads();
   tmem_fence_after();
@@ -165,98 +166,135 @@ __device__ __forceinline__ bool umma_drain_stage(UmmaState* us, int st) {
 
 // All threads, at the end of the kernel: wait for the outstanding MMAs, then free the
 // accumulators (warp 0).  Contains __syncthreads().
-__device__ __forceinline__ void umma_release(UmmaState* us) {
-  if (threadIdx.x == 0) {
-    umma_drain_stage(us, 0);
-    umma_drain_stage(us, 1);
-  }
+__device__ __forceinline__ void umma_release(UmmaState* us, unsigned ncols = UMMA_TMEM_COLS) {
+  __syncthreads();
+  if (threadIdx.x == UMMA_ISSUER)
+    for (int k = 0; k < UMMA_NSTAGE; ++k) umma_drain_stage(us, k);
   tmem_fence_before();
   __syncthreads();
   tmem_fence_after();
-  if (threadIdx.x < 32) tmem_dealloc(us->tmem);
+  __syncwarp();
+  if (threadIdx.x < 32) tmem_dealloc(us->tmem, ncols);
 }
 
-// Thread 0: issue one tile step from stage buffer `stage` (the left tile at plane 0,
-// the right tile at UMMA_RIGHT_PLANE, zero planes around it; 512-byte aligned) and
-// commit it to bar[st].  q: plane shift of the left tile (>= OZ_S: nothing to add);
-// trans: the left planes are stored [k][m]; fresh: groups whose next MMA starts a new
-// sum (cleared here for the groups written).
-__device__ __forceinline__ void umma_oz_step(UmmaState* us, int st, const __half* stage, int q, bool trans,
-                                             unsigned& fresh) {
-  const unsigned lbase = smem_u32(stage), rbase = lbase + UMMA_RIGHT_PLANE * OZ_PLANE * 2;
-  const unsigned idesc = umma_idesc(trans);
+// Thread 0: issue one tile step from stage buffer `stage` (layout above, 512-byte
+// aligned) and commit it to bar[st].  trans: the left planes are stored [k][m]
+// (MN-major: 32-column blocks one plane apart, 8-row K groups 512 bytes apart; with
+// mn_swap the two offsets trade descriptor fields); fresh: the accumulators start a
+// new sum (cleared here).
+__device__ __forceinline__ void umma_oz_step(UmmaState* us, int st, const __half* stage, bool trans, bool& fresh,
+                                             bool mn_swap = false) {
+  constexpr unsigned PB = OZ_PLANE * 2;   // bytes per plane
+  const unsigned base = smem_u32(stage), rbase = base + UMMA_RIGHT_PLANE * PB;
+  const unsigned lbo = trans ? (mn_swap ? 512u : PB) : 512u, sbo = trans ? (mn_swap ? PB : 512u) : 512u;
   tmem_fence_after();
 #pragma unroll
-  for (int gi = 0; gi < UMMA_GROUPS; ++gi) {
-    const int d0 = umma_group_d0(gi), smax = umma_group_smax(gi);
-    const unsigned dt = us->tmem + (unsigned)(gi * 32);
-    for (int s = q; s <= smax; ++s) {
-      const unsigned a0 = rbase + (unsigned)((d0 - s) * OZ_PLANE * 2);
-      const unsigned b0 = lbase + (unsigned)((s - q) * OZ_PLANE * 2);
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const unsigned acc = ((fresh >> gi) & 1u) ? 0u : 1u;
-        umma_f16(dt, umma_sdesc(a0 + h * 32), umma_sdesc(b0 + (trans ? h * 1024 : h * 32)), idesc, acc);
-        fresh &= ~(1u << gi);
-      }
-    }
+  for (int h = 0; h < 2; ++h) {
+    const unsigned ka = h * 32, kb = trans ? h * 1024 : h * 32;
+    umma_f16(us->tmem, umma_sdesc(rbase + ka), umma_sdesc(base + kb, lbo, sbo), umma_idesc(trans, 256),
+             (fresh && h == 0) ? 0u : 1u);
   }
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const unsigned ka = h * 32, kb = trans ? h * 1024 : h * 32;
+    umma_f16(us->tmem + 128, umma_sdesc(rbase + 4 * PB + ka), umma_sdesc(base + kb, lbo, sbo),
+             umma_idesc(trans, 128), 1u);
+  }
+  fresh = false;
   umma_commit(&us->bar[st]);
   us->pending |= 1u << st;
 }
 
 // Output element ownership of the folded accumulator: thread (warp w, lane n) holds
-// elements (m = 8 w + e, n), e = 0 .. 7.
-__device__ __forceinline__ int umma_row(int e) { return 8 * (threadIdx.x >> 5) + e; }
+// elements (m, n) with m = 8 r + 2 w + k, e = 2 r + k (r = 0..3, k = 0..1).
+__device__ __forceinline__ int umma_row(int e) { return 8 * (e >> 1) + 2 * (threadIdx.x >> 5) + (e & 1); }
 __device__ __forceinline__ int umma_col() { return threadIdx.x & 31; }
 
+// All threads: the pair (4, 4) of one tile step, c += X_4 Y_4^T, on mma.sync (warp w:
+// the 16 x 16 block at rows (w/2)*16, columns (w%2)*16; mma C layout, see oz_row /
+// oz_col).  The left plane is read transposed when trans (stored [k][m]).
+__device__ __forceinline__ void oz_pair44(float (&c)[2][4], const __half* stage, bool trans) {
+  __syncwarp();   // ldmatrix and mma.sync need the whole warp (a lane may come from single-thread work)
+  const __half* As = stage + 4 * OZ_PLANE;
+  const __half* Bs = stage + (UMMA_RIGHT_PLANE + 4) * OZ_PLANE;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int m0 = (w >> 1) * 16, n0 = (w & 1) * 16;
+  const int ar = m0 + (lane & 7) + ((lane >> 3) & 1) * 8, ac = (lane >> 4) * 8;
+  const int tr = (lane >> 4) * 8 + (lane & 7), tc = m0 + ((lane >> 3) & 1) * 8;
+  const int br = n0 + (lane & 7) + (lane >> 4) * 8, bc = ((lane >> 3) & 1) * 8;
+#pragma unroll
+  for (int kk = 0; kk < TS; kk += 16) {
+    unsigned a[4], b[4];
+    if (trans)
+      ldsm_x4_trans(a, As + oz_swz(kk + tr, tc));
+    else
+      ldsm_x4(a, As + oz_swz(ar, kk + ac));
+    ldsm_x4(b, Bs + oz_swz(br, kk + bc));
+    mma16816(c[0], a, b[0], b[1]);
+    mma16816(c[1], a, b[2], b[3]);
+  }
+}
+
 // All threads: v[e] -= sum_d P_d(m, n) 2^(esum - 12 - 7 d) for the thread's elements,
-// from the accumulator groups in `written` (the others count as zero).  The caller
-// has made the last step's MMAs complete (bar wait by thread 0, then a barrier) and
-// passes xch: 9 KB of shared scratch.  Contains __syncthreads().
-__device__ __forceinline__ void umma_fold_sub(const UmmaState* us, unsigned written, int esum, double (&v)[8],
-                                              float* xch) {
+// from the accumulator cells and the (4, 4) sums p44 (cleared here).  The caller has
+// made the last step's MMAs complete (bar wait by thread 0, then a barrier) and passes
+// xch (32 KB) and x44 (4 KB) of shared scratch that no copy is filling.  Warp w reads
+// lane block w, where cell (w, i) of element (m, n) holds diagonal w + i.  Round r
+// covers the columns m = 8 r .. 8 r + 7: every warp stores its raw cells of those
+// columns, and each element's owner adds the cells of each diagonal as integers,
+// combines the nine diagonals exactly into two 64-bit words (diagonals 0..3 and 4..8,
+// as the mma.sync fold does) and folds them into FP64.  Contains __syncthreads().
+__device__ __forceinline__ void umma_fold_sub(const UmmaState* us, int esum, double (&v)[8], float (&p44)[2][4],
+                                              float* xch, float* x44) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned tl = us->tmem + ((unsigned)(32 * w) << 16);
+  const double sc = __longlong_as_double((long long)(1023 + esum - 33) << 52);
+  __syncwarp();
+#pragma unroll
+  for (int n = 0; n < 2; ++n)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      x44[oz_row(n, j) * TS + oz_col(n, j)] = p44[n][j];
+      p44[n][j] = 0.f;
+    }
   tmem_fence_after();
-  // rounds r: elements m = 8 r .. 8 r + 7 (accumulator columns) go to warp r through
-  // xch[d][e][n]
 #pragma unroll 1
   for (int r = 0; r < 4; ++r) {
-    float pv[8];
-    if (w == 0 && (written & 1u)) {
-      tmem_ld8(tl + 8 * r, pv);
+    // columns 32 i + 8 r + e, i = 0..7, into xch[w][i][e][lane]
+    unsigned cv[8][8];
 #pragma unroll
-      for (int e = 0; e < 8; ++e) xch[(0 * 8 + e) * 32 + lane] = pv[e];
-    }
-    if (written & 2u) {
-      tmem_ld8(tl + 32 + 8 * r, pv);
-#pragma unroll
-      for (int e = 0; e < 8; ++e) xch[((1 + w) * 8 + e) * 32 + lane] = pv[e];
-    }
-    if (written & 4u) {
-      tmem_ld8(tl + 64 + 8 * r, pv);
-#pragma unroll
-      for (int e = 0; e < 8; ++e) xch[((5 + w) * 8 + e) * 32 + lane] = pv[e];
-    }
+    for (int i = 0; i < 8; ++i)
+      asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                   : "=r"(cv[i][0]), "=r"(cv[i][1]), "=r"(cv[i][2]), "=r"(cv[i][3]), "=r"(cv[i][4]), "=r"(cv[i][5]),
+                     "=r"(cv[i][6]), "=r"(cv[i][7])
+                   : "r"(tl + 32 * i + 8 * r)
+                   : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
     if (r == 3) tmem_fence_before();
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int e = 0; e < 8; ++e) xch[((w * 8 + i) * 8 + e) * 32 + lane] = __uint_as_float(cv[i][e]);
     __syncthreads();
-    if (w == r) {
 #pragma unroll
-      for (int e = 0; e < 8; ++e) {
-        int I[OZ_ND];
+    for (int k = 0; k < 2; ++k) {
+      const int e = 2 * w + k;   // column 8 r + e
+      int I[OZ_ND];
 #pragma unroll
-        for (int d = 0; d < OZ_ND; ++d) {
-          const unsigned gbit = d == 0 ? 1u : (d <= 4 ? 2u : 4u);
-          I[d] = (written & gbit) ? __float2int_rn(xch[(d * 8 + e) * 32 + lane]) : 0;
-        }
-        const long long hi = (((long long)I[0] * 128 + I[1]) * 128 + I[2]) * 128 + I[3];
-        const long long lo = ((((long long)I[4] * 128 + I[5]) * 128 + I[6]) * 128 + I[7]) * 128 + I[8];
-        const double vv = fma((double)lo, 0x1p-35, (double)hi);
-        const double sc = __longlong_as_double((long long)(1023 + esum - 33) << 52);
-        v[e] = fma(-vv, sc, v[e]);
-      }
+      for (int d = 0; d < OZ_ND; ++d) I[d] = 0;
+#pragma unroll
+      for (int ww = 0; ww < 4; ++ww)
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+          if (ww + i < OZ_ND) I[ww + i] += __float2int_rn(xch[((ww * 8 + i) * 8 + e) * 32 + lane]);
+      I[8] += __float2int_rn(x44[(8 * r + e) * TS + lane]);
+      const long long hi = (((long long)I[0] * 128 + I[1]) * 128 + I[2]) * 128 + I[3];
+      const long long lo = ((((long long)I[4] * 128 + I[5]) * 128 + I[6]) * 128 + I[7]) * 128 + I[8];
+      const double vv = fma((double)lo, 0x1p-35, (double)hi);
+      double& acc = r == 0 ? v[k] : (r == 1 ? v[2 + k] : (r == 2 ? v[4 + k] : v[6 + k]));
+      acc = fma(-vv, sc, acc);
     }
+    if (r == 3) fence_async_smem();   // xch, x44 lie in stage buffers that bulk copies refill
     __syncthreads();
   }
 }
@@ -265,21 +303,6 @@ __device__ __forceinline__ void umma_fold_sub(const UmmaState* us, unsigned writ
 // (the launch adds 512 bytes).
 __device__ __forceinline__ unsigned char* smem_align512(unsigned char* p) {
   return p + ((512u - (smem_u32(p) & 511u)) & 511u);
-}
-
-// All threads: zero the zero planes of `nstages` stage buffers of UMMA_STAGE_PLANES
-// planes each, visible to the tensor core.  Contains __syncthreads().
-__device__ __forceinline__ void umma_zero_planes(__half* stages, int nstages) {
-  constexpr int PER_PLANE = OZ_PLANE / 8;   // uint4 per plane
-  constexpr int NZ = UMMA_ZLEAD + 1;
-  for (int idx = threadIdx.x; idx < nstages * NZ * PER_PLANE; idx += NT) {
-    const int st = idx / (NZ * PER_PLANE), z = (idx / PER_PLANE) % NZ, k = idx % PER_PLANE;
-    const int plane = z < UMMA_ZLEAD ? OZ_S + z : UMMA_STAGE_PLANES - 1;
-    reinterpret_cast<uint4*>(stages + ((size_t)st * UMMA_STAGE_PLANES + plane) * OZ_PLANE)[k] =
-        make_uint4(0u, 0u, 0u, 0u);
-  }
-  fence_async_smem();
-  __syncthreads();
 }
 
 }  // namespace gbta

@@ -35,13 +35,14 @@ def tile_cycles(iters: int = 200) -> dict:
 def umma_check(iters: int = 200) -> dict:
     """tcgen05 tile step against the mma.sync tile step (gbta_probe_umma)."""
     lib = _lib.load()
-    mis = np.zeros(9, dtype=np.int32)
-    cyc = np.zeros(2, dtype=np.int64)
+    mis = np.zeros(10, dtype=np.int32)
+    cyc = np.zeros(4, dtype=np.int64)
     _lib.check(lib.gbta_probe_umma(int(iters), mis.ctypes.data, cyc.ctypes.data))
-    names = ["plain_q0", "trans_q0", "plain_q2", "trans_q3", "plain_q5", "trans_q7", "plain_q8", "fold_bits",
-             "two_steps"]
+    names = ["plain_q0", "trans_q0", "plain_q2", "trans_q3", "plain_q5", "trans_q7", "plain_q7",
+             "trans_swapped_offsets", "two_steps_trans", "two_steps_plain"]
     return {"mismatches": {n: int(m) for n, m in zip(names, mis)},
-            "cycles_per_step": {"tcgen05": int(cyc[0]), "mma_sync": int(cyc[1])}}
+            "cycles_per_step": {"tcgen05": int(cyc[0]), "mma_sync": int(cyc[1])},
+            "cycles_tcgen05_issue_one_step": int(cyc[2]), "cycles_fold": int(cyc[3])}
 
 
 def primitive_cycles() -> dict:
