@@ -14,7 +14,8 @@
 // leaving only  y_g = u - M y_neighbour  (one 32 x 32 matrix-vector product spread
 // over the whole CTA) between the neighbour's publication and its own.  The forward
 // sweep also leaves the arrow contribution R_i(:,r) y(i,r) of each tile in a partial
-// buffer that the arrow task sums in a fixed order.
+// buffer, after publishing the tile and under a flag of its own (off the chain), and
+// the arrow task sums the partials in a fixed order.
 #pragma once
 
 #include "bta_common.cuh"
@@ -40,6 +41,8 @@ struct SolveArgs {
 };
 
 static __device__ __forceinline__ int vflag(const Geom& g, int i, int r) { return i * g.B + r; }
+// Flag of the forward sweep's arrow partial of tile gi (published after the tile).
+static __device__ __forceinline__ int pflag(const Geom& g, int gi) { return g.nt * g.B + 1 + gi; }
 
 // Vectors are TS x NC, stored [row][col] in shared memory (V[row*NC + col]).
 // res[q] = sum_m M[row][m] v[m][q] for q < nc, with M[row][m] = Ms[row*LDS + m]
@@ -130,7 +133,7 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
       if (fwd) {
         bool ok = true;
         for (int k = 0; k < ntile; ++k) {
-          if (!(ok = cta_wait(c, c.flags + k, nullptr, &s_ok))) break;
+          if (!(ok = cta_wait(c, c.flags + pflag(g, k), nullptr, &s_ok))) break;
           s -= __ldcg(p.part + (size_t)k * TS * NC + threadIdx.x);
         }
         if (!ok) return false;
@@ -303,8 +306,10 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
         if (q < p.nc && row < rows) p.B[(size_t)(row0 + row) * p.ldb + q] = u[q];
       }
     }
+    cta_publish(c, c.flags + vflag(g, i, r));   // the next tile's wait ends here
     if (fwd && p.use_arrow) {
-      // arrow partial R_i(:, r) y(i, r) (rows >= a of the staged tile are zero)
+      // arrow partial R_i(:, r) y(i, r) (rows >= a of the staged tile are zero), off
+      // the chain, under its own flag
       tile_load(Ts, make_tile(p.R + i * ab, g.b, 0, r * TS, g.a, g.b));
       __syncthreads();
       double res[NC];
@@ -313,8 +318,8 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
         const int row = threadIdx.x >> 2;
         for (int q = 0; q < NC; ++q) p.part[(size_t)gi * TS * NC + row * NC + q] = (q < p.nc) ? res[q] : 0.0;
       }
+      cta_publish(c, c.flags + pflag(g, gi));
     }
-    cta_publish(c, c.flags + vflag(g, i, r));
     trace_task(c, t, 0, t_task0);
   }
   return true;
