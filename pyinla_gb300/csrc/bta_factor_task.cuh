@@ -92,18 +92,23 @@ static __device__ bool factor_feed_rows(const FactorArgs& p, int t, int i, int q
   const Tile ft = feeder_tile(p, i, col, slot, grow0);
   const int gc = i * g.B + col, row0 = q * FEED_ROWS;
   trace_clear_marks(c, t);
-  if (!cta_wait(c, p.feed_pre + gc, c.flags + g.fD(i, col, col), s_ok)) return false;
-  trace_mark(c, t, 0);   // products and diagonal factor tile ready
-  {   // the diagonal factor tile and this group's rows: all loads issued before any store
+  const bool digits = p.method == GBTA_METHOD_OZAKI && p.digits;
+  // the group's rows (their products were formed ahead of the diagonal tile) are
+  // loaded while the diagonal tile is awaited
+  if (!cta_wait(c, p.feed_pre + gc, nullptr, s_ok)) return false;
+  constexpr int RPT = FEED_ROWS * TS / NT;
+  double xv[RPT];
+#pragma unroll
+  for (int k = 0; k < RPT; ++k) {
+    const int idx = threadIdx.x + k * NT, rr = row0 + idx / TS, cc = idx % TS;
+    xv[k] = (rr < ft.rows && cc < ft.cols) ? __ldcg(ft.p + (size_t)rr * ft.ld + cc) : 0.0;
+  }
+  if (digits && threadIdx.x < TS) erow_t[threadIdx.x] = threadIdx.x < ft.rows ? p.erow[grow0 + threadIdx.x] : 0;
+  if (!cta_wait(c, c.flags + g.fD(i, col, col), nullptr, s_ok)) return false;
+  trace_mark(c, t, 0);   // diagonal factor tile ready
+  {
     double fv[PER_THREAD];
     tile_ldg(fv, btile(Dblk(p, i), g, col, col));
-    constexpr int RPT = FEED_ROWS * TS / NT;
-    double xv[RPT];
-#pragma unroll
-    for (int k = 0; k < RPT; ++k) {
-      const int idx = threadIdx.x + k * NT, rr = row0 + idx / TS, cc = idx % TS;
-      xv[k] = (rr < ft.rows && cc < ft.cols) ? __ldcg(ft.p + (size_t)rr * ft.ld + cc) : 0.0;
-    }
     tile_sts(F, fv);
 #pragma unroll
     for (int k = 0; k < RPT; ++k) {
@@ -111,8 +116,6 @@ static __device__ bool factor_feed_rows(const FactorArgs& p, int t, int i, int q
       X[(row0 + idx / TS) * LDS + idx % TS] = xv[k];
     }
   }
-  const bool digits = p.method == GBTA_METHOD_OZAKI && p.digits;
-  if (digits && threadIdx.x < TS) erow_t[threadIdx.x] = threadIdx.x < ft.rows ? p.erow[grow0 + threadIdx.x] : 0;
   __syncthreads();
   tile_pad_identity(F, g.vrows(col));
   __syncthreads();
