@@ -312,13 +312,13 @@ int reset_ticket(gbta_batch* bt) {
   return GBTA_OK;
 }
 
-int grid_of(const gbta_batch* bt, const void* kernel, size_t smem, int ntasks, int tmem_cols = 0) {
+int grid_of(const gbta_batch* bt, const void* kernel, size_t smem, int ntasks) {
   gbta::LaunchCtl lc;
   lc.grid = 1;
   lc.nsm = bt->nsm;
   lc.ctas_per_sm = bt->ctas_per_sm;
   lc.ntasks = ntasks;
-  return gbta::launch_grid(kernel, gbta::NT, smem, lc, tmem_cols);
+  return gbta::launch_grid(kernel, gbta::NT, smem, lc);
 }
 
 int run_async(gbta_batch* bt, int phases, double* logdet_out) {

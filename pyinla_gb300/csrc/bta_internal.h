@@ -64,13 +64,12 @@ struct LaunchCtl {
 
 // Persistent grid of a kernel with `threads` threads and `smem` bytes of dynamic
 // shared memory: lc.grid when lc.nsm == 0, else nsm x (ctas_per_sm, capped by the
-// kernel's occupancy; all that fit when 0), at most ntasks.  tmem_cols > 0: the
-// kernel allocates that many tensor-memory columns per CTA, and the occupancy is
-// resident_ctas (the occupancy calculator reports one CTA per SM for every kernel
-// that allocates tensor memory).
-int launch_grid(const void* kernel, int threads, size_t smem, const LaunchCtl& lc, int tmem_cols = 0);
+// kernel's occupancy; all that fit when 0), at most ntasks.
+int launch_grid(const void* kernel, int threads, size_t smem, const LaunchCtl& lc);
 // CTAs per SM that fit a kernel's registers, shared memory and threads, and, with
-// tmem_cols > 0, the SM's 512 tensor-memory columns.
+// tmem_cols > 0, the SM's 512 tensor-memory columns.  This is the occupancy rule for
+// a kernel that allocates tensor memory: the CUDA occupancy calculator reports one
+// CTA per SM for every such kernel, whatever it allocates.
 int resident_ctas(const void* kernel, int threads, size_t smem, int tmem_cols);
 
 // Task lists of the factorization and selected-inversion DAGs (bta_api.cu).

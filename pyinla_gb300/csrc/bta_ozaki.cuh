@@ -185,7 +185,7 @@ __device__ __forceinline__ void oz_load_async(__half* sdst, const __half* gsrc) 
 // signal one mbarrier per stage buffer.  OzPipe is the per-CTA state: the two
 // barriers and the parity of the next completion of each (kept across tasks).
 struct OzPipe {
-  unsigned long long bar[3];
+  unsigned long long bar[2];
   unsigned phase;   // bit st: parity of the next completion of stage st
 };
 
@@ -193,7 +193,6 @@ __device__ __forceinline__ void oz_pipe_init(OzPipe* pp) {
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&pp->bar[0])) : "memory");
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&pp->bar[1])) : "memory");
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&pp->bar[2])) : "memory");
     pp->phase = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }

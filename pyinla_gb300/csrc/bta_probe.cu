@@ -38,13 +38,10 @@ int resident_ctas(const void* kernel, int threads, size_t smem, int tmem_cols) {
   return n < 1 ? 1 : (int)n;
 }
 
-int launch_grid(const void* kernel, int threads, size_t smem, const LaunchCtl& lc, int tmem_cols) {
+int launch_grid(const void* kernel, int threads, size_t smem, const LaunchCtl& lc) {
   if (lc.nsm <= 0) return lc.grid;
   int occ = 1;
-  if (tmem_cols > 0)
-    occ = resident_ctas(kernel, threads, smem, tmem_cols);
-  else if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem) != cudaSuccess || occ < 1)
-    occ = 1;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, smem) != cudaSuccess || occ < 1) occ = 1;
   const int per = lc.ctas_per_sm > 0 ? (lc.ctas_per_sm < occ ? lc.ctas_per_sm : occ) : occ;
   long long g = (long long)lc.nsm * per;
   if (lc.ntasks > 0 && g > lc.ntasks) g = lc.ntasks;
