@@ -287,9 +287,11 @@ __device__ __forceinline__ void oz_clear_partials(OzAcc& a) {
       for (int j = 0; j < 4; ++j) a.p[d][n][j] = 0.f;
 }
 
-// One tile step: p[s+t] += d_s(A) * d_t(B)^T for the 43 pairs s + t <= 8.  The A
+// One tile step: p[s+t] += d_s(A) * d_t(B)^T for the 43 pairs s + t <= 8, or only for
+// s >= S0 when the A planes below S0 are known to be zero (a left tile staged S0 or
+// more planes down): neither their loads nor their products are issued.  The A
 // planes hold A(m, k) at [m][k], or, with TA, at [k][m] (read with ldmatrix.trans).
-template <bool TA>
+template <bool TA, int S0 = 0>
 __device__ __forceinline__ void oz_step_t(OzAcc& acc, const __half* As, const __half* Bs) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int m0 = (w >> 1) * 16, n0 = (w & 1) * 16;
@@ -302,15 +304,16 @@ __device__ __forceinline__ void oz_step_t(OzAcc& acc, const __half* As, const __
     unsigned a[OZ_S][4], b[OZ_S][4];
     if (TA) {
 #pragma unroll
-      for (int s = 0; s < OZ_S; ++s) ldsm_x4_trans(a[s], As + s * OZ_PLANE + oz_swz(kk + tr, tc));
+      for (int s = S0; s < OZ_S; ++s) ldsm_x4_trans(a[s], As + s * OZ_PLANE + oz_swz(kk + tr, tc));
     } else {
 #pragma unroll
-      for (int s = 0; s < OZ_S; ++s) ldsm_x4(a[s], As + s * OZ_PLANE + oz_swz(ar, kk + ac));
+      for (int s = S0; s < OZ_S; ++s) ldsm_x4(a[s], As + s * OZ_PLANE + oz_swz(ar, kk + ac));
     }
 #pragma unroll
-    for (int s = 0; s < OZ_S; ++s) ldsm_x4(b[s], Bs + s * OZ_PLANE + oz_swz(br, kk + bc));
-#pragma unroll
     for (int s = 0; s < OZ_S; ++s)
+      if (s <= OZ_ND - 1 - S0) ldsm_x4(b[s], Bs + s * OZ_PLANE + oz_swz(br, kk + bc));
+#pragma unroll
+    for (int s = S0; s < OZ_S; ++s)
 #pragma unroll
       for (int t = 0; t + s < OZ_ND && t < OZ_S; ++t) {
         mma16816(acc.p[s + t][0], a[s], b[t][0], b[t][1]);

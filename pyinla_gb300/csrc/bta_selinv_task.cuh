@@ -466,7 +466,9 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
     // planes: bulk copies of its leading OZ_S - q planes and of the right tile, the
     // q planes below the shift zeroed by the CTA
     unsigned ph = pp->phase;
+    int qst[2] = {0, 0};   // plane shift of the left tile in each stage buffer
     auto stage = [&](int st, const SigTile& lt, int q, int s) {
+      qst[st] = q;
       __half* dst = stages + st * OZS_STAGE;
       const int slot = (int)(lt.flag - c.flags);
       const unsigned abytes = q < OZ_S ? (unsigned)((OZ_S - q) * OZ_PLANE * sizeof(__half)) : 0u;
@@ -533,10 +535,25 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
             have = true;
           }
         }
-        if (tcur)
-          oz_step_t<true>(acc, cur, cur + OZ_OPER);
-        else
-          oz_step_t<false>(acc, cur, cur + OZ_OPER);
+        // the left tile was staged qcur planes down: its planes below qcur are zero
+        // (all of them from OZ_S on: nothing to add)
+        const int qcur = qst[s & 1];
+        if (qcur >= OZ_S) {
+        } else if (tcur) {
+          if (qcur >= 2)
+            oz_step_t<true, 2>(acc, cur, cur + OZ_OPER);
+          else if (qcur == 1)
+            oz_step_t<true, 1>(acc, cur, cur + OZ_OPER);
+          else
+            oz_step_t<true, 0>(acc, cur, cur + OZ_OPER);
+        } else {
+          if (qcur >= 2)
+            oz_step_t<false, 2>(acc, cur, cur + OZ_OPER);
+          else if (qcur == 1)
+            oz_step_t<false, 1>(acc, cur, cur + OZ_OPER);
+          else
+            oz_step_t<false, 0>(acc, cur, cur + OZ_OPER);
+        }
         ++since_fold;
         if (more) {
           if (!have) {
