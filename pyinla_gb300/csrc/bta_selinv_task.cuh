@@ -420,6 +420,9 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       const int cc = col * TS + threadIdx.x;
       ecol_t[threadIdx.x] = cc < g.b ? p.ecol[(size_t)i * g.b + cc] : 0;
     }
+    // the diagonal task's C_col does not depend on other tasks: load it now, off the
+    // column chain (F is not used by the product loop)
+    if (type == ST_DIAG) tile_load(F, make_tile(p.cinv + (size_t)(i * g.B + col) * TS * TS, TS, 0, 0, TS, TS));
     __syncthreads();
     OzAcc acc;
     oz_clear_partials(acc);
@@ -598,8 +601,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       const int code = sig_store_digits(p, (int)(d.flag - c.flags), X, d.t.rows, d.t.cols, red4);
       cta_publish_val(c, const_cast<int*>(d.flag), code);
     } else {
-      tile_load(F, make_tile(p.cinv + (size_t)(i * g.B + col) * TS * TS, TS, 0, 0, TS, TS));
-      __syncthreads();
+      __syncthreads();   // (C_col was loaded into F before the product loop)
       diag_from_cinv(X, F);
       const SigTile d = sig_dest(p, i, col, col);
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
