@@ -44,6 +44,12 @@ class GB300SerinvSolver:
         self.A_arrow_tip_block = torch.empty((a, a), dtype=f64, device=dev) if a > 0 else None
         self._h = BtaHandle.get(b, nt, a)
         self._torch = torch
+        # index structures derived from the sparsity pattern of the matrices passed in
+        # (the same at every theta): input scatter indices, output gather indices and
+        # the permutation that yields the CSC data of the symmetric result
+        self._in_cache = None
+        self._out_cache = {}
+        self._pinned = {}
         self.total_bytes = 0
         self.t_cholesky = 0.0
         self.t_solve = 0.0
@@ -138,25 +144,61 @@ class GB300SerinvSolver:
         else:
             _lib.check(h.lib.gbta_pobtsi(h.ptr, D, L))
 
+    @staticmethod
+    def _same_pattern(A, key) -> bool:
+        """A (CSR or CSC) has the sparsity pattern recorded in key."""
+        fmt, shape, indptr, indices = key
+        return (A.format == fmt and A.shape == shape and A.indptr.size == indptr.size
+                and A.indices.size == indices.size and np.array_equal(A.indptr, indptr)
+                and np.array_equal(A.indices, indices))
+
+    @staticmethod
+    def _pattern_key(A):
+        return (A.format, A.shape, A.indptr.copy(), A.indices.copy())
+
+    def _to_device(self, x: np.ndarray, slot: str):
+        """Host array to a device tensor through a pinned staging buffer kept per slot."""
+        torch = self._torch
+        src = torch.from_numpy(np.ascontiguousarray(x))
+        buf = self._pinned.get(slot)
+        if buf is None or buf.numel() < src.numel() or buf.dtype != src.dtype:
+            buf = torch.empty(src.numel(), dtype=src.dtype, pin_memory=True)
+            self._pinned[slot] = buf
+        stage = buf[: src.numel()]
+        stage.copy_(src)
+        return stage.to("cuda")   # (blocking: the staging buffer is reused by the next call)
+
     def _spmatrix_to_structured(self, A, sparsity: str) -> None:
         """Zero-fill and scatter the symmetric sparse matrix into the BTA blocks
-        (structured_solver.py:192-250) with one device scatter."""
+        (structured_solver.py:192-250) with one device scatter.  For CSR / CSC input
+        the scatter indices are kept per sparsity pattern, so a matrix with the
+        pattern of an earlier call moves only its values."""
         self._check_sparsity(sparsity)
         torch = self._torch
-        coo = sps.coo_matrix(A)
-        rows = torch.from_numpy(coo.row.astype(np.int64)).cuda()
-        cols = torch.from_numpy(coo.col.astype(np.int64)).cuda()
-        vals = torch.from_numpy(np.ascontiguousarray(coo.data, dtype=np.float64)).cuda()
+        if sps.issparse(A) and A.format in ("csr", "csc"):
+            if self._in_cache is None or not self._same_pattern(A, self._in_cache[0]):
+                coo = A.tocoo()   # entries in the order of A.data
+                rows = torch.from_numpy(coo.row.astype(np.int64)).cuda()
+                cols = torch.from_numpy(coo.col.astype(np.int64)).cuda()
+                self._in_cache = (self._pattern_key(A), rows, cols)
+            _, rows, cols = self._in_cache
+            vals = self._to_device(np.asarray(A.data, dtype=np.float64), "in")
+            nnz = int(A.data.size)
+        else:
+            coo = sps.coo_matrix(A)
+            rows = torch.from_numpy(coo.row.astype(np.int64)).cuda()
+            cols = torch.from_numpy(coo.col.astype(np.int64)).cuda()
+            vals = torch.from_numpy(np.ascontiguousarray(coo.data, dtype=np.float64)).cuda()
+            nnz = int(coo.nnz)
         h = self._h
         h.set_stream(current_stream_ptr())
         D, L, R, T = self._ptrs("bta")
-        _lib.check(h.lib.gbta_scatter_coo(h.ptr, rows.data_ptr(), cols.data_ptr(), vals.data_ptr(), int(coo.nnz),
+        _lib.check(h.lib.gbta_scatter_coo(h.ptr, rows.data_ptr(), cols.data_ptr(), vals.data_ptr(), nnz,
                                           D, L, R, T, 1 if R is not None else 0))
 
-    def _structured_to_spmatrix(self, A, sparsity: str):
-        """Sigma (or the factor) on the lower pattern of ``A``, symmetrised, as CSC
-        (structured_solver.py:470-538)."""
-        self._check_sparsity(sparsity)
+    def _output_structure(self, A, sparsity: str):
+        """Gather indices of the lower BTA pattern of A and the structure of the
+        symmetrised result: the result's data is vals[perm] for the gathered vals."""
         torch = self._torch
         Bl = sps.tril(sps.csc_matrix(A)).tocoo()
         b, nt = self.diagonal_blocksize, self.n_diag_blocks
@@ -165,15 +207,46 @@ class GB300SerinvSolver:
         in_bt = (r < nb) & (c < nb) & ((r // b == c // b) | (r // b == c // b + 1))
         keep = in_bt | ((r >= nb) if sparsity == "bta" else np.zeros_like(in_bt))
         r, c = r[keep], c[keep]
-        rows, cols = torch.from_numpy(r).cuda(), torch.from_numpy(c).cuda()
-        vals = torch.empty(r.size, dtype=torch.float64, device="cuda")
+        # the reference's construction, run once on markers 1..m (exact in float64)
+        marks = np.arange(1, r.size + 1, dtype=np.float64)
+        out = sps.coo_matrix((marks, (r, c)), shape=Bl.shape).tocsc()
+        res = out + sps.tril(out, k=-1).T
+        perm = res.data.astype(np.int64) - 1
+        return {
+            "rows": torch.from_numpy(r).cuda(), "cols": torch.from_numpy(c).cuda(),
+            "perm": torch.from_numpy(perm).cuda(), "format": res.format, "shape": res.shape,
+            "indices": res.indices.copy(), "indptr": res.indptr.copy(),
+        }
+
+    def _structured_to_spmatrix(self, A, sparsity: str):
+        """Sigma (or the factor) on the lower pattern of ``A``, symmetrised, as CSC
+        (structured_solver.py:470-538).  The index work depends only on the sparsity
+        pattern of A and is kept per pattern; each call gathers the values on the
+        device, orders them as the result's data and copies them to the host."""
+        self._check_sparsity(sparsity)
+        torch = self._torch
+        A = A if (sps.issparse(A) and A.format in ("csr", "csc")) else sps.csc_matrix(A)
+        ent = self._out_cache.get(sparsity)
+        if ent is None or not self._same_pattern(A, ent[0]):
+            ent = (self._pattern_key(A), self._output_structure(A, sparsity))
+            self._out_cache[sparsity] = ent
+        st = ent[1]
+        rows, cols = st["rows"], st["cols"]
+        vals = torch.empty(rows.numel(), dtype=torch.float64, device="cuda")
         h = self._h
         h.set_stream(current_stream_ptr())
         D, L, R, T = self._ptrs(sparsity)
-        _lib.check(h.lib.gbta_gather_coo(h.ptr, rows.data_ptr(), cols.data_ptr(), int(r.size), D, L, R, T,
+        _lib.check(h.lib.gbta_gather_coo(h.ptr, rows.data_ptr(), cols.data_ptr(), int(rows.numel()), D, L, R, T,
                                          1 if R is not None else 0, vals.data_ptr()))
-        out = sps.coo_matrix((vals.cpu().numpy(), (r, c)), shape=Bl.shape).tocsc()
-        return out + sps.tril(out, k=-1).T
+        data = vals[st["perm"]]
+        host = self._pinned.get("out")
+        if host is None or host.numel() < data.numel():
+            host = torch.empty(data.numel(), dtype=torch.float64, pin_memory=True)
+            self._pinned["out"] = host
+        host[: data.numel()].copy_(data)
+        cls = sps.csc_matrix if st["format"] == "csc" else sps.csr_matrix
+        return cls((host[: data.numel()].numpy().copy(), st["indices"].copy(), st["indptr"].copy()),
+                   shape=st["shape"])
 
     def get_solver_memory(self) -> int:
         """Bytes of the block buffers plus the library workspace (structured_solver.py:540-550)."""

@@ -271,3 +271,38 @@ def test_drop_in_solver_against_reference_wrapper(torch):
     assert abs(s.logdet("bt") - float(g["wrapper_bt_logdet"])) <= RTOL * abs(float(g["wrapper_bt_logdet"]))
     assert s.t_cholesky > 0 and s.t_solve > 0
     assert s.get_solver_memory() > D.nbytes
+
+
+def test_drop_in_solver_pattern_cache(torch):
+    """Matrices with the sparsity pattern of an earlier call reuse its index work
+    (new arrays, same pattern), a CSR input and a COO input take the other paths,
+    and all give the results of a fresh conversion."""
+    import scipy.sparse as sps
+
+    from pyinla_gb300.solver import GB300SerinvSolver
+
+    g, D, L, R, T, rhs = _golden("ragged")
+    A = sps.csc_matrix(orc.bta_to_dense(D, L, R, T))
+    s = GB300SerinvSolver(None, diagonal_blocksize=int(g["b"]), n_diag_blocks=int(g["nt"]),
+                          arrowhead_blocksize=int(g["a"]))
+    s.cholesky(A, sparsity="bta")
+    ld1 = s.logdet("bta")
+    s.selected_inversion("bta")
+    S1 = s._structured_to_spmatrix(A, "bta")
+    A2 = A.copy()
+    A2.data = A2.data * 1.7
+    s.cholesky(A2, sparsity="bta")
+    ld2 = s.logdet("bta")
+    s.selected_inversion("bta")
+    S2 = s._structured_to_spmatrix(A2, "bta")
+    n = A.shape[0]
+    assert abs(ld2 - (ld1 + n * np.log(1.7))) <= 1e-10 * abs(ld2)
+    assert S2.format == S1.format and np.array_equal(S2.indices, S1.indices) and np.array_equal(S2.indptr, S1.indptr)
+    assert relerr(S2.data * 1.7, S1.data) < RTOL
+    for B in (A2.tocsr(), A2.tocoo()):
+        s2 = GB300SerinvSolver(None, diagonal_blocksize=int(g["b"]), n_diag_blocks=int(g["nt"]),
+                               arrowhead_blocksize=int(g["a"]))
+        s2.cholesky(B, sparsity="bta")
+        s2.selected_inversion("bta")
+        S3 = s2._structured_to_spmatrix(B, "bta")
+        assert np.abs((S3 - S2).toarray()).max() <= RTOL * np.abs(S2.data).max()
