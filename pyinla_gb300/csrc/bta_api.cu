@@ -52,7 +52,8 @@ struct gbta_solver {
   int* d_flags = nullptr;
   int4* d_ftasks = nullptr;
   int n_ftasks = 0;
-  int4* d_stasks = nullptr;
+  int4* d_stasks = nullptr;    // selected-inversion tasks (FP64 method)
+  int4* d_stasks_m = nullptr;  // merged list of the tensor-core method (same count)
   int n_stasks = 0;
   double* d_tip_part = nullptr;
   double* d_arrow_part = nullptr;
@@ -99,15 +100,29 @@ std::vector<int4> factor_task_list(const Geom& g) {
   return t;
 }
 
-std::vector<int4> selinv_task_list(const Geom& g) {
+// Merged form (tensor-core method): the column chain of the inversion runs diagonal
+// tile -> sub-diagonal tile of the next column -> its diagonal tile -> ...; the
+// sub-diagonal tile's last product needs the diagonal tile just finished, so the
+// diagonal task finishes it itself, from the partial sum of its other products that
+// an ST_PART task (placed before that diagonal task) leaves.
+std::vector<int4> selinv_task_list(const Geom& g, bool merged) {
   std::vector<int4> t;
+  const int B = g.B;
+  auto sub_code = [&](int i, int c) { return c + 1 < B ? c + 1 : (i < g.nt - 1 ? B : -1); };
   if (g.a > 0) t.push_back(make_int4(ST_TIP, 0, 0, 0));
   for (int i = g.nt - 1; i >= 0; --i)
-    for (int c = g.B - 1; c >= 0; --c) {
-      if (g.a > 0) t.push_back(make_int4(ST_OFF, i, 2 * g.B, c));
+    for (int c = B - 1; c >= 0; --c) {
+      const int sub = merged ? sub_code(i, c) : -1;
+      if (g.a > 0) t.push_back(make_int4(ST_OFF, i, 2 * B, c));
       if (i < g.nt - 1)
-        for (int r = 0; r < g.B; ++r) t.push_back(make_int4(ST_OFF, i, g.B + r, c));
-      for (int r = c + 1; r < g.B; ++r) t.push_back(make_int4(ST_OFF, i, r, c));
+        for (int r = 0; r < B; ++r)
+          if (B + r != sub) t.push_back(make_int4(ST_OFF, i, B + r, c));
+      for (int r = c + 1; r < B; ++r)
+        if (r != sub) t.push_back(make_int4(ST_OFF, i, r, c));
+      if (merged) {   // the partial of the next column's sub-diagonal tile
+        if (c > 0) t.push_back(make_int4(ST_PART, i, c, c - 1));
+        else if (i > 0) t.push_back(make_int4(ST_PART, i - 1, B, B - 1));
+      }
       t.push_back(make_int4(ST_DIAG, i, c, c));
     }
   return t;
@@ -208,7 +223,8 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   CREATE_CUDA(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
   s->stream = s->own_stream;
 
-  const std::vector<int4> ft = gbta::factor_task_list(s->g), st = gbta::selinv_task_list(s->g);
+  const std::vector<int4> ft = gbta::factor_task_list(s->g), st = gbta::selinv_task_list(s->g),
+                          stm = gbta::selinv_task_list(s->g, true);
   s->n_ftasks = (int)ft.size();
   s->n_stasks = (int)st.size();
   const size_t ntile = (size_t)nt * s->g.B;
@@ -216,6 +232,7 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   CREATE_CUDA(cudaMalloc(&s->d_flags, (size_t)nflags * sizeof(int)));
   CREATE_CUDA(cudaMalloc(&s->d_ftasks, ft.size() * sizeof(int4)));
   CREATE_CUDA(cudaMalloc(&s->d_stasks, st.size() * sizeof(int4)));
+  CREATE_CUDA(cudaMalloc(&s->d_stasks_m, stm.size() * sizeof(int4)));
   CREATE_CUDA(cudaMalloc(&s->d_tip_part, ntile * gbta::TS * gbta::TS * sizeof(double)));
   CREATE_CUDA(cudaMalloc(&s->d_arrow_part, ntile * gbta::TS * gbta::SOLVE_NC * sizeof(double)));
   CREATE_CUDA(cudaMalloc(&s->d_faux, ntile * sizeof(int)));
@@ -226,6 +243,7 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   CREATE_CUDA(cudaMemsetAsync(s->d_flags, 0, (size_t)nflags * sizeof(int), s->stream));
   CREATE_CUDA(cudaMemcpyAsync(s->d_ftasks, ft.data(), ft.size() * sizeof(int4), cudaMemcpyHostToDevice, s->stream));
   CREATE_CUDA(cudaMemcpyAsync(s->d_stasks, st.data(), st.size() * sizeof(int4), cudaMemcpyHostToDevice, s->stream));
+  CREATE_CUDA(cudaMemcpyAsync(s->d_stasks_m, stm.data(), stm.size() * sizeof(int4), cudaMemcpyHostToDevice, s->stream));
   CREATE_CUDA(cudaStreamSynchronize(s->stream));
 #undef CREATE_CUDA
   s->ws_bytes = CTRL_INTS * sizeof(int) + (size_t)nflags * sizeof(int) + (ft.size() + st.size()) * sizeof(int4) +
@@ -243,6 +261,7 @@ int gbta_destroy(gbta_solver* s) {
   cudaFree(s->d_flags);
   cudaFree(s->d_ftasks);
   cudaFree(s->d_stasks);
+  cudaFree(s->d_stasks_m);
   cudaFree(s->d_tip_part);
   cudaFree(s->d_arrow_part);
   cudaFree(s->d_faux);
@@ -466,8 +485,9 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
   if (int r = reset_ticket(s)) return r;
   const gbta::LaunchCtl lc = next_launch(s, s->n_stasks);
   if (s->method == GBTA_METHOD_OZAKI)
-    gbta::launch_selinv_oz(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks,
-                           (__half*)s->d_digits, s->d_erow, cinv, (__half*)s->d_sdig, lc);
+    gbta::launch_selinv_oz(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks_m, s->n_stasks,
+                           (__half*)s->d_digits, s->d_erow, cinv, (__half*)s->d_sdig, s->d_tip_part, s->d_faux,
+                           lc);
   else
     gbta::launch_selinv(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks, cinv, lc);
   GBTA_CUDA(cudaGetLastError());

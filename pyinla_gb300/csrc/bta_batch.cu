@@ -282,6 +282,9 @@ int build_args(gbta_batch* bt) {
     s.fdig = q.digits;
     s.ecol = q.erow;
     s.sdig = q.sdig;
+    s.merged = q.method == GBTA_METHOD_OZAKI;
+    s.part = q.tip_part;                  // the factorization's tip partials are dead here
+    s.part_flag = bt->d_faux + q.faux_off;
     s.cinv = q.selws + (size_t)g.nt * g.B * gbta::TS * gbta::TS;
     s.c = batch_ctl(bt, flags, EP_SELINV);
     for (int dir = 0; dir < 2; ++dir) {
@@ -429,7 +432,7 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
     q.method = methods ? methods[k] : GBTA_METHOD_OZAKI;
     const gbta::Geom& g = q.g;
     ft[k] = gbta::factor_task_list(g);
-    st[k] = gbta::selinv_task_list(g);
+    st[k] = gbta::selinv_task_list(g, q.method == GBTA_METHOD_OZAKI);
     q.n_ftasks = (int)ft[k].size();
     q.n_stasks = (int)st[k].size();
     q.n_vtasks = g.nt * g.B + (g.a > 0 ? 1 : 0);

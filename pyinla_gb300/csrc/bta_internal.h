@@ -24,7 +24,9 @@ enum FactorTask { FT_DIAG = 0, FT_OFFD = 1, FT_LOW = 2, FT_ARW = 3, FT_TIP = 4, 
 constexpr int FT_PRE = 8;
 constexpr int FEED_ROWS = 8;   // rows of a feeder tile solved by one FT_FEEDQ task
 // Task codes of the selected-inversion DAG.
-enum SelinvTask { ST_TIP = 0, ST_OFF = 1, ST_DIAG = 2 };
+// ST_PART: the products of the sub-diagonal tile of a column except its last (tensor-
+// core method; the diagonal task of the previous column finishes that tile).
+enum SelinvTask { ST_TIP = 0, ST_OFF = 1, ST_DIAG = 2, ST_PART = 3 };
 
 // Geometry of one BTA matrix and the flag layout shared by all kernels.
 struct Geom {
@@ -74,7 +76,9 @@ int resident_ctas(const void* kernel, int threads, size_t smem, int tmem_cols);
 
 // Task lists of the factorization and selected-inversion DAGs (bta_api.cu).
 std::vector<int4> factor_task_list(const Geom& g);
-std::vector<int4> selinv_task_list(const Geom& g);
+// merged: the list of the tensor-core method, where each diagonal task also finishes
+// the sub-diagonal tile of the next column (ST_PART tasks form its other products).
+std::vector<int4> selinv_task_list(const Geom& g, bool merged = false);
 
 // Host-side count of kernel launches issued by this library (see gbta_kernel_launches).
 void count_launches(int n);
@@ -107,11 +111,13 @@ size_t selinv_oz_digit_bytes(const Geom& g);
 void launch_selinv_oz_prepare(const Geom& g, const double* D, const double* L, const double* R, int use_arrow,
                               __half* fdig, int* ecol, cudaStream_t stream);
 // sdig: digit planes (selinv_oz_digit_bytes) of the Sigma tiles, written by the tasks
-// that produce them (their exponents travel in the tiles' flag words).
+// that produce them (their exponents travel in the tiles' flag words).  tasks: the
+// merged list (selinv_task_list(g, true)); part: nt*B FP64 tiles and part_flag: nt*B
+// epoch-stamped flags for the partial sums of the sub-diagonal tiles.
 void launch_selinv_oz(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                       double* SD, double* SL, double* SR, double* ST, int use_arrow, const int4* tasks,
-                      int ntasks, __half* fdig, int* ecol, const double* cinv, __half* sdig,
-                      const LaunchCtl& lc);
+                      int ntasks, __half* fdig, int* ecol, const double* cinv, __half* sdig, double* part,
+                      int* part_flag, const LaunchCtl& lc);
 
 void launch_solve(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                   double* Bv, int ldb, int nc, int trans, int use_arrow, double* arrow_part,

@@ -177,6 +177,10 @@ void launch_selinv(const Geom& g, const double* D, const double* L, const double
   p.fdig = nullptr;
   p.ecol = nullptr;
   p.cinv = cinv;
+  p.sdig = nullptr;
+  p.part = nullptr;
+  p.part_flag = nullptr;
+  p.merged = 0;
   p.c.ctrl = lc.ctrl;
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;

@@ -110,7 +110,8 @@ size_t selinv_oz_digit_bytes(const Geom& g) { return (size_t)g.nflags() * OZ_TIL
 
 void launch_selinv_oz(const Geom& g, const double* D, const double* L, const double* R, const double* T, double* SD,
                       double* SL, double* SR, double* ST, int use_arrow, const int4* tasks, int ntasks, __half* fdig,
-                      int* ecol, const double* cinv, __half* sdig, const LaunchCtl& lc) {
+                      int* ecol, const double* cinv, __half* sdig, double* part, int* part_flag,
+                      const LaunchCtl& lc) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_selinv_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZS_SMEM);
@@ -137,6 +138,9 @@ void launch_selinv_oz(const Geom& g, const double* D, const double* L, const dou
   p.ecol = ecol;
   p.cinv = cinv;
   p.sdig = sdig;
+  p.part = part;
+  p.part_flag = part_flag;
+  p.merged = 1;
   p.c.ctrl = lc.ctrl;
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;

@@ -59,6 +59,9 @@ struct SelinvArgs {
   const double* cinv;   // [nt*B][TS*TS]: F_cc^{-T} F_cc^{-1} of every diagonal factor tile
   __half* sdig;         // Ozaki: digit planes of every Sigma tile per flag slot (their
                         // exponents ride in the tiles' flag words, see sig_exp_code)
+  double* part;         // Ozaki, merged task list: [nt*B][TS*TS] partial sums of the
+  int* part_flag;       // sub-diagonal tiles and their epoch-stamped flags [nt*B]
+  int merged;           // the task list is selinv_task_list(g, true)
   Ctl c;
 };
 
@@ -415,7 +418,8 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       return true;
     }
 
-    const int np = pat_size(p, i, col);
+    // a partial task (ST_PART) leaves out its last step: the diagonal tile j itself
+    const int np = pat_size(p, i, col) - (type == ST_PART ? 1 : 0);
     if (threadIdx.x < TS) {
       const int cc = col * TS + threadIdx.x;
       ecol_t[threadIdx.x] = cc < g.b ? p.ecol[(size_t)i * g.b + cc] : 0;
@@ -444,7 +448,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       const int l = pat_code(p, i, col, s);
       int slot;
       bool tr;
-      if (type == ST_OFF) {
+      if (type == ST_OFF || type == ST_PART) {
         const SigTile st_ = sig_tile(p, i, j, l);
         slot = (int)(st_.flag - c.flags);
         tr = st_.trans;
@@ -600,13 +604,74 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
       const int code = sig_store_digits(p, (int)(d.flag - c.flags), X, d.t.rows, d.t.cols, red4);
       cta_publish_val(c, const_cast<int*>(d.flag), code);
+    } else if (type == ST_PART) {   // the partial sum, for the diagonal task that finishes the tile
+      __syncthreads();
+      tile_store(p.part + (size_t)(i * g.B + col) * TS * TS, TS, TS, TS, X);
+      cta_publish(c, p.part_flag + i * g.B + col);
     } else {
       __syncthreads();   // (C_col was loaded into F before the product loop)
       diag_from_cinv(X, F);
       const SigTile d = sig_dest(p, i, col, col);
-      tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
-      const int code = sig_store_digits(p, (int)(d.flag - c.flags), X, d.t.rows, d.t.cols, red4);
-      cta_publish_val(c, const_cast<int*>(d.flag), code);
+      // Merged task list: this task also finishes the sub-diagonal tile of the next
+      // column, Sigma(j2, c2) of block column i2, whose last product needs this tile:
+      // Sigma(j2, c2) = partial - Sigma(col, col) G(j2, c2) (the tile is symmetric, so
+      // it is its own left operand untransposed).  That tile is the next link of the
+      // column chain, so it is published first; this tile's store, digits and flag
+      // follow (its other consumers are later columns' products).
+      const int i2 = col > 0 ? i : i - 1, c2 = col > 0 ? col - 1 : g.B - 1, j2 = col > 0 ? col : g.B;
+      if (p.merged && i2 >= 0) {
+        __half* A0 = stages;   // stage 0: this tile's digits (no copy is in flight after the loop)
+        __half* B0 = stages + OZ_OPER;
+        double* X2 = reinterpret_cast<double*>(stages + OZS_STAGE);   // stage 1: Sigma(j2, c2)
+        if (!cta_wait(c, p.part_flag + i2 * g.B + c2, nullptr, &s_ok)) return false;
+        tile_load(F, make_tile(p.part + (size_t)(i2 * g.B + c2) * TS * TS, TS, 0, 0, TS, TS));
+        if (threadIdx.x < TS) {
+          const int cc = c2 * TS + threadIdx.x;
+          ecol_t[threadIdx.x] = cc < g.b ? p.ecol[(size_t)i2 * g.b + cc] : 0;
+        }
+        oz_load_async(B0, p.fdig + (size_t)fac_slot(g, i2, j2, c2) * OZ_TILE);
+        cp_async_commit();
+        const int Ed = smem_tile_exponent7(X, d.t.rows, d.t.cols, red4);   // contains barriers
+        oz_store_digits_uniform(A0, X, d.t.rows, d.t.cols, Ed == NO_EXP ? 0 : Ed);
+        cp_async_wait_all();
+        __syncthreads();
+        OzAcc a2;
+        oz_clear_partials(a2);
+        int es[2][4];
+#pragma unroll
+        for (int n = 0; n < 2; ++n)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            a2.v[n][q] = F[oz_row(n, q) * LDS + oz_col(n, q)];
+            es[n][q] = Ed + ecol_t[oz_col(n, q)];
+          }
+        if (Ed > NO_EXP) {
+          oz_step_t<false>(a2, A0, B0);
+          oz_fold_sub(a2, es);
+        }
+#pragma unroll
+        for (int n = 0; n < 2; ++n)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) X2[oz_row(n, q) * LDS + oz_col(n, q)] = a2.v[n][q];
+        __syncthreads();
+        const SigTile d2 = sig_dest(p, i2, j2, c2);
+        tile_store(const_cast<double*>(d2.t.p), d2.t.ld, d2.t.rows, d2.t.cols, X2);
+        const int code2 = sig_store_digits(p, (int)(d2.flag - c.flags), X2, d2.t.rows, d2.t.cols, red4);
+        cta_publish_val(c, const_cast<int*>(d2.flag), code2);
+        // this tile: its digits are the ones in A0
+        tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
+        {
+          const uint4* src = reinterpret_cast<const uint4*>(A0);
+          uint4* dst = reinterpret_cast<uint4*>(p.sdig + (size_t)(d.flag - c.flags) * OZ_TILE);
+          for (int k = threadIdx.x; k < OZ_CHUNKS16; k += NT) dst[k] = src[k];
+        }
+        cta_publish_val(c, const_cast<int*>(d.flag), sig_exp_code(Ed));
+        fence_async_smem();   // stages 0 and 1 are refilled by bulk copies later
+      } else {
+        tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
+        const int code = sig_store_digits(p, (int)(d.flag - c.flags), X, d.t.rows, d.t.cols, red4);
+        cta_publish_val(c, const_cast<int*>(d.flag), code);
+      }
     }
     trace_task(c, t, type, t_task0);
   }

@@ -72,7 +72,6 @@ __device__ __forceinline__ void umma_commit(unsigned long long* bar) {
 }
 __device__ __forceinline__ void tmem_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tmem_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
 // Warp-wide: allocate / free ncols columns (a power of two >= 32; the address goes to
 // *s_addr).
