@@ -81,8 +81,8 @@ static __device__ __forceinline__ Tile feeder_tile(const FactorArgs& p, int i, i
 
 // FT_FEEDQ task: rows FEED_ROWS q .. of the feeder of diagonal tile (i, col) <- their
 // products (left there by the FT_PRE task) times D_i(col, col)^{-T}, plus their digit
-// planes (tensor-core method).  The task that completes the last row group publishes
-// the tile.  X, F, FS: shared tiles; rd: TS doubles; erow_t: TS ints (digits only).
+// planes (tensor-core method).  Each group adds its share of the epoch to the
+// feeder's ready flag, which reaches the epoch when the last group has written.  X, F, FS: shared tiles; rd: TS doubles; erow_t: TS ints (digits only).
 static __device__ bool factor_feed_rows(const FactorArgs& p, int t, int i, int q, int col, double* X, double* F,
                                         double* FS, double* rd, int* erow_t, int* s_ok, unsigned long long t_task0) {
   const Geom& g = p.g;
