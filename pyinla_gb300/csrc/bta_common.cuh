@@ -104,16 +104,17 @@ __device__ __forceinline__ void raise_abort(const Ctl& c) { atomicExch(c.ctrl + 
 // short sleep.
 constexpr unsigned long long SPIN_NS = 200000;
 
-static __device__ bool spin_ready(const Ctl& c, const int* flag, int* seen = nullptr) {
+static __device__ bool spin_ready(const Ctl& c, const int* flag, int* seen = nullptr, int plus = 0) {
+  const int want = c.epoch + plus;
   int v = ld_acquire(flag);
-  if (v >= c.epoch) {
+  if (v >= want) {
     if (seen) *seen = v;
     return true;
   }
   const unsigned long long t0 = gtimer();
   for (unsigned it = 1;; ++it) {
     v = ld_acquire(flag);
-    if (v >= c.epoch) {
+    if (v >= want) {
       if (seen) *seen = v;
       return true;
     }
@@ -149,6 +150,16 @@ static __device__ bool cta_wait(const Ctl& c, const int* f0, const int* f1, int*
 // every thread through *s_val.  Contains __syncthreads().
 static __device__ bool cta_wait_val(const Ctl& c, const int* f, int* s_ok, int* s_val) {
   if (threadIdx.x == 0) *s_ok = spin_ready(c, f, s_val) ? 1 : 0;
+  __syncthreads();
+  const bool ok = *s_ok != 0;
+  __syncthreads();
+  return ok;
+}
+
+// Wait until *f >= epoch + plus: a flag that was published (epoch) and then raised by
+// `plus` with cta_raise for a second product of the same task.
+static __device__ bool cta_wait_plus(const Ctl& c, const int* f, int plus, int* s_ok) {
+  if (threadIdx.x == 0) *s_ok = spin_ready(c, f, nullptr, plus) ? 1 : 0;
   __syncthreads();
   const bool ok = *s_ok != 0;
   __syncthreads();
@@ -238,6 +249,14 @@ static __device__ bool cta_poll(const Ctl& c, const int* f0, const int* f1, int*
 __device__ __forceinline__ void cta_publish(const Ctl& c, int* flag) {
   __syncthreads();   // every thread's writes before thread 0's (cumulative) release store
   if (threadIdx.x == 0) st_release(flag, c.epoch);
+}
+
+// Raise a published flag by v (< 512, so it stays below the next launch's epoch) once
+// every thread's writes since the publication are done; the barrier and the cumulative
+// release order them as in cta_publish.
+__device__ __forceinline__ void cta_raise(int* flag, int v) {
+  __syncthreads();
+  if (threadIdx.x == 0) red_add_release(flag, v);
 }
 
 // Pull the next ticket (CTA-uniform).
@@ -499,60 +518,99 @@ __device__ __forceinline__ void nbar_sync(int id) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(NT) : "memory");
 }
 
+// Named barriers with a thread count other than NT (both sides must agree on N).
+template <int N> __device__ __forceinline__ void nbar_arrive_n(int id) {
+  asm volatile("bar.arrive %0, %1;" ::"r"(id), "n"(N) : "memory");
+}
+template <int N> __device__ __forceinline__ void nbar_sync_n(int id) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(N) : "memory");
+}
+
+// Barrier ids of smem_potrf: POTRF_BAR_L + (j & 7) hands pivot column j from the pivot
+// warp to the three update warps (NT threads); POTRF_BAR_C + (j & 3) hands column j+2,
+// updated through pivot j, from its owner to the pivot warp (64 threads).
+constexpr int POTRF_BAR_L = 1, POTRF_BAR_C = 9;
+
+// Update warp W (1..3) of smem_potrf: owns columns c = W + 1 + 3q (q = 0..9) in
+// registers, lane = row.  For every pivot j it first applies pivot j to column j+2 if
+// it owns it and hands that column to the pivot warp, then applies pivot j to its later
+// columns.  All column tests are compile-time, so no predicated-off FMA is issued.
+template <int W>
+__device__ __forceinline__ void potrf_update_warp(double* S, int r) {
+  double acc[10];
+#pragma unroll
+  for (int q = 0; q < 10; ++q) acc[q] = S[r * LDS + W + 1 + 3 * q];
+#pragma unroll
+  for (int j = 0; j < TS - 2; ++j) {
+    nbar_sync(POTRF_BAR_L + (j & 7));
+    const double lj = S[r * LDS + j];   // l_rj
+    if (j + 1 >= W && (j + 1 - W) % 3 == 0) {
+      const int q = (j + 1 - W) / 3;   // column j + 2
+      acc[q] = fma(-lj, S[(j + 2) * LDS + j], acc[q]);
+      S[r * LDS + j + 2] = acc[q];
+      nbar_arrive_n<64>(POTRF_BAR_C + (j & 3));
+    }
+#pragma unroll
+    for (int q = 0; q < 10; ++q)
+      if (W + 1 + 3 * q > j + 2) acc[q] = fma(-lj, S[(W + 1 + 3 * q) * LDS + j], acc[q]);
+  }
+}
+
 // In-place lower Cholesky of S (TS x TS; entries past n must already be identity).
 // Returns 0, or the 1-based column of the first non-positive (or NaN) pivot (the
 // tile then holds NaNs).  The strict upper triangle is zeroed.
-// Warp g keeps columns g, g+4, ... in registers (lane = row) and produces their pivot
-// columns (l_kk = d y, l_rk = a_rk y, y = 1/sqrt(d)) into S, handing each one to the
-// other warps with a named barrier instead of a CTA-wide barrier per column: warps
-// drift apart by up to four columns, so the FP64 work of the trailing updates spreads
-// over the steps instead of being paced by the slowest warp of every step.  The owner
-// of column j+1 applies pivot j to that column first and produces pivot j+1 at once
-// (look-ahead), then applies pivot j to its other columns.  A warp consumes pivot p
-// before any pivot past p+4 can exist, so eight barrier ids in rotation suffice.
+// Warp 0 does nothing but the pivot chain: for pivot k it takes column k, already
+// updated through pivot k-2 by its owner, applies pivot k-1 itself (it holds l_{:,k-1}
+// in registers, so the multiplier l_{k,k-1} is one shuffle), forms y = 1/sqrt(d) and
+// l_rk = a_rk y (l_kk = d y) and publishes the column to S.  Warps 1-3 apply every
+// pivot to the later columns (potrf_update_warp), the column that the pivot warp needs
+// next first.  Every entry receives its updates in pivot order with the same FMAs as a
+// plain right-looking sweep, so the result does not depend on this split.  The pivot
+// warp's FP64 unit serves only the chain (one FMA, the refinement of rsqrt, one
+// multiply per pivot), and the trailing updates run on the other three sub-partitions.
+// Barrier ids rotate over 8 (pivot columns) and 4 (look-ahead columns): before the
+// pivot warp publishes pivot p+8, each update warp has handed it one of columns
+// p+6 .. p+8 and so consumed pivot p+4; the pivot warp consumes look-ahead column p
+// before it can publish the pivot that look-ahead column p+4 needs.
 static __device__ int smem_potrf(double* S) {
   __shared__ int s_info;
   const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
   if (threadIdx.x == 0) s_info = TS + 1;
   __syncthreads();
-  double acc[8];
-#pragma unroll
-  for (int q = 0; q < 8; ++q) acc[q] = S[r * LDS + g + 4 * q];
   if (g == 0) {
-    const double d = __shfl_sync(0xffffffffu, acc[0], 0);
-    const double y = rsqrt3(d);
-    acc[0] *= y;   // row 0 holds d itself: l_00 = d y, l_r0 = a_r0 y
-    S[r * LDS] = acc[0];
-    if (r == 0 && !(d > 0.0)) atomicMin(&s_info, 1);
-    nbar_arrive(1);
-  }
+    const double a0 = S[r * LDS];
+    const double a1 = S[r * LDS + 1];   // column 1 takes no update before pivot 0
+    const double d0 = __shfl_sync(0xffffffffu, a0, 0);
+    const double y0 = rsqrt3(d0);
+    double lp = a0 * y0;   // row 0 holds d itself: l_00 = d y, l_r0 = a_r0 y
+    S[r * LDS] = lp;
+    if (r == 0 && !(d0 > 0.0)) atomicMin(&s_info, 1);
+    nbar_arrive(POTRF_BAR_L);
 #pragma unroll
-  for (int j = 0; j < TS; ++j) {
-    double lj;   // l_rj
-    if (g == (j & 3)) {
-      lj = acc[j >> 2];
-    } else {
-      nbar_sync(1 + (j & 7));
-      lj = S[r * LDS + j];
-    }
-    if (j + 1 < TS && g == ((j + 1) & 3)) {
-      const int qn = (j + 1) >> 2;
-      const double a = fma(-lj, S[(j + 1) * LDS + j], acc[qn]);
-      const double d = __shfl_sync(0xffffffffu, a, j + 1);
+    for (int k = 1; k < TS; ++k) {
+      double a;
+      if (k == 1) {
+        a = a1;
+      } else {
+        nbar_sync_n<64>(POTRF_BAR_C + ((k - 2) & 3));
+        a = S[r * LDS + k];
+      }
+      const double m = __shfl_sync(0xffffffffu, lp, k);   // l_{k,k-1}
+      a = fma(-lp, m, a);
+      const double d = __shfl_sync(0xffffffffu, a, k);
       const double y = rsqrt3(d);
-      const double l = (r > j) ? a * y : 0.0;   // lane j+1 holds d = a: one multiply for l_kk and l_rk
-      acc[qn] = l;
-      S[r * LDS + j + 1] = l;
-      if (r == 0 && !(d > 0.0)) atomicMin(&s_info, j + 2);
-      nbar_arrive(1 + ((j + 1) & 7));
-#pragma unroll
-      for (int q = 0; q < 8; ++q)
-        if (col_after(q, j + 1, g)) acc[q] = fma(-lj, S[(g + 4 * q) * LDS + j], acc[q]);
-    } else {
-#pragma unroll
-      for (int q = 0; q < 8; ++q)
-        if (col_after(q, j, g)) acc[q] = fma(-lj, S[(g + 4 * q) * LDS + j], acc[q]);
+      const double l = (r >= k) ? a * y : 0.0;   // lane k holds d = a: one multiply for l_kk and l_rk
+      S[r * LDS + k] = l;
+      if (r == 0 && !(d > 0.0)) atomicMin(&s_info, k + 1);
+      if (k < TS - 2) nbar_arrive(POTRF_BAR_L + (k & 7));
+      lp = l;
     }
+  } else if (g == 1) {
+    potrf_update_warp<1>(S, r);
+  } else if (g == 2) {
+    potrf_update_warp<2>(S, r);
+  } else {
+    potrf_update_warp<3>(S, r);
   }
   __syncthreads();
   const int info = s_info;

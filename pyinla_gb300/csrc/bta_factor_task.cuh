@@ -162,6 +162,38 @@ static __device__ bool load_diag_factor(const FactorArgs& p, int i, int c, doubl
   return true;
 }
 
+// X <- X * F^{-T} for the target of an off-diagonal task (F: the padded diagonal factor
+// tile, rd: TS doubles).  An arrow tile has only a rows of the factor, so for a <= 16 the
+// 8-row solve (lane = column, no barrier per column) runs on those rows alone; FS is a
+// free tile of shared memory for the row-scaled copy of F it reads.
+static __device__ __forceinline__ void offdiag_trsm(double* X, const double* F, double* FS, double* rd,
+                                                    bool arrow, int a) {
+  tile_diag_recip(F, rd);
+  if (arrow && a <= 2 * FEED_ROWS) {
+    __syncthreads();
+    tile_scale_rows_by_recip(FS, F, rd);
+    for (int row0 = 0; row0 < a; row0 += FEED_ROWS) smem_trsm_rlt_rows8(X, FS, rd, row0);
+  } else {
+    smem_trsm_rlt(X, F, rd);
+  }
+}
+
+// Tip partial P = X X^T of an arrow tile (F is scratch), written for the tip task.
+static __device__ __forceinline__ void arrow_tip_partial(const FactorArgs& p, int i, int col, const double* X,
+                                                         double* F) {
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < TS * TS; idx += NT) F[(idx % TS) * LDS + idx / TS] = X[(idx / TS) * LDS + idx % TS];
+  __syncthreads();
+  Acc pacc;
+  acc_zero(pacc);
+  tile_mma<false>(pacc, X, F);
+  double* P = p.tip_part + (size_t)(i * p.g.B + col) * TS * TS;
+#pragma unroll
+  for (int ii = 0; ii < 2; ++ii)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) P[acc_row(ii) * TS + acc_col(q)] = pacc.v[ii][q];
+}
+
 // Shared memory of the FP64 factor task: 4 tiles (K-loop double buffer; the target X
 // and the diagonal factor F alias its first two, used only before / after the loop),
 // TS pivots, and the wait flag.
@@ -195,7 +227,7 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
       acc_from_smem(acc, X);
       bool ok = true;
       for (int k = 0; k < g.nt * g.B && ok; ++k) {
-        ok = cta_wait(c, c.flags + g.fR(k / g.B, k % g.B), nullptr, &s_ok);
+        ok = cta_wait_plus(c, c.flags + g.fR(k / g.B, k % g.B), 1, &s_ok);   // partial written
         if (!ok) break;
         const double* P = p.tip_part + (size_t)k * TS * TS;
 #pragma unroll
@@ -316,29 +348,21 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
 
     // Off-diagonal targets: X <- X * D_i(col,col)^{-T}.
     if (!load_diag_factor(p, i, col, F, &s_ok)) return false;
-    tile_diag_recip(F, vec);
-    smem_trsm_rlt(X, F, vec);
+    offdiag_trsm(X, F, sm + 2 * TILE_SMEM, vec, type == FT_ARW, g.a);
     tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
     if (type == FT_OFFD) {
       // The factor's strict upper triangle is zero: clear the mirrored tile.
       const Tile up = btile(Dblk(p, i), g, col, r);
       tile_store_zero(const_cast<double*>(up.p), g.b, up.rows, up.cols);
     }
-    if (type == FT_ARW) {
-      // Partial tip update P = X X^T, consumed in order by the tip task.
-      __syncthreads();
-      for (int idx = threadIdx.x; idx < TS * TS; idx += NT) F[(idx % TS) * LDS + idx / TS] = X[(idx / TS) * LDS + idx % TS];
-      __syncthreads();
-      Acc pacc;
-      acc_zero(pacc);
-      tile_mma<false>(pacc, X, F);
-      double* P = p.tip_part + (size_t)(i * g.B + col) * TS * TS;
-#pragma unroll
-      for (int ii = 0; ii < 2; ++ii)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) P[acc_row(ii) * TS + acc_col(q)] = pacc.v[ii][q];
-    }
     cta_publish(c, tgt_flag);
+    if (type == FT_ARW) {
+      // The next arrow tile of the row needs this one: the tip partial P = X X^T comes
+      // after the publication and raises the flag by one when written (the tip task
+      // consumes the partials in order).
+      arrow_tip_partial(p, i, col, X, F);
+      cta_raise(tgt_flag, 1);
+    }
     trace_task(c, t, type, t_task0);
   }
   return true;
@@ -409,7 +433,7 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
       acc_from_smem(acc, X);
       bool ok = true;
       for (int k = 0; k < g.nt * g.B && ok; ++k) {
-        ok = cta_wait(c, c.flags + g.fR(k / g.B, k % g.B), nullptr, &s_ok);
+        ok = cta_wait_plus(c, c.flags + g.fR(k / g.B, k % g.B), 1, &s_ok);   // partial written
         if (!ok) break;
         const double* P = p.tip_part + (size_t)k * TS * TS;
 #pragma unroll
@@ -607,27 +631,16 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
     __syncthreads();
     tile_pad_identity(F, g.vrows(col));
     __syncthreads();
-    tile_diag_recip(F, vec);
-    smem_trsm_rlt(X, F, vec);
+    offdiag_trsm(X, F, reinterpret_cast<double*>(stages), vec, type == FT_ARW, g.a);
     trace_mark(c, t, 2);   // triangular solve done
     tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
     oz_store_digits(p.digits + (size_t)tgt_slot * OZ_TILE, X, tgt.rows, tgt.cols, erow_t);
     trace_mark(c, t, 3);   // tile and digits written
-    if (type == FT_ARW) {
-      // tip partial P = X X^T in FP64 (consumed in order by the tip task)
-      __syncthreads();
-      for (int idx = threadIdx.x; idx < TS * TS; idx += NT) F[(idx % TS) * LDS + idx / TS] = X[(idx / TS) * LDS + idx % TS];
-      __syncthreads();
-      Acc pacc;
-      acc_zero(pacc);
-      tile_mma<false>(pacc, X, F);
-      double* P = p.tip_part + (size_t)(i * g.B + col) * TS * TS;
-#pragma unroll
-      for (int ii = 0; ii < 2; ++ii)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) P[acc_row(ii) * TS + acc_col(q)] = pacc.v[ii][q];
-    }
     cta_publish(c, c.flags + tgt_slot);
+    if (type == FT_ARW) {   // tip partial after the publication, as in factor_fp64_task
+      arrow_tip_partial(p, i, col, X, F);
+      cta_raise(c.flags + tgt_slot, 1);
+    }
     if (type == FT_OFFD) {
       // The factor's strict upper triangle is zero: clear the mirrored tile (read by
       // no task of the factorization, so after the publication).

@@ -17,7 +17,7 @@ __global__ void __launch_bounds__(NT, 1) k_selinv(SelinvArgs p) {
 }
 
 // ---- pre-pass: G tiles and the diagonal inverses ------------------------------------
-// "column c is not after column k" for the register layout of smem_potrf (c = g + 4q).
+// "column c is not after column k" for the register layout of the tile routines (c = g + 4q).
 __device__ __forceinline__ bool col_upto(int q, int k, int g) { return !col_after(q, k, g); }
 
 // X <- X W with W lower triangular (rows of X: lane, columns: warp + 4 q).
