@@ -526,65 +526,79 @@ template <int N> __device__ __forceinline__ void nbar_sync_n(int id) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(N) : "memory");
 }
 
-// Barrier ids of smem_potrf: POTRF_BAR_L + (j & 7) hands pivot column j from the pivot
-// warp to the three update warps (NT threads); POTRF_BAR_C + (j & 3) hands column j+2,
+// Barrier ids of smem_potrf: POTRF_BAR_L + (j & 7) hands pivot j from the pivot warp
+// to the three update warps (NT threads); POTRF_BAR_C + (j & 3) hands column j+2,
 // updated through pivot j, from its owner to the pivot warp (64 threads).
 constexpr int POTRF_BAR_L = 1, POTRF_BAR_C = 9;
+
+// 1/d with the third-order refinement in three dependent FMAs (for a chain that counts
+// FP64 instructions): e = 1 - d y, y <- y + y (e + e^2).
+__device__ __forceinline__ double rcp3_fma(double d) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(d));
+  const double e = fma(-d, y, 1.0);
+  return fma(y, fma(e, e, e), y);
+}
 
 // Update warp W (1..3) of smem_potrf: owns columns c = W + 1 + 3q (q = 0..9) in
 // registers, lane = row.  For every pivot j it first applies pivot j to column j+2 if
 // it owns it and hands that column to the pivot warp, then applies pivot j to its later
-// columns.  All column tests are compile-time, so no predicated-off FMA is issued.
+// columns: a_rc -= w_rj u_cj (w_rj = u_rj / d_j from the pivot warp's ring, u_cj from
+// S).  All column tests are compile-time, so no predicated-off FMA is issued.
 template <int W>
-__device__ __forceinline__ void potrf_update_warp(double* S, int r) {
+__device__ __forceinline__ void potrf_update_warp(double* S, const double (*wring)[TS], int r) {
   double acc[10];
 #pragma unroll
   for (int q = 0; q < 10; ++q) acc[q] = S[r * LDS + W + 1 + 3 * q];
 #pragma unroll
   for (int j = 0; j < TS - 2; ++j) {
     nbar_sync(POTRF_BAR_L + (j & 7));
-    const double lj = S[r * LDS + j];   // l_rj
+    const double wj = wring[j & 7][r];
     if (j + 1 >= W && (j + 1 - W) % 3 == 0) {
       const int q = (j + 1 - W) / 3;   // column j + 2
-      acc[q] = fma(-lj, S[(j + 2) * LDS + j], acc[q]);
+      acc[q] = fma(-wj, S[(j + 2) * LDS + j], acc[q]);
       S[r * LDS + j + 2] = acc[q];
       nbar_arrive_n<64>(POTRF_BAR_C + (j & 3));
     }
 #pragma unroll
     for (int q = 0; q < 10; ++q)
-      if (W + 1 + 3 * q > j + 2) acc[q] = fma(-lj, S[(W + 1 + 3 * q) * LDS + j], acc[q]);
+      if (W + 1 + 3 * q > j + 2) acc[q] = fma(-wj, S[(W + 1 + 3 * q) * LDS + j], acc[q]);
   }
 }
 
 // In-place lower Cholesky of S (TS x TS; entries past n must already be identity).
 // Returns 0, or the 1-based column of the first non-positive (or NaN) pivot (the
 // tile then holds NaNs).  The strict upper triangle is zeroed.
-// Warp 0 does nothing but the pivot chain: for pivot k it takes column k, already
-// updated through pivot k-2 by its owner, applies pivot k-1 itself (it holds l_{:,k-1}
-// in registers, so the multiplier l_{k,k-1} is one shuffle), forms y = 1/sqrt(d) and
-// l_rk = a_rk y (l_kk = d y) and publishes the column to S.  Warps 1-3 apply every
-// pivot to the later columns (potrf_update_warp), the column that the pivot warp needs
-// next first.  Every entry receives its updates in pivot order with the same FMAs as a
-// plain right-looking sweep, so the result does not depend on this split.  The pivot
-// warp's FP64 unit serves only the chain (one FMA, the refinement of rsqrt, one
-// multiply per pivot), and the trailing updates run on the other three sub-partitions.
-// Barrier ids rotate over 8 (pivot columns) and 4 (look-ahead columns): before the
-// pivot warp publishes pivot p+8, each update warp has handed it one of columns
-// p+6 .. p+8 and so consumed pivot p+4; the pivot warp consumes look-ahead column p
-// before it can publish the pivot that look-ahead column p+4 needs.
+// The elimination runs in the square-root-free form S = U D^-1 U^T (u_rk: column k
+// after pivots 0..k-1, d_k = u_kk), and L = U D^{-1/2} is formed at the end, all
+// columns at once.  Warp 0 does nothing but the pivot chain: for pivot k it takes
+// column k, already updated through pivot k-2 by its owner, applies pivot k-1 itself
+// (it holds w_{:,k-1} = u_{:,k-1} / d_{k-1} in registers, the multiplier u_{k,k-1} is
+// one shuffle), stores u_{:,k} to S, forms 1/d_k and w_{:,k}, and hands w_{:,k} to the
+// update warps through an eight-slot ring.  That is five FP64 instructions per pivot on
+// the chain (GB300 issues one FP64 warp instruction per ~64 cycles on a sub-partition),
+// against seven for l_rk = a_rk / sqrt(d_k) with a refined reciprocal square root.
+// Warps 1-3 apply every pivot to the later columns (potrf_update_warp), the column that
+// the pivot warp needs next first; each entry receives its updates in pivot order.
+// Barrier ids rotate over 8 (pivots) and 4 (look-ahead columns): before the pivot warp
+// publishes pivot p+8 (and overwrites ring slot p & 7), each update warp has handed it
+// one of columns p+6 .. p+8 and so consumed pivot p+4; the pivot warp consumes
+// look-ahead column p before it can publish the pivot that look-ahead column p+4 needs.
 static __device__ int smem_potrf(double* S) {
   __shared__ int s_info;
+  __shared__ double s_wring[8][TS];
+  __shared__ double s_y[TS];
   const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
   if (threadIdx.x == 0) s_info = TS + 1;
   __syncthreads();
   if (g == 0) {
-    const double a0 = S[r * LDS];
+    const double u0 = S[r * LDS];       // column 0 of U is column 0 of S
     const double a1 = S[r * LDS + 1];   // column 1 takes no update before pivot 0
-    const double d0 = __shfl_sync(0xffffffffu, a0, 0);
-    const double y0 = rsqrt3(d0);
-    double lp = a0 * y0;   // row 0 holds d itself: l_00 = d y, l_r0 = a_r0 y
-    S[r * LDS] = lp;
-    if (r == 0 && !(d0 > 0.0)) atomicMin(&s_info, 1);
+    double dk = __shfl_sync(0xffffffffu, u0, 0);   // lane k keeps d_k
+    if (r == 0 && !(dk > 0.0)) atomicMin(&s_info, 1);
+    double up = u0;
+    double wp = u0 * rcp3_fma(dk);
+    s_wring[0][r] = wp;
     nbar_arrive(POTRF_BAR_L);
 #pragma unroll
     for (int k = 1; k < TS; ++k) {
@@ -595,22 +609,36 @@ static __device__ int smem_potrf(double* S) {
         nbar_sync_n<64>(POTRF_BAR_C + ((k - 2) & 3));
         a = S[r * LDS + k];
       }
-      const double m = __shfl_sync(0xffffffffu, lp, k);   // l_{k,k-1}
-      a = fma(-lp, m, a);
+      const double ub = __shfl_sync(0xffffffffu, up, k);   // u_{k,k-1}
+      a = fma(-wp, ub, a);
+      const double u = (r >= k) ? a : 0.0;
       const double d = __shfl_sync(0xffffffffu, a, k);
-      const double y = rsqrt3(d);
-      const double l = (r >= k) ? a * y : 0.0;   // lane k holds d = a: one multiply for l_kk and l_rk
-      S[r * LDS + k] = l;
+      if (r == k) dk = d;
+      S[r * LDS + k] = u;
       if (r == 0 && !(d > 0.0)) atomicMin(&s_info, k + 1);
-      if (k < TS - 2) nbar_arrive(POTRF_BAR_L + (k & 7));
-      lp = l;
+      if (k < TS - 1) {
+        const double w = u * rcp3_fma(d);
+        if (k < TS - 2) {
+          s_wring[k & 7][r] = w;
+          nbar_arrive(POTRF_BAR_L + (k & 7));
+        }
+        up = u;
+        wp = w;
+      }
     }
+    s_y[r] = rsqrt3(dk);
   } else if (g == 1) {
-    potrf_update_warp<1>(S, r);
+    potrf_update_warp<1>(S, s_wring, r);
   } else if (g == 2) {
-    potrf_update_warp<2>(S, r);
+    potrf_update_warp<2>(S, s_wring, r);
   } else {
-    potrf_update_warp<3>(S, r);
+    potrf_update_warp<3>(S, s_wring, r);
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {   // L = U D^{-1/2}: warp g scales columns g + 4q
+    const int cc = g + 4 * q;
+    S[r * LDS + cc] *= s_y[cc];
   }
   __syncthreads();
   const int info = s_info;
