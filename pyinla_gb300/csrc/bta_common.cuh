@@ -540,29 +540,53 @@ __device__ __forceinline__ double rcp3_fma(double d) {
   return fma(y, fma(e, e, e), y);
 }
 
-// Update warp W (1..3) of smem_potrf: owns columns c = W + 1 + 3q (q = 0..9) in
-// registers, lane = row.  For every pivot j it first applies pivot j to column j+2 if
-// it owns it and hands that column to the pivot warp, then applies pivot j to its later
-// columns: a_rc -= w_rj u_cj (w_rj = u_rj / d_j from the pivot warp's ring, u_cj from
-// S).  All column tests are compile-time, so no predicated-off FMA is issued.
+// Register slots of the update warps of smem_potrf.  Slot s < 14 holds column s + 2
+// (lane = row); slot s >= 14 holds the pair of columns c0 = 16 + 2 (s - 14) and c0 + 1,
+// rows 16..31 only (lane l: row 16 + (l & 15), column c0 + (l >> 4)): a column c needs
+// rows c..31, so for c >= 16 half a warp covers it.  Owners rotate over the three warps
+// (any seven consecutive columns have all three owners).
+constexpr int POTRF_SLOTS = 22, POTRF_FULL = 14;
+__host__ __device__ constexpr int potrf_slot_col(int s) { return s < POTRF_FULL ? s + 2 : 16 + 2 * (s - POTRF_FULL); }
+__host__ __device__ constexpr int potrf_slot_last(int s) { return s < POTRF_FULL ? s + 2 : 17 + 2 * (s - POTRF_FULL); }
+__host__ __device__ constexpr int potrf_slot_owner(int s) { return s < POTRF_FULL ? s % 3 : (s - 12) % 3; }
+
+// Update warp W (0..2; warp W + 1) of smem_potrf.  For every pivot j it first applies
+// pivot j to column j + 2 if it owns it and hands that column to the pivot warp, then
+// applies pivot j to its slots whose columns come later: a_rc -= w_rj u_cj (w_rj =
+// u_rj / d_j from the pivot warp's ring, u_cj from S).  Slot tests are compile-time, so
+// no predicated-off FMA is issued.
 template <int W>
-__device__ __forceinline__ void potrf_update_warp(double* S, const double (*wring)[TS], int r) {
-  double acc[10];
+__device__ __forceinline__ void potrf_update_warp(double* S, const double (*wring)[TS], int lane) {
+  const int prow = 16 + (lane & 15), half = lane >> 4;
+  double acc[POTRF_SLOTS];
 #pragma unroll
-  for (int q = 0; q < 10; ++q) acc[q] = S[r * LDS + W + 1 + 3 * q];
+  for (int s = 0; s < POTRF_SLOTS; ++s)
+    if (potrf_slot_owner(s) == W)
+      acc[s] = s < POTRF_FULL ? S[lane * LDS + potrf_slot_col(s)] : S[prow * LDS + potrf_slot_col(s) + half];
 #pragma unroll
   for (int j = 0; j < TS - 2; ++j) {
     nbar_sync(POTRF_BAR_L + (j & 7));
-    const double wj = wring[j & 7][r];
-    if (j + 1 >= W && (j + 1 - W) % 3 == 0) {
-      const int q = (j + 1 - W) / 3;   // column j + 2
-      acc[q] = fma(-wj, S[(j + 2) * LDS + j], acc[q]);
-      S[r * LDS + j + 2] = acc[q];
-      nbar_arrive_n<64>(POTRF_BAR_C + (j & 3));
+    const double wf = wring[j & 7][lane];   // w of this lane's row (full slots)
+    const double wp = wring[j & 7][prow];   // w of the pair slots' row
+#pragma unroll
+    for (int s = 0; s < POTRF_SLOTS; ++s) {   // the look-ahead column j + 2 first
+      if (potrf_slot_owner(s) != W) continue;
+      if (s < POTRF_FULL && potrf_slot_col(s) == j + 2) {
+        acc[s] = fma(-wf, S[(j + 2) * LDS + j], acc[s]);
+        S[lane * LDS + j + 2] = acc[s];
+        nbar_arrive_n<64>(POTRF_BAR_C + (j & 3));
+      } else if (s >= POTRF_FULL && (potrf_slot_col(s) == j + 2 || potrf_slot_col(s) + 1 == j + 2)) {
+        acc[s] = fma(-wp, S[(potrf_slot_col(s) + half) * LDS + j], acc[s]);
+        if (potrf_slot_col(s) + half == j + 2) S[prow * LDS + j + 2] = acc[s];
+        nbar_arrive_n<64>(POTRF_BAR_C + (j & 3));
+      }
     }
 #pragma unroll
-    for (int q = 0; q < 10; ++q)
-      if (W + 1 + 3 * q > j + 2) acc[q] = fma(-wj, S[(W + 1 + 3 * q) * LDS + j], acc[q]);
+    for (int s = 0; s < POTRF_SLOTS; ++s) {
+      if (potrf_slot_owner(s) != W || potrf_slot_last(s) <= j + 2) continue;
+      if (s < POTRF_FULL) acc[s] = fma(-wf, S[potrf_slot_col(s) * LDS + j], acc[s]);
+      else if (potrf_slot_col(s) > j + 2) acc[s] = fma(-wp, S[(potrf_slot_col(s) + half) * LDS + j], acc[s]);
+    }
   }
 }
 
@@ -582,8 +606,9 @@ __device__ __forceinline__ void potrf_update_warp(double* S, const double (*wrin
 // the pivot warp needs next first; each entry receives its updates in pivot order.
 // Barrier ids rotate over 8 (pivots) and 4 (look-ahead columns): before the pivot warp
 // publishes pivot p+8 (and overwrites ring slot p & 7), each update warp has handed it
-// one of columns p+6 .. p+8 and so consumed pivot p+4; the pivot warp consumes
-// look-ahead column p before it can publish the pivot that look-ahead column p+4 needs.
+// one of columns p+2 .. p+8 (seven consecutive columns have all three owners) and so
+// consumed pivot p; the pivot warp consumes look-ahead column p before it can publish
+// the pivot that look-ahead column p+4 needs.
 static __device__ int smem_potrf(double* S) {
   __shared__ int s_info;
   __shared__ double s_wring[8][TS];
@@ -628,11 +653,11 @@ static __device__ int smem_potrf(double* S) {
     }
     s_y[r] = rsqrt3(dk);
   } else if (g == 1) {
-    potrf_update_warp<1>(S, s_wring, r);
+    potrf_update_warp<0>(S, s_wring, r);
   } else if (g == 2) {
-    potrf_update_warp<2>(S, s_wring, r);
+    potrf_update_warp<1>(S, s_wring, r);
   } else {
-    potrf_update_warp<3>(S, s_wring, r);
+    potrf_update_warp<2>(S, s_wring, r);
   }
   __syncthreads();
 #pragma unroll
