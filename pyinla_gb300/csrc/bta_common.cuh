@@ -596,7 +596,8 @@ __device__ __forceinline__ void potrf_update_warp(double* S, const double (*wrin
 // The elimination runs in the square-root-free form S = U D^-1 U^T (u_rk: column k
 // after pivots 0..k-1, d_k = u_kk), and L = U D^{-1/2} is formed at the end, all
 // columns at once.  Warp 0 does nothing but the pivot chain: for pivot k it takes
-// column k, already updated through pivot k-2 by its owner, applies pivot k-1 itself
+// column k, already updated through pivot k-2 by its owner (awaited and loaded while
+// pivot k-1's reciprocal was formed), applies pivot k-1 itself
 // (it holds w_{:,k-1} = u_{:,k-1} / d_{k-1} in registers, the multiplier u_{k,k-1} is
 // one shuffle), stores u_{:,k} to S, forms 1/d_k and w_{:,k}, and hands w_{:,k} to the
 // update warps through an eight-slot ring.  That is five FP64 instructions per pivot on
@@ -621,34 +622,33 @@ static __device__ int smem_potrf(double* S) {
     const double a1 = S[r * LDS + 1];   // column 1 takes no update before pivot 0
     double dk = __shfl_sync(0xffffffffu, u0, 0);   // lane k keeps d_k
     if (r == 0 && !(dk > 0.0)) atomicMin(&s_info, 1);
-    double up = u0;
     double wp = u0 * rcp3_fma(dk);
     s_wring[0][r] = wp;
     nbar_arrive(POTRF_BAR_L);
+    double a = a1;
+    double ub = __shfl_sync(0xffffffffu, u0, 1);   // u_{1,0}
 #pragma unroll
     for (int k = 1; k < TS; ++k) {
-      double a;
-      if (k == 1) {
-        a = a1;
-      } else {
-        nbar_sync_n<64>(POTRF_BAR_C + ((k - 2) & 3));
-        a = S[r * LDS + k];
-      }
-      const double ub = __shfl_sync(0xffffffffu, up, k);   // u_{k,k-1}
-      a = fma(-wp, ub, a);
+      a = fma(-wp, ub, a);   // column k through pivot k-1
       const double u = (r >= k) ? a : 0.0;
       const double d = __shfl_sync(0xffffffffu, a, k);
       if (r == k) dk = d;
       S[r * LDS + k] = u;
       if (r == 0 && !(d > 0.0)) atomicMin(&s_info, k + 1);
       if (k < TS - 1) {
-        const double w = u * rcp3_fma(d);
+        const double sk = rcp3_fma(d);
+        // Column k+1, updated through pivot k-1 by its owner, is awaited and loaded
+        // while this pivot's reciprocal is formed, off the chain.
+        nbar_sync_n<64>(POTRF_BAR_C + ((k - 1) & 3));
+        const double an = S[r * LDS + k + 1];
+        const double w = u * sk;
+        ub = __shfl_sync(0xffffffffu, u, k + 1);   // u_{k+1,k}
         if (k < TS - 2) {
           s_wring[k & 7][r] = w;
           nbar_arrive(POTRF_BAR_L + (k & 7));
         }
-        up = u;
         wp = w;
+        a = an;
       }
     }
     s_y[r] = rsqrt3(dk);
