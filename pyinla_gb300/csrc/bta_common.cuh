@@ -491,12 +491,12 @@ __device__ __forceinline__ void tile_diag_recip(const double* F, double* rd) {
 }
 
 // ---- register-resident tile factorization and triangular solves ------------------
-// Thread (lane r, warp g) holds row r of the tile at the eight columns c = g + 4q
-// (q = 0..7) in registers, so every FP64 instruction has 32 useful lanes.  Columns
-// are processed in order; the warp owning the current column finalises it and
-// publishes it through shared memory (the triangular solves with one CTA barrier per
-// column, the Cholesky with named barriers between the owner and the other warps), and
-// every warp then updates its later columns with one FMA per element.  The loops over
+// In the triangular solves, thread (lane r, warp g) holds row r of the tile at the
+// eight columns c = g + 4q (q = 0..7) in registers, so every FP64 instruction has 32
+// useful lanes.  Columns are processed in order; the warp owning the current column
+// finalises it and publishes it through shared memory with one CTA barrier per column,
+// and every warp then updates its later columns with one FMA per element (the
+// Cholesky, smem_potrf below, splits the work differently).  The loops over
 // columns and register slots are fully unrolled: the conditions "column c = g + 4q
 // is after column j" are written as a compile-time part plus a runtime part that
 // only the one boundary slot needs, because an FP64 instruction issued under a false
