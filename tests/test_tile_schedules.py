@@ -1,4 +1,6 @@
-"""CPU checks of the tile Cholesky's warp schedule (csrc/bta_common.cuh, smem_potrf).
+"""CPU checks of the tile-level schedules and recurrences of the dataflow kernels.
+
+The tile Cholesky's warp schedule (csrc/bta_common.cuh, smem_potrf):
 
 The kernel splits a 32 x 32 Cholesky between a pivot warp and three update warps that
 hold columns in register slots; pivots travel through an eight-slot ring of shared
@@ -7,6 +9,9 @@ constants from the CUDA source, check the invariant that makes the rotation safe
 replay the kernel's exact sequence of operations (lane by lane, with the same slot
 layout and hand-over order) against numpy's Cholesky.  They run on the CPU and test
 the schedule, not the GPU code's arithmetic (the GPU parity tests do that).
+
+The selected inversion's tile recurrences (csrc/bta_selinv_task.cuh) are checked on a
+dense matrix, including the two-product form of a diagonal-chain step.
 """
 import re
 
@@ -131,3 +136,40 @@ def test_replayed_schedule_is_cholesky(seed):
     L = _replay(A)
     np.testing.assert_allclose(L, np.linalg.cholesky(A), rtol=0, atol=1e-12 * np.abs(A).max())
     assert not np.triu(L, 1).any()
+
+
+def test_selected_inversion_tile_recurrences():
+    """The tile Takahashi recurrences of the selected inversion (csrc/bta_selinv_task.cuh)
+    on a dense SPD matrix cut into 8 x 8 tiles, with G(l, c) = F(l, c) F(c, c)^-1 and
+    C_c = F(c, c)^-T F(c, c)^-1:
+      Sigma(j, c) = -sum_{l>c} Sigma(j, l) G(l, c)            (j > c)
+      Sigma(c, c) = C_c - sum_{l>c} Sigma(l, c)^T G(l, c)
+    and the two-product form of one column step of the diagonal chain: with
+    G = G(c, c-1) and P = -sum_{l>c} Sigma(c, l) G(l, c-1) (the partial sum of the
+    sub-diagonal tile), Sigma(c, c-1) = P - Sigma(c, c) G and
+      Sigma(c-1, c-1) = C_{c-1} - Z' - P^T G + G^T Sigma(c, c) G,
+    Z' = sum_{l>c} Sigma(l, c-1)^T G(l, c-1)."""
+    t, nb = 8, 6
+    rng = np.random.default_rng(7)
+    M = rng.standard_normal((t * nb, t * nb))
+    A = M @ M.T + t * nb * np.eye(t * nb)
+    F = np.linalg.cholesky(A)
+    S = np.linalg.inv(A)
+    blk = lambda X, r, c: X[r * t:(r + 1) * t, c * t:(c + 1) * t]
+    Finv = [np.linalg.inv(blk(F, c, c)) for c in range(nb)]
+    G = {(l, c): blk(F, l, c) @ Finv[c] for c in range(nb) for l in range(c + 1, nb)}
+    C = [Finv[c].T @ Finv[c] for c in range(nb)]
+    tol = 1e-12 * np.abs(S).max()
+    for c in range(nb):
+        for j in range(c + 1, nb):
+            rhs = -sum(blk(S, j, l) @ G[(l, c)] for l in range(c + 1, nb))
+            np.testing.assert_allclose(blk(S, j, c), rhs, atol=tol)
+        diag = C[c] - sum((blk(S, l, c).T @ G[(l, c)] for l in range(c + 1, nb)), np.zeros((t, t)))
+        np.testing.assert_allclose(blk(S, c, c), diag, atol=tol)
+    for c in range(1, nb):
+        Gc = G[(c, c - 1)]
+        P = -sum((blk(S, c, l) @ G[(l, c - 1)] for l in range(c + 1, nb)), np.zeros((t, t)))
+        np.testing.assert_allclose(blk(S, c, c - 1), P - blk(S, c, c) @ Gc, atol=tol)
+        Zp = sum((blk(S, l, c - 1).T @ G[(l, c - 1)] for l in range(c + 1, nb)), np.zeros((t, t)))
+        two_product = C[c - 1] - Zp - P.T @ Gc + Gc.T @ blk(S, c, c) @ Gc
+        np.testing.assert_allclose(blk(S, c - 1, c - 1), two_product, atol=tol)
