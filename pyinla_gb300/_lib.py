@@ -44,11 +44,6 @@ SIGNATURES = {
     "gbta_version": (_c_int, []),
     "gbta_kernel_launches": (_c_ll, []),
     "gbta_probe_fp64_peak": (_c_int, [_c_int, _dp]),
-    "gbta_probe_tiles": (_c_int, [_c_int, _vp]),
-    "gbta_probe_umma": (_c_int, [_c_int, _vp, _vp]),
-    "gbta_probe_tmem_pairs": (_c_int, [_vp]),
-    "gbta_probe_latencies": (_c_int, [_vp]),
-    "gbta_probe_tensor_rates": (_c_int, [_c_int, _vp]),
     "gbta_last_error": (ctypes.c_char_p, []),
     "gbta_geometry": (_c_int, [_vp, ctypes.POINTER(_c_int), ctypes.POINTER(_c_int), ctypes.POINTER(_c_int),
                                ctypes.POINTER(_vp)]),
@@ -62,6 +57,8 @@ SIGNATURES = {
     "gbta_set_ctas_per_sm": (_c_int, [_vp, _c_int]),
     "gbta_set_trace": (_c_int, [_vp, _c_int]),
     "gbta_get_trace": (_c_ll, [_vp, _vp, _c_ll]),
+    "gbta_set_kernel_timing": (_c_int, [_vp, _c_int]),
+    "gbta_kernel_ms": (_c_int, [_vp, _dp]),
     "gbta_workspace_bytes": (ctypes.c_size_t, [_vp]),
     "gbta_status": (_c_int, [_vp]),
     "gbta_pobtaf": (_c_int, [_vp, _vp, _vp, _vp, _vp]),

@@ -18,7 +18,7 @@ CSRC = HERE / "csrc"
 BUILD = HERE / "_build"
 LIB = HERE / "libpyinla_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["bta_api.cu", "bta_factor.cu", "bta_solve.cu", "bta_selinv.cu", "bta_logdet.cu", "bta_sparse.cu", "bta_assemble.cu", "bta_probe.cu", "bta_noalloc.cu", "bta_factor_oz.cu", "bta_selinv_oz.cu", "bta_batch.cu", "bta_probe_tiles.cu", "bta_probe_umma.cu", "bta_marginals.cu", "bta_laplace.cu"]
+SOURCES = ["bta_api.cu", "bta_factor.cu", "bta_solve.cu", "bta_selinv.cu", "bta_logdet.cu", "bta_sparse.cu", "bta_assemble.cu", "bta_probe.cu", "bta_noalloc.cu", "bta_factor_oz.cu", "bta_selinv_oz.cu", "bta_batch.cu", "bta_marginals.cu", "bta_laplace.cu"]
 
 
 def nvcc() -> str:

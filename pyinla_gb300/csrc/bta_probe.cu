@@ -1,4 +1,4 @@
-// FP64 peak probe and kernel-launch accounting.
+// FP64 peak probe, launch-shape helpers and kernel-launch accounting.
 //
 // GB300 has no FP64 tensor-core rate worth using (its DMMA path measures below the
 // CUDA-core DFMA rate), so the roofline denominator of the FP64 kernels is the DFMA
@@ -95,95 +95,5 @@ extern "C" int gbta_probe_fp64_peak(int iters, double* tflops) {
   gbta::count_launches(2);
   if (e != cudaSuccess) return gbta_set_error(GBTA_ERR_CUDA, cudaGetErrorString(e));
   *tflops = 2.0 * 8.0 * (double)iters * blocks * threads / (ms * 1e-3) / 1e12;
-  return GBTA_OK;
-}
-
-// Chip-wide throughput of the candidate arithmetic paths for FP64 tile products,
-// 2 CTAs of 256 threads per SM, register-only loops timed with CUDA events:
-// [0] DMMA mma.sync.m8n8k4.f64, [1] HMMA mma.sync.m16n8k16 f16 -> f32, [2] FFMA.
-namespace gbta {
-__global__ void __launch_bounds__(256) k_rate_dmma(double* out, int iters) {
-  double a = 1.0 + threadIdx.x * 1e-9, b = 0.5;
-  double c[8][2];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) c[k][0] = c[k][1] = k;
-  for (int i = 0; i < iters; ++i) {
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
-                   : "+d"(c[k][0]), "+d"(c[k][1])
-                   : "d"(a), "d"(b));
-  }
-  double s = 0;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) s += c[k][0] + c[k][1];
-  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
-}
-__global__ void __launch_bounds__(256) k_rate_hmma(double* out, int iters) {
-  const unsigned a0 = 0x3c003c00u, b0 = 0x3c003c00u;   // fp16 ones
-  float c[8][4];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) c[k][0] = c[k][1] = c[k][2] = c[k][3] = 0.f;
-  for (int i = 0; i < iters; ++i) {
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-      asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                   "{%0,%1,%2,%3};"
-                   : "+f"(c[k][0]), "+f"(c[k][1]), "+f"(c[k][2]), "+f"(c[k][3])
-                   : "r"(a0), "r"(a0), "r"(a0), "r"(a0), "r"(b0), "r"(b0));
-  }
-  float s = 0;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) s += c[k][0] + c[k][1] + c[k][2] + c[k][3];
-  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
-}
-__global__ void __launch_bounds__(256) k_rate_ffma(double* out, int iters) {
-  float x[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) x[k] = threadIdx.x * 1e-6f + k;
-  for (int i = 0; i < iters; ++i) {
-#pragma unroll
-    for (int k = 0; k < 8; ++k) x[k] = fmaf(x[k], 0.9999f, 1e-7f);
-  }
-  float s = 0;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) s += x[k];
-  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
-}
-}  // namespace gbta
-
-extern "C" int gbta_probe_tensor_rates(int iters, double* tflops) {
-  if (!tflops || iters < 1) return gbta_set_error(GBTA_ERR_ARG, "probe: need iters >= 1 and an output");
-  int dev = 0, nsm = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    return gbta_set_error(GBTA_ERR_CUDA, "probe: no device");
-  const int blocks = nsm * 2, threads = 256;
-  double* out = nullptr;
-  if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess)
-    return gbta_set_error(GBTA_ERR_ALLOC, "probe: cudaMalloc failed");
-  cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
-  // flops per thread and iteration: DMMA 8 x (8*8*4*2)/32, HMMA 8 x (16*8*16*2)/32, FFMA 8 x 2
-  const double per_thread_iter[3] = {8.0 * 512 / 32, 8.0 * 4096 / 32, 16.0};
-  cudaError_t err = cudaSuccess;
-  for (int k = 0; k < 3 && err == cudaSuccess; ++k) {
-    for (int rep = 0; rep < 2; ++rep) {   // the first run warms up
-      cudaEventRecord(e0);
-      if (k == 0) gbta::k_rate_dmma<<<blocks, threads>>>(out, iters);
-      if (k == 1) gbta::k_rate_hmma<<<blocks, threads>>>(out, iters);
-      if (k == 2) gbta::k_rate_ffma<<<blocks, threads>>>(out, iters);
-      cudaEventRecord(e1);
-      err = cudaEventSynchronize(e1);
-    }
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    tflops[k] = per_thread_iter[k] * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
-  }
-  gbta::count_launches(6);
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
-  cudaFree(out);
-  if (err != cudaSuccess) return gbta_set_error(GBTA_ERR_CUDA, cudaGetErrorString(err));
   return GBTA_OK;
 }
