@@ -5,16 +5,22 @@
 // outside it (custom-call hooks of other frameworks, long-running services that
 // reserve their whole arena up front), and latency-sensitive loops where the implicit
 // device-wide synchronisation of cudaMalloc/cudaFree is not acceptable.  For them,
-// gbta_pobtaf_noalloc runs the same dataflow factorization kernel as gbta_pobtaf, with
-// every piece of its scratch -- control words, per-tile ready flags, the task list and
-// the arrow-tip partial products -- placed in one file-scope __device__ array of
-// GBTA_NOALLOC_SCRATCH_BYTES (64 MiB).  The caller passes only the block buffers.
+// gbta_pobtaf_noalloc runs the FP64-product dataflow factorization kernel (k_factor),
+// with every piece of its scratch -- control words, per-tile ready flags, the task
+// list and the arrow-tip partial products -- placed in one file-scope __device__ array
+// of GBTA_NOALLOC_SCRATCH_BYTES (64 MiB).  The caller passes only the block buffers.
 //
-// That array exists on every GPU that loads this library and is held until the
-// process exits.  All calls on a device share it and it keeps the previous call's
-// contents: each call clears the part that must start at zero (control words and
-// ready flags) and regenerates the rest, and calls whose work overlaps on the GPU
-// (different streams, or different host threads, at the same time) race on it.
+// The array is part of this file's device module.  The library is built with one
+// module per source file, and CUDA loads modules lazily by default, so the array (and
+// the code of this path) takes device memory when the module is first used on a GPU
+// -- the first call there -- and keeps it until the process exits; with
+// CUDA_MODULE_LOADING=EAGER the load happens at context creation instead.  A caller
+// that reserves a memory pool makes its first call before reserving it.
+//
+// All calls on a device share the array and it keeps the previous call's contents:
+// each call clears the part that must start at zero (control words and ready flags)
+// and regenerates the rest, and calls whose work overlaps on the GPU (different
+// streams, or different host threads, at the same time) race on it.
 //
 // In host code the array's name is only a host-side stand-in, not a device address,
 // so its device address is looked up with cudaGetSymbolAddress, once per device with
@@ -32,9 +38,11 @@ namespace gbta {
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[GBTA_NOALLOC_SCRATCH_BYTES];
 
-// Writes the factorization task list in the order the regular path builds it on the
-// host (bta_api.cu: factor_task_list): per block i, per column c: DIAG, OFFD (r > c),
-// LOW (i < nt-1), ARW (a > 0); then TIP (a > 0).  One thread per (i, c).
+// Writes the factorization task list without the feeder split (no FT_PRE products and
+// no FT_FEEDQ row groups, which k_factor accepts when it is given no feeder flags):
+// per block i, per column c: DIAG, OFFD (r > c), LOW (i < nt-1), ARW (a > 0); then TIP
+// (a > 0).  Every task waits only for tasks earlier in this order.  One thread per
+// (i, c); the offset of column (i, c) is the number of tasks of the columns before it.
 __global__ void k_gen_factor_tasks(Geom g, int4* tasks) {
   const int ic = blockIdx.x * blockDim.x + threadIdx.x;
   if (ic >= g.nt * g.B) return;
@@ -103,8 +111,15 @@ extern "C" int gbta_pobtaf_noalloc(int b, int nt, int a, double* D, double* L, d
       const cudaError_t e = cudaGetSymbolAddress(&g_addr[dev], gbta::g_noalloc_scratch);
       if (e != cudaSuccess) {
         g_addr[dev] = nullptr;
-        return gbta_set_error(GBTA_ERR_CUDA, (std::string("noalloc pobtaf: cudaGetSymbolAddress: ") +
-                                              cudaGetErrorString(e)).c_str());
+        return gbta_set_error(GBTA_ERR_CUDA, (std::string("noalloc pobtaf: loading the library's fixed ") +
+                                              std::to_string((size_t)GBTA_NOALLOC_SCRATCH_BYTES >> 20) +
+                                              " MiB scratch array on this device failed (" + cudaGetErrorString(e) +
+                                              (e == cudaErrorMemoryAllocation
+                                                   ? "): the first call on a device loads it; make that call "
+                                                     "before reserving the device memory pool, or set "
+                                                     "CUDA_MODULE_LOADING=EAGER"
+                                                   : ")"))
+                                                 .c_str());
       }
     }
     base = g_addr[dev];
@@ -142,7 +157,14 @@ extern "C" int gbta_pobtaf_noalloc(int b, int nt, int a, double* D, double* L, d
   lc.stream = st;
   gbta::launch_factor(g, D, L, R, T, a > 0 ? 1 : 0, tasks, (int)ntasks, tip_part, lc);
   gbta::count_launches(1);
-  if ((e = cudaGetLastError()) != cudaSuccess) return gbta_set_error(GBTA_ERR_CUDA, cudaGetErrorString(e));
+  if ((e = cudaGetLastError()) != cudaSuccess)
+    return gbta_set_error(GBTA_ERR_CUDA, (std::string("noalloc pobtaf: launch failed (") + cudaGetErrorString(e) +
+                                          (e == cudaErrorMemoryAllocation
+                                               ? "): loading the factorization kernel's code on its first use "
+                                                 "needs device memory; make the first call before reserving the "
+                                                 "device memory pool, or set CUDA_MODULE_LOADING=EAGER"
+                                               : ")"))
+                                             .c_str());
   int h_ctrl[8] = {0};
   if ((e = cudaMemcpyAsync(h_ctrl, ctrl, sizeof(h_ctrl), cudaMemcpyDeviceToHost, st)) != cudaSuccess ||
       (e = cudaStreamSynchronize(st)) != cudaSuccess)

@@ -1,8 +1,13 @@
-"""GPU test of gbta_pobtaf_noalloc, the factorization for callers that cannot allocate
-device memory (its scratch is a fixed array inside the library).
+"""Tests of gbta_pobtaf_noalloc, the factorization for callers that cannot allocate
+device memory when they factor (hosts with a fixed device-memory pool, loops that
+cannot take cudaMalloc's implicit synchronisation); its scratch is a fixed 64 MiB
+array inside the library.
 
-Collected last on purpose: if it fails, a run that stops at the first failure has
-already run every other test.  Works alone in a fresh process and after the others.
+The GPU tests compare it with gbta_pobtaf on two calls in a row and check that a call
+after the first takes no device memory; a CPU test checks the task count behind
+gbta_noalloc_scratch_bytes against the task list the kernel writes.  Collected last on
+purpose: if a GPU test here fails, a run that stops at the first failure has already
+run every other test.  Works alone in a fresh process and after the others.
 """
 import ctypes
 
@@ -11,8 +16,8 @@ import pytest
 
 from oracle import bta_oracle as orc
 
-pytestmark = pytest.mark.gpu
 RTOL = 1e-10
+TS = 32
 
 
 def relerr(x, y):
@@ -27,6 +32,7 @@ def lib():
     return _lib.load()
 
 
+@pytest.mark.gpu
 @pytest.mark.parametrize("seed,nt,b,a", [(31, 6, 70, 5), (32, 1, 40, 0), (33, 16, 128, 4)])
 def test_noalloc_matches_pobtaf_on_two_calls(lib, seed, nt, b, a):
     import torch
@@ -57,6 +63,7 @@ def test_noalloc_matches_pobtaf_on_two_calls(lib, seed, nt, b, a):
                 assert relerr(g, want) < RTOL, call
 
 
+@pytest.mark.gpu
 def test_noalloc_rejects_oversized_problem(lib):
     from pyinla_gb300 import _lib
 
@@ -66,6 +73,7 @@ def test_noalloc_rejects_oversized_problem(lib):
     assert "scratch" in _lib.last_error()
 
 
+@pytest.mark.gpu
 def test_noalloc_reports_non_spd_row(lib):
     import torch
 
@@ -77,3 +85,74 @@ def test_noalloc_reports_non_spd_row(lib):
     dev = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (D, L, R, T)]
     code = lib.gbta_pobtaf_noalloc(40, 3, 2, *[t.data_ptr() for t in dev], current_stream_ptr())
     assert code == 46, (code, _lib.last_error())
+
+
+@pytest.mark.gpu
+def test_noalloc_call_takes_no_device_memory(lib):
+    """After the first call on the device (which loads the array), a call of a new
+    geometry leaves the device's free memory unchanged."""
+    import torch
+
+    from pyinla_gb300 import _lib
+    from pyinla_gb300.device import current_stream_ptr
+
+    stream = current_stream_ptr()
+    first = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in orc.make_bta_c1(35, nt=2, b=33, a=1)[:4]]
+    assert lib.gbta_pobtaf_noalloc(33, 2, 1, *[t.data_ptr() for t in first], stream) == 0, _lib.last_error()
+    dev = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in orc.make_bta_c1(36, nt=9, b=200, a=7)[:4]]
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    assert lib.gbta_pobtaf_noalloc(200, 9, 7, *[t.data_ptr() for t in dev], stream) == 0, _lib.last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 >= free0, (free0, free1)
+
+
+def plain_factor_tasks(nt, B, a):
+    """The factorization task list without the feeder split, as (kind, i, r, c)."""
+    out = []
+    for i in range(nt):
+        for c in range(B):
+            out.append(("DIAG", i, c, c))
+            out += [("OFFD", i, r, c) for r in range(c + 1, B)]
+            if i < nt - 1:
+                out += [("LOW", i, r, c) for r in range(B)]
+            if a > 0:
+                out.append(("ARW", i, 0, c))
+    if a > 0:
+        out.append(("TIP", 0, 0, 0))
+    return out
+
+
+def kernel_column_offset(nt, B, a, i, c):
+    """Offset of column (i, c)'s first task as k_gen_factor_tasks computes it."""
+    lb = B if nt > 1 else 0
+    ab = 1 if a > 0 else 0
+    per_block = B * (1 + lb + ab) + B * (B - 1) // 2
+    if i == nt - 1 and i > 0:
+        return i * per_block + c * (1 + ab) + c * (B - 1) - c * (c - 1) // 2
+    return i * per_block + c * (1 + lb + ab) + c * (B - 1) - c * (c - 1) // 2
+
+
+def align256(n):
+    return (n + 255) // 256 * 256
+
+
+@pytest.mark.parametrize("nt,b,a", [(1, 40, 0), (1, 70, 5), (6, 70, 0), (6, 70, 5), (3, 32, 1), (16, 128, 4),
+                                    (2, 1, 0)])
+def test_noalloc_task_count_and_offsets(lib, nt, b, a):
+    """CPU: the kernel's per-column offsets tile the plain task list exactly (no gap,
+    no overlap, TIP last), and gbta_noalloc_scratch_bytes sizes exactly that many
+    tasks next to the control words, flags and tip partials."""
+    B = (b + TS - 1) // TS
+    tasks = plain_factor_tasks(nt, B, a)
+    pos = 0
+    for i in range(nt):
+        for c in range(B):
+            assert kernel_column_offset(nt, B, a, i, c) == pos, (i, c)
+            assert tasks[pos] == ("DIAG", i, c, c)
+            pos += 1 + (B - 1 - c) + (B if i < nt - 1 else 0) + (1 if a > 0 else 0)
+    assert pos + (1 if a > 0 else 0) == len(tasks)
+    nflags = (2 * nt - 1) * B * B + nt * B + 1
+    want = align256(8 * 4) + align256(nflags * 4) + align256(len(tasks) * 16) + align256(nt * B * TS * TS * 8)
+    assert lib.gbta_noalloc_scratch_bytes(b, nt, a) == want
