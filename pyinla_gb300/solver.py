@@ -10,7 +10,8 @@ selected inversion, pattern gather) running in libpyinla_gb300.so.
 
 It does not import pyinla.  To use it inside the reference, replace the class the
 driver instantiates (``pyinla.core.pyinla.SerinvSolver``) with this one, or inject
-:mod:`pyinla_gb300.algs` as ``serinv.algs``; both are shown in INTEGRATION.md.
+:mod:`pyinla_gb300.algs` as ``serinv.algs`` (``sys.modules["serinv.algs"]``) before the
+reference's solver module is imported.
 """
 from __future__ import annotations
 

@@ -1,7 +1,7 @@
 """Generate the golden fixtures under tests/golden/ from the reference itself.
 
 Run in a container where the reference source tree is available (it is read from
-``$PYINLA_REFERENCE_SRC``, default ``/root/reference/src``); the fixtures it writes are
+``$PYINLA_REFERENCE_SRC``, required: the reference's ``src/`` directory); the fixtures it writes are
 committed, so tests never need the reference at run time.
 
 What is pinned, per case (all float64):
@@ -39,7 +39,10 @@ from oracle import bta_oracle as orc  # noqa: E402
 
 
 def _import_reference():
-    src = os.environ.get("PYINLA_REFERENCE_SRC", "/root/reference/src")
+    src = os.environ.get("PYINLA_REFERENCE_SRC")
+    if not src:
+        raise SystemExit("set PYINLA_REFERENCE_SRC to the reference's src/ directory (the tree that holds "
+                         "the pyinla package) to regenerate the fixtures")
     os.environ.setdefault("ARRAY_MODULE", "numpy")
     # matplotlib is imported at module level by the reference's
     # utils/sparse_diagABAt.py:11 but is not used on this path; it is not installed.

@@ -1,7 +1,6 @@
 """Generate the theta-Hessian fixture under tests/golden/ from the reference itself.
 
-Run where the reference source tree is available (``$PYINLA_REFERENCE_SRC``, default
-``/root/reference/src``); the fixture is committed, so tests never read the reference.
+Run where the reference source tree is available (``$PYINLA_REFERENCE_SRC``, required: the reference's ``src/`` directory); the fixture is committed, so tests never read the reference.
 
 The reference's own ``PyINLA._evaluate_hessian_f`` (src/pyinla/core/pyinla.py:767-910)
 and ``PyINLA.compute_covariance_hp`` (pyinla.py:747-765) run unmodified on a stand-in

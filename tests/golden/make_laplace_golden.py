@@ -1,7 +1,6 @@
 """Generate the non-Gaussian objective fixtures under tests/golden/ from the reference.
 
-Run where the reference source tree is available (``$PYINLA_REFERENCE_SRC``, default
-``/root/reference/src``); the fixtures are committed, so tests never read the reference.
+Run where the reference source tree is available (``$PYINLA_REFERENCE_SRC``, required: the reference's ``src/`` directory); the fixtures are committed, so tests never read the reference.
 
 What runs is the reference's own code: PyINLA._evaluate_f (non-Gaussian branch,
 src/pyinla/core/pyinla.py:692-729), PyINLA._inner_iteration (:1025-1074),

@@ -1,7 +1,6 @@
 """Generate the marginal-variance fixtures under tests/golden/ from the reference itself.
 
-Run where the reference source tree is available (``$PYINLA_REFERENCE_SRC``, default
-``/root/reference/src``); the fixtures are committed, so tests never read the
+Run where the reference source tree is available (``$PYINLA_REFERENCE_SRC``, required: the reference's ``src/`` directory); the fixtures are committed, so tests never read the
 reference at run time.
 
 Per case, Q_cond = (seeded SPD BTA matrix of ``oracle.bta_oracle.make_bta_c1``) +
