@@ -74,52 +74,6 @@ long long gbta_kernel_launches(void);
  * SM (`iters` FMA rounds per thread); the roofline denominator of the FP64 kernels. */
 int gbta_probe_fp64_peak(int iters, double* tflops);
 
-/* Clock cycles per call of the 32 x 32 tile routines, each timed alone on one CTA:
- * cycles[0] tile reload (included in the others), [1] tile Cholesky, [2] reciprocals
- * + X F^{-T}, [3] reciprocals + X F^{-1}, [4] digit planes, [5] tile store, [6]
- * reciprocals + row scaling + X F^{-T} on 8 rows, [7] one tensor-core tile step (43
- * digit-plane pairs of 32 x 32 x 32, operands in shared memory), [8] staging both
- * operands' digit planes (2 x 16 KB) from global into shared memory (cycles holds 9
- * values).  No
- * reference counterpart (a measurement aid). */
-int gbta_probe_tiles(int iters, long long* cycles);
-
-/* Check of the tcgen05 tile step (digit-plane products on the 5th-generation tensor
- * cores, accumulators in tensor memory) against the mma.sync tile step on one CTA,
- * with pseudo-random digits; each entry counts FP64 results (after the exact fold)
- * that differ in any bit: mismatches[0..6] for (left orientation, plane shift) =
- * (plain, 0), (transposed, 0), (plain, 2), (transposed, 3), (plain, 5), (transposed,
- * 7), (plain, 7); [7] transposed with the MN-major offsets in the other descriptor
- * fields (a layout check: nonzero is expected); [8], [9] two accumulated steps,
- * transposed and plain (-1: an MMA completion wait ran out).  cycles[0] per tcgen05
- * tile step, [1] per mma.sync tile step, [2] issuing one tcgen05 tile step (one
- * thread, no MMA in flight), [3] one fold of the tensor-memory accumulators into FP64
- * (cycles holds 4 values).  No reference counterpart (a measurement and correctness
- * aid). */
-int gbta_probe_umma(int iters, int* mismatches, long long* cycles);
-
-/* Residency of CTAs holding tensor memory (a launch-shape check): a probe kernel with
- * 100 KB of shared memory and 256 tensor-memory columns per CTA, launched with two
- * CTAs per SM.  out[0] CTAs per SM the occupancy calculator allows for it (it reports
- * one for every kernel that allocates tensor memory); out[1] SMs that ran two of its
- * CTAs at the same time; out[2] SMs that received two; out[3] the longest wait of a
- * CTA for its tensor memory in ns; out[4] CTAs per SM that fit its registers, shared
- * and tensor memory (the rule launch_grid applies to tensor-memory kernels).  out
- * holds 5 values.  No reference counterpart. */
-int gbta_probe_tmem_pairs(long long* out);
-
-/* Clock cycles of the primitives those routines are built from, on one CTA:
- * cycles[0] dependent DFMA (one warp), [1] independent DFMA per warp instruction (one
- * warp), [2] the same with four warps, [3] DFMA under a warp-uniform false predicate,
- * [4] dependent rsqrt.approx.f64 + DADD, [5] dependent 64-bit shuffle, [6] dependent
- * shared load, [7] bar.sync of four warps.  No reference counterpart. */
-int gbta_probe_latencies(long long* cycles);
-
-/* Chip-wide TFLOP/s of the candidate paths for FP64 tile products: tflops[0] DMMA
- * (mma.m8n8k4.f64), [1] HMMA (mma.m16n8k16 f16 -> f32), [2] FFMA.  No reference
- * counterpart (a measurement aid). */
-int gbta_probe_tensor_rates(int iters, double* tflops);
-
 /* Text of the last error raised on the calling thread ("" if none). */
 const char* gbta_last_error(void);
 
@@ -164,6 +118,17 @@ int gbta_set_ctas_per_sm(gbta_solver* s, int n);
 int gbta_set_trace(gbta_solver* s, int enable);
 long long gbta_get_trace(gbta_solver* s, long long* out, long long max_records);
 
+/* Kernel timing (off by default; a measurement aid with no reference counterpart).
+ * When enabled, the solver records CUDA events on its stream around the dataflow
+ * kernel of each factorization (k_factor / k_factor_oz, without the exponent and flag
+ * preparation), each selected inversion (k_selinv / k_selinv_oz, without the pre-pass
+ * and the write-back) and each solve call (all its sweep launches).  gbta_kernel_ms
+ * waits for the last recorded events and writes ms[0] factorization, ms[1] selected
+ * inversion, ms[2] solve call, in milliseconds (-1 where none was recorded since
+ * timing was enabled). */
+int gbta_set_kernel_timing(gbta_solver* s, int enable);
+int gbta_kernel_ms(gbta_solver* s, double* ms);
+
 /* Bytes of device workspace held by the solver (SerinvSolver.get_solver_memory,
  * structured_solver.py:540-550, minus the caller-owned block buffers). */
 size_t gbta_workspace_bytes(const gbta_solver* s);
@@ -181,17 +146,31 @@ int gbta_pobtf_async(gbta_solver* s, double* D, double* L);
 /* No counterpart in the reference.  For callers that cannot allocate device memory
  * when they factor -- hosts that own a fixed device-memory pool and forbid
  * allocations outside it, or loops that cannot afford the implicit device
- * synchronisation of cudaMalloc/cudaFree -- gbta_pobtaf_noalloc factors like
- * gbta_pobtaf (same kernel, same results, same return codes, synchronous on
- * `stream`; NULL = the CUDA default stream) without a solver object and without
- * calling cudaMalloc, cudaFree or any allocating routine.  Its scratch lives in one
- * fixed array of GBTA_NOALLOC_SCRATCH_BYTES in device memory, held by every GPU that
- * loads the library until the process exits; problems whose scratch
- * (gbta_noalloc_scratch_bytes) exceeds it are rejected with GBTA_ERR_ARG.  All calls
- * on a device share the array and it keeps the last call's contents (each call
- * clears what must start at zero): calls that overlap on the GPU race.  The first
- * call on a device looks up the array's device address (with that device current);
- * make that first call before any stream capture. */
+ * synchronisation of cudaMalloc/cudaFree -- gbta_pobtaf_noalloc factors D, L, R, T in
+ * place without a solver object and without calling cudaMalloc, cudaFree or any
+ * allocating routine.  It runs the FP64-product factorization kernel (the kernel of
+ * gbta_pobtaf under GBTA_METHOD_FP64, with a task list that leaves out the feeder
+ * row-group split), so its results agree with gbta_pobtaf to rounding (both product
+ * methods), and its return codes are gbta_pobtaf's.  It is synchronous: it returns
+ * after the work enqueued on `stream` (NULL = the CUDA default stream) has finished
+ * and its status has been read back.
+ *
+ * Its scratch (control words, ready flags, the task list, the arrow-tip partials)
+ * lives in one fixed array of GBTA_NOALLOC_SCRATCH_BYTES (64 MiB) of device memory
+ * inside the library.  Problems whose scratch (gbta_noalloc_scratch_bytes) exceeds it
+ * are rejected with GBTA_ERR_ARG before any device work.  All calls on a device share
+ * the array and it keeps the last call's contents (each call clears what must start
+ * at zero): calls that overlap on the GPU race.
+ *
+ * The array and the code of this path occupy device memory from the moment the part
+ * of the library that holds them is loaded on a GPU until the process exits.  Under
+ * CUDA's default lazy module loading that happens during the FIRST call on each
+ * device, which also looks up the array's device address (with that device current):
+ * that first call does take device memory (the 64 MiB plus kernel code), so make it --
+ * any small problem will do -- before the caller reserves its memory pool, and before
+ * any stream capture.  With CUDA_MODULE_LOADING=EAGER in the environment the memory is
+ * taken when the process creates its CUDA context instead.  If the load fails for lack
+ * of memory, the call returns GBTA_ERR_CUDA with a message that says so. */
 #define GBTA_NOALLOC_SCRATCH_BYTES (64u << 20)
 size_t gbta_noalloc_scratch_bytes(int b, int nt, int a);
 int gbta_pobtaf_noalloc(int b, int nt, int a, double* D, double* L, double* R, double* T, void* stream);

@@ -72,6 +72,11 @@ struct gbta_solver {
   long long* d_trace = nullptr;   // task trace of the last launch (when enabled)
   long long trace_cap = 0;        // records
   long long trace_n = 0;          // records of the last traced launch
+  // Kernel timing (off by default): CUDA events around the dataflow launch of the last
+  // factorization [0, 1], selected inversion [2, 3] and solve call [4, 5].
+  bool timing = false;
+  cudaEvent_t tev[6] = {};
+  bool timed[3] = {false, false, false};
 };
 
 namespace gbta {
@@ -273,8 +278,34 @@ int gbta_destroy(gbta_solver* s) {
   cudaFree(s->d_sdig);
   cudaFree(s->d_erow);
   if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
+  for (cudaEvent_t ev : s->tev)
+    if (ev) cudaEventDestroy(ev);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
   delete s;
+  return GBTA_OK;
+}
+
+int gbta_set_kernel_timing(gbta_solver* s, int enable) {
+  if (int r = check_solver(s)) return r;
+  if (enable)
+    for (cudaEvent_t& ev : s->tev)
+      if (!ev) GBTA_CUDA(cudaEventCreate(&ev));
+  s->timing = enable != 0;
+  for (bool& t : s->timed) t = false;
+  return GBTA_OK;
+}
+
+int gbta_kernel_ms(gbta_solver* s, double* ms) {
+  if (int r = check_solver(s)) return r;
+  if (!ms) return fail(GBTA_ERR_ARG, "ms is null");
+  for (int k = 0; k < 3; ++k) {
+    ms[k] = -1.0;
+    if (!s->timed[k]) continue;
+    GBTA_CUDA(cudaEventSynchronize(s->tev[2 * k + 1]));
+    float v = 0.f;
+    GBTA_CUDA(cudaEventElapsedTime(&v, s->tev[2 * k], s->tev[2 * k + 1]));
+    ms[k] = v;
+  }
   return GBTA_OK;
 }
 
@@ -376,12 +407,17 @@ static int factor_async(gbta_solver* s, double* D, double* L, double* R, double*
   if (int r = reset_ticket(s)) return r;
   gbta::launch_clear_feeders(s->g, s->d_flags, s->stream);
   const gbta::LaunchCtl lc = next_launch(s, s->n_ftasks);
+  if (s->timing) GBTA_CUDA(cudaEventRecord(s->tev[0], s->stream));
   if (s->method == GBTA_METHOD_OZAKI)
     gbta::launch_factor_oz(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part,
                            (__half*)s->d_digits, s->d_erow, lc, s->d_faux);
   else
     gbta::launch_factor(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part, lc, s->d_faux);
   GBTA_CUDA(cudaGetLastError());
+  if (s->timing) {
+    GBTA_CUDA(cudaEventRecord(s->tev[1], s->stream));
+    s->timed[0] = true;
+  }
   return GBTA_OK;
 }
 
@@ -407,12 +443,17 @@ static int solve_async(gbta_solver* s, const double* D, const double* L, const d
   if (nrhs < 1) return fail(GBTA_ERR_ARG, "nrhs must be >= 1");
   if (trans != 0 && trans != 1) return fail(GBTA_ERR_ARG, "trans must be 0 (N) or 1 (C)");
   const int ntasks = s->g.nt * s->g.B + (use_arrow ? 1 : 0);
+  if (s->timing) GBTA_CUDA(cudaEventRecord(s->tev[4], s->stream));
   for (int c0 = 0; c0 < nrhs; c0 += gbta::SOLVE_NC) {
     const int nc = nrhs - c0 < gbta::SOLVE_NC ? nrhs - c0 : gbta::SOLVE_NC;
     if (int r = reset_ticket(s)) return r;
     const gbta::LaunchCtl lc = next_launch(s, ntasks);
     gbta::launch_solve(s->g, D, L, R, T, B + c0, nrhs, nc, trans, use_arrow, s->d_arrow_part, lc);
     GBTA_CUDA(cudaGetLastError());
+  }
+  if (s->timing) {
+    GBTA_CUDA(cudaEventRecord(s->tev[5], s->stream));
+    s->timed[2] = true;
   }
   return GBTA_OK;
 }
@@ -484,6 +525,7 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
   gbta::launch_selinv_prepare(g, D, L, R, use_arrow, s->d_selws, s->stream);
   if (int r = reset_ticket(s)) return r;
   const gbta::LaunchCtl lc = next_launch(s, s->n_stasks);
+  if (s->timing) GBTA_CUDA(cudaEventRecord(s->tev[2], s->stream));
   if (s->method == GBTA_METHOD_OZAKI)
     gbta::launch_selinv_oz(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks_m, s->n_stasks,
                            (__half*)s->d_digits, s->d_erow, cinv, (__half*)s->d_sdig, s->d_tip_part, s->d_faux,
@@ -491,6 +533,10 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
   else
     gbta::launch_selinv(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks, cinv, lc);
   GBTA_CUDA(cudaGetLastError());
+  if (s->timing) {
+    GBTA_CUDA(cudaEventRecord(s->tev[3], s->stream));
+    s->timed[1] = true;
+  }
   gbta::launch_selinv_writeback(g, SD, SL, SR, ST, D, L, R, T, use_arrow, s->stream);
   GBTA_CUDA(cudaGetLastError());
   return GBTA_OK;
