@@ -75,6 +75,16 @@ def _variate_arrays(y, tau_y, obs_variate):
     return tau_y, ov, tau_y[ov]
 
 
+def conditional_system(spatial_terms, term_vw, ns, nv, nt, nb, A, y, tip_prec, alpha, beta, tau_y,
+                       obs_variate=None):
+    """Q_prior, Q_cond = Q_prior + A^T diag(tau_y of each row) A (model.py:421) and the
+    information vector A^T (tau_y y) at x = 0 (model.py:445-447), as SciPy matrices."""
+    _, _, tau_row = _variate_arrays(y, tau_y, obs_variate)
+    Qp = kron_prior(spatial_terms, term_vw, alpha, beta, ns, nv, nt, nb, tip_prec)
+    Qc = (Qp + A.T @ (sps.diags(tau_row) @ A)).tocsr()
+    return Qp, Qc, np.asarray(A.T @ (tau_row * y), dtype=np.float64)
+
+
 def objective(spatial_terms, term_vw, ns, nv, nt, nb, A, y, tip_prec, alpha, beta, tau_y, theta_y, log_prior,
               obs_variate=None):
     """f(theta) for the Gaussian branch of PyINLA._evaluate_f, on the CPU.
@@ -87,15 +97,14 @@ def objective(spatial_terms, term_vw, ns, nv, nt, nb, A, y, tip_prec, alpha, bet
     b = nv * ns
     tau_y, ov, tau_row = _variate_arrays(y, tau_y, obs_variate)
     theta_y = np.atleast_1d(np.asarray(theta_y, dtype=np.float64))
-    Qp = kron_prior(spatial_terms, term_vw, alpha, beta, ns, nv, nt, nb, tip_prec)
-    Qc = (Qp + A.T @ (sps.diags(tau_row) @ A)).tocsr()
+    Qp, Qc, rhs = conditional_system(spatial_terms, term_vw, ns, nv, nt, nb, A, y, tip_prec, alpha, beta, tau_y,
+                                     obs_variate)
     Dp, Lp, Rp, Tp = sparse_to_bta(Qp, nt, b, nb)
     orc.pobtf(Dp, Lp)
     logdet_p = orc.logdet(Dp, None, "bt")
     Dc, Lc, Rc, Tc = sparse_to_bta(Qc, nt, b, nb)
     orc.pobtaf(Dc, Lc, Rc, Tc)
     logdet_c = orc.logdet(Dc, Tc, "bta")
-    rhs = A.T @ (tau_row * y)
     mu = rhs.copy()
     orc.pobtas(Dc, Lc, Rc, Tc, mu, "N")
     orc.pobtas(Dc, Lc, Rc, Tc, mu, "C")
