@@ -14,6 +14,12 @@ available).
 metric: FP64 TFLOP/s of factor + selected inversion, counted with the fixed
 algorithmic flop counts F_f + F_s of the BTA recurrences (LAPACK conventions),
 divided by the device time of the whole step.
+
+The same line carries the adjoint theta-gradient against one plain evaluation and
+against a measured central-difference gradient, the parity of the timed step's
+results against the oracle, the CPU baseline, and two further workloads timed in the
+same run: 41 mixed instances in one graph launch ("batch41") and the trivariate
+coregional model with b = 3072 ("coreg3").
 """
 from __future__ import annotations
 
@@ -130,20 +136,6 @@ class ClockSampler:
 
 
 # ----------------------------------------------------------------------------- CPU baseline
-def cpu_sample_tflops(b: int, a: int, nt_sample: int, seed: int = 3):
-    """Time the oracle's block-level NumPy/OpenBLAS pobtaf + pobtasi (the restatement of
-    the reference's Serinv CPU path) on a bounded sample with nt_sample blocks."""
-    from oracle import bta_oracle as orc
-
-    D, L, R, T, _ = orc.make_bta_c1(seed, nt=nt_sample, b=b, a=a)
-    t0 = time.perf_counter()
-    orc.pobtaf(D, L, R, T)
-    orc.pobtasi(D, L, R, T)
-    dt = time.perf_counter() - t0
-    ff, fs = bta_flops(nt_sample, b, a)
-    return (ff + fs) / dt / 1e12, dt
-
-
 def host_cores() -> int:
     try:
         return len(os.sched_getaffinity(0))
@@ -151,39 +143,125 @@ def host_cores() -> int:
         return os.cpu_count() or 1
 
 
+def oracle_qcond(spec, theta, nt_keep: int | None = None):
+    """The workload's Q_cond as BTA blocks, from the oracle's own sparse assembly and
+    sparse-to-BTA mapping, and the information vector.  nt_keep < nt keeps the leading
+    nt_keep time blocks and the arrow: a principal submatrix, so still SPD."""
+    from oracle import model_oracle as mo
+
+    c = spec.coefficients(theta)
+    _, Qc, rhs = mo.conditional_system(spec.terms, spec.term_vw, spec.ns, spec.nv, spec.nt, spec.nb, spec.A, spec.y,
+                                       spec.tip_prec, c.alpha, c.beta, c.tau_y, spec.obs_variates())
+    D, L, R, T = mo.sparse_to_bta(Qc, spec.nt, spec.b, spec.nb)
+    if nt_keep is not None and nt_keep < spec.nt:
+        b = spec.b
+        rhs = np.concatenate([rhs[: nt_keep * b], rhs[spec.nt * b:]])
+        D, L, R = D[:nt_keep].copy(), L[: nt_keep - 1].copy(), R[:nt_keep].copy()
+    return D, L, R, T, rhs
+
+
+def oracle_pass(D, L, R, T, rhs):
+    """The oracle's pobtaf, logdet, pobtas N and C, pobtasi in place (the restatement
+    of the reference's Serinv CPU path, NumPy/OpenBLAS on every host core); returns the
+    seconds of pobtaf + pobtasi, the logdet and the solution."""
+    from oracle import bta_oracle as orc
+
+    t0 = time.perf_counter()
+    orc.pobtaf(D, L, R, T)
+    t_f = time.perf_counter() - t0
+    ld = orc.logdet(D, T, "bta")
+    x = rhs.copy()
+    orc.pobtas(D, L, R, T, x, "N")
+    orc.pobtas(D, L, R, T, x, "C")
+    t0 = time.perf_counter()
+    orc.pobtasi(D, L, R, T)
+    t_s = time.perf_counter() - t0
+    return t_f + t_s, ld, x
+
+
+def relerr(x, y) -> float:
+    x = np.asarray(x)
+    y = np.asarray(y)
+    return float(np.max(np.abs(x - y)) / max(float(np.max(np.abs(y))), 1e-300))
+
+
+def cpu_baseline_and_parity(spec, theta, gpu: dict):
+    """cpu_baseline: the oracle on this step's whole Q_cond (every time block), timed on
+    the host cores.  Its results are the parity check of the timed step's GPU results
+    (logdet, mean, every Sigma block), at the 1e-10 relative bar."""
+    D, L, R, T, rhs = oracle_qcond(spec, theta)
+    b, nt, a = spec.b, spec.nt, spec.nb
+    dt, ld, x = oracle_pass(D, L, R, T, rhs)
+    ff, fs = bta_flops(nt, b, a)
+    diag_o = np.concatenate([np.diagonal(D, axis1=1, axis2=2).ravel(), np.diagonal(T)])
+    diag_g = np.concatenate([np.diagonal(gpu["SD"], axis1=1, axis2=2).ravel(), np.diagonal(gpu["ST"])])
+    blocks = {k: relerr(gpu[k], o) for k, o in (("SD", D), ("SL", L), ("SR", R), ("ST", T))}
+    parity = {"rtol": 1e-10, "logdet": abs(gpu["logdet"] - ld) / abs(ld), "mu": relerr(gpu["mu"], x),
+              "sigma_diag": relerr(diag_g, diag_o), "sigma_blocks": max(blocks.values()), "per_block": blocks,
+              "against": f"oracle (NumPy/OpenBLAS restatement of Serinv) on the same Q_cond, all {nt} time "
+                         "blocks; max-abs error over max-abs value per array"}
+    parity["pass"] = all(parity[k] < 1e-10 for k in ("logdet", "mu", "sigma_diag", "sigma_blocks"))
+    cpu = {"value": (ff + fs) / dt / 1e12, "unit": UNIT, "cores": host_cores(), "kind": "port",
+           "sample": f"the whole workload: oracle pobtaf + pobtasi of this Q_cond (nt={nt}, b={b}, a={a}), "
+                     f"{dt:.1f} s, no extrapolation"}
+    return cpu, parity
+
+
 # ----------------------------------------------------------------------------- reference arm
+REF_NT_SAMPLE = 16
+
+
 def run_reference(args, rank: int, world: int):
+    """The reference's CPU implementation of the path on the host cores: the oracle
+    port of Serinv's pobtaf + pobtasi (Serinv itself is absent), on a bounded sample of
+    this workload's own Q_cond -- its leading 16 of 128 time blocks and the arrow."""
     if rank != 0:
         return
+    from pyinla_gb300.model import SeparableSpdeAr1
+
     wl = workload(args.small)
     cores = host_cores()
-    b, nt, a = wl["n_side"] ** 2, wl["nt"], wl["nb"]
-    nt_sample = 8
-    vals = []
-    for _ in range(max(args.warmup, 0)):
-        cpu_sample_tflops(b, a, nt_sample)
-    for _ in range(args.steps):
-        v, _ = cpu_sample_tflops(b, a, nt_sample)
-        vals.append(v)
-    value = statistics.median(vals)
-    ff, fs = bta_flops(nt, b, a)
+    spec = SeparableSpdeAr1.synthetic(wl["n_side"], wl["nt"], wl["nb"], wl["n_obs"], wl["seed"])
+    nts = min(REF_NT_SAMPLE, spec.nt)
+    blocks = oracle_qcond(spec, spec.theta0, nts)
+    b, a = spec.b, spec.nb
+    ff, fs = bta_flops(nts, b, a)
+    times = []
+    for k in range(args.warmup + args.steps):
+        D, L, R, T, rhs = [x.copy() for x in blocks]
+        dt, _, _ = oracle_pass(D, L, R, T, rhs)
+        if k >= args.warmup:
+            times.append(dt)
+    dt = statistics.median(times)
+    value = (ff + fs) / dt / 1e12
+    sample = (f"oracle pobtaf + pobtasi (NumPy/OpenBLAS restatement of Serinv) of the leading {nts} of "
+              f"{spec.nt} time blocks of this workload's Q_cond with its arrow (b={b}, a={a}); "
+              f"ms_per_step is that sample's time, not extrapolated")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": (ff + fs) / (value * 1e12) * 1e3,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded; reference datasets unavailable)",
-        "config": {"workload": wl["name"], "b": b, "nt": nt, "a": a,
+        "config": {"workload": wl["name"], "b": b, "nt": spec.nt, "a": a, "nt_sample": nts,
                    "note": "Serinv is not installable offline; the reference arm times the oracle's "
                            "Serinv-equivalent NumPy/OpenBLAS restatement on the host cores"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"pobtaf+pobtasi on {nt_sample} of {nt} diagonal blocks (b={b}, a={a}); "
-                                   f"ms_per_step extrapolates to the full {nt} blocks"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
 # ----------------------------------------------------------------------------- our arm
+def tensor_peak():
+    """Sustained bf16 tensor throughput of the GB300s (a kernel timed inside
+    seconds-long back-to-back steps)."""
+    try:
+        mp = json.loads((REPO / "MEASURED_PEAKS.json").read_text())
+        return float(mp["bf16_tflops_sustained"]), "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
+    except (OSError, ValueError, KeyError):
+        return 1700.0, "fallback sustained bf16 figure, 1.7 PFLOP/s (of fallback: MEASURED_PEAKS.json absent)"
+
+
 def run_ours(args, rank: int, world: int, local_rank: int):
     import torch
 
@@ -217,6 +295,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     mu = model.mu
     ev = {k: [torch.cuda.Event(enable_timing=True) for _ in range(2)] for k in ("asm", "fac", "sol", "sel")}
     timings = {k: [] for k in ev}
+    kernel_ms = {"factor": [], "selinv": [], "solve": []}
+    logdet = ctypes.c_double(0.0)
 
     def step(record: bool):
         e = ev if record else None
@@ -225,6 +305,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         model._assemble(ptrs, Dc, Lc, Rc, Tc, with_lik=True)
         if e: e["asm"][1].record(); e["fac"][0].record()
         _lib.check(lib.gbta_pobtaf_async(h.ptr, Dc.data_ptr(), Lc.data_ptr(), Rc.data_ptr(), Tc.data_ptr()))
+        _lib.check(lib.gbta_logdet(h.ptr, Dc.data_ptr(), Tc.data_ptr(), 1, ctypes.byref(logdet)))
         if e: e["fac"][1].record(); e["sol"][0].record()
         torch.mv(model._Aty_v.t(), tau_dev, out=mu)
         _lib.check(lib.gbta_pobtas_async(h.ptr, Dc.data_ptr(), Lc.data_ptr(), Rc.data_ptr(), Tc.data_ptr(),
@@ -238,6 +319,10 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     def collect():
         for k, (e0, e1) in ev.items():
             timings[k].append(e0.elapsed_time(e1))
+        km = np.zeros(3)
+        _lib.check(lib.gbta_kernel_ms(h.ptr, km.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        for k, v in zip(("factor", "selinv", "solve"), km):
+            kernel_ms[k].append(float(v))
 
     for _ in range(args.warmup):
         step(False)
@@ -245,7 +330,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     torch.cuda.synchronize()
     peak = ctypes.c_double(0.0)
     _lib.check(lib.gbta_probe_fp64_peak(4000, ctypes.byref(peak)))
-    peak_tf = float(peak.value)
+    dfma_peak = float(peak.value)
+    _lib.check(lib.gbta_set_kernel_timing(h.ptr, 1))
 
     if dist:
         dist.barrier()
@@ -267,6 +353,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     launches = lib.gbta_kernel_launches() - launches0
     clk = clocks.stop()
     _lib.check(lib.gbta_status(h.ptr))
+    _lib.check(lib.gbta_set_kernel_timing(h.ptr, 0))
     elapsed_ms = t_start.elapsed_time(t_end)
     if dist:
         tt = torch.tensor([elapsed_ms], device="cuda", dtype=torch.float64)
@@ -274,33 +361,32 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         elapsed_ms = float(tt.item())
     ms_per_step = elapsed_ms / args.steps
     value = world * args.steps * (ff + fs) / (elapsed_ms * 1e-3) / 1e12
+    # results of the last timed step, for the parity check against the oracle
+    gpu_out = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        gpu_out = {"logdet": float(logdet.value), "mu": mu.cpu().numpy(), "SD": Dc.cpu().numpy(),
+                   "SL": Lc.cpu().numpy(), "SR": Rc.cpu().numpy(), "ST": Tc.cpu().numpy()}
 
     avg = {k: statistics.mean(v) for k, v in timings.items()}
-    dominant = "sel" if avg["sel"] >= avg["fac"] else "fac"
-    dom_flops = fs if dominant == "sel" else ff
-    achieved = dom_flops / (avg[dominant] * 1e-3) / 1e12
-    traffic = None
+    kavg = {k: statistics.mean(v) for k, v in kernel_ms.items()}
+    dominant = "selinv" if kavg["selinv"] >= kavg["factor"] else "factor"
+    kname = {"factor": "k_factor_oz", "selinv": "k_selinv_oz"}[dominant]
+    # the dominant kernel against the tensor pipe: the fp16 mma work of its digit-plane
+    # tile products (43 plane pairs per 32x32x32 step) per launch over its CUDA-event time
+    fsteps, ssteps = oz_tile_steps(nt, b, a)
+    tflop_launch = (ssteps if dominant == "selinv" else fsteps) * OZ_STEP_TENSOR_FLOPS
+    tachieved = tflop_launch / (kavg[dominant] * 1e-3) / 1e12
+    tpeak, tsrc = tensor_peak()
+    fp64_flops = fs if dominant == "selinv" else ff
+    fp64_achieved = fp64_flops / (kavg[dominant] * 1e-3) / 1e12
+    traffic, traffic_src = None, None
     tfile = REPO / "profiles" / "traffic.json"
     if tfile.exists():
         try:
-            traffic = json.loads(tfile.read_text()).get(wl["name"], {}).get("k_selinv" if dominant == "sel" else "k_factor")
+            tj = json.loads(tfile.read_text()).get(wl["name"], {})
+            traffic, traffic_src = tj.get(kname), tj.get("method")
         except (ValueError, OSError):
-            traffic = None
-
-    # the same launch seen from the tensor pipe: fp16 mma work of its digit-plane
-    # products against the measured bf16 tensor peak of this machine (a kernel timed
-    # inside back-to-back seconds-long steps: the sustained figure)
-    fsteps, ssteps = oz_tile_steps(nt, b, a)
-    tflops = (ssteps if dominant == "sel" else fsteps) * OZ_STEP_TENSOR_FLOPS
-    tachieved = tflops / (avg[dominant] * 1e-3) / 1e12
-    try:
-        mp = json.loads((REPO / "MEASURED_PEAKS.json").read_text())
-        tpeak, tsrc = float(mp["bf16_tflops_sustained"]), "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
-    except (OSError, ValueError, KeyError):
-        tpeak, tsrc = 1700.0, "fallback sustained bf16 figure (MEASURED_PEAKS.json absent)"
-    tensor_pipe = {"achieved": tachieved, "peak": tpeak, "unit": "TFLOP/s", "frac": tachieved / tpeak,
-                   "peak_source": tsrc,
-                   "work": "fp16 mma.sync work of the digit-plane tile products (43x their FP64 flops)"}
+            pass
 
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -309,20 +395,28 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         "config": {"workload": wl["name"], "b": b, "nt": nt, "a": a, "n_obs": wl["n_obs"],
                    "parallelism": f"replicas{world}", "l2": "inputs larger than L2 (BTA blocks "
                    f"{(2 * nt - 1) * b * b * 8 / 1e9:.2f} GB)",
-                   "step": "assemble Q_cond + pobtaf + pobtas(N,C) + pobtasi",
+                   "step": "assemble Q_cond + pobtaf + logdet + pobtas(N,C) + pobtasi",
                    "flops_per_step": ff + fs, "flops_factor": ff, "flops_selinv": fs},
-        "phases_ms": {"assemble": avg["asm"], "factor": avg["fac"], "solve": avg["sol"], "selinv": avg["sel"]},
-        "roofline": {"bound": "tensor", "achieved": achieved, "peak": peak_tf, "unit": "TFLOP/s",
-                     "frac": achieved / peak_tf if peak_tf else None, "traffic": traffic,
-                     "kernel": "k_selinv" if dominant == "sel" else "k_factor",
-                     "peak_source": "measured FP64 DFMA rate of this GPU (gbta_probe_fp64_peak; the "
-                                    "pool's MEASURED_PEAKS.json carries no FP64 figure); GB300's FP64 "
-                                    "tensor (DMMA) path measures below it"},
-        "tensor_pipe": tensor_pipe,
-        "frac_of_peak_step": value / world / peak_tf if peak_tf else None,
+        "phases_ms": {"assemble": avg["asm"], "factor_and_logdet": avg["fac"], "solve": avg["sol"],
+                      "selinv": avg["sel"]},
+        "kernels_ms": kavg,
+        "roofline": {"bound": "tensor", "achieved": tachieved, "peak": tpeak, "unit": "TFLOP/s",
+                     "frac": tachieved / tpeak, "traffic": traffic, "kernel": kname, "peak_source": tsrc,
+                     "work": "fp16 mma.sync flops of the kernel's digit-plane tile products per launch "
+                             f"({tflop_launch / 1e12:.2f} TFLOP: 43 plane pairs per 32x32x32 tile step)",
+                     "traffic_source": traffic_src,
+                     "fp64": {"achieved": fp64_achieved, "unit": "TFLOP/s", "dfma_peak": dfma_peak,
+                              "frac_of_dfma": fp64_achieved / dfma_peak if dfma_peak else None,
+                              "note": "algorithmic FP64 flops of the kernel's recurrence per launch against the "
+                                      "measured FP64 FMA rate of this GPU (gbta_probe_fp64_peak)"}},
         "gpu_launches": int(launches),
         "clocks": clk,
     }
+    # pobtas N and C: both sweeps read the factor once each (their algorithmic bytes)
+    sb = solve_bytes(nt, b, a)
+    result["solve_hbm"] = {"bytes": sb, "ms": avg["sol"], "achieved_gbs": sb / (avg["sol"] * 1e-3) / 1e9,
+                           "peak_gbs": hbm_peak()[0], "frac": sb / (avg["sol"] * 1e-3) / 1e9 / hbm_peak()[0],
+                           "peak_source": hbm_peak()[1]}
 
     # ---- e2e through the reference-facing drop-in (host sparse Q_cond in, host results out)
     if not args.no_e2e:
@@ -365,23 +459,10 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                                  "solve + selected_inversion + _structured_to_spmatrix"}
         del solver
 
-    # ---- adjoint gradient vs one plain evaluation and vs central differences
+    # ---- adjoint gradient vs one plain evaluation and vs measured central differences
     if not args.no_adjoint:
-        model.evaluate(theta)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        f0 = model.evaluate(theta)
-        torch.cuda.synchronize()
-        t_plain = time.perf_counter() - t0
-        t0 = time.perf_counter()
-        f1, g = model.evaluate(theta, gradient=True)
-        torch.cuda.synchronize()
-        t_grad = time.perf_counter() - t0
+        result["adjoint"] = adjoint_figures(model, theta, reps=5, torch=torch)
         d = theta.size
-        result["adjoint"] = {"plain_eval_ms": t_plain * 1e3, "value_and_grad_ms": t_grad * 1e3,
-                             "ratio_vs_plain": t_grad / t_plain, "central_fd_ratio": 2 * d + 1,
-                             "speedup_vs_fd": (2 * d + 1) * t_plain / t_grad,
-                             "gradients_per_s": 1.0 / t_grad, "dim_theta": int(d)}
         # theta-Hessian: differences of 2d adjoint gradients, against the reference's
         # differences of f (1 + 2d + 2d(d-1) evaluations, pyinla.py:767-910)
         t0 = time.perf_counter()
@@ -391,20 +472,78 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         n_fd = 1 + 2 * d + 2 * d * (d - 1)
         result["hessian"] = {"ms": t_hess * 1e3, "gradient_evaluations": 2 * int(d),
                              "reference_f_evaluations": int(n_fd),
-                             "speedup_vs_fd_of_f": n_fd * t_plain / t_hess}
+                             "speedup_vs_fd_of_f": n_fd * result["adjoint"]["plain_eval_ms"] / (t_hess * 1e3)}
 
-    # ---- CPU baseline (rank 0, N = 1 only): the oracle on the host cores
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        nt_sample = 8
-        v, dt = cpu_sample_tflops(b, a, nt_sample)
-        result["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": host_cores(), "kind": "port",
-                                  "sample": f"oracle pobtaf+pobtasi (NumPy/OpenBLAS block restatement of "
-                                            f"Serinv) on {nt_sample} of {nt} diagonal blocks, b={b}, a={a}; "
-                                            f"{dt:.1f} s"}
+    # ---- CPU baseline (rank 0, N = 1 only): the oracle on the host cores, which also
+    # checks the timed step's results
+    if gpu_out is not None:
+        result["cpu_baseline"], result["parity"] = cpu_baseline_and_parity(spec, theta, gpu_out)
+        del gpu_out
+
+    del model, Dc, Lc, Rc, Tc, mu
+    torch.cuda.empty_cache()
+    if rank == 0 and world == 1 and not args.no_extra:
+        sub = argparse.Namespace(**vars(args))
+        sub.steps, sub.warmup = min(args.steps, 3), 3
+        result["batch41"] = run_batch41(sub)
+        torch.cuda.empty_cache()
+        result["coreg3"] = run_coreg3(sub)
+        torch.cuda.empty_cache()
     if rank == 0:
         print(json.dumps(result), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def solve_bytes(nt: int, b: int, a: int) -> float:
+    """Algorithmic bytes of pobtas N + C with one right-hand side: the factor read once
+    per sweep (lower triangles of the diagonal blocks, the off-diagonal and arrow blocks,
+    the tip's triangle) plus four passes over the vector."""
+    N = nt * b + a
+    return 2 * 8.0 * (nt * b * (b + 1) / 2 + (nt - 1) * b * b + nt * a * b + a * (a + 1) / 2) + 4 * 8.0 * N
+
+
+def hbm_peak():
+    try:
+        mp = json.loads((REPO / "MEASURED_PEAKS.json").read_text())
+        return float(mp["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (of measured)"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback 6.8 TB/s (of fallback: MEASURED_PEAKS.json absent)"
+
+
+def adjoint_figures(model, theta, reps: int, torch) -> dict:
+    """Median times of reps plain evaluations and reps value-and-gradient evaluations,
+    and one measured central-difference gradient (2 dim(theta) + 1 evaluations, step
+    1e-4, as the reference's PyINLA._objective_function does with its own step,
+    pyinla.py:546-580), with its relative distance from the adjoint gradient."""
+    d = theta.size
+    model.evaluate(theta)
+    torch.cuda.synchronize()
+    tp, tg = [], []
+    g = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        model.evaluate(theta)
+        torch.cuda.synchronize()
+        tp.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        _, g = model.evaluate(theta, gradient=True)
+        torch.cuda.synchronize()
+        tg.append(time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    model.evaluate(theta)
+    fd = np.zeros(d)
+    for k in range(d):
+        e = np.zeros(d)
+        e[k] = 1e-4
+        fd[k] = (model.evaluate(theta + e) - model.evaluate(theta - e)) / 2e-4
+    torch.cuda.synchronize()
+    t_fd = time.perf_counter() - t0
+    t_plain, t_grad = statistics.median(tp), statistics.median(tg)
+    return {"plain_eval_ms": t_plain * 1e3, "value_and_grad_ms": t_grad * 1e3,
+            "ratio_vs_plain": t_grad / t_plain, "reps": reps, "central_fd_evaluations": 2 * d + 1,
+            "central_fd_ms": t_fd * 1e3, "speedup_vs_fd": t_fd / t_grad,
+            "fd_rel_diff": relerr(g, fd), "gradients_per_s": 1.0 / t_grad, "dim_theta": int(d)}
 
 
 # ----------------------------------------------------------------------------- other workloads
@@ -521,7 +660,7 @@ def run_batch41(args):
         "graph_kernels": graph_kernels, "gpu_launches": int(launches),
         "sequential_ms": seq_ms, "batch_speedup_vs_sequential": seq_ms / ms, "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_coreg3(args):
@@ -548,7 +687,10 @@ def run_coreg3(args):
     coef = spec.coefficients(theta)
     Dc, Lc, Rc, Tc = model.Dc, model.Lc, model.Rc, model.Tc
     fac, sel = [], []
+    clocks = ClockSampler(0)
     for s in range(args.warmup + args.steps):
+        if s == args.warmup:
+            clocks.start()
         ptrs = model._upload_coef(coef)
         model._assemble(ptrs, Dc, Lc, Rc, Tc, with_lik=True)
         e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
@@ -561,17 +703,8 @@ def run_coreg3(args):
         if s >= args.warmup:
             fac.append(e[0].elapsed_time(e[1]))
             sel.append(e[1].elapsed_time(e[2]))
-    model.evaluate(theta)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    model.evaluate(theta)
-    torch.cuda.synchronize()
-    t_plain = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    model.evaluate(theta, gradient=True)
-    torch.cuda.synchronize()
-    t_grad = time.perf_counter() - t0
-    d = theta.size
+    clk = clocks.stop()
+    adj = adjoint_figures(model, theta, reps=3, torch=torch)
     fm, sm = statistics.median(fac), statistics.median(sel)
     line = {
         "metric": METRIC, "value": (ff + fs) / ((fm + sm) * 1e-3) / 1e12, "unit": UNIT, "n_gpus": 1,
@@ -580,11 +713,10 @@ def run_coreg3(args):
         "config": {"workload": "coreg3_spde32x32_ar1_nt64_nb9_obs300k", "b": b, "nt": nt, "a": a,
                    "flops_factor": ff, "flops_selinv": fs, "host_setup_s": t_setup},
         "phases_ms": {"factor": fm, "selinv": sm},
-        "adjoint": {"plain_eval_ms": t_plain * 1e3, "value_and_grad_ms": t_grad * 1e3,
-                    "ratio_vs_plain": t_grad / t_plain, "central_fd_ratio": 2 * d + 1,
-                    "speedup_vs_fd": (2 * d + 1) * t_plain / t_grad, "dim_theta": int(d)},
+        "adjoint": adj, "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
+    del model, Dc, Lc, Rc, Tc
+    return line
 
 
 def main():
@@ -596,15 +728,18 @@ def main():
     ap.add_argument("--small", action="store_true", help="reduced workload (profiler captures)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the oracle leg (CPU baseline and parity)")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batch41 and coreg3 workloads")
     ap.add_argument("--workload", choices=["spde", "batch41", "coreg3"], default="spde",
                     help="spde: the headline single-model step (default); batch41: the mixed 41-instance "
                          "graph-captured launch; coreg3: the 3-variate coregional model with adjoint")
     args = ap.parse_args()
     if args.impl == "ours" and args.workload == "batch41":
-        return run_batch41(args)
+        print(json.dumps(run_batch41(args)), flush=True)
+        return
     if args.impl == "ours" and args.workload == "coreg3":
-        return run_coreg3(args)
+        print(json.dumps(run_coreg3(args)), flush=True)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.impl == "reference" else 1)))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
