@@ -76,6 +76,24 @@ def check_assembly(m, spec, theta):
     assert torch.equal(D1, m.Dc)
 
 
+def test_objective_matches_reference_fixture(built):
+    """The device objective and mean against the reference's own Gaussian _evaluate_f
+    (fixture made by tests/golden/make_gaussian_golden.py), univariate and coregional,
+    at 1e-10."""
+    from tests.conftest import GOLDEN
+    from tests.golden import make_gaussian_golden as gg
+
+    g = np.load(GOLDEN / "gaussian_objective.npz")
+    for tag, spec in (("uni", gg.uni_spec()), ("coreg", gg.coreg_spec())):
+        m = KronGaussianModel(spec)
+        for k in range(3):
+            theta = g[f"{tag}_theta{k}"]
+            f = m.evaluate(theta)
+            fr = float(g[f"{tag}_f{k}"])
+            assert abs(f - fr) <= 1e-10 * abs(fr), (tag, k, f, fr)
+            assert relerr(m.mu.cpu().numpy(), g[f"{tag}_x{k}"]) < 1e-10, (tag, k)
+
+
 def test_objective_matches_oracle(built):
     spec = SeparableSpdeAr1.synthetic(8, 5, 6, 3000, seed=7)
     m = KronGaussianModel(spec)

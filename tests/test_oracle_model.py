@@ -1,8 +1,11 @@
 """CPU checks of the model oracle (oracle/model_oracle.py) and of the adjoint formula.
 
-The gradient formula used on the GPU -- traces of Q^{-1} dQ/dtheta plus the mean
-terms -- is checked here with dense FP64 algebra against central differences of the
-oracle objective, which restates PyINLA._evaluate_f for the Gaussian branch.
+The oracle objective, which restates PyINLA._evaluate_f for the Gaussian branch, is
+pinned to the reference's own _evaluate_f (fixture tests/golden/gaussian_objective.npz,
+made by tests/golden/make_gaussian_golden.py) for a univariate and a bivariate
+coregional model.  The gradient formula used on the GPU -- traces of Q^{-1}
+dQ/dtheta plus the mean terms -- is checked with dense FP64 algebra against central
+differences of the oracle objective.
 """
 import numpy as np
 import pytest
@@ -11,6 +14,7 @@ from oracle import bta_oracle as orc
 from oracle import model_oracle as mo
 from pyinla_gb300 import spde
 from pyinla_gb300.model import CoregionalSpdeAr1, SeparableSpdeAr1, union_pattern
+from tests.conftest import GOLDEN
 
 
 def small_spec(seed=0, n_side=5, nt=4, nb=2, n_obs=300):
@@ -23,6 +27,27 @@ def oracle_f(spec, theta):
                         spec.tip_prec, c.alpha, c.beta, c.tau_y, theta[spec.lik_theta_indices()],
                         spec.log_prior(theta), spec.obs_variates())
     return f
+
+
+def test_oracle_objective_matches_reference_fixture():
+    """f(theta) and the conditional mean against the reference's own Gaussian
+    _evaluate_f (src/pyinla/core/pyinla.py:631-688, 1076-1167) at three theta points,
+    univariate and coregional (per-variate noise precisions), at 1e-10."""
+    from tests.golden import make_gaussian_golden as gg
+
+    g = np.load(GOLDEN / "gaussian_objective.npz")
+    for tag, spec in (("uni", gg.uni_spec()), ("coreg", gg.coreg_spec())):
+        np.testing.assert_allclose(gg.input_checksum(spec), g[f"{tag}_checksum"], rtol=1e-13, atol=0)
+        for k in range(3):
+            theta = g[f"{tag}_theta{k}"]
+            c = spec.coefficients(theta)
+            f, aux = mo.objective(spec.terms, spec.term_vw, spec.ns, spec.nv, spec.nt, spec.nb, spec.A, spec.y,
+                                  spec.tip_prec, c.alpha, c.beta, c.tau_y, theta[spec.lik_theta_indices()],
+                                  spec.log_prior(theta), spec.obs_variates())
+            fr = float(g[f"{tag}_f{k}"])
+            assert abs(f - fr) <= 1e-10 * abs(fr), (tag, k, f, fr)
+            xr = g[f"{tag}_x{k}"]
+            assert np.max(np.abs(aux["mu"] - xr)) <= 1e-10 * np.max(np.abs(xr)), (tag, k)
 
 
 def test_oracle_objective_matches_dense():
