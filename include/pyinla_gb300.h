@@ -96,12 +96,29 @@ int gbta_destroy(gbta_solver* s);
 int gbta_set_stream(gbta_solver* s, void* stream);
 
 /* Limit, in milliseconds, on any inter-CTA wait inside a kernel; after it the
- * kernel records GBTA_ERR_TIMEOUT and returns instead of waiting further. */
+ * kernel records GBTA_ERR_TIMEOUT and returns instead of waiting further.  The default
+ * is 20 s, or GBTA_WAIT_LIMIT_MS from the environment when the solver is created. */
 int gbta_set_wait_limit_ms(gbta_solver* s, double ms);
 
 /* Select / query the product method of the factorization (see GBTA_METHOD_*). */
 int gbta_set_method(gbta_solver* s, int method);
 int gbta_get_method(const gbta_solver* s);
+
+/* Elimination order of the block recurrences (no reference counterpart: the factor
+ * blocks between gbta_pobtaf and the sweeps / inversion are internal state).  With
+ * twist = 1 (the default for nt >= 3) the blocks are eliminated from both ends towards
+ * the middle block m = nt/2 -- blocks 0..m-1 top-down and nt-1..m+1 bottom-up, side
+ * by side, then m -- which halves the longest chain of dependent work at the same
+ * flop count; twist = 0 is the top-down order of Serinv's recurrence.  The logdet,
+ * the solutions and the selected inverse are the same either way (to rounding); the
+ * factor itself differs: after a twisted factorization D_i holds the Cholesky factor
+ * of the partially eliminated block i, and for j >= m the L buffer's block j holds the
+ * factor's coupling of block j to block j+1 in the orientation Q(j, j+1) (the
+ * transpose of the reference's L_j).  A factor is valid input only to sweeps and
+ * inversions under the same setting; gbta_pobtasi restores the reference's layout of
+ * Sigma in every buffer. */
+int gbta_set_twist(gbta_solver* s, int twist);
+int gbta_get_twist(const gbta_solver* s);
 
 /* Persistent CTAs per SM of the dataflow launches (0, the default: as many as the
  * kernel's registers and shared memory allow; GBTA_CTAS_PER_SM in the environment

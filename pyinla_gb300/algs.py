@@ -26,7 +26,22 @@ import numpy as np
 from . import _lib
 from .device import BtaHandle, current_stream_ptr, require_torch_cuda
 
-__all__ = ["pobtaf", "pobtas", "pobtasi", "pobtf", "pobts", "pobtsi", "logdet", "install_as_serinv"]
+__all__ = ["pobtaf", "pobtas", "pobtasi", "pobtf", "pobts", "pobtsi", "logdet", "install_as_serinv",
+           "set_twisted"]
+
+# Elimination order of these drop-ins.  False (the default) is Serinv's top-down block
+# recurrence, so the factor blocks and each half-sweep hold what Serinv's would; True
+# eliminates from both ends towards the middle block (half the critical path of the
+# dataflow kernels), which changes the factor and the intermediate of a lone "N" sweep
+# but not the logdet, the solution of an N-then-C solve or the selected inverse.
+_TWIST = False
+
+
+def set_twisted(enable: bool) -> None:
+    """Choose the elimination order of the functions of this module (see _TWIST); a
+    factor must be swept and inverted under the order it was made with."""
+    global _TWIST
+    _TWIST = bool(enable)
 
 
 class _Staged:
@@ -69,7 +84,7 @@ def pobtaf(A_diagonal_blocks, A_lower_diagonal_blocks, A_arrow_bottom_blocks, A_
     b, nt, a = _geometry(A_diagonal_blocks, A_arrow_bottom_blocks, A_arrow_tip_block)
     bufs = [_Staged(x, torch) for x in (A_diagonal_blocks, A_lower_diagonal_blocks,
                                         A_arrow_bottom_blocks if a else None, A_arrow_tip_block if a else None)]
-    h = BtaHandle.get(b, nt, a)
+    h = BtaHandle.get(b, nt, a, _TWIST)
     h.set_stream(current_stream_ptr())
     code = h.lib.gbta_pobtaf(h.ptr, *[s.ptr() for s in bufs])
     _lib.check(code)
@@ -82,7 +97,7 @@ def pobtf(A_diagonal_blocks, A_lower_diagonal_blocks) -> None:
     torch = require_torch_cuda()
     b, nt, _ = _geometry(A_diagonal_blocks, None, None)
     bufs = [_Staged(x, torch) for x in (A_diagonal_blocks, A_lower_diagonal_blocks)]
-    h = BtaHandle.get(b, nt, 0)
+    h = BtaHandle.get(b, nt, 0, _TWIST)
     h.set_stream(current_stream_ptr())
     _lib.check(h.lib.gbta_pobtf(h.ptr, bufs[0].ptr(), bufs[1].ptr()))
     for s in bufs:
@@ -113,7 +128,7 @@ def pobtas(A_diagonal_blocks, A_lower_diagonal_blocks, A_arrow_bottom_blocks, A_
                                                        A_arrow_bottom_blocks if a else None,
                                                        A_arrow_tip_block if a else None)]
     rhs = _Staged(B, torch)
-    h = BtaHandle.get(b, nt, a)
+    h = BtaHandle.get(b, nt, a, _TWIST)
     h.set_stream(current_stream_ptr())
     _lib.check(h.lib.gbta_pobtas(h.ptr, *[s.ptr() for s in fac], rhs.ptr(), nrhs, _trans_code(trans)))
     rhs.write_back()
@@ -129,7 +144,7 @@ def pobts(A_diagonal_blocks, A_lower_diagonal_blocks, B, trans: str = "N") -> No
     nrhs = 1 if B.ndim == 1 else int(np.prod(B.shape[1:]))
     fac = [_Staged(x, torch, writable=False) for x in (A_diagonal_blocks, A_lower_diagonal_blocks)]
     rhs = _Staged(B, torch)
-    h = BtaHandle.get(b, nt, 0)
+    h = BtaHandle.get(b, nt, 0, _TWIST)
     h.set_stream(current_stream_ptr())
     _lib.check(h.lib.gbta_pobts(h.ptr, fac[0].ptr(), fac[1].ptr(), rhs.ptr(), nrhs, _trans_code(trans)))
     rhs.write_back()
@@ -141,7 +156,7 @@ def pobtasi(A_diagonal_blocks, A_lower_diagonal_blocks, A_arrow_bottom_blocks, A
     b, nt, a = _geometry(A_diagonal_blocks, A_arrow_bottom_blocks, A_arrow_tip_block)
     bufs = [_Staged(x, torch) for x in (A_diagonal_blocks, A_lower_diagonal_blocks,
                                         A_arrow_bottom_blocks if a else None, A_arrow_tip_block if a else None)]
-    h = BtaHandle.get(b, nt, a)
+    h = BtaHandle.get(b, nt, a, _TWIST)
     h.set_stream(current_stream_ptr())
     _lib.check(h.lib.gbta_pobtasi(h.ptr, *[s.ptr() for s in bufs]))
     for s in bufs:
@@ -153,7 +168,7 @@ def pobtsi(A_diagonal_blocks, A_lower_diagonal_blocks) -> None:
     torch = require_torch_cuda()
     b, nt, _ = _geometry(A_diagonal_blocks, None, None)
     bufs = [_Staged(x, torch) for x in (A_diagonal_blocks, A_lower_diagonal_blocks)]
-    h = BtaHandle.get(b, nt, 0)
+    h = BtaHandle.get(b, nt, 0, _TWIST)
     h.set_stream(current_stream_ptr())
     _lib.check(h.lib.gbta_pobtsi(h.ptr, bufs[0].ptr(), bufs[1].ptr()))
     for s in bufs:
@@ -170,7 +185,7 @@ def logdet(A_diagonal_blocks, A_arrow_tip_block=None, sparsity: str = "bta") -> 
     a = int(A_arrow_tip_block.shape[0]) if (A_arrow_tip_block is not None and sparsity == "bta") else 0
     D = _Staged(A_diagonal_blocks, torch, writable=False)
     T = _Staged(A_arrow_tip_block if a else None, torch, writable=False)
-    h = BtaHandle.get(b, nt, a)
+    h = BtaHandle.get(b, nt, a, _TWIST)
     h.set_stream(current_stream_ptr())
     import ctypes
     out = ctypes.c_double(0.0)

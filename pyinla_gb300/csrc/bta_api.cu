@@ -83,24 +83,34 @@ namespace gbta {
 
 // Task lists in a topological order of the dataflow DAGs (each task only waits for
 // tasks earlier in the list, so the ticket dispenser cannot deadlock).
-// Per block i, per column c: the feeder's products (they do not need the diagonal tile,
+// Per block column (i, c): the feeder's products (they do not need the diagonal tile,
 // so they come first), the diagonal tile, the feeder's row groups (triangular solves
 // split over FEED_ROWS-row tasks, so that the solve on the critical path of the
-// factorization runs on several SMs), the other tiles of the column; then the tip.
+// factorization runs on several SMs), the other tiles of the column.  The columns of
+// the two chains of the elimination order (Geom) are interleaved one for one, so that
+// the CTAs holding the earliest tickets serve both chains; then the separator's
+// columns, then the tip.
+static void factor_column_tasks(const Geom& g, int i, int c, std::vector<int4>& t) {
+  const int fk = g.feeder_kind(i, c);
+  if (fk == 1) t.push_back(make_int4(FT_OFFD | FT_PRE, i, c + 1, c));
+  if (fk == 2) t.push_back(make_int4(FT_LOW | FT_PRE, i, 0, c));
+  t.push_back(make_int4(FT_DIAG, i, c, c));
+  for (int q = 0; q < g.feeder_quarters(i, c); ++q) t.push_back(make_int4(FT_FEEDQ, i, q, c));
+  for (int r = c + 1 + (fk == 1 ? 1 : 0); r < g.B; ++r) t.push_back(make_int4(FT_OFFD, i, r, c));
+  if (g.nxt(i) >= 0)
+    for (int r = (fk == 2 ? 1 : 0); r < g.B; ++r) t.push_back(make_int4(FT_LOW, i, r, c));
+  if (g.a > 0) t.push_back(make_int4(FT_ARW, i, 0, c));
+}
+
 std::vector<int4> factor_task_list(const Geom& g) {
   std::vector<int4> t;
-  for (int i = 0; i < g.nt; ++i)
-    for (int c = 0; c < g.B; ++c) {
-      const int fk = g.feeder_kind(i, c);
-      if (fk == 1) t.push_back(make_int4(FT_OFFD | FT_PRE, i, c + 1, c));
-      if (fk == 2) t.push_back(make_int4(FT_LOW | FT_PRE, i, 0, c));
-      t.push_back(make_int4(FT_DIAG, i, c, c));
-      for (int q = 0; q < g.feeder_quarters(i, c); ++q) t.push_back(make_int4(FT_FEEDQ, i, q, c));
-      for (int r = c + 1 + (fk == 1 ? 1 : 0); r < g.B; ++r) t.push_back(make_int4(FT_OFFD, i, r, c));
-      if (i < g.nt - 1)
-        for (int r = (fk == 2 ? 1 : 0); r < g.B; ++r) t.push_back(make_int4(FT_LOW, i, r, c));
-      if (g.a > 0) t.push_back(make_int4(FT_ARW, i, 0, c));
-    }
+  const int s = g.sep(), n1 = s * g.B, n2 = (g.nt - 1 - s) * g.B;
+  for (int u = 0; u < n1 + n2; ++u) {
+    int k;
+    const int i = Geom::interleave(n1, n2, u, &k) == 0 ? k / g.B : g.nt - 1 - k / g.B;
+    factor_column_tasks(g, i, k % g.B, t);
+  }
+  for (int c = 0; c < g.B; ++c) factor_column_tasks(g, s, c, t);
   if (g.a > 0) t.push_back(make_int4(FT_TIP, 0, 0, 0));
   return t;
 }
@@ -109,27 +119,42 @@ std::vector<int4> factor_task_list(const Geom& g) {
 // tile -> sub-diagonal tile of the next column -> its diagonal tile -> ...; the
 // sub-diagonal tile's last product needs the diagonal tile just finished, so the
 // diagonal task finishes it itself, from the partial sum of its other products that
-// an ST_PART task (placed before that diagonal task) leaves.
+// an ST_PART task (placed before that diagonal task) leaves.  The next column after
+// (i, 0) is (prev(i, 0), B-1); the separator has two such columns (one per chain), and
+// their sub-diagonal tiles are computed by ordinary tasks.
+// Order: the tip, the separator's columns from the last, then the columns of the two
+// chains outwards from the separator, interleaved one for one.
+static void selinv_column_tasks(const Geom& g, int i, int c, bool merged, std::vector<int4>& t) {
+  const int B = g.B;
+  auto sub_code = [&](int bi, int bc) {
+    if (bc + 1 < B) return bc + 1;
+    const int n = g.nxt(bi);
+    return (n >= 0 && g.nprev(n) == 1) ? B : -1;
+  };
+  const int sub = merged ? sub_code(i, c) : -1;
+  if (g.a > 0) t.push_back(make_int4(ST_OFF, i, 2 * B, c));
+  if (g.nxt(i) >= 0)
+    for (int r = 0; r < B; ++r)
+      if (B + r != sub) t.push_back(make_int4(ST_OFF, i, B + r, c));
+  for (int r = c + 1; r < B; ++r)
+    if (r != sub) t.push_back(make_int4(ST_OFF, i, r, c));
+  if (merged) {   // the partial of the next column's sub-diagonal tile
+    if (c > 0) t.push_back(make_int4(ST_PART, i, c, c - 1));
+    else if (g.nprev(i) == 1) t.push_back(make_int4(ST_PART, g.prev(i, 0), B, B - 1));
+  }
+  t.push_back(make_int4(ST_DIAG, i, c, c));
+}
+
 std::vector<int4> selinv_task_list(const Geom& g, bool merged) {
   std::vector<int4> t;
-  const int B = g.B;
-  auto sub_code = [&](int i, int c) { return c + 1 < B ? c + 1 : (i < g.nt - 1 ? B : -1); };
+  const int B = g.B, s = g.sep(), n1 = s * B, n2 = (g.nt - 1 - s) * B;
   if (g.a > 0) t.push_back(make_int4(ST_TIP, 0, 0, 0));
-  for (int i = g.nt - 1; i >= 0; --i)
-    for (int c = B - 1; c >= 0; --c) {
-      const int sub = merged ? sub_code(i, c) : -1;
-      if (g.a > 0) t.push_back(make_int4(ST_OFF, i, 2 * B, c));
-      if (i < g.nt - 1)
-        for (int r = 0; r < B; ++r)
-          if (B + r != sub) t.push_back(make_int4(ST_OFF, i, B + r, c));
-      for (int r = c + 1; r < B; ++r)
-        if (r != sub) t.push_back(make_int4(ST_OFF, i, r, c));
-      if (merged) {   // the partial of the next column's sub-diagonal tile
-        if (c > 0) t.push_back(make_int4(ST_PART, i, c, c - 1));
-        else if (i > 0) t.push_back(make_int4(ST_PART, i - 1, B, B - 1));
-      }
-      t.push_back(make_int4(ST_DIAG, i, c, c));
-    }
+  for (int c = B - 1; c >= 0; --c) selinv_column_tasks(g, s, c, merged, t);
+  for (int u = 0; u < n1 + n2; ++u) {
+    int k;
+    const int i = Geom::interleave(n1, n2, u, &k) == 0 ? s - 1 - k / B : s + 1 + k / B;
+    selinv_column_tasks(g, i, B - 1 - k % B, merged, t);
+  }
   return t;
 }
 
@@ -203,6 +228,7 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   s->g.nt = nt;
   s->g.a = a;
   s->g.B = (b + gbta::TS - 1) / gbta::TS;
+  s->g.m = gbta::default_sep(nt);
   const long long nflags = (long long)(2 * nt - 1) * s->g.B * s->g.B + (long long)nt * s->g.B + 1;
   if (nflags > (1ll << 31) - 1) {
     delete s;
@@ -224,6 +250,10 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   if (const char* v = std::getenv("GBTA_CTAS_PER_SM")) {
     const int k = std::atoi(v);
     if (k >= 0 && k <= 8) s->ctas_per_sm = k;
+  }
+  if (const char* v = std::getenv("GBTA_WAIT_LIMIT_MS")) {
+    const double ms = std::atof(v);
+    if (ms > 0.0) s->wait_ns = (unsigned long long)(ms * 1e6);
   }
   CREATE_CUDA(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
   s->stream = s->own_stream;
@@ -284,6 +314,25 @@ int gbta_destroy(gbta_solver* s) {
   delete s;
   return GBTA_OK;
 }
+
+int gbta_set_twist(gbta_solver* s, int enable) {
+  if (int r = check_solver(s)) return r;
+  const int m = enable ? gbta::default_sep(s->g.nt) : s->g.nt - 1;
+  if (m == s->g.sep()) return GBTA_OK;
+  GBTA_CUDA(cudaStreamSynchronize(s->stream));
+  s->g.m = m;
+  // the lists keep their lengths (every block but the separator has a coupling slot)
+  const std::vector<int4> ft = gbta::factor_task_list(s->g), st = gbta::selinv_task_list(s->g),
+                          stm = gbta::selinv_task_list(s->g, true);
+  if ((int)ft.size() != s->n_ftasks || (int)st.size() != s->n_stasks || stm.size() != st.size())
+    return fail(GBTA_ERR_ARG, "internal: task list length changed with the elimination order");
+  GBTA_CUDA(cudaMemcpy(s->d_ftasks, ft.data(), ft.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  GBTA_CUDA(cudaMemcpy(s->d_stasks, st.data(), st.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  GBTA_CUDA(cudaMemcpy(s->d_stasks_m, stm.data(), stm.size() * sizeof(int4), cudaMemcpyHostToDevice));
+  return GBTA_OK;
+}
+
+int gbta_get_twist(const gbta_solver* s) { return s ? (s->g.twisted() ? 1 : 0) : -1; }
 
 int gbta_set_kernel_timing(gbta_solver* s, int enable) {
   if (int r = check_solver(s)) return r;
@@ -405,6 +454,7 @@ static int factor_async(gbta_solver* s, double* D, double* L, double* R, double*
   if (s->method == GBTA_METHOD_OZAKI)
     if (int r = ensure_digits(s)) return r;
   if (int r = reset_ticket(s)) return r;
+  if (s->g.nt > 1) gbta::launch_transpose_lslots(s->g, L, s->stream);
   gbta::launch_clear_feeders(s->g, s->d_flags, s->stream);
   const gbta::LaunchCtl lc = next_launch(s, s->n_ftasks);
   if (s->timing) GBTA_CUDA(cudaEventRecord(s->tev[0], s->stream));

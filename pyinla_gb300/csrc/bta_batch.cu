@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -340,6 +341,8 @@ int run_async(gbta_batch* bt, int phases, double* logdet_out) {
   const gbta::Ctl c = batch_ctl(bt, nullptr, 0);
   if (phases & GBTA_PHASE_FACTOR) {
     for (const BatchInst& q : bt->inst)
+      if (q.g.nt > 1) gbta::launch_transpose_lslots(q.g, q.L, st);
+    for (const BatchInst& q : bt->inst)
       if (q.method == GBTA_METHOD_OZAKI) gbta::launch_row_exponents(q.g, q.D, q.T, q.g.a > 0, q.erow, st);
     gbta::k_factor_batch<<<grid_of(bt, (const void*)gbta::k_factor_batch, gbta::BATCH_FACTOR_SMEM, bt->n_forder), gbta::NT,
                             gbta::BATCH_FACTOR_SMEM, st>>>(
@@ -419,6 +422,10 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
   } while (0)
   CREATE_CUDA(cudaGetDevice(&bt->device));
   CREATE_CUDA(cudaDeviceGetAttribute(&bt->nsm, cudaDevAttrMultiProcessorCount, bt->device));
+  if (const char* v = std::getenv("GBTA_WAIT_LIMIT_MS")) {
+    const double ms = std::atof(v);
+    if (ms > 0.0) bt->wait_ns = (unsigned long long)(ms * 1e6);
+  }
   CREATE_CUDA(cudaStreamCreateWithFlags(&bt->own_stream, cudaStreamNonBlocking));
   bt->stream = bt->own_stream;
   // ---- plan the pool
@@ -429,6 +436,7 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
   for (int k = 0; k < n; ++k) {
     BatchInst& q = bt->inst[k];
     q.g = gbta::Geom{b[k], nt[k], a[k], (b[k] + gbta::TS - 1) / gbta::TS};
+    q.g.m = gbta::default_sep(nt[k]);   // the single-instance solver's elimination order
     q.method = methods ? methods[k] : GBTA_METHOD_OZAKI;
     const gbta::Geom& g = q.g;
     ft[k] = gbta::factor_task_list(g);

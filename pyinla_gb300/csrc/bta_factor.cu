@@ -21,8 +21,42 @@ __global__ void k_clear_feeders(Geom g, int* flags) {
     const int i = k / g.B, c = k - i * g.B;
     const int fk = g.feeder_kind(i, c);
     if (fk == 1) flags[g.fD(i, c + 1, c)] = 0;
-    if (fk == 2) flags[g.fL(i, 0, c)] = 0;
+    if (fk == 2) flags[g.fL(g.lslot(i), 0, c)] = 0;
   }
+}
+
+// One CTA per pair of tiles (R, C), (C, R) with R >= C of one L slot below the separator:
+// both are read, then written back transposed (a tile on the diagonal is its own pair).
+__global__ void __launch_bounds__(256) k_transpose_lslots(double* L, Geom g, int j0) {
+  __shared__ double A[TS][TS + 1], At[TS][TS + 1];
+  const int B = g.B, pairs = B * (B + 1) / 2;
+  const int slot = j0 + blockIdx.x / pairs;
+  const int q = blockIdx.x % pairs;
+  int R = (int)((sqrtf(8.f * q + 1.f) - 1.f) * 0.5f);
+  while ((R + 1) * (R + 2) / 2 <= q) ++R;
+  while (R * (R + 1) / 2 > q) --R;
+  const int C = q - R * (R + 1) / 2;
+  double* blk = L + (size_t)slot * g.b * g.b;
+  const int r0 = R * TS, c0 = C * TS;
+  for (int idx = threadIdx.x; idx < TS * TS; idx += blockDim.x) {
+    const int rr = idx / TS, cc = idx % TS;
+    if (r0 + rr < g.b && c0 + cc < g.b) A[rr][cc] = blk[(size_t)(r0 + rr) * g.b + c0 + cc];
+    if (c0 + rr < g.b && r0 + cc < g.b) At[rr][cc] = blk[(size_t)(c0 + rr) * g.b + r0 + cc];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < TS * TS; idx += blockDim.x) {
+    const int rr = idx / TS, cc = idx % TS;
+    if (r0 + rr < g.b && c0 + cc < g.b) blk[(size_t)(r0 + rr) * g.b + c0 + cc] = At[cc][rr];
+    if (c0 + rr < g.b && r0 + cc < g.b) blk[(size_t)(c0 + rr) * g.b + r0 + cc] = A[cc][rr];
+  }
+}
+
+void launch_transpose_lslots(const Geom& g, double* L, cudaStream_t stream) {
+  const int j0 = g.sep(), nslots = g.nt - 1 - j0;
+  if (nslots <= 0) return;
+  const long long blocks = (long long)nslots * (g.B * (g.B + 1) / 2);
+  k_transpose_lslots<<<(unsigned)blocks, 256, 0, stream>>>(L, g, j0);
+  count_launches(1);
 }
 
 void launch_clear_feeders(const Geom& g, int* flags, cudaStream_t stream) {

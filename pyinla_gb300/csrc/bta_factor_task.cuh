@@ -8,10 +8,12 @@
 //   D_i <- chol(D_i); L_i <- L_i D_i^{-T}; R_i <- R_i D_i^{-T};
 //   D_{i+1} -= L_i L_i^T; R_{i+1} -= R_i L_i^T; T -= R_i R_i^T; T <- chol(T)
 // by a left-looking tile Cholesky of the banded tile matrix.  One task finalises one
-// TS x TS tile of D_i (lower), L_i or R_i: it subtracts the products of already
-// final tiles to its left (including the previous block column, which is the
-// Schur update D_{i+1} -= L_i L_i^T / R_{i+1} -= R_i L_i^T), then factors (diagonal
-// tile) or solves against the diagonal tile of its column.  Tiles of the next
+// TS x TS tile of D_i (lower), of block i's coupling slot in L, or of R_i: it subtracts
+// the products of already final tiles to its left (including the block columns of the
+// neighbours eliminated before block i, which is the Schur update D_{i+1} -= L_i L_i^T /
+// R_{i+1} -= R_i L_i^T), then factors (diagonal tile) or solves against the diagonal
+// tile of its column.  The blocks are eliminated in the order of Geom (top-down, or
+// from both ends towards the separator block).  Tiles of the next
 // block start as soon as the panels they need are final, so consecutive diagonal
 // blocks overlap instead of running one after the other.
 //
@@ -74,9 +76,10 @@ static __device__ __forceinline__ Tile feeder_tile(const FactorArgs& p, int i, i
     row0 = (long long)i * g.b + (c + 1) * TS;
     return btile(Dblk(p, i), g, c + 1, c);
   }
-  slot = g.fL(i, 0, c);
-  row0 = (long long)(i + 1) * g.b;
-  return btile(Lblk(p, i), g, 0, c);
+  const int ls = g.lslot(i);
+  slot = g.fL(ls, 0, c);
+  row0 = (long long)g.nxt(i) * g.b;
+  return btile(Lblk(p, ls), g, 0, c);
 }
 
 // FT_FEEDQ task: rows FEED_ROWS q .. of the feeder of diagonal tile (i, col) <- their
@@ -266,9 +269,9 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
       tgt = btile(tgt_blk, g, r, col);
       tgt_flag = c.flags + g.fD(i, r, col);
     } else if (type == FT_LOW) {
-      tgt_blk = Lblk(p, i);
+      tgt_blk = Lblk(p, g.lslot(i));
       tgt = btile(tgt_blk, g, r, col);
-      tgt_flag = c.flags + g.fL(i, r, col);
+      tgt_flag = c.flags + g.fL(g.lslot(i), r, col);
     } else {   // FT_ARW
       tgt_blk = Rblk(p, i);
       tgt = atile(tgt_blk, g, col);
@@ -279,32 +282,34 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
     acc_from_smem(acc, X);
     __syncthreads();
 
-    const bool prev = (i > 0) && (type != FT_LOW);
-    const int nprev = prev ? g.B : 0;
+    // previous block columns: the Schur terms of the (one or two) neighbours eliminated
+    // before block i, through their coupling slots (L tiles have none: Q(nxt(i), p) = 0)
+    const int nprev = (type != FT_LOW) ? g.nprev(i) * g.B : 0;
     const int nsteps = nprev + col;
+    const int lsi = g.lslot(i);
     auto step_of = [&](int s) -> Step {
       Step st;
       st.ta = false;
       st.tb = true;
-      if (s < nprev) {   // previous block column: Schur terms with L_{i-1}
-        const int k = s;
+      if (s < nprev) {
+        const int pb = g.prev(i, s / g.B), ls = g.lslot(pb), k = s % g.B;
         if (type == FT_ARW) {
-          st.a = atile(Rblk(p, i - 1), g, k);
-          st.fa = c.flags + g.fR(i - 1, k);
+          st.a = atile(Rblk(p, pb), g, k);
+          st.fa = c.flags + g.fR(pb, k);
         } else {
-          st.a = btile(Lblk(p, i - 1), g, r, k);
-          st.fa = c.flags + g.fL(i - 1, r, k);
+          st.a = btile(Lblk(p, ls), g, r, k);
+          st.fa = c.flags + g.fL(ls, r, k);
         }
-        st.b = btile(Lblk(p, i - 1), g, col, k);
-        st.fb = c.flags + g.fL(i - 1, col, k);
+        st.b = btile(Lblk(p, ls), g, col, k);
+        st.fb = c.flags + g.fL(ls, col, k);
       } else {           // within the block column: tiles k < col of the same row
         const int k = s - nprev;
         if (type == FT_ARW) {
           st.a = atile(Rblk(p, i), g, k);
           st.fa = c.flags + g.fR(i, k);
         } else if (type == FT_LOW) {
-          st.a = btile(Lblk(p, i), g, r, k);
-          st.fa = c.flags + g.fL(i, r, k);
+          st.a = btile(Lblk(p, lsi), g, r, k);
+          st.fa = c.flags + g.fL(lsi, r, k);
         } else {
           st.a = btile(Dblk(p, i), g, r, k);
           st.fa = c.flags + g.fD(i, r, k);
@@ -471,9 +476,9 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
       tgt_slot = g.fD(i, r, col);
       row_base = (long long)i * g.b + r * TS;
     } else if (type == FT_LOW) {
-      tgt = make_tile(p.L + i * bb, g.b, r * TS, col * TS, g.b, g.b);
-      tgt_slot = g.fL(i, r, col);
-      row_base = (long long)(i + 1) * g.b + r * TS;
+      tgt = make_tile(p.L + g.lslot(i) * bb, g.b, r * TS, col * TS, g.b, g.b);
+      tgt_slot = g.fL(g.lslot(i), r, col);
+      row_base = (long long)g.nxt(i) * g.b + r * TS;
     } else {
       tgt = make_tile(p.R + i * ab, g.b, 0, col * TS, g.a, g.b);
       tgt_slot = g.fR(i, col);
@@ -499,17 +504,17 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
 
     // ---- product loop over the final tiles left of the target (previous block
     //      column first, then columns k < col of this block)
-    const bool prev = (i > 0) && (type != FT_LOW);
-    const int nprev = prev ? g.B : 0;
+    const int nprev = (type != FT_LOW) ? g.nprev(i) * g.B : 0;
     const int nsteps = nprev + col;
+    const int lsi = g.lslot(i);
     auto slots = [&](int s, int& sa, int& sb) {
       if (s < nprev) {
-        const int k = s;
-        sa = (type == FT_ARW) ? g.fR(i - 1, k) : g.fL(i - 1, r, k);
-        sb = g.fL(i - 1, col, k);
+        const int pb = g.prev(i, s / g.B), ls = g.lslot(pb), k = s % g.B;
+        sa = (type == FT_ARW) ? g.fR(pb, k) : g.fL(ls, r, k);
+        sb = g.fL(ls, col, k);
       } else {
         const int k = s - nprev;
-        sa = (type == FT_ARW) ? g.fR(i, k) : (type == FT_LOW) ? g.fL(i, r, k) : g.fD(i, r, k);
+        sa = (type == FT_ARW) ? g.fR(i, k) : (type == FT_LOW) ? g.fL(lsi, r, k) : g.fD(i, r, k);
         sb = g.fD(i, col, k);
       }
     };

@@ -29,8 +29,26 @@ constexpr int FEED_ROWS = 8;   // rows of a feeder tile solved by one FT_FEEDQ t
 enum SelinvTask { ST_TIP = 0, ST_OFF = 1, ST_DIAG = 2, ST_PART = 3 };
 
 // Geometry of one BTA matrix and the flag layout shared by all kernels.
+//
+// Elimination order.  With the separator block m = sep() < nt - 1 the blocks are
+// eliminated from both ends towards m (a "twisted" block Cholesky): the top chain
+// 0, 1, ..., m-1 downwards, the bottom chain nt-1, nt-2, ..., m+1 upwards, side by side,
+// then m, then the arrow tip.  Both chains are ordinary block-tridiagonal recurrences,
+// so nothing fills in and the flop count is the sequential one, while the longest chain
+// of dependent tile columns is about half as long.  m = nt - 1 (the default m = -1) is
+// the plain top-down order of the reference's Serinv recurrence.
+//
+// Block i is coupled to nxt(i), the neighbour eliminated after it (i + 1 above the
+// separator, i - 1 below it, none for m), through the b x b slot lslot(i) of the L
+// buffer, whose rows are those of block nxt(i) and whose columns those of block i.
+// Above the separator that is the caller's L_i = Q(i+1, i) itself; below it the slot
+// L_{i-1} holds Q(i-1, i), i.e. the caller's block transposed (launch_transpose_lslots
+// transposes those slots before a factorization; the selected inversion's write-back
+// transposes them back).  prev(i, k) lists the (one or two) neighbours eliminated
+// before i, whose Schur updates block i receives.
 struct Geom {
   int b, nt, a, B;   // block size, number of diagonal blocks, arrow size, tiles per block edge
+  int m = -1;        // separator block (-1: nt - 1, the top-down order)
   __host__ __device__ int fD(int i, int r, int c) const { return (i * B + r) * B + c; }
   __host__ __device__ int fL(int i, int r, int c) const { return nt * B * B + (i * B + r) * B + c; }
   __host__ __device__ int fR(int i, int c) const { return (2 * nt - 1) * B * B + i * B + c; }
@@ -40,16 +58,65 @@ struct Geom {
     const int v = b - r * TS;
     return v < TS ? v : TS;
   }
+  __host__ __device__ int sep() const { return m < 0 ? nt - 1 : m; }
+  __host__ __device__ bool twisted() const { return sep() < nt - 1; }
+  __host__ __device__ int nxt(int i) const {
+    const int s = sep();
+    return i < s ? i + 1 : (i > s ? i - 1 : -1);
+  }
+  __host__ __device__ int lslot(int i) const {
+    const int s = sep();
+    return i < s ? i : (i > s ? i - 1 : -1);
+  }
+  // row block and column block of L slot j
+  __host__ __device__ int lrow(int j) const { return j < sep() ? j + 1 : j; }
+  __host__ __device__ int lcol(int j) const { return j < sep() ? j : j + 1; }
+  // neighbours eliminated before block i (the top one first)
+  __host__ __device__ int nprev(int i) const {
+    const int s = sep();
+    if (i < s) return i > 0 ? 1 : 0;
+    if (i > s) return i < nt - 1 ? 1 : 0;
+    return (s > 0 ? 1 : 0) + (s < nt - 1 ? 1 : 0);
+  }
+  __host__ __device__ int prev(int i, int k) const {
+    const int s = sep();
+    if (i < s) return i - 1;
+    if (i > s) return i + 1;
+    return (k == 0 && s > 0) ? s - 1 : s + 1;
+  }
+  // Position u of a sequence that interleaves the top chain's n1 units with the bottom
+  // chain's n2 units (top, bottom, top, ... while both last, then the rest of the longer
+  // one): returns 0 (top) or 1 (bottom) and the unit index within that chain.
+  __host__ __device__ static int interleave(int n1, int n2, int u, int* k) {
+    const int mn = n1 < n2 ? n1 : n2;
+    if (u < 2 * mn) {
+      *k = u >> 1;
+      return u & 1;
+    }
+    *k = mn + (u - 2 * mn);
+    return n1 > mn ? 0 : 1;
+  }
+  // Blocks in elimination order: position q < nt -> block (interleaved chains, then m).
+  __host__ __device__ int elim_block(int q) const {
+    const int s = sep(), n1 = s, n2 = nt - 1 - s;
+    if (q >= n1 + n2) return s;
+    int k;
+    return interleave(n1, n2, q, &k) == 0 ? k : nt - 1 - k;
+  }
   // The feeder of diagonal tile (i, c): the tile right below it in the next global tile
-  // row, whose solve against (i, c) and product with itself are the last steps before
-  // the next diagonal tile can be factored.  0: none (last tile column of the matrix),
-  // 1: D_i(c + 1, c), 2: L_i(0, c) (c = B - 1, i < nt - 1).
-  __host__ __device__ int feeder_kind(int i, int c) const { return c + 1 < B ? 1 : (i < nt - 1 ? 2 : 0); }
+  // row of the elimination, whose solve against (i, c) and product with itself are the
+  // last steps before the next diagonal tile can be factored.  0: none (last tile column
+  // of the separator), 1: D_i(c + 1, c), 2: tile (0, c) of slot lslot(i).
+  __host__ __device__ int feeder_kind(int i, int c) const { return c + 1 < B ? 1 : (nxt(i) >= 0 ? 2 : 0); }
   __host__ __device__ int feeder_rows(int i, int c) const { return feeder_kind(i, c) == 1 ? vrows(c + 1) : vrows(0); }
   __host__ __device__ int feeder_quarters(int i, int c) const {
     return feeder_kind(i, c) ? (feeder_rows(i, c) + FEED_ROWS - 1) / FEED_ROWS : 0;
   }
 };
+
+// Separator block of the elimination order the solvers use: the middle block once there
+// are three or more blocks (two chains of about nt/2 blocks), else the plain order.
+inline int default_sep(int nt) { return nt >= 3 ? nt / 2 : nt - 1; }
 
 struct LaunchCtl {
   int* ctrl;
@@ -88,6 +155,11 @@ void count_launches(int n);
 // must be zero at launch (launch_clear_feeders, or a cleared flag array).
 void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow,
                    const int4* tasks, int ntasks, double* tip_part, const LaunchCtl& lc, int* feed_aux = nullptr);
+
+// Transpose, in place, the L slots below the separator (slots sep() .. nt-2): before a
+// factorization they hold the caller's Q(j+1, j), afterwards the factor needs Q(j, j+1).
+// No launch when the order is top-down.
+void launch_transpose_lslots(const Geom& g, double* L, cudaStream_t stream);
 
 // Zero the ready flags of the feeder tiles (Geom::feeder_kind): the FT_FEEDQ tasks of
 // a factorization add shares of the epoch to them.

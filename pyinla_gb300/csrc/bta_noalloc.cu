@@ -5,7 +5,9 @@
 // outside it (custom-call hooks of other frameworks, long-running services that
 // reserve their whole arena up front), and latency-sensitive loops where the implicit
 // device-wide synchronisation of cudaMalloc/cudaFree is not acceptable.  For them,
-// gbta_pobtaf_noalloc runs the FP64-product dataflow factorization kernel (k_factor),
+// gbta_pobtaf_noalloc runs the FP64-product dataflow factorization kernel (k_factor) in
+// the elimination order of gbta_pobtaf (so the sweeps and the inversion of a solver
+// accept its factor),
 // with every piece of its scratch -- control words, per-tile ready flags, the task
 // list and the arrow-tip partial products -- placed in one file-scope __device__ array
 // of GBTA_NOALLOC_SCRATCH_BYTES (64 MiB).  The caller passes only the block buffers.
@@ -39,28 +41,47 @@ namespace gbta {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[GBTA_NOALLOC_SCRATCH_BYTES];
 
 // Writes the factorization task list without the feeder split (no FT_PRE products and
-// no FT_FEEDQ row groups, which k_factor accepts when it is given no feeder flags):
-// per block i, per column c: DIAG, OFFD (r > c), LOW (i < nt-1), ARW (a > 0); then TIP
-// (a > 0).  Every task waits only for tasks earlier in this order.  One thread per
-// (i, c); the offset of column (i, c) is the number of tasks of the columns before it.
+// no FT_FEEDQ row groups, which k_factor accepts when it is given no feeder flags), in
+// the elimination order of the regular path: the columns of the two chains interleaved
+// one for one (Geom::interleave), then the separator's columns, then TIP (a > 0).  Per
+// column (i, c): DIAG, OFFD (r > c), LOW (every block but the separator), ARW (a > 0).
+// Every task waits only for tasks earlier in this order.  One thread per column; its
+// offset is the number of tasks of the columns before it, in closed form: a column c of
+// a chain has f(c) = 2B + ab - c tasks, one of the separator B + ab - c.
+__device__ __forceinline__ long long noalloc_chain_tasks(long long n, int B, int ab) {   // sum_{k<n} f(k % B)
+  const long long full = n / B, q = n % B;
+  const long long fb = (long long)B * (2 * B + ab) - (long long)B * (B - 1) / 2;
+  return full * fb + q * (2 * B + ab) - q * (q - 1) / 2;
+}
+
 __global__ void k_gen_factor_tasks(Geom g, int4* tasks) {
-  const int ic = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ic >= g.nt * g.B) return;
-  const int i = ic / g.B, c = ic % g.B;
-  const int lb = g.nt > 1 ? g.B : 0;                 // LOW tasks per column of a non-final block
-  const int ab = g.a > 0 ? 1 : 0;
-  const long long per_block = (long long)g.B * (1 + lb + ab) + (long long)g.B * (g.B - 1) / 2;
-  const int lo = (i < g.nt - 1) ? g.B : 0;
-  long long off = (long long)i * per_block + (long long)c * (1 + lb + ab) + (long long)c * (g.B - 1) -
-                  (long long)c * (c - 1) / 2;
-  // the final block has no LOW tasks: its columns are shorter
-  if (i == g.nt - 1 && i > 0) off = (long long)i * per_block + (long long)c * (1 + ab) + (long long)c * (g.B - 1) -
-                                    (long long)c * (c - 1) / 2;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= g.nt * g.B) return;
+  const int B = g.B, ab = g.a > 0 ? 1 : 0, sp = g.sep();
+  const int n1 = sp * B, n2 = (g.nt - 1 - sp) * B, mn = n1 < n2 ? n1 : n2;
+  int i, c;
+  long long off;
+  if (q < n1 + n2) {
+    int k;
+    const int ch = Geom::interleave(n1, n2, q, &k);
+    i = ch == 0 ? k / B : g.nt - 1 - k / B;
+    c = k % B;
+    if (q < 2 * mn)
+      off = 2 * noalloc_chain_tasks(q >> 1, B, ab) + ((q & 1) ? 2 * B + ab - c : 0);
+    else
+      off = noalloc_chain_tasks(mn, B, ab) + noalloc_chain_tasks(k, B, ab);
+  } else {
+    i = sp;
+    c = q - (n1 + n2);
+    const long long osep = noalloc_chain_tasks(mn, B, ab) + noalloc_chain_tasks(n1 + n2 - mn, B, ab);
+    off = osep + (long long)c * (B + ab) - (long long)c * (c - 1) / 2;
+  }
   tasks[off++] = make_int4(FT_DIAG, i, c, c);
-  for (int r = c + 1; r < g.B; ++r) tasks[off++] = make_int4(FT_OFFD, i, r, c);
-  for (int r = 0; r < lo; ++r) tasks[off++] = make_int4(FT_LOW, i, r, c);
+  for (int r = c + 1; r < B; ++r) tasks[off++] = make_int4(FT_OFFD, i, r, c);
+  if (g.nxt(i) >= 0)
+    for (int r = 0; r < B; ++r) tasks[off++] = make_int4(FT_LOW, i, r, c);
   if (ab) tasks[off++] = make_int4(FT_ARW, i, 0, c);
-  if (ab && ic == g.nt * g.B - 1) tasks[off] = make_int4(FT_TIP, 0, 0, 0);
+  if (ab && q == g.nt * B - 1) tasks[off] = make_int4(FT_TIP, 0, 0, 0);
 }
 
 }  // namespace gbta
@@ -128,6 +149,7 @@ extern "C" int gbta_pobtaf_noalloc(int b, int nt, int a, double* D, double* L, d
     return gbta_set_error(GBTA_ERR_CUDA, "noalloc pobtaf: cannot query the SM count");
 
   gbta::Geom g{b, nt, a, (b + gbta::TS - 1) / gbta::TS};
+  g.m = gbta::default_sep(nt);   // the elimination order of gbta_pobtaf
   const long long nflags = (2LL * nt - 1) * g.B * g.B + (long long)nt * g.B + 1;
   const long long per_block = (long long)g.B * (1 + (nt > 1 ? g.B : 0) + (a > 0 ? 1 : 0)) + (long long)g.B * (g.B - 1) / 2;
   const long long ntasks = nt * per_block - (nt > 1 ? (long long)g.B * g.B : 0) + (a > 0 ? 1 : 0);
@@ -148,6 +170,7 @@ extern "C" int gbta_pobtaf_noalloc(int b, int nt, int a, double* D, double* L, d
   if (e != cudaSuccess) return gbta_set_error(GBTA_ERR_CUDA, cudaGetErrorString(e));
   const int ncol = nt * g.B;
   gbta::k_gen_factor_tasks<<<(ncol + 127) / 128, 128, 0, st>>>(g, tasks);
+  if (nt > 1) gbta::launch_transpose_lslots(g, L, st);
   gbta::LaunchCtl lc;
   lc.ctrl = ctrl;
   lc.flags = flags;

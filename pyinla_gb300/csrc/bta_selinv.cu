@@ -79,7 +79,8 @@ __global__ void __launch_bounds__(NT) k_diag_inverses(const double* D, Geom g, d
 }
 
 // One CTA per off-diagonal pattern tile F(l, c) of block column i (the slots of D_i
-// below the diagonal, L_i and R_i): G = F(l, c) F(c, c)^{-1}, in place.
+// below the diagonal, block i's coupling slot lslot(i) and R_i): G = F(l, c) F(c, c)^{-1},
+// in place.
 __global__ void __launch_bounds__(NT) k_g_tiles(double* D, double* L, double* R, Geom g, int use_arrow,
                                                 const double* finv) {
   __shared__ double X[TILE_SMEM], W[TILE_SMEM];
@@ -99,10 +100,11 @@ __global__ void __launch_bounds__(NT) k_g_tiles(double* D, double* L, double* R,
     rows = g.b;
   } else if (slot < (2 * g.nt - 1) * B * B) {
     const int s2 = slot - g.nt * B * B;
-    i = s2 / (B * B);
+    const int j = s2 / (B * B);   // L slot j: columns of block lcol(j)
     const int r = (s2 / B) % B;
     c = s2 % B;
-    base = L + i * bb;
+    i = g.lcol(j);
+    base = L + j * bb;
     row0 = r * TS;
     rows = g.b;
   } else if (slot < (2 * g.nt - 1) * B * B + g.nt * B) {
@@ -134,7 +136,9 @@ void launch_selinv_prepare(const Geom& g, const double* D, double* L, double* R,
   count_launches(2);
 }
 
-// Copy Sigma back into the caller's buffers; D_i and T become full symmetric.
+// Copy Sigma back into the caller's buffers; D_i and T become full symmetric, and the
+// coupling slots below the separator (Sigma(j, j+1)) are transposed to the caller's
+// Sigma(j+1, j).
 __global__ void k_writeback(const double* SD, const double* SL, const double* SR, const double* ST, double* D,
                             double* L, double* R, double* T, Geom g, int use_arrow) {
   const size_t bb = (size_t)g.b * g.b;
@@ -148,7 +152,13 @@ __global__ void k_writeback(const double* SD, const double* SL, const double* SR
       const bool lower = (r / TS) >= (cc / TS);   // tiles on/below the diagonal are stored
       D[e] = lower ? SD[blk * bb + (size_t)r * g.b + cc] : SD[blk * bb + (size_t)cc * g.b + r];
     } else if (e < nD + nL) {
-      L[e - nD] = SL[e - nD];
+      const size_t blk = (e - nD) / bb, rem = (e - nD) % bb;
+      if ((int)blk >= g.sep()) {
+        const int r = (int)(rem / g.b), cc = (int)(rem % g.b);
+        L[e - nD] = SL[blk * bb + (size_t)cc * g.b + r];
+      } else {
+        L[e - nD] = SL[e - nD];
+      }
     } else if (e < nD + nL + nR) {
       R[e - nD - nL] = SR[e - nD - nL];
     } else {

@@ -8,7 +8,8 @@ namespace gbta {
 
 // ---- pre-passes over the factor ---------------------------------------------------
 // One CTA per (block i, column tile c): ecol[i*b + c*TS + j] = exponent of
-// max |F(m, j)| over the rows m of the column's pattern (D_i below tile c, L_i, R_i).
+// max |F(m, j)| over the rows m of the column's pattern (D_i below tile c, block i's
+// coupling slot, R_i).
 __global__ void __launch_bounds__(NT) k_fac_col_exponents(const double* D, const double* L, const double* R, Geom g,
                                                           int use_arrow, int* ecol) {
   __shared__ double red[NT];
@@ -20,8 +21,10 @@ __global__ void __launch_bounds__(NT) k_fac_col_exponents(const double* D, const
   double m = 0.0;
   if (col < g.b) {
     for (int row = (c + 1) * TS + r0; row < g.b; row += NT / TS) m = fmax(m, fabs(D[i * bb + (size_t)row * g.b + col]));
-    if (i < g.nt - 1)
-      for (int row = r0; row < g.b; row += NT / TS) m = fmax(m, fabs(L[i * bb + (size_t)row * g.b + col]));
+    if (g.nxt(i) >= 0) {
+      const size_t ls = (size_t)g.lslot(i);
+      for (int row = r0; row < g.b; row += NT / TS) m = fmax(m, fabs(L[ls * bb + (size_t)row * g.b + col]));
+    }
     if (use_arrow)
       for (int row = r0; row < g.a; row += NT / TS) m = fmax(m, fabs(R[i * ab + (size_t)row * g.b + col]));
   }
@@ -50,10 +53,11 @@ __global__ void __launch_bounds__(NT) k_fac_digits_t(const double* D, const doub
     t = make_tile(D + i * bb, g.b, r * TS, c * TS, g.b, g.b);
   } else if (slot < (2 * g.nt - 1) * B * B) {
     const int s2 = slot - g.nt * B * B;
-    i = s2 / (B * B);
+    const int j = s2 / (B * B);   // L slot j: columns of block lcol(j)
     r = (s2 / B) % B;
     c = s2 % B;
-    t = make_tile(L + i * bb, g.b, r * TS, c * TS, g.b, g.b);
+    i = g.lcol(j);
+    t = make_tile(L + j * bb, g.b, r * TS, c * TS, g.b, g.b);
   } else if (slot < (2 * g.nt - 1) * B * B + g.nt * B) {
     if (!use_arrow) return;
     const int s3 = slot - (2 * g.nt - 1) * B * B;

@@ -13,10 +13,13 @@
 // tile and C_k = F(k,k)^{-T} F(k,k)^{-1} per diagonal tile; then
 //   Sigma(j,k) = -sum_l Sigma(j,l) G(l,k),   Sigma(k,k) = C_k - sum_l Sigma(l,k)^T G(l,k)
 // and no task ends in a triangular solve.
-// P_k of tile column c of block i is: tiles of D_i below c, all tiles of L_i (block
-// row i+1) and the arrow tile.  Every Sigma(j,l) needed lies in a later column, so
-// tasks run column by column from the tip backwards; a task of column k starts its
-// products while column k+1 is still finishing.
+// P_k of tile column c of block i is: tiles of D_i below c, all tiles of block i's
+// coupling slot lslot(i) (block row nxt(i), the neighbour eliminated after i; see Geom)
+// and the arrow tile.  Every Sigma(j,l) needed lies in a column eliminated later, so
+// tasks run column by column in reverse elimination order: the tip, the separator
+// block, then the two chains outwards; a task of column k starts its products while
+// the column before it is still finishing.  Sigma of a coupling slot below the
+// separator is produced as Sigma(j, j+1) and transposed by the write-back.
 //
 // Sigma is written to a separate workspace (the factor tiles F(l,k) of a column are
 // read by all tasks of that column) and copied back into the caller's buffers by
@@ -66,7 +69,7 @@ struct SelinvArgs {
 };
 
 // Row descriptor of a tile row in the pattern of column (i, c):
-//   code in [0, B): block i row tile; [B, 2B): block i+1 row tile; 2B: arrow.
+//   code in [0, B): block i row tile; [B, 2B): block nxt(i) row tile; 2B: arrow.
 struct SigTile {
   Tile t;
   bool trans;
@@ -94,7 +97,7 @@ static __device__ SigTile sig_tile(const SelinvArgs& p, int i, int j, int l) {
     s.flag = F + g.fT();
   } else if (j == A || l == A) {
     const int other = (j == A) ? l : j;
-    const int blk = other < B ? i : i + 1;
+    const int blk = other < B ? i : g.nxt(i);
     const int r = other % B;
     s.t = make_tile(p.SR + blk * ab, g.b, 0, r * TS, g.a, g.b);
     s.trans = (l == A);
@@ -104,16 +107,16 @@ static __device__ SigTile sig_tile(const SelinvArgs& p, int i, int j, int l) {
     s.t = dtile(i, hi, lo);
     s.trans = j < l;
     s.flag = F + g.fD(i, hi, lo);
-  } else if (j >= B && l >= B) {   // both in block i+1
-    const int hi = max(j, l) - B, lo = min(j, l) - B;
-    s.t = dtile(i + 1, hi, lo);
+  } else if (j >= B && l >= B) {   // both in block nxt(i)
+    const int hi = max(j, l) - B, lo = min(j, l) - B, nx = g.nxt(i);
+    s.t = dtile(nx, hi, lo);
     s.trans = j < l;
-    s.flag = F + g.fD(i + 1, hi, lo);
-  } else {   // one in block i+1 (rows of SL_i), one in block i (cols of SL_i)
-    const int rl = (j >= B ? j : l) - B, cd = (j >= B ? l : j);
-    s.t = make_tile(p.SL + i * bb, g.b, rl * TS, cd * TS, g.b, g.b);
+    s.flag = F + g.fD(nx, hi, lo);
+  } else {   // one in block nxt(i) (rows of the coupling slot), one in block i (its cols)
+    const int rl = (j >= B ? j : l) - B, cd = (j >= B ? l : j), ls = g.lslot(i);
+    s.t = make_tile(p.SL + ls * bb, g.b, rl * TS, cd * TS, g.b, g.b);
     s.trans = j < B;
-    s.flag = F + g.fL(i, rl, cd);
+    s.flag = F + g.fL(ls, rl, cd);
   }
   return s;
 }
@@ -124,7 +127,7 @@ static __device__ __forceinline__ Tile fac_tile(const SelinvArgs& p, int i, int 
   const size_t bb = (size_t)g.b * g.b, ab = (size_t)g.a * g.b;
   const int B = g.B;
   if (l == 2 * B) return make_tile(p.R + i * ab, g.b, 0, c * TS, g.a, g.b);
-  if (l >= B) return make_tile(p.L + i * bb, g.b, (l - B) * TS, c * TS, g.b, g.b);
+  if (l >= B) return make_tile(p.L + g.lslot(i) * bb, g.b, (l - B) * TS, c * TS, g.b, g.b);
   return make_tile(p.D + i * bb, g.b, l * TS, c * TS, g.b, g.b);
 }
 
@@ -139,8 +142,8 @@ static __device__ __forceinline__ SigTile sig_dest(const SelinvArgs& p, int i, i
     s.t = make_tile(p.SR + i * ab, g.b, 0, c * TS, g.a, g.b);
     s.flag = p.c.flags + g.fR(i, c);
   } else if (j >= B) {
-    s.t = make_tile(p.SL + i * bb, g.b, (j - B) * TS, c * TS, g.b, g.b);
-    s.flag = p.c.flags + g.fL(i, j - B, c);
+    s.t = make_tile(p.SL + g.lslot(i) * bb, g.b, (j - B) * TS, c * TS, g.b, g.b);
+    s.flag = p.c.flags + g.fL(g.lslot(i), j - B, c);
   } else {
     s.t = make_tile(p.SD + i * bb, g.b, j * TS, c * TS, g.b, g.b);
     s.flag = p.c.flags + g.fD(i, j, c);
@@ -149,10 +152,10 @@ static __device__ __forceinline__ SigTile sig_dest(const SelinvArgs& p, int i, i
 }
 
 // Pattern of column (i, c), ordered so that the most recently produced Sigma tiles
-// come last: arrow, block i+1 rows descending, block i rows descending (> c).
+// come last: arrow, block nxt(i) rows descending, block i rows descending (> c).
 static __device__ __forceinline__ int pat_size(const SelinvArgs& p, int i, int c) {
   const Geom& g = p.g;
-  return (p.use_arrow ? 1 : 0) + (i < g.nt - 1 ? g.B : 0) + (g.B - 1 - c);
+  return (p.use_arrow ? 1 : 0) + (g.nxt(i) >= 0 ? g.B : 0) + (g.B - 1 - c);
 }
 static __device__ __forceinline__ int pat_code(const SelinvArgs& p, int i, int c, int s) {
   const Geom& g = p.g;
@@ -160,7 +163,7 @@ static __device__ __forceinline__ int pat_code(const SelinvArgs& p, int i, int c
     if (s == 0) return 2 * g.B;
     --s;
   }
-  if (i < g.nt - 1) {
+  if (g.nxt(i) >= 0) {
     if (s < g.B) return 2 * g.B - 1 - s;
     s -= g.B;
   }
@@ -299,7 +302,7 @@ static __device__ __forceinline__ bool selinv_fp64_task(const SelinvArgs& p, int
 static __device__ __forceinline__ int fac_slot(const Geom& g, int i, int l, int c) {
   const int B = g.B;
   if (l == 2 * B) return g.fR(i, c);
-  if (l >= B) return g.fL(i, l - B, c);
+  if (l >= B) return g.fL(g.lslot(i), l - B, c);
   return g.fD(i, l, c);
 }
 // Exponent value of an all-zero tile.
@@ -617,8 +620,11 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       // Sigma(j2, c2) = partial - Sigma(col, col) G(j2, c2) (the tile is symmetric, so
       // it is its own left operand untransposed).  That tile is the next link of the
       // column chain, so it is published first; this tile's store, digits and flag
-      // follow (its other consumers are later columns' products).
-      const int i2 = col > 0 ? i : i - 1, c2 = col > 0 ? col - 1 : g.B - 1, j2 = col > 0 ? col : g.B;
+      // follow (its other consumers are later columns' products).  After column (i, 0)
+      // the chain goes on in the one neighbour eliminated before i (none for the first
+      // block of a chain; two for the separator, whose next tiles ordinary tasks form).
+      const int i2 = col > 0 ? i : (g.nprev(i) == 1 ? g.prev(i, 0) : -1);
+      const int c2 = col > 0 ? col - 1 : g.B - 1, j2 = col > 0 ? col : g.B;
       if (p.merged && i2 >= 0) {
         __half* A0 = stages;   // stage 0: this tile's digits (no copy is in flight after the loop)
         __half* B0 = stages + OZ_OPER;

@@ -1,5 +1,7 @@
 // Per-task body of the BTA triangular sweeps, shared by the single-instance kernel
-// (bta_solve.cu) and the multi-instance kernel (bta_batch.cu).
+// (bta_solve.cu) and the multi-instance kernel (bta_batch.cu).  The tiles are solved in
+// the elimination order of the factor (Geom: top-down, or both chains towards the
+// separator block and then the separator; the backward sweep in reverse).
 //
 // Replaces the block forward / backward substitutions the reference runs through
 // Serinv (src/pyinla/solvers/structured_solver.py:112-140): trans = 0 solves
@@ -108,15 +110,43 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
   const bool fwd = p.trans == 0;
   {
     const unsigned long long t_task0 = c.trace ? gtimer() : 0ull;
+    // ticket -> tile in the elimination order of the blocks (Geom): forward, the tiles of
+    // the two chains interleaved one for one, then the separator's, then the arrow;
+    // backward, the arrow, the separator's tiles from the last, then both chains outwards
     bool is_arrow;
-    int gi;
-    if (fwd) {
-      is_arrow = t == ntile;
-      gi = t;
-    } else {
-      is_arrow = p.use_arrow && t == 0;
-      gi = ntile - 1 - (t - (p.use_arrow ? 1 : 0));
+    int i = 0, r = 0;
+    {
+      const int sp = g.sep(), n1 = sp * g.B, n2 = (g.nt - 1 - sp) * g.B;
+      if (fwd) {
+        is_arrow = t == ntile;
+        if (!is_arrow) {
+          if (t < n1 + n2) {
+            int k;
+            const int ch = Geom::interleave(n1, n2, t, &k);
+            i = ch == 0 ? k / g.B : g.nt - 1 - k / g.B;
+            r = k % g.B;
+          } else {
+            i = sp;
+            r = t - (n1 + n2);
+          }
+        }
+      } else {
+        is_arrow = p.use_arrow && t == 0;
+        const int u = t - (p.use_arrow ? 1 : 0);
+        if (!is_arrow) {
+          if (u < g.B) {
+            i = sp;
+            r = g.B - 1 - u;
+          } else {
+            int k;
+            const int ch = Geom::interleave(n1, n2, u - g.B, &k);
+            i = ch == 0 ? sp - 1 - k / g.B : sp + 1 + k / g.B;
+            r = g.B - 1 - k % g.B;
+          }
+        }
+      }
     }
+    const int gi = i * g.B + r;
     const int srow = threadIdx.x / NC, scol = threadIdx.x % NC;
 
     if (is_arrow) {
@@ -155,7 +185,6 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
       return true;
     }
 
-    const int i = gi / g.B, r = gi % g.B;
     const int rows = g.vrows(r);
     const int row0 = i * g.b + r * TS;
     // ---- independent of other tasks: Linv of the diagonal tile and M
@@ -168,6 +197,11 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
     smem_trsm_rln(Ws, Fs, rd);   // Ws = F^{-1}
     bool has_nb = false;
     DepTile nb;
+    // the neighbour tile: forward, the tile eliminated just before (i, r-1), or for r = 0
+    // the last tile of the first neighbour block eliminated before i, through its coupling
+    // slot; backward, the tile eliminated just after: (i, r+1), or for r = B-1 the first
+    // tile of nxt(i), through block i's coupling slot
+    const int np = g.nprev(i), nx = g.nxt(i), lsi = g.lslot(i);
     if (fwd) {
       if (r > 0) {
         has_nb = true;
@@ -175,12 +209,13 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
         nb.vrow0 = i * g.b + (r - 1) * TS;
         nb.vrows = g.vrows(r - 1);
         nb.flag = c.flags + vflag(g, i, r - 1);
-      } else if (i > 0) {
+      } else if (np > 0) {
+        const int p0 = g.prev(i, 0);
         has_nb = true;
-        nb.t = make_tile(p.L + (i - 1) * bb, g.b, 0, (g.B - 1) * TS, g.b, g.b);
-        nb.vrow0 = (i - 1) * g.b + (g.B - 1) * TS;
+        nb.t = make_tile(p.L + g.lslot(p0) * bb, g.b, 0, (g.B - 1) * TS, g.b, g.b);
+        nb.vrow0 = p0 * g.b + (g.B - 1) * TS;
         nb.vrows = g.vrows(g.B - 1);
-        nb.flag = c.flags + vflag(g, i - 1, g.B - 1);
+        nb.flag = c.flags + vflag(g, p0, g.B - 1);
       }
     } else {
       if (r < g.B - 1) {
@@ -189,12 +224,12 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
         nb.vrow0 = i * g.b + (r + 1) * TS;
         nb.vrows = g.vrows(r + 1);
         nb.flag = c.flags + vflag(g, i, r + 1);
-      } else if (i < g.nt - 1) {
+      } else if (nx >= 0) {
         has_nb = true;
-        nb.t = make_tile(p.L + i * bb, g.b, 0, r * TS, g.b, g.b);
-        nb.vrow0 = (i + 1) * g.b;
+        nb.t = make_tile(p.L + lsi * bb, g.b, 0, r * TS, g.b, g.b);
+        nb.vrow0 = nx * g.b;
         nb.vrows = g.vrows(0);
-        nb.flag = c.flags + vflag(g, i + 1, 0);
+        nb.flag = c.flags + vflag(g, nx, 0);
       }
     }
     if (has_nb) {
@@ -218,14 +253,17 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
     // ---- the other dependencies (all solved before the neighbour): s -= A_k v_k
     Ss[threadIdx.x] = (srow < rows && scol < p.nc) ? __ldcg(p.B + (size_t)(row0 + srow) * p.ldb + scol) : 0.0;
     __syncthreads();
-    int ndep, nfirst;
+    int ndep, nfirst, n0 = 0;
     if (fwd) {
-      // L_{i-1}(r, k) y(i-1, k) for k < B, D_i(r, k) y(i, k) for k < r, minus the neighbour
-      nfirst = (i > 0) ? ((r == 0) ? g.B - 1 : g.B) : 0;
+      // for each neighbour block p eliminated before i: S_p(r, k) y(p, k) for k < B (S_p
+      // its coupling slot), then D_i(r, k) y(i, k) for k < r, minus the neighbour tile
+      n0 = np > 0 ? ((r == 0) ? g.B - 1 : g.B) : 0;
+      nfirst = n0 + (np > 1 ? g.B : 0);
       ndep = nfirst + (r > 0 ? r - 1 : 0);
     } else {
-      // arrow, L_i(k, r)^T x(i+1, k) for k < B, D_i(k, r)^T x(i, k) for k > r, minus the neighbour
-      nfirst = (i < g.nt - 1) ? ((r == g.B - 1) ? g.B - 1 : g.B) : 0;
+      // arrow, S_i(k, r)^T x(nxt(i), k) for k < B, D_i(k, r)^T x(i, k) for k > r, minus the
+      // neighbour tile
+      nfirst = (nx >= 0) ? ((r == g.B - 1) ? g.B - 1 : g.B) : 0;
       ndep = (p.use_arrow ? 1 : 0) + nfirst + (r < g.B - 1 ? g.B - 2 - r : 0);
     }
     bool ok = true;
@@ -233,10 +271,11 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
       DepTile d;
       if (fwd) {
         if (st < nfirst) {
-          d.t = make_tile(p.L + (i - 1) * bb, g.b, r * TS, st * TS, g.b, g.b);
-          d.vrow0 = (i - 1) * g.b + st * TS;
-          d.vrows = g.vrows(st);
-          d.flag = c.flags + vflag(g, i - 1, st);
+          const int pb = g.prev(i, st < n0 ? 0 : 1), k = st < n0 ? st : st - n0;
+          d.t = make_tile(p.L + g.lslot(pb) * bb, g.b, r * TS, k * TS, g.b, g.b);
+          d.vrow0 = pb * g.b + k * TS;
+          d.vrows = g.vrows(k);
+          d.flag = c.flags + vflag(g, pb, k);
         } else {
           const int k = st - nfirst;   // k < r - 1
           d.t = make_tile(p.D + i * bb, g.b, r * TS, k * TS, g.b, g.b);
@@ -254,11 +293,11 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
         } else {
           if (p.use_arrow) --s2;
           if (s2 < nfirst) {
-            const int k = g.B - 1 - s2;   // L_i rows B-1 down to (r == B-1 ? 1 : 0)
-            d.t = make_tile(p.L + i * bb, g.b, k * TS, r * TS, g.b, g.b);
-            d.vrow0 = (i + 1) * g.b + k * TS;
+            const int k = g.B - 1 - s2;   // coupling slot rows B-1 down to (r == B-1 ? 1 : 0)
+            d.t = make_tile(p.L + lsi * bb, g.b, k * TS, r * TS, g.b, g.b);
+            d.vrow0 = nx * g.b + k * TS;
             d.vrows = g.vrows(k);
-            d.flag = c.flags + vflag(g, i + 1, k);
+            d.flag = c.flags + vflag(g, nx, k);
           } else {
             const int k = g.B - 1 - (s2 - nfirst);   // D_i rows B-1 down to r+2
             d.t = make_tile(p.D + i * bb, g.b, k * TS, r * TS, g.b, g.b);

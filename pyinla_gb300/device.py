@@ -31,24 +31,32 @@ def current_stream_ptr() -> int:
 
 
 class BtaHandle:
-    """Owns one ``gbta_solver`` (geometry b, nt, a on the current device)."""
+    """Owns one ``gbta_solver`` (geometry b, nt, a on the current device).
 
-    def __init__(self, b: int, nt: int, a: int):
+    ``twist`` selects the elimination order of the block recurrences (gbta_set_twist):
+    True, the library's default, eliminates from both ends towards the middle block
+    (half the critical path); False keeps Serinv's top-down order, whose factor blocks
+    and half-sweeps match Serinv's own.  Logdet, full solves and the selected inverse
+    agree either way."""
+
+    def __init__(self, b: int, nt: int, a: int, twist: bool = True):
         self.lib = _lib.load()
         self.b, self.nt, self.a = int(b), int(nt), int(a)
         h = ctypes.c_void_p()
         _lib.check(self.lib.gbta_create(self.b, self.nt, self.a, ctypes.byref(h)))
         self.ptr = h
+        _lib.check(self.lib.gbta_set_twist(self.ptr, 1 if twist else 0))
+        self.twist = bool(twist)
 
     @classmethod
-    def get(cls, b: int, nt: int, a: int) -> "BtaHandle":
+    def get(cls, b: int, nt: int, a: int, twist: bool = True) -> "BtaHandle":
         import torch
 
-        key = (int(b), int(nt), int(a), torch.cuda.current_device())
+        key = (int(b), int(nt), int(a), bool(twist), torch.cuda.current_device())
         with _hlock:
             h = _handles.get(key)
             if h is None:
-                h = cls(b, nt, a)
+                h = cls(b, nt, a, twist)
                 _handles[key] = h
             return h
 

@@ -37,12 +37,14 @@ def torch():
 
 
 def single_reference(torch, D, L, R, T, rhs, method):
-    """The single-instance path (algs + the C ABI) with the given product method."""
+    """The single-instance path (algs + the C ABI) with the given product method, in the
+    batch's elimination order (both ends towards the middle block)."""
     from pyinla_gb300 import algs
     from pyinla_gb300.device import BtaHandle
 
     nt, b, a = D.shape[0], D.shape[1], (R.shape[1] if R is not None else 0)
-    h = BtaHandle.get(b, nt, a)
+    algs.set_twisted(True)
+    h = BtaHandle.get(b, nt, a, True)
     old = h.method()
     h.set_method(method)
     try:
@@ -70,6 +72,7 @@ def single_reference(torch, D, L, R, T, rhs, method):
         return out
     finally:
         h.set_method(old)
+        algs.set_twisted(False)
 
 
 def make_instances(shapes):

@@ -40,19 +40,36 @@ METHODS = [0, 1]   # GBTA_METHOD_FP64, GBTA_METHOD_OZAKI
 
 @pytest.fixture
 def use_method(torch):
-    """Set the product method of the cached solver handles for one test."""
+    """Set the product method of the cached solver handles the algs drop-ins use (in
+    their current elimination order) for one test."""
+    from pyinla_gb300 import algs
     from pyinla_gb300.device import BtaHandle
 
     touched = []
 
     def _set(b, nt, a, method):
-        h = BtaHandle.get(b, nt, a)
+        h = BtaHandle.get(b, nt, a, algs._TWIST)
         touched.append((h, h.method()))
         h.set_method(method)
 
     yield _set
     for h, m in touched:
         h.set_method(m)
+
+
+TWIST = [False, True]   # Serinv's top-down order; both ends towards the middle block
+
+
+@pytest.fixture
+def order(torch):
+    """Run the algs drop-ins in the given elimination order for one test."""
+    from pyinla_gb300 import algs
+
+    def _set(twisted):
+        algs.set_twisted(twisted)
+
+    yield _set
+    algs.set_twisted(False)
 
 
 def dev(torch, *arrs):
@@ -73,11 +90,13 @@ def _golden(name):
     return g, D, L, R, T, rhs
 
 
+@pytest.mark.parametrize("twisted", TWIST)
 @pytest.mark.parametrize("method", METHODS)
 @pytest.mark.parametrize("name", GOLDEN_CASES)
-def test_bta_against_reference_golden(torch, use_method, name, method):
+def test_bta_against_reference_golden(torch, use_method, order, name, method, twisted):
     from pyinla_gb300 import algs
 
+    order(twisted)
     g, D, L, R, T, rhs = _golden(name)
     use_method(int(g["b"]), int(g["nt"]), int(g["a"]), method)
     Dd, Ld, Rd, Td = dev(torch, D, L, R, T)
@@ -110,11 +129,13 @@ def test_bta_against_reference_golden(torch, use_method, name, method):
     assert np.array_equal(ST, ST.T)
 
 
+@pytest.mark.parametrize("twisted", TWIST)
 @pytest.mark.parametrize("method", METHODS)
 @pytest.mark.parametrize("name", GOLDEN_CASES)
-def test_bt_against_reference_golden(torch, use_method, name, method):
+def test_bt_against_reference_golden(torch, use_method, order, name, method, twisted):
     from pyinla_gb300 import algs
 
+    order(twisted)
     g, D, L, R, T, rhs = _golden(name)
     use_method(int(g["b"]), int(g["nt"]), 0, method)
     nt, b = D.shape[0], D.shape[1]
@@ -147,26 +168,35 @@ SHAPES = [
 ]
 
 
+@pytest.mark.parametrize("twisted", TWIST)
 @pytest.mark.parametrize("method", METHODS)
 @pytest.mark.parametrize("seed,nt,b,a", SHAPES)
-def test_against_oracle_shapes(torch, use_method, seed, nt, b, a, method):
+def test_against_oracle_shapes(torch, use_method, order, seed, nt, b, a, method, twisted):
+    """In Serinv's order the factor and the lone N sweep match the oracle's as well;
+    in the two-sided order (a different factor of the same matrix) the logdet, the
+    N-then-C solution and the selected inverse do."""
     from pyinla_gb300 import algs
 
+    order(twisted)
     D, L, R, T, rhs = orc.make_bta_c1(seed, nt=nt, b=b, a=a, nrhs=5)
     use_method(b, nt, a, method)
     ref = [x.copy() for x in (D, L, R, T)]
     orc.pobtaf(*ref)
     Dd, Ld, Rd, Td = dev(torch, D, L, R, T)
     algs.pobtaf(Dd, Ld, Rd, Td)
-    for d, r in zip((Dd, Ld, Rd, Td), ref):
-        if r.size:
-            assert relerr(host(d), r) < RTOL
+    if not twisted:
+        for d, r in zip((Dd, Ld, Rd, Td), ref):
+            if r.size:
+                assert relerr(host(d), r) < RTOL
+    for i in range(nt):   # the factor's diagonal blocks are lower triangular either way
+        assert np.all(np.triu(host(Dd[i]), 1) == 0.0)
     assert abs(algs.logdet(Dd, Td, "bta") - orc.logdet(ref[0], ref[3])) <= RTOL * abs(orc.logdet(ref[0], ref[3]))
     xr = rhs.copy()
     orc.pobtas(*ref, xr, "N")
     x = torch.from_numpy(rhs.copy()).cuda()
     algs.pobtas(Dd, Ld, Rd, Td, x, "N")
-    assert relerr(host(x), xr) < RTOL
+    if not twisted:
+        assert relerr(host(x), xr) < RTOL
     orc.pobtas(*ref, xr, "C")
     algs.pobtas(Dd, Ld, Rd, Td, x, "C")
     assert relerr(host(x), xr) < RTOL
@@ -230,7 +260,7 @@ def test_wait_limit_timeout_is_reported_and_recoverable(torch):
     from pyinla_gb300.device import BtaHandle, current_stream_ptr
 
     D, L, R, T, rhs = orc.make_bta_c1(8, nt=24, b=96, a=4)
-    h = BtaHandle(96, 24, 4)
+    h = BtaHandle(96, 24, 4, twist=False)   # Serinv's order: the factor is compared below
     h.set_stream(current_stream_ptr())
     h.set_wait_limit_ms(1e-6)
     Dd, Ld, Rd, Td = dev(torch, D, L, R, T)

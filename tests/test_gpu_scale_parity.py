@@ -15,7 +15,9 @@ benchmark's own models, not on diagonally dominant random blocks:
   (b = 3072, 9 fixed effects) with nt = 2.
 
 Each is factored, solved (N then C), and inverted on the selected pattern with both
-product methods, and logdet, solution and every Sigma block are compared with the
+product methods and both elimination orders (both ends towards the middle block, the
+solvers' default, and Serinv's top-down order), and logdet, solution and every Sigma
+block are compared with the
 oracle (oracle/bta_oracle.py, pinned to the reference's DenseSolver and SerinvSolver
 wrapper by the golden fixtures) at 1e-10 relative: max-abs error over max-abs value of
 each block array.  The reference path these replace is
@@ -90,15 +92,17 @@ def torch():
     return _t
 
 
-@pytest.mark.parametrize("method", [0, 1])   # GBTA_METHOD_FP64, GBTA_METHOD_OZAKI
+@pytest.mark.parametrize("twisted", [True, False])   # the solvers' default order; Serinv's
+@pytest.mark.parametrize("method", [0, 1])            # GBTA_METHOD_FP64, GBTA_METHOD_OZAKI
 @pytest.mark.parametrize("name", CASES)
-def test_benchmark_sizes_match_oracle(torch, name, method):
+def test_benchmark_sizes_match_oracle(torch, name, method, twisted):
     from pyinla_gb300 import algs
     from pyinla_gb300.device import BtaHandle
 
     o = oracle_case(name)
     b, nt, a = o["geom"]
-    h = BtaHandle.get(b, nt, a)
+    algs.set_twisted(twisted)
+    h = BtaHandle.get(b, nt, a, twisted)
     old = h.method()
     h.set_method(method)
     try:
@@ -112,10 +116,11 @@ def test_benchmark_sizes_match_oracle(torch, name, method):
         torch.cuda.synchronize()
     finally:
         h.set_method(old)
+        algs.set_twisted(False)
     errs = {"logdet": abs(ld - o["logdet"]) / abs(o["logdet"]), "x": relerr(x.cpu().numpy(), o["x"])}
     for key, got, want in zip(("SD", "SL", "SR", "ST"), (Dd, Ld, Rd, Td), o["sigma"]):
         errs[key] = relerr(got.cpu().numpy(), want)
-    print(name, "method", method, {k: f"{v:.2e}" for k, v in errs.items()})
+    print(name, "method", method, "twisted", twisted, {k: f"{v:.2e}" for k, v in errs.items()})
     bad = {k: v for k, v in errs.items() if not v < RTOL}
     assert not bad, (name, method, errs)
 

@@ -108,30 +108,68 @@ def test_noalloc_call_takes_no_device_memory(lib):
     assert free1 >= free0, (free0, free1)
 
 
+def default_sep(nt):
+    """Separator block of the solvers' elimination order (middle block for nt >= 3)."""
+    return nt // 2 if nt >= 3 else nt - 1
+
+
+def interleave(n1, n2, u):
+    """(chain, index) of position u when n1 top-chain units and n2 bottom-chain units
+    are interleaved one for one, the longer chain's rest last."""
+    mn = min(n1, n2)
+    if u < 2 * mn:
+        return u & 1, u >> 1
+    return (0 if n1 > mn else 1), mn + (u - 2 * mn)
+
+
+def column_order(nt, B):
+    """Block columns (i, c) in elimination order: both chains interleaved, then the
+    separator block's columns."""
+    sp = default_sep(nt)
+    n1, n2 = sp * B, (nt - 1 - sp) * B
+    out = []
+    for u in range(n1 + n2):
+        ch, k = interleave(n1, n2, u)
+        out.append((k // B if ch == 0 else nt - 1 - k // B, k % B))
+    return out + [(sp, c) for c in range(B)]
+
+
 def plain_factor_tasks(nt, B, a):
     """The factorization task list without the feeder split, as (kind, i, r, c)."""
+    sp = default_sep(nt)
     out = []
-    for i in range(nt):
-        for c in range(B):
-            out.append(("DIAG", i, c, c))
-            out += [("OFFD", i, r, c) for r in range(c + 1, B)]
-            if i < nt - 1:
-                out += [("LOW", i, r, c) for r in range(B)]
-            if a > 0:
-                out.append(("ARW", i, 0, c))
+    for i, c in column_order(nt, B):
+        out.append(("DIAG", i, c, c))
+        out += [("OFFD", i, r, c) for r in range(c + 1, B)]
+        if i != sp:
+            out += [("LOW", i, r, c) for r in range(B)]
+        if a > 0:
+            out.append(("ARW", i, 0, c))
     if a > 0:
         out.append(("TIP", 0, 0, 0))
     return out
 
 
-def kernel_column_offset(nt, B, a, i, c):
-    """Offset of column (i, c)'s first task as k_gen_factor_tasks computes it."""
-    lb = B if nt > 1 else 0
+def kernel_column_offset(nt, B, a, q):
+    """Offset of the q-th column's first task as k_gen_factor_tasks computes it."""
     ab = 1 if a > 0 else 0
-    per_block = B * (1 + lb + ab) + B * (B - 1) // 2
-    if i == nt - 1 and i > 0:
-        return i * per_block + c * (1 + ab) + c * (B - 1) - c * (c - 1) // 2
-    return i * per_block + c * (1 + lb + ab) + c * (B - 1) - c * (c - 1) // 2
+    sp = default_sep(nt)
+    n1, n2 = sp * B, (nt - 1 - sp) * B
+    mn = min(n1, n2)
+
+    def chain(n):   # tasks of the first n chain columns, f(c) = 2B + ab - c
+        full, rem = divmod(n, B)
+        fb = B * (2 * B + ab) - B * (B - 1) // 2
+        return full * fb + rem * (2 * B + ab) - rem * (rem - 1) // 2
+
+    if q < n1 + n2:
+        _, k = interleave(n1, n2, q)
+        c = k % B
+        if q < 2 * mn:
+            return 2 * chain(q >> 1) + ((2 * B + ab - c) if q & 1 else 0)
+        return chain(mn) + chain(k)
+    c = q - (n1 + n2)
+    return chain(mn) + chain(n1 + n2 - mn) + c * (B + ab) - c * (c - 1) // 2
 
 
 def align256(n):
@@ -139,19 +177,20 @@ def align256(n):
 
 
 @pytest.mark.parametrize("nt,b,a", [(1, 40, 0), (1, 70, 5), (6, 70, 0), (6, 70, 5), (3, 32, 1), (16, 128, 4),
-                                    (2, 1, 0)])
+                                    (2, 1, 0), (7, 33, 2), (9, 64, 0)])
 def test_noalloc_task_count_and_offsets(lib, nt, b, a):
-    """CPU: the kernel's per-column offsets tile the plain task list exactly (no gap,
-    no overlap, TIP last), and gbta_noalloc_scratch_bytes sizes exactly that many
-    tasks next to the control words, flags and tip partials."""
+    """CPU: the kernel's per-column offsets tile the plain task list of the regular
+    path's elimination order exactly (no gap, no overlap, TIP last), and
+    gbta_noalloc_scratch_bytes sizes exactly that many tasks next to the control words,
+    flags and tip partials."""
     B = (b + TS - 1) // TS
     tasks = plain_factor_tasks(nt, B, a)
+    sp = default_sep(nt)
     pos = 0
-    for i in range(nt):
-        for c in range(B):
-            assert kernel_column_offset(nt, B, a, i, c) == pos, (i, c)
-            assert tasks[pos] == ("DIAG", i, c, c)
-            pos += 1 + (B - 1 - c) + (B if i < nt - 1 else 0) + (1 if a > 0 else 0)
+    for q, (i, c) in enumerate(column_order(nt, B)):
+        assert kernel_column_offset(nt, B, a, q) == pos, (q, i, c)
+        assert tasks[pos] == ("DIAG", i, c, c)
+        pos += 1 + (B - 1 - c) + (B if i != sp else 0) + (1 if a > 0 else 0)
     assert pos + (1 if a > 0 else 0) == len(tasks)
     nflags = (2 * nt - 1) * B * B + nt * B + 1
     want = align256(8 * 4) + align256(nflags * 4) + align256(len(tasks) * 16) + align256(nt * B * TS * TS * 8)
