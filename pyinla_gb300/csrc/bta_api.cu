@@ -58,6 +58,7 @@ struct gbta_solver {
   double* d_tip_part = nullptr;
   double* d_arrow_part = nullptr;
   int* d_faux = nullptr;      // feeder "products done" flags [nt*B]
+  int* d_dpre = nullptr;      // diagonal and feeder tiles' "partial stored" flags [2*nt*B]
   double* d_ld = nullptr;   // logdet partials [nt + 1] + result [1]
   double* d_sig = nullptr;  // selected-inversion output blocks (lazy)
   double* d_selws = nullptr;  // selected-inversion pre-pass: diagonal inverses (lazy)
@@ -68,6 +69,7 @@ struct gbta_solver {
   void* d_digits = nullptr;         // Ozaki digit planes (lazy)
   void* d_sdig = nullptr;           // Ozaki digit planes of the Sigma tiles (lazy)
   int* d_erow = nullptr;            // Ozaki row exponents (lazy)
+  int* d_tz = nullptr;              // Ozaki: leading zero digit planes per tile slot (lazy)
   size_t digit_bytes = 0;
   long long* d_trace = nullptr;   // task trace of the last launch (when enabled)
   long long trace_cap = 0;        // records
@@ -90,27 +92,50 @@ namespace gbta {
 // the two chains of the elimination order (Geom) are interleaved one for one, so that
 // the CTAs holding the earliest tickets serve both chains; then the separator's
 // columns, then the tip.
-static void factor_column_tasks(const Geom& g, int i, int c, std::vector<int4>& t) {
+// With diag_split, the products of diagonal tile (i, c) and of the feeder of column c,
+// except their last step(s), form FT_PART tasks at the end of column c-2's group (their
+// last operands before the last step are OFFD tasks of that group); column 1's, which
+// have only the neighbour blocks' terms, open column 0's group; a block's first column's
+// close column B-2's group of the block before it in the chain (the separator, with two
+// neighbours, opens its own first group).  The diagonal and feeder tasks themselves
+// become FT_TAIL tasks.
+static void column_partials(const Geom& g, int i, int c, std::vector<int4>& t) {
+  if (diag_has_partial(g, i, c)) t.push_back(make_int4(FT_DIAG | FT_PART, i, c, c));
   const int fk = g.feeder_kind(i, c);
-  if (fk == 1) t.push_back(make_int4(FT_OFFD | FT_PRE, i, c + 1, c));
-  if (fk == 2) t.push_back(make_int4(FT_LOW | FT_PRE, i, 0, c));
-  t.push_back(make_int4(FT_DIAG, i, c, c));
+  if (feeder_has_partial(g, i, c)) {
+    if (fk == 1) t.push_back(make_int4(FT_OFFD | FT_PRE | FT_PART, i, c + 1, c));
+    else t.push_back(make_int4(FT_LOW | FT_PRE | FT_PART, i, 0, c));
+  }
+}
+
+static void factor_column_tasks(const Geom& g, int i, int c, bool split, std::vector<int4>& t) {
+  const int fk = g.feeder_kind(i, c);
+  if (split && c == 0 && g.nprev(i) > 1) column_partials(g, i, 0, t);
+  if (split && c == 0 && g.B >= 2) column_partials(g, i, 1, t);
+  const int ftail = (split && feeder_has_partial(g, i, c)) ? FT_TAIL : 0;
+  if (fk == 1) t.push_back(make_int4(FT_OFFD | FT_PRE | ftail, i, c + 1, c));
+  if (fk == 2) t.push_back(make_int4(FT_LOW | FT_PRE | ftail, i, 0, c));
+  t.push_back(make_int4(FT_DIAG | (split && diag_has_partial(g, i, c) ? FT_TAIL : 0), i, c, c));
   for (int q = 0; q < g.feeder_quarters(i, c); ++q) t.push_back(make_int4(FT_FEEDQ, i, q, c));
   for (int r = c + 1 + (fk == 1 ? 1 : 0); r < g.B; ++r) t.push_back(make_int4(FT_OFFD, i, r, c));
   if (g.nxt(i) >= 0)
     for (int r = (fk == 2 ? 1 : 0); r < g.B; ++r) t.push_back(make_int4(FT_LOW, i, r, c));
   if (g.a > 0) t.push_back(make_int4(FT_ARW, i, 0, c));
+  if (split && c + 2 < g.B) column_partials(g, i, c + 2, t);
+  // the next block of the chain (the one whose only earlier neighbour is i)
+  const int n = g.nxt(i);
+  if (split && n >= 0 && g.nprev(n) == 1 && c == (g.B >= 2 ? g.B - 2 : 0)) column_partials(g, n, 0, t);
 }
 
-std::vector<int4> factor_task_list(const Geom& g) {
+std::vector<int4> factor_task_list(const Geom& g, bool diag_split) {
   std::vector<int4> t;
   const int s = g.sep(), n1 = s * g.B, n2 = (g.nt - 1 - s) * g.B;
   for (int u = 0; u < n1 + n2; ++u) {
     int k;
     const int i = Geom::interleave(n1, n2, u, &k) == 0 ? k / g.B : g.nt - 1 - k / g.B;
-    factor_column_tasks(g, i, k % g.B, t);
+    factor_column_tasks(g, i, k % g.B, diag_split, t);
   }
-  for (int c = 0; c < g.B; ++c) factor_column_tasks(g, s, c, t);
+  for (int c = 0; c < g.B; ++c) factor_column_tasks(g, s, c, diag_split, t);
   if (g.a > 0) t.push_back(make_int4(FT_TIP, 0, 0, 0));
   return t;
 }
@@ -168,6 +193,7 @@ gbta::LaunchCtl next_launch(gbta_solver* s, int ntasks) {
   if (s->epoch >= (1 << (31 - gbta::EPOCH_SHIFT)) - 1) {   // wrap: clear every epoch-stamped word
     cudaMemsetAsync(s->d_flags, 0, (size_t)s->g.nflags() * sizeof(int), s->stream);
     cudaMemsetAsync(s->d_faux, 0, (size_t)s->g.nt * s->g.B * sizeof(int), s->stream);
+    cudaMemsetAsync(s->d_dpre, 0, 2 * (size_t)s->g.nt * s->g.B * sizeof(int), s->stream);
     s->epoch = 1;
   }
   lc.ctrl = s->d_ctrl;
@@ -272,6 +298,8 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   CREATE_CUDA(cudaMalloc(&s->d_arrow_part, ntile * gbta::TS * gbta::SOLVE_NC * sizeof(double)));
   CREATE_CUDA(cudaMalloc(&s->d_faux, ntile * sizeof(int)));
   CREATE_CUDA(cudaMemsetAsync(s->d_faux, 0, ntile * sizeof(int), s->stream));
+  CREATE_CUDA(cudaMalloc(&s->d_dpre, 2 * ntile * sizeof(int)));
+  CREATE_CUDA(cudaMemsetAsync(s->d_dpre, 0, 2 * ntile * sizeof(int), s->stream));
   CREATE_CUDA(cudaMalloc(&s->d_ld, (nt + 2) * sizeof(double)));
   CREATE_CUDA(cudaMallocHost(&s->h_ctrl, CTRL_INTS * sizeof(int)));
   CREATE_CUDA(cudaMemsetAsync(s->d_ctrl, 0, CTRL_INTS * sizeof(int), s->stream));
@@ -283,7 +311,7 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
 #undef CREATE_CUDA
   s->ws_bytes = CTRL_INTS * sizeof(int) + (size_t)nflags * sizeof(int) + (ft.size() + st.size()) * sizeof(int4) +
                 ntile * gbta::TS * (gbta::TS + gbta::SOLVE_NC) * sizeof(double) + (nt + 2) * sizeof(double) +
-                ntile * sizeof(int);
+                3 * ntile * sizeof(int);
   *out = s;
   g_last_error.clear();
   return GBTA_OK;
@@ -300,6 +328,7 @@ int gbta_destroy(gbta_solver* s) {
   cudaFree(s->d_tip_part);
   cudaFree(s->d_arrow_part);
   cudaFree(s->d_faux);
+  cudaFree(s->d_dpre);
   cudaFree(s->d_ld);
   cudaFree(s->d_sig);
   cudaFree(s->d_selws);
@@ -307,6 +336,7 @@ int gbta_destroy(gbta_solver* s) {
   cudaFree(s->d_digits);
   cudaFree(s->d_sdig);
   cudaFree(s->d_erow);
+  cudaFree(s->d_tz);
   if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
   for (cudaEvent_t ev : s->tev)
     if (ev) cudaEventDestroy(ev);
@@ -321,11 +351,20 @@ int gbta_set_twist(gbta_solver* s, int enable) {
   if (m == s->g.sep()) return GBTA_OK;
   GBTA_CUDA(cudaStreamSynchronize(s->stream));
   s->g.m = m;
-  // the lists keep their lengths (every block but the separator has a coupling slot)
+  // the inversion's lists keep their lengths (every block but the separator has a
+  // coupling slot); the factorization's depends on which diagonal tiles get a partial
   const std::vector<int4> ft = gbta::factor_task_list(s->g), st = gbta::selinv_task_list(s->g),
                           stm = gbta::selinv_task_list(s->g, true);
-  if ((int)ft.size() != s->n_ftasks || (int)st.size() != s->n_stasks || stm.size() != st.size())
-    return fail(GBTA_ERR_ARG, "internal: task list length changed with the elimination order");
+  if ((int)st.size() != s->n_stasks || stm.size() != st.size())
+    return fail(GBTA_ERR_ARG, "internal: selected-inversion task list length changed with the elimination order");
+  if ((int)ft.size() != s->n_ftasks) {
+    int4* d = nullptr;
+    GBTA_CUDA(cudaMalloc(&d, ft.size() * sizeof(int4)));
+    cudaFree(s->d_ftasks);
+    s->d_ftasks = d;
+    s->ws_bytes = s->ws_bytes - (size_t)s->n_ftasks * sizeof(int4) + ft.size() * sizeof(int4);
+    s->n_ftasks = (int)ft.size();
+  }
   GBTA_CUDA(cudaMemcpy(s->d_ftasks, ft.data(), ft.size() * sizeof(int4), cudaMemcpyHostToDevice));
   GBTA_CUDA(cudaMemcpy(s->d_stasks, st.data(), st.size() * sizeof(int4), cudaMemcpyHostToDevice));
   GBTA_CUDA(cudaMemcpy(s->d_stasks_m, stm.data(), stm.size() * sizeof(int4), cudaMemcpyHostToDevice));
@@ -440,9 +479,11 @@ static int ensure_digits(gbta_solver* s) {
   GBTA_CUDA(cudaStreamSynchronize(s->stream));
   const size_t bytes = gbta::factor_oz_digit_bytes(s->g);
   const size_t ebytes = ((size_t)s->g.nt * s->g.b + s->g.a) * sizeof(int);
+  const size_t zbytes = (size_t)s->g.nflags() * sizeof(int);
   GBTA_CUDA(cudaMalloc(&s->d_digits, bytes));
   GBTA_CUDA(cudaMalloc(&s->d_erow, ebytes));
-  s->digit_bytes = bytes + ebytes;
+  GBTA_CUDA(cudaMalloc(&s->d_tz, zbytes));
+  s->digit_bytes = bytes + ebytes + zbytes;
   return GBTA_OK;
 }
 
@@ -460,9 +501,10 @@ static int factor_async(gbta_solver* s, double* D, double* L, double* R, double*
   if (s->timing) GBTA_CUDA(cudaEventRecord(s->tev[0], s->stream));
   if (s->method == GBTA_METHOD_OZAKI)
     gbta::launch_factor_oz(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part,
-                           (__half*)s->d_digits, s->d_erow, lc, s->d_faux);
+                           (__half*)s->d_digits, s->d_erow, lc, s->d_faux, s->d_dpre);
   else
-    gbta::launch_factor(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part, lc, s->d_faux);
+    gbta::launch_factor(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part, lc, s->d_faux,
+                        s->d_dpre);
   GBTA_CUDA(cudaGetLastError());
   if (s->timing) {
     GBTA_CUDA(cudaEventRecord(s->tev[1], s->stream));
@@ -545,8 +587,9 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
   if (use_arrow && (!R || !T)) return fail(GBTA_ERR_ARG, "R/T must be device pointers for the bta selected inversion");
   const gbta::Geom& g = s->g;
   const size_t bb = (size_t)g.b * g.b;
+  const bool inplace = s->method == GBTA_METHOD_OZAKI;   // Sigma over the factor (see below)
   const size_t need = g.nt * bb + (g.nt - 1) * bb + (size_t)g.nt * g.a * g.b + (size_t)g.a * g.a;
-  if (s->sig_elems < need) {
+  if (!inplace && s->sig_elems < need) {
     GBTA_CUDA(cudaStreamSynchronize(s->stream));
     cudaFree(s->d_sig);
     s->d_sig = nullptr;
@@ -559,10 +602,14 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
     GBTA_CUDA(cudaMalloc(&s->d_selws, gbta::selinv_prepare_bytes(g)));
   }
   const double* cinv = s->d_selws + (size_t)g.nt * g.B * gbta::TS * gbta::TS;
-  double* SD = s->d_sig;
-  double* SL = SD + g.nt * bb;
-  double* SR = SL + (g.nt - 1) * bb;
-  double* ST = SR + (size_t)g.nt * g.a * g.b;
+  // The tensor-core method reads the factor only through its digit planes, sliced by the
+  // pre-pass, and the tip task reads T before it writes Sigma_T: Sigma goes straight
+  // into the caller's buffers.  The FP64 method reads the factor tiles during the
+  // inversion, so Sigma goes to a workspace and is copied back.
+  double* SD = inplace ? D : s->d_sig;
+  double* SL = inplace ? L : SD + g.nt * bb;
+  double* SR = inplace ? R : SL + (g.nt - 1) * bb;
+  double* ST = inplace ? T : SR + (size_t)g.nt * g.a * g.b;
   if (s->method == GBTA_METHOD_OZAKI) {
     if (int r = ensure_digits(s)) return r;
     if (!s->d_sdig) {
@@ -579,7 +626,8 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
   if (s->method == GBTA_METHOD_OZAKI)
     gbta::launch_selinv_oz(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks_m, s->n_stasks,
                            (__half*)s->d_digits, s->d_erow, cinv, (__half*)s->d_sdig, s->d_tip_part, s->d_faux,
-                           lc);
+                           lc,
+                           g.nflags() < (1 << 24) ? s->d_tz : nullptr);
   else
     gbta::launch_selinv(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks, cinv, lc);
   GBTA_CUDA(cudaGetLastError());
@@ -587,7 +635,10 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
     GBTA_CUDA(cudaEventRecord(s->tev[3], s->stream));
     s->timed[1] = true;
   }
-  gbta::launch_selinv_writeback(g, SD, SL, SR, ST, D, L, R, T, use_arrow, s->stream);
+  if (inplace)
+    gbta::launch_selinv_finish_inplace(g, D, L, s->stream);
+  else
+    gbta::launch_selinv_writeback(g, SD, SL, SR, ST, D, L, R, T, use_arrow, s->stream);
   GBTA_CUDA(cudaGetLastError());
   return GBTA_OK;
 }

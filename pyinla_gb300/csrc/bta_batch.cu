@@ -141,6 +141,7 @@ struct BatchInst {
   __half* digits = nullptr;   // Ozaki only
   int* erow = nullptr;        // Ozaki only
   __half* sdig = nullptr;     // Ozaki only: digit planes of the Sigma tiles
+  int* tz = nullptr;          // Ozaki only: leading zero digit planes per tile slot
   // bound caller buffers
   double *D = nullptr, *L = nullptr, *R = nullptr, *T = nullptr, *rhs = nullptr;
 };
@@ -264,6 +265,7 @@ int build_args(gbta_batch* bt) {
     f.erow = q.erow;
     f.info = bt->d_info + k;
     f.feed_pre = bt->d_faux + q.faux_off;
+    f.diag_pre = bt->d_faux + q.faux_off + (size_t)g.nt * g.B;
     f.c = batch_ctl(bt, flags, EP_FACTOR);
     gbta::SelinvArgs& s = sa[k];
     const size_t bb = (size_t)g.b * g.b;
@@ -271,16 +273,24 @@ int build_args(gbta_batch* bt) {
     s.L = q.L;
     s.R = q.R;
     s.T = q.T;
-    s.SD = q.sig;
-    s.SL = q.sig + (size_t)g.nt * bb;
-    s.SR = s.SL + (size_t)(g.nt - 1) * bb;
-    s.ST = s.SR + (size_t)g.nt * g.a * g.b;
+    if (q.method == GBTA_METHOD_OZAKI) {   // Sigma over the factor (gbta_pobtasi does the same)
+      s.SD = q.D;
+      s.SL = q.L;
+      s.SR = q.R;
+      s.ST = q.T;
+    } else {
+      s.SD = q.sig;
+      s.SL = q.sig + (size_t)g.nt * bb;
+      s.SR = s.SL + (size_t)(g.nt - 1) * bb;
+      s.ST = s.SR + (size_t)g.nt * g.a * g.b;
+    }
     s.g = g;
     s.use_arrow = use_arrow;
     s.method = q.method;
     s.tasks = q.stasks;
     s.ntasks = q.n_stasks;
     s.fdig = q.digits;
+    s.fdz = q.g.nflags() < (1 << 24) ? q.tz : nullptr;
     s.ecol = q.erow;
     s.sdig = q.sdig;
     s.merged = q.method == GBTA_METHOD_OZAKI;
@@ -371,7 +381,8 @@ int run_async(gbta_batch* bt, int phases, double* logdet_out) {
       gbta::launch_selinv_prepare(q.g, q.D, q.L, q.R, q.g.a > 0, q.selws, st);
     for (const BatchInst& q : bt->inst)
       if (q.method == GBTA_METHOD_OZAKI)
-        gbta::launch_selinv_oz_prepare(q.g, q.D, q.L, q.R, q.g.a > 0, q.digits, q.erow, st);
+        gbta::launch_selinv_oz_prepare(q.g, q.D, q.L, q.R, q.g.a > 0, q.digits, q.erow,
+                                       q.g.nflags() < (1 << 24) ? q.tz : nullptr, st);
     if (int r = reset_ticket(bt)) return r;
     gbta::k_selinv_batch<<<grid_of(bt, (const void*)gbta::k_selinv_batch, gbta::BATCH_SELINV_SMEM, bt->n_sorder), gbta::NT,
                             gbta::BATCH_SELINV_SMEM, st>>>(
@@ -379,6 +390,10 @@ int run_async(gbta_batch* bt, int phases, double* logdet_out) {
     gbta::count_launches(1);
     for (const BatchInst& q : bt->inst) {
       const gbta::Geom& g = q.g;
+      if (q.method == GBTA_METHOD_OZAKI) {
+        gbta::launch_selinv_finish_inplace(g, q.D, q.L, st);
+        continue;
+      }
       const size_t bb = (size_t)g.b * g.b;
       double* SD = q.sig;
       double* SL = SD + (size_t)g.nt * bb;
@@ -432,7 +447,7 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
   size_t off = 0, flags_total = 0;
   std::vector<std::vector<int4>> ft(n), st(n);
   std::vector<size_t> o_ft(n), o_st(n), o_tip(n), o_arw(n), o_ld(n), o_sig(n), o_sel(n), o_dig(n), o_erow(n),
-      o_sdig(n);
+      o_sdig(n), o_tz(n);
   for (int k = 0; k < n; ++k) {
     BatchInst& q = bt->inst[k];
     q.g = gbta::Geom{b[k], nt[k], a[k], (b[k] + gbta::TS - 1) / gbta::TS};
@@ -446,7 +461,7 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
     q.n_vtasks = g.nt * g.B + (g.a > 0 ? 1 : 0);
     q.flags_off = flags_total;
     q.faux_off = bt->nfaux_total;
-    bt->nfaux_total += (size_t)g.nt * g.B;
+    bt->nfaux_total += 3 * (size_t)g.nt * g.B;   // feeder flags, then diagonal- and feeder-partial flags
     flags_total += (size_t)g.nflags();
     const size_t ntile = (size_t)g.nt * g.B, bb = (size_t)g.b * g.b;
     o_ft[k] = off;
@@ -459,11 +474,13 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
     off = align_up(off + ntile * gbta::TS * gbta::SOLVE_NC * sizeof(double));
     o_ld[k] = off;
     off = align_up(off + (g.nt + 2) * sizeof(double));
-    o_sig[k] = off;
-    off = align_up(off + (g.nt * bb + (g.nt - 1) * bb + (size_t)g.nt * g.a * g.b + (size_t)g.a * g.a) * sizeof(double));
+    o_sig[k] = off;   // Sigma workspace: FP64 method only (the tensor-core method writes in place)
+    if (q.method != GBTA_METHOD_OZAKI)
+      off = align_up(off + (g.nt * bb + (g.nt - 1) * bb + (size_t)g.nt * g.a * g.b + (size_t)g.a * g.a) *
+                               sizeof(double));
     o_sel[k] = off;
     off = align_up(off + gbta::selinv_prepare_bytes(g));
-    o_dig[k] = o_erow[k] = o_sdig[k] = 0;
+    o_dig[k] = o_erow[k] = o_sdig[k] = o_tz[k] = 0;
     if (q.method == GBTA_METHOD_OZAKI) {
       o_dig[k] = off;
       off = align_up(off + gbta::factor_oz_digit_bytes(g));
@@ -471,6 +488,8 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
       off = align_up(off + ((size_t)g.nt * g.b + g.a) * sizeof(int));
       o_sdig[k] = off;
       off = align_up(off + gbta::selinv_oz_digit_bytes(g));
+      o_tz[k] = off;
+      off = align_up(off + (size_t)g.nflags() * sizeof(int));
     }
   }
   bt->pool_bytes = off;
@@ -499,6 +518,7 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
       q.digits = reinterpret_cast<__half*>(base + o_dig[k]);
       q.erow = reinterpret_cast<int*>(base + o_erow[k]);
       q.sdig = reinterpret_cast<__half*>(base + o_sdig[k]);
+      q.tz = reinterpret_cast<int*>(base + o_tz[k]);
     }
     CREATE_CUDA(cudaMemcpy(q.ftasks, ft[k].data(), ft[k].size() * sizeof(int4), cudaMemcpyHostToDevice));
     CREATE_CUDA(cudaMemcpy(q.stasks, st[k].data(), st[k].size() * sizeof(int4), cudaMemcpyHostToDevice));

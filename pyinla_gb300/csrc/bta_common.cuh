@@ -180,8 +180,10 @@ __device__ __forceinline__ void cta_publish_val(const Ctl& c, int* flag, int pay
 // second, each with an acquire load, so one memory round trip covers all of them and
 // no GPU-scope fence is needed (a fence waits for the CTA's own outstanding writes,
 // which costs thousands of cycles in a busy kernel).  `flags_of(s, f0, f1)` returns the
-// step's flags (nullptr = none).  The caller synchronises the CTA afterwards, which
-// extends the acquires to all its threads.
+// step's flags (nullptr = none).  The caller synchronises the CTA before the call (the
+// other warps decide from *s_ready whether to call it, so they must have read it before
+// warp 0 rewrites it; a warp that read the new value would skip the call and its
+// barriers) and afterwards, which extends the acquires to all its threads.
 constexpr int SCAN_AHEAD = 16;
 static_assert(2 * SCAN_AHEAD <= 32, "one lane per flag");
 
@@ -260,7 +262,11 @@ __device__ __forceinline__ void cta_raise(int* flag, int v) {
 }
 
 // Pull the next ticket (CTA-uniform).
+// Between tasks every thread also orders its generic shared-memory writes (a task's
+// FP64 scratch) before the bulk copies (async proxy) that a later task issues into the
+// same bytes.
 __device__ __forceinline__ int cta_ticket(const Ctl& c, int* s_t) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   __syncthreads();
   if (threadIdx.x == 0) *s_t = ld_relaxed(c.ctrl + CTRL_ABORT) ? -1 : atomicAdd(c.ctrl + CTRL_TICKET, 1);
   __syncthreads();

@@ -67,7 +67,7 @@ void launch_clear_feeders(const Geom& g, int* flags, cudaStream_t stream) {
 }
 
 void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow, const int4* tasks,
-                   int ntasks, double* tip_part, const LaunchCtl& lc, int* feed_aux) {
+                   int ntasks, double* tip_part, const LaunchCtl& lc, int* feed_aux, int* diag_pre) {
   FactorArgs p;
   p.D = D;
   p.L = L;
@@ -83,6 +83,7 @@ void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, in
   p.erow = nullptr;
   p.info = nullptr;
   p.feed_pre = feed_aux;
+  p.diag_pre = diag_pre;
   p.c.ctrl = lc.ctrl;
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;

@@ -46,8 +46,49 @@ struct FactorArgs {
   const int* erow;      // Ozaki: [nt*b + a] row exponents
   int* info;            // where a failed pivot is recorded (null: the control block)
   int* feed_pre;        // [nt*B] flag: the feeder of diagonal tile (i, c) has its products
+  int* diag_pre;        // [2*nt*B] flags: diagonal tile (i, c), then the feeder of column
+                        // (i, c), holds its partial products (split loops; see FT_PART)
   Ctl c;
 };
+
+// Product steps of a task's left-looking loop: the (one or two) neighbour blocks'
+// columns first (prev = true, neighbour pb, column k), then the columns k < col of its
+// own block.  A diagonal tile's loop and its column's feeder loop are split into a
+// partial (every step but the last: k = col - 1, or k = B - 1 of each neighbour when
+// col = 0) and a tail (those last steps) when the task list splits them (FT_PART /
+// FT_TAIL).
+struct StepRange {
+  int n;      // steps
+  int mode;   // 0 full, 1 partial, 2 tail
+  int nprev;  // leading steps that are neighbour-block terms
+};
+static __device__ __forceinline__ StepRange step_range(const Geom& g, int type, int mode, int i, int col) {
+  const int np = (type != FT_LOW) ? g.nprev(i) : 0;
+  if (mode == 1) return col == 0 ? StepRange{np * (g.B - 1), 1, np * (g.B - 1)} : StepRange{np * g.B + col - 1, 1, np * g.B};
+  if (mode == 2) return col == 0 ? StepRange{np, 2, np} : StepRange{1, 2, 0};
+  return StepRange{np * g.B + col, 0, np * g.B};
+}
+// Step s of a range: a neighbour-block term (prev: neighbour pb, its column k) or a term
+// of the task's own block (column k).
+static __device__ __forceinline__ void step_src(const Geom& g, const StepRange& sr, int i, int col, int s, bool& prev,
+                                                int& pb, int& k) {
+  prev = s < sr.nprev;
+  if (!prev) {
+    pb = i;
+    k = sr.mode == 2 ? col - 1 : s - sr.nprev;
+    return;
+  }
+  if (sr.mode == 2) {          // the feeder tile of each neighbour's last column
+    pb = g.prev(i, s);
+    k = g.B - 1;
+  } else if (sr.mode == 1 && col == 0) {   // every neighbour column but the last
+    pb = g.prev(i, s / (g.B - 1));
+    k = s % (g.B - 1);
+  } else {
+    pb = g.prev(i, s / g.B);
+    k = s % g.B;
+  }
+}
 
 static __device__ __forceinline__ const double* Dblk(const FactorArgs& p, int i) {
   return p.D + (size_t)i * p.g.b * p.g.b;
@@ -219,6 +260,9 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
     const int4 tk = p.tasks[t];
     const int type = tk.x & 7, i = tk.y, r = tk.z, col = tk.w;
     const bool pre_only = (tk.x & FT_PRE) != 0;
+    // split loops (FT_PART / FT_TAIL on a diagonal task or a feeder's FT_PRE task)
+    const int dmode = (tk.x & FT_PART) ? 1 : ((tk.x & FT_TAIL) ? 2 : 0);
+    int* part_flag = (type == FT_DIAG ? p.diag_pre : p.diag_pre + g.nt * g.B) + i * g.B + col;
     if (!p.use_arrow && (type == FT_ARW || type == FT_TIP)) return true;
     if (type == FT_FEEDQ) return factor_feed_rows(p, t, i, r, col, X, F, sm + 2 * TILE_SMEM, vec, nullptr, &s_ok, t_task0);
 
@@ -277,6 +321,8 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
       tgt = atile(tgt_blk, g, col);
       tgt_flag = c.flags + g.fR(i, col);
     }
+    // a tail starts from the partial its FT_PART task stored
+    if (dmode == 2 && !cta_wait(c, part_flag, nullptr, &s_ok)) return false;
     tile_load(X, tgt);
     __syncthreads();
     acc_from_smem(acc, X);
@@ -284,15 +330,18 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
 
     // previous block columns: the Schur terms of the (one or two) neighbours eliminated
     // before block i, through their coupling slots (L tiles have none: Q(nxt(i), p) = 0)
-    const int nprev = (type != FT_LOW) ? g.nprev(i) * g.B : 0;
-    const int nsteps = nprev + col;
+    const StepRange sr = step_range(g, type, dmode, i, col);
+    const int nsteps = sr.n;
     const int lsi = g.lslot(i);
     auto step_of = [&](int s) -> Step {
       Step st;
       st.ta = false;
       st.tb = true;
-      if (s < nprev) {
-        const int pb = g.prev(i, s / g.B), ls = g.lslot(pb), k = s % g.B;
+      bool isprev;
+      int pb, k;
+      step_src(g, sr, i, col, s, isprev, pb, k);
+      if (isprev) {
+        const int ls = g.lslot(pb);
         if (type == FT_ARW) {
           st.a = atile(Rblk(p, pb), g, k);
           st.fa = c.flags + g.fR(pb, k);
@@ -303,7 +352,6 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
         st.b = btile(Lblk(p, ls), g, col, k);
         st.fb = c.flags + g.fL(ls, col, k);
       } else {           // within the block column: tiles k < col of the same row
-        const int k = s - nprev;
         if (type == FT_ARW) {
           st.a = atile(Rblk(p, i), g, k);
           st.fa = c.flags + g.fR(i, k);
@@ -324,6 +372,12 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
     acc_to_smem(acc, X);
     __syncthreads();
 
+    if (dmode == 1) {   // a partial: stored for its tail task
+      tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
+      cta_publish(c, part_flag);
+      trace_task(c, t, type, t_task0);
+      return true;
+    }
     if (pre_only) {   // feeder products: the FT_FEEDQ tasks finish the tile
       tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
       cta_publish(c, p.feed_pre + i * g.B + col);
@@ -425,6 +479,9 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
     const int4 tk = p.tasks[t];
     const int type = tk.x & 7, i = tk.y, r = tk.z, col = tk.w;
     const bool pre_only = (tk.x & FT_PRE) != 0;
+    // split loops (FT_PART / FT_TAIL on a diagonal task or a feeder's FT_PRE task)
+    const int dmode = (tk.x & FT_PART) ? 1 : ((tk.x & FT_TAIL) ? 2 : 0);
+    int* part_flag = (type == FT_DIAG ? p.diag_pre : p.diag_pre + g.nt * g.B) + i * g.B + col;
     if (!p.use_arrow && (type == FT_ARW || type == FT_TIP)) return true;
     if (type == FT_FEEDQ)
       return factor_feed_rows(p, t, i, r, col, X, F, reinterpret_cast<double*>(stages), vec, erow_t, &s_ok, t_task0);
@@ -489,6 +546,8 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
       erow_t[threadIdx.x] = (threadIdx.x < tgt.rows) ? p.erow[row_base + threadIdx.x] : 0;
       ecol_t[threadIdx.x] = (threadIdx.x < tgt.cols) ? p.erow[col_base + threadIdx.x] : 0;
     }
+    // a tail starts from the partial its FT_PART task stored
+    if (dmode == 2 && !cta_wait(c, part_flag, nullptr, &s_ok)) return false;
     tile_load(X, tgt);
     __syncthreads();
     OzAcc acc;
@@ -504,16 +563,18 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
 
     // ---- product loop over the final tiles left of the target (previous block
     //      column first, then columns k < col of this block)
-    const int nprev = (type != FT_LOW) ? g.nprev(i) * g.B : 0;
-    const int nsteps = nprev + col;
+    const StepRange sr = step_range(g, type, dmode, i, col);
+    const int nsteps = sr.n;
     const int lsi = g.lslot(i);
     auto slots = [&](int s, int& sa, int& sb) {
-      if (s < nprev) {
-        const int pb = g.prev(i, s / g.B), ls = g.lslot(pb), k = s % g.B;
+      bool isprev;
+      int pb, k;
+      step_src(g, sr, i, col, s, isprev, pb, k);
+      if (isprev) {
+        const int ls = g.lslot(pb);
         sa = (type == FT_ARW) ? g.fR(pb, k) : g.fL(ls, r, k);
         sb = g.fL(ls, col, k);
       } else {
-        const int k = s - nprev;
         sa = (type == FT_ARW) ? g.fR(i, k) : (type == FT_LOW) ? g.fL(lsi, r, k) : g.fD(i, r, k);
         sb = g.fD(i, col, k);
       }
@@ -565,7 +626,8 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
         bool issued = false;
         int na = 0, nb = 0;
         if (more) {
-          if (s_ready <= s + 1) {   // uniform: read after the barrier
+          if (s_ready <= s + 1) {   // uniform: read after the barrier, rewritten after the next one
+            __syncthreads();   // every warp has read s_ready before warp 0 advances it
             scan_ready(c, nsteps, flags_of, &s_ready);
             __syncthreads();
             if (c.trace && s_ready >= nsteps && !t_alldeps) t_alldeps = gtimer();
@@ -599,6 +661,12 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
       for (int j = 0; j < 4; ++j) X[oz_row(n, j) * LDS + oz_col(n, j)] = acc.v[n][j];
     __syncthreads();
 
+    if (dmode == 1) {   // a partial: stored for its tail task
+      tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
+      cta_publish(c, part_flag);
+      trace_task(c, t, type, t_task0);
+      return true;
+    }
     if (pre_only) {   // feeder products: the FT_FEEDQ tasks finish the tile and its digits
       tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
       cta_publish(c, p.feed_pre + i * g.B + col);

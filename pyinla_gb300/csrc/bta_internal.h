@@ -22,6 +22,16 @@ constexpr int EPOCH_SHIFT = 9;
 // FT_FEEDQ tasks of its rows (the feeder tile of a diagonal tile, see Geom).
 enum FactorTask { FT_DIAG = 0, FT_OFFD = 1, FT_LOW = 2, FT_ARW = 3, FT_TIP = 4, FT_FEEDQ = 5 };
 constexpr int FT_PRE = 8;
+// Split product loops.  A diagonal tile (i, c) and the feeder tile of column c share the
+// same left-looking loop, whose last step -- the product with the previous column's
+// feeder tile (k = c - 1), or with each neighbour block's last column when c = 0 -- is
+// the only one that waits on the factorization's column chain.  FT_PART on an FT_DIAG
+// task or on a feeder's FT_PRE task: every step but that last one, stored in the tile
+// and flagged (diag_pre / feed_part); FT_TAIL: the tile from that partial, the last
+// step(s) and the rest of the task.  Placed two columns ahead, the partials take both
+// long product loops off the chain.
+constexpr int FT_TAIL = 16;
+constexpr int FT_PART = 32;
 constexpr int FEED_ROWS = 8;   // rows of a feeder tile solved by one FT_FEEDQ task
 // Task codes of the selected-inversion DAG.
 // ST_PART: the products of the sub-diagonal tile of a column except its last (tensor-
@@ -142,7 +152,22 @@ int launch_grid(const void* kernel, int threads, size_t smem, const LaunchCtl& l
 int resident_ctas(const void* kernel, int threads, size_t smem, int tmem_cols);
 
 // Task lists of the factorization and selected-inversion DAGs (bta_api.cu).
-std::vector<int4> factor_task_list(const Geom& g);
+// diag_split: split the diagonal and feeder tiles' loops into FT_PART and FT_TAIL tasks
+// (the kernel then needs the diag_pre flags).
+std::vector<int4> factor_task_list(const Geom& g, bool diag_split = true);
+// Whether diagonal tile (i, c) has products besides its last step(s) (the condition for
+// its FT_DIAG|FT_PART task).
+inline bool diag_has_partial(const Geom& g, int i, int c) {
+  if (c >= 1) return g.nprev(i) * g.B + c - 1 > 0;
+  return g.nprev(i) > 0 && g.B >= 2;
+}
+// The same for the feeder of diagonal tile (i, c): an OFFD feeder (c + 1, c) has the
+// diagonal tile's loop, an L-slot feeder (0, B - 1) only its own block's B - 1 steps.
+inline bool feeder_has_partial(const Geom& g, int i, int c) {
+  const int fk = g.feeder_kind(i, c);
+  if (fk == 1) return diag_has_partial(g, i, c);
+  return fk == 2 && g.B >= 3;
+}
 // merged: the list of the tensor-core method, where each diagonal task also finishes
 // the sub-diagonal tile of the next column (ST_PART tasks form its other products).
 std::vector<int4> selinv_task_list(const Geom& g, bool merged = false);
@@ -153,8 +178,12 @@ void count_launches(int n);
 // feed_aux: nt * B ints (feeder "products done" flags), or null when the task list has
 // no FT_PRE / FT_FEEDQ tasks.  With FT_FEEDQ tasks the feeder tiles' own ready flags
 // must be zero at launch (launch_clear_feeders, or a cleared flag array).
+// diag_pre: 2 * nt * B ints -- flags of the diagonal tiles' partial products, then of
+// the feeder tiles' partial products -- or null when the task list has no FT_PART /
+// FT_TAIL tasks.
 void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow,
-                   const int4* tasks, int ntasks, double* tip_part, const LaunchCtl& lc, int* feed_aux = nullptr);
+                   const int4* tasks, int ntasks, double* tip_part, const LaunchCtl& lc, int* feed_aux = nullptr,
+                   int* diag_pre = nullptr);
 
 // Transpose, in place, the L slots below the separator (slots sep() .. nt-2): before a
 // factorization they hold the caller's Q(j+1, j), afterwards the factor needs Q(j, j+1).
@@ -171,7 +200,7 @@ constexpr int SOLVE_NC = 4;   // right-hand-side columns per solve launch
 size_t factor_oz_digit_bytes(const Geom& g);
 void launch_factor_oz(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow,
                       const int4* tasks, int ntasks, double* tip_part, __half* digits, int* erow,
-                      const LaunchCtl& lc, int* feed_aux = nullptr);
+                      const LaunchCtl& lc, int* feed_aux = nullptr, int* diag_pre = nullptr);
 
 // Row exponents of the input matrix (before a tensor-core factorization).
 void launch_row_exponents(const Geom& g, const double* D, const double* T, int use_arrow, int* erow,
@@ -180,8 +209,9 @@ void launch_row_exponents(const Geom& g, const double* D, const double* T, int u
 size_t selinv_oz_digit_bytes(const Geom& g);
 // Column exponents and transposed digit planes of the factor (before a tensor-core
 // selected inversion).
+// fdz (flag-slot count of ints, or null): the leading zero digit planes of every G tile.
 void launch_selinv_oz_prepare(const Geom& g, const double* D, const double* L, const double* R, int use_arrow,
-                              __half* fdig, int* ecol, cudaStream_t stream);
+                              __half* fdig, int* ecol, int* fdz, cudaStream_t stream);
 // sdig: digit planes (selinv_oz_digit_bytes) of the Sigma tiles, written by the tasks
 // that produce them (their exponents travel in the tiles' flag words).  tasks: the
 // merged list (selinv_task_list(g, true)); part: nt*B FP64 tiles and part_flag: nt*B
@@ -189,7 +219,7 @@ void launch_selinv_oz_prepare(const Geom& g, const double* D, const double* L, c
 void launch_selinv_oz(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                       double* SD, double* SL, double* SR, double* ST, int use_arrow, const int4* tasks,
                       int ntasks, __half* fdig, int* ecol, const double* cinv, __half* sdig, double* part,
-                      int* part_flag, const LaunchCtl& lc);
+                      int* part_flag, const LaunchCtl& lc, int* fdz = nullptr);
 
 void launch_solve(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                   double* Bv, int ldb, int nc, int trans, int use_arrow, double* arrow_part,
@@ -206,6 +236,12 @@ void launch_selinv(const Geom& g, const double* D, const double* L, const double
 size_t selinv_prepare_bytes(const Geom& g);
 void launch_selinv_prepare(const Geom& g, const double* D, double* L, double* R, int use_arrow, double* ws,
                            cudaStream_t stream);
+
+// Finish of a selected inversion with tensor-core products written in place over the
+// factor (its product loops read only digit planes, so Sigma can overwrite the factor
+// tiles): mirror each D block's lower tiles into its upper tiles and transpose the
+// coupling slots below the separator back to the caller's orientation.
+void launch_selinv_finish_inplace(const Geom& g, double* D, double* L, cudaStream_t stream);
 
 void launch_selinv_writeback(const Geom& g, const double* SD, const double* SL, const double* SR,
                              const double* ST, double* D, double* L, double* R, double* T, int use_arrow,

@@ -94,6 +94,37 @@ __device__ __forceinline__ void oz_zero_digits(int (&f)[OZ_S]) {
   for (int s = 0; s < OZ_S; ++s) f[s] = OZ_ZERO;
 }
 
+// Number of leading zero digits (0 .. OZ_S; OZ_S for x = 0) of a digit vector.
+__device__ __forceinline__ int oz_lead_zeros(const int (&f)[OZ_S]) {
+  int z = 0;
+#pragma unroll
+  for (int s = 0; s < OZ_S; ++s)
+    if (z == s && f[s] == OZ_ZERO) z = s + 1;
+  return z;
+}
+
+// Minimum of v over the CTA (every thread gets it); red: NT / 32 ints of shared memory.
+// Contains barriers.
+__device__ __forceinline__ int cta_min_int(int v, int* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  int m = red[0];
+#pragma unroll
+  for (int w = 1; w < NT / 32; ++w) m = min(m, red[w]);
+  __syncthreads();
+  return m;
+}
+
+// Two tiles whose digit planes below z_A, z_B are zero (z = OZ_S: the tile is zero)
+// multiply only through the pairs (s, t) with z_A <= s < OZ_S, z_B <= t < OZ_S and
+// s + t <= OZ_ND - 1: there are none when this returns true, and the step is skipped.
+__device__ __forceinline__ bool oz_pairs_vanish(int za, int zb) {
+  return za >= OZ_S || zb >= OZ_S || za + zb > OZ_ND - 1;
+}
+
 // Two digits given by their biased fields (0 <= f <= 128) as an exact fp16 pair
 // without conversion instructions: the fp16 bit pattern 0x6400 + f is the integer
 // 1024 + f, so (0x6400 + f) - 1088 = f - 64 = d exactly (1088 = 0x6440), one half2
@@ -291,10 +322,12 @@ __device__ __forceinline__ void oz_clear_partials(OzAcc& a) {
 }
 
 // One tile step: p[s+t] += d_s(A) * d_t(B)^T for the 43 pairs s + t <= 8, or only for
-// s >= S0 when the A planes below S0 are known to be zero (a left tile staged S0 or
-// more planes down): neither their loads nor their products are issued.  The A
-// planes hold A(m, k) at [m][k], or, with TA, at [k][m] (read with ldmatrix.trans).
-template <bool TA, int S0 = 0>
+// s >= SA, t >= SB when the A planes below SA and the B planes below SB are known to be
+// zero (a left tile staged SA or more planes down, a right tile whose leading digits
+// vanish): neither their loads nor their products are issued (the products left out
+// are exact zeros, so the result is the full step's).  The A planes hold A(m, k) at
+// [m][k], or, with TA, at [k][m] (read with ldmatrix.trans).
+template <bool TA, int SA = 0, int SB = 0>
 __device__ __forceinline__ void oz_step_t(OzAcc& acc, const __half* As, const __half* Bs) {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int m0 = (w >> 1) * 16, n0 = (w & 1) * 16;
@@ -307,18 +340,20 @@ __device__ __forceinline__ void oz_step_t(OzAcc& acc, const __half* As, const __
     unsigned a[OZ_S][4], b[OZ_S][4];
     if (TA) {
 #pragma unroll
-      for (int s = S0; s < OZ_S; ++s) ldsm_x4_trans(a[s], As + s * OZ_PLANE + oz_swz(kk + tr, tc));
+      for (int s = SA; s < OZ_S; ++s)
+        if (s + SB <= OZ_ND - 1) ldsm_x4_trans(a[s], As + s * OZ_PLANE + oz_swz(kk + tr, tc));
     } else {
 #pragma unroll
-      for (int s = S0; s < OZ_S; ++s) ldsm_x4(a[s], As + s * OZ_PLANE + oz_swz(ar, kk + ac));
+      for (int s = SA; s < OZ_S; ++s)
+        if (s + SB <= OZ_ND - 1) ldsm_x4(a[s], As + s * OZ_PLANE + oz_swz(ar, kk + ac));
     }
 #pragma unroll
-    for (int s = 0; s < OZ_S; ++s)
-      if (s <= OZ_ND - 1 - S0) ldsm_x4(b[s], Bs + s * OZ_PLANE + oz_swz(br, kk + bc));
+    for (int t = SB; t < OZ_S; ++t)
+      if (t + SA <= OZ_ND - 1) ldsm_x4(b[t], Bs + t * OZ_PLANE + oz_swz(br, kk + bc));
 #pragma unroll
-    for (int s = S0; s < OZ_S; ++s)
+    for (int s = SA; s < OZ_S; ++s)
 #pragma unroll
-      for (int t = 0; t + s < OZ_ND && t < OZ_S; ++t) {
+      for (int t = SB; t + s < OZ_ND && t < OZ_S; ++t) {
         mma16816(acc.p[s + t][0], a[s], b[t][0], b[t][1]);
         mma16816(acc.p[s + t][1], a[s], b[t][2], b[t][3]);
       }
@@ -327,6 +362,27 @@ __device__ __forceinline__ void oz_step_t(OzAcc& acc, const __half* As, const __
 
 __device__ __forceinline__ void oz_step(OzAcc& acc, const __half* As, const __half* Bs) {
   oz_step_t<false>(acc, As, Bs);
+}
+
+// The tile step for runtime counts of zero leading planes za (A) and zb (B): the
+// variant that leaves out min(za, 2) A planes and min(zb, 3) B planes (compile-time
+// plane ranges keep the operands in registers).  Requires !oz_pairs_vanish(za, zb).
+template <bool TA>
+__device__ __forceinline__ void oz_step_z(OzAcc& acc, const __half* As, const __half* Bs, int za, int zb) {
+  switch ((za < 2 ? za : 2) * 4 + (zb < 3 ? zb : 3)) {
+    case 0: oz_step_t<TA, 0, 0>(acc, As, Bs); break;
+    case 1: oz_step_t<TA, 0, 1>(acc, As, Bs); break;
+    case 2: oz_step_t<TA, 0, 2>(acc, As, Bs); break;
+    case 3: oz_step_t<TA, 0, 3>(acc, As, Bs); break;
+    case 4: oz_step_t<TA, 1, 0>(acc, As, Bs); break;
+    case 5: oz_step_t<TA, 1, 1>(acc, As, Bs); break;
+    case 6: oz_step_t<TA, 1, 2>(acc, As, Bs); break;
+    case 7: oz_step_t<TA, 1, 3>(acc, As, Bs); break;
+    case 8: oz_step_t<TA, 2, 0>(acc, As, Bs); break;
+    case 9: oz_step_t<TA, 2, 1>(acc, As, Bs); break;
+    case 10: oz_step_t<TA, 2, 2>(acc, As, Bs); break;
+    default: oz_step_t<TA, 2, 3>(acc, As, Bs); break;
+  }
 }
 
 // Fold the exact partial sums into the FP64 accumulator:

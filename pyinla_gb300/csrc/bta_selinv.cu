@@ -167,6 +167,40 @@ __global__ void k_writeback(const double* SD, const double* SL, const double* SR
   }
 }
 
+// In-place finish of a tensor-core selected inversion (Sigma written over the factor):
+// one CTA per tile pair R > C of a diagonal block writes upper tile (C, R) as the
+// transpose of lower tile (R, C), so D_i becomes full symmetric (reads and writes touch
+// disjoint tiles).
+__global__ void __launch_bounds__(256) k_mirror_upper(double* D, Geom g) {
+  __shared__ double A[TS][TS + 1];
+  const int B = g.B, pairs = B * (B - 1) / 2;
+  const int blk = blockIdx.x / pairs, q = blockIdx.x % pairs;
+  int R = (int)((1.f + sqrtf(1.f + 8.f * q)) * 0.5f);   // R (R - 1) / 2 <= q < R (R + 1) / 2
+  while (R * (R - 1) / 2 > q) --R;
+  while ((R + 1) * R / 2 <= q) ++R;
+  const int C = q - R * (R - 1) / 2;
+  double* d = D + (size_t)blk * g.b * g.b;
+  const int r0 = R * TS, c0 = C * TS;
+  for (int idx = threadIdx.x; idx < TS * TS; idx += blockDim.x) {
+    const int rr = idx / TS, cc = idx % TS;
+    if (r0 + rr < g.b && c0 + cc < g.b) A[rr][cc] = d[(size_t)(r0 + rr) * g.b + c0 + cc];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < TS * TS; idx += blockDim.x) {
+    const int rr = idx / TS, cc = idx % TS;   // element (c0 + rr, r0 + cc) of tile (C, R)
+    if (c0 + rr < g.b && r0 + cc < g.b) d[(size_t)(c0 + rr) * g.b + r0 + cc] = A[cc][rr];
+  }
+}
+
+void launch_selinv_finish_inplace(const Geom& g, double* D, double* L, cudaStream_t stream) {
+  const long long blocks = (long long)g.nt * (g.B * (g.B - 1) / 2);
+  if (blocks > 0) {
+    k_mirror_upper<<<(unsigned)blocks, 256, 0, stream>>>(D, g);
+    count_launches(1);
+  }
+  if (g.nt > 1) launch_transpose_lslots(g, L, stream);
+}
+
 void launch_selinv(const Geom& g, const double* D, const double* L, const double* R, const double* T, double* SD,
                    double* SL, double* SR, double* ST, int use_arrow, const int4* tasks, int ntasks,
                    const double* cinv, const LaunchCtl& lc) {
@@ -185,6 +219,7 @@ void launch_selinv(const Geom& g, const double* D, const double* L, const double
   p.tasks = tasks;
   p.ntasks = ntasks;
   p.fdig = nullptr;
+  p.fdz = nullptr;
   p.ecol = nullptr;
   p.cinv = cinv;
   p.sdig = nullptr;

@@ -37,9 +37,13 @@ __global__ void __launch_bounds__(NT) k_fac_col_exponents(const double* D, const
 }
 
 // One CTA per flag slot that is a factor tile of some column pattern: digits relative
-// to the column exponents, stored transposed: dst[s][j][m] = digit s of F[m][j].
+// to the column exponents, stored transposed: dst[s][j][m] = digit s of F[m][j]; and
+// dz[slot] = the number of leading digit planes that are zero over the whole tile (8:
+// the tile is zero -- the coupling blocks of banded couplings have many), which lets
+// the inversion leave out the products those planes would contribute.
 __global__ void __launch_bounds__(NT) k_fac_digits_t(const double* D, const double* L, const double* R, Geom g,
-                                                     int use_arrow, const int* ecol, __half* dig) {
+                                                     int use_arrow, const int* ecol, __half* dig, int* dz) {
+  __shared__ int red[NT / 32];
   const int slot = blockIdx.x;
   const int B = g.B;
   const size_t bb = (size_t)g.b * g.b, ab = (size_t)g.a * g.b;
@@ -68,6 +72,7 @@ __global__ void __launch_bounds__(NT) k_fac_digits_t(const double* D, const doub
     return;
   }
   __half* dst = dig + (size_t)slot * OZ_TILE;
+  int lz = OZ_S;
   // pairs of rows (m, m+1) of one column jj: adjacent in the transposed layout
 #pragma unroll
   for (int q = 0; q < PER_THREAD / 2; ++q) {
@@ -86,15 +91,18 @@ __global__ void __launch_bounds__(NT) k_fac_digits_t(const double* D, const doub
     unsigned* w = reinterpret_cast<unsigned*>(dst + oz_swz(jj, m));
 #pragma unroll
     for (int s = 0; s < OZ_S; ++s) w[s * (OZ_PLANE / 2)] = oz_digit_pair(d0[s], d1[s]);
+    lz = min(lz, min(oz_lead_zeros(d0), oz_lead_zeros(d1)));
   }
+  lz = cta_min_int(lz, red);
+  if (dz && threadIdx.x == 0) dz[slot] = lz;
 }
 
 // Column exponents and transposed digit planes of the factor (before a selected
 // inversion with tensor-core products).
 void launch_selinv_oz_prepare(const Geom& g, const double* D, const double* L, const double* R, int use_arrow,
-                              __half* fdig, int* ecol, cudaStream_t stream) {
+                              __half* fdig, int* ecol, int* fdz, cudaStream_t stream) {
   k_fac_col_exponents<<<g.nt * g.B, NT, 0, stream>>>(D, L, R, g, use_arrow, ecol);
-  k_fac_digits_t<<<g.nflags(), NT, 0, stream>>>(D, L, R, g, use_arrow, ecol, fdig);
+  k_fac_digits_t<<<g.nflags(), NT, 0, stream>>>(D, L, R, g, use_arrow, ecol, fdig, fdz);
   count_launches(2);
 }
 
@@ -115,7 +123,7 @@ size_t selinv_oz_digit_bytes(const Geom& g) { return (size_t)g.nflags() * OZ_TIL
 void launch_selinv_oz(const Geom& g, const double* D, const double* L, const double* R, const double* T, double* SD,
                       double* SL, double* SR, double* ST, int use_arrow, const int4* tasks, int ntasks, __half* fdig,
                       int* ecol, const double* cinv, __half* sdig, double* part, int* part_flag,
-                      const LaunchCtl& lc) {
+                      const LaunchCtl& lc, int* fdz) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_selinv_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZS_SMEM);
@@ -123,7 +131,7 @@ void launch_selinv_oz(const Geom& g, const double* D, const double* L, const dou
     cudaFuncSetAttribute(k_selinv_oz, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     attr_set = true;
   }
-  launch_selinv_oz_prepare(g, D, L, R, use_arrow, fdig, ecol, lc.stream);
+  launch_selinv_oz_prepare(g, D, L, R, use_arrow, fdig, ecol, fdz, lc.stream);
   SelinvArgs p;
   p.D = D;
   p.L = L;
@@ -139,6 +147,7 @@ void launch_selinv_oz(const Geom& g, const double* D, const double* L, const dou
   p.tasks = tasks;
   p.ntasks = ntasks;
   p.fdig = fdig;
+  p.fdz = fdz;
   p.ecol = ecol;
   p.cinv = cinv;
   p.sdig = sdig;

@@ -58,6 +58,8 @@ struct SelinvArgs {
   const int4* tasks;
   int ntasks;
   const __half* fdig;   // Ozaki: transposed digits of the G tiles per flag slot
+  const int* fdz;       // Ozaki: leading zero digit planes of each G tile (per flag slot; 8 =
+                        // zero tile), or null; steps with a zero G tile are dropped
   const int* ecol;      // Ozaki: per global column (nt*b) exponent of the G column pattern
   const double* cinv;   // [nt*B][TS*TS]: F_cc^{-T} F_cc^{-1} of every diagonal factor tile
   __half* sdig;         // Ozaki: digit planes of every Sigma tile per flag slot (their
@@ -422,7 +424,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
     }
 
     // a partial task (ST_PART) leaves out its last step: the diagonal tile j itself
-    const int np = pat_size(p, i, col) - (type == ST_PART ? 1 : 0);
+    int np = pat_size(p, i, col) - (type == ST_PART ? 1 : 0);
     if (threadIdx.x < TS) {
       const int cc = col * TS + threadIdx.x;
       ecol_t[threadIdx.x] = cc < g.b ? p.ecol[(size_t)i * g.b + cc] : 0;
@@ -446,7 +448,8 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         for (int q = 0; q < 4; ++q) esum[n][q] = E + ecol_t[oz_col(n, q)];
     };
     // step s: left tile (Sigma digits, its flag slot and orientation) and right tile
-    // (G digits), as a descriptor (left slot << 1 | transposed, right slot)
+    // (G digits), as a descriptor (left slot << 1 | transposed, right slot | the right
+    // tile's leading zero planes << 24)
     auto compute_desc = [&](int s) -> int2 {
       const int l = pat_code(p, i, col, s);
       int slot;
@@ -459,11 +462,33 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         slot = (int)(sig_dest(p, i, l, col).flag - c.flags);
         tr = true;
       }
-      return make_int2((slot << 1) | (tr ? 1 : 0), fac_slot(g, i, l, col));
+      const int rs = fac_slot(g, i, l, col);
+      return make_int2((slot << 1) | (tr ? 1 : 0), rs | ((p.fdz ? p.fdz[rs] : 0) << 24));
     };
     for (int s = threadIdx.x; s < np && s < OZS_DESC; s += NT) sdesc[s] = compute_desc(s);
     __syncthreads();
-    auto desc_of = [&](int s) -> int2 { return s < OZS_DESC ? sdesc[s] : compute_desc(s); };
+    // Steps whose right tile is zero contribute nothing: drop them up front (in order,
+    // by warp 0), so their left tiles are not even waited for.
+    const int np_all = np;
+    if (p.fdz && np <= OZS_DESC) {
+      if (threadIdx.x < 32) {
+        int cnt = 0;
+        for (int base = 0; base < np; base += 32) {
+          const int s = base + threadIdx.x;
+          const int2 d = s < np ? sdesc[s] : make_int2(0, OZ_S << 24);
+          const bool live = (d.y >> 24) < OZ_S;
+          const unsigned m = __ballot_sync(0xffffffffu, live);
+          __syncwarp();
+          if (live) sdesc[cnt + __popc(m & ((1u << threadIdx.x) - 1u))] = d;
+          cnt += __popc(m);
+          __syncwarp();
+        }
+        if (threadIdx.x == 0) s_val[1] = cnt;
+      }
+      __syncthreads();
+      np = s_val[1];
+    }
+    auto desc_of = [&](int s) -> int2 { return np_all <= OZS_DESC ? sdesc[s] : compute_desc(s); };
     auto left_of = [&](int s) -> SigTile {
       const int2 d = desc_of(s);
       SigTile st_;
@@ -471,14 +496,17 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       st_.trans = (d.x & 1) != 0;
       return st_;
     };
-    auto right_of = [&](int s) -> const __half* { return p.fdig + (size_t)desc_of(s).y * OZ_TILE; };
+    auto right_of = [&](int s) -> const __half* { return p.fdig + (size_t)(desc_of(s).y & 0xffffff) * OZ_TILE; };
+    auto zero_planes_of = [&](int s) -> int { return desc_of(s).y >> 24; };
     // stage step s's operands into stage buffer st with the left tile shifted by q
     // planes: bulk copies of its leading OZ_S - q planes and of the right tile, the
     // q planes below the shift zeroed by the CTA
     unsigned ph = pp->phase;
     int qst[2] = {0, 0};   // plane shift of the left tile in each stage buffer
+    int zst[2] = {0, 0};   // leading zero planes of the right tile in each stage buffer
     auto stage = [&](int st, const SigTile& lt, int q, int s) {
       qst[st] = q;
+      zst[st] = zero_planes_of(s);
       __half* dst = stages + st * OZS_STAGE;
       const int slot = (int)(lt.flag - c.flags);
       const unsigned abytes = q < OZ_S ? (unsigned)((OZ_S - q) * OZ_PLANE * sizeof(__half)) : 0u;
@@ -489,6 +517,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       }
       for (int idx = threadIdx.x; idx < q * (OZ_PLANE / 8); idx += NT)
         reinterpret_cast<uint4*>(dst)[idx] = make_uint4(0u, 0u, 0u, 0u);
+      if (q) fence_async_smem();   // a later copy into this stage may cover these planes
     };
     // wait for stage st; a copy that never lands aborts the launch
     auto stage_wait = [&](int st) -> bool {
@@ -535,7 +564,8 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         int En = NO_EXP;
         if (more) {
           nt_ = left_of(s + 1);
-          if (s_ready <= s + 1) {   // uniform: read after the barrier
+          if (s_ready <= s + 1) {   // uniform: read after the barrier, rewritten after the next one
+            __syncthreads();   // every warp has read s_ready before warp 0 advances it
             scan_ready(c, np, flags_of, &s_ready, ring);
             __syncthreads();
           }
@@ -547,22 +577,12 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         }
         // the left tile was staged qcur planes down: its planes below qcur are zero
         // (all of them from OZ_S on: nothing to add)
-        const int qcur = qst[s & 1];
-        if (qcur >= OZ_S) {
+        const int qcur = qst[s & 1], zcur = zst[s & 1];
+        if (oz_pairs_vanish(qcur, zcur)) {
         } else if (tcur) {
-          if (qcur >= 2)
-            oz_step_t<true, 2>(acc, cur, cur + OZ_OPER);
-          else if (qcur == 1)
-            oz_step_t<true, 1>(acc, cur, cur + OZ_OPER);
-          else
-            oz_step_t<true, 0>(acc, cur, cur + OZ_OPER);
+          oz_step_z<true>(acc, cur, cur + OZ_OPER, qcur, zcur);
         } else {
-          if (qcur >= 2)
-            oz_step_t<false, 2>(acc, cur, cur + OZ_OPER);
-          else if (qcur == 1)
-            oz_step_t<false, 1>(acc, cur, cur + OZ_OPER);
-          else
-            oz_step_t<false, 0>(acc, cur, cur + OZ_OPER);
+          oz_step_z<false>(acc, cur, cur + OZ_OPER, qcur, zcur);
         }
         ++since_fold;
         if (more) {
@@ -651,8 +671,9 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
             a2.v[n][q] = F[oz_row(n, q) * LDS + oz_col(n, q)];
             es[n][q] = Ed + ecol_t[oz_col(n, q)];
           }
-        if (Ed > NO_EXP) {
-          oz_step_t<false>(a2, A0, B0);
+        const int z2 = p.fdz ? p.fdz[fac_slot(g, i2, j2, c2)] : 0;
+        if (Ed > NO_EXP && !oz_pairs_vanish(0, z2)) {
+          oz_step_z<false>(a2, A0, B0, 0, z2);
           oz_fold_sub(a2, es);
         }
 #pragma unroll
