@@ -59,6 +59,7 @@ struct gbta_solver {
   double* d_arrow_part = nullptr;
   int* d_faux = nullptr;      // feeder "products done" flags [nt*B]
   int* d_dpre = nullptr;      // diagonal and feeder tiles' "partial stored" flags [2*nt*B]
+  int* d_kf = nullptr;        // first nonzero column tile per coupling-slot row tile [(nt-1)*B]
   double* d_ld = nullptr;   // logdet partials [nt + 1] + result [1]
   double* d_sig = nullptr;  // selected-inversion output blocks (lazy)
   double* d_selws = nullptr;  // selected-inversion pre-pass: diagonal inverses (lazy)
@@ -300,6 +301,7 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   CREATE_CUDA(cudaMemsetAsync(s->d_faux, 0, ntile * sizeof(int), s->stream));
   CREATE_CUDA(cudaMalloc(&s->d_dpre, 2 * ntile * sizeof(int)));
   CREATE_CUDA(cudaMemsetAsync(s->d_dpre, 0, 2 * ntile * sizeof(int), s->stream));
+  if (nt > 1) CREATE_CUDA(cudaMalloc(&s->d_kf, (size_t)(nt - 1) * s->g.B * sizeof(int)));
   CREATE_CUDA(cudaMalloc(&s->d_ld, (nt + 2) * sizeof(double)));
   CREATE_CUDA(cudaMallocHost(&s->h_ctrl, CTRL_INTS * sizeof(int)));
   CREATE_CUDA(cudaMemsetAsync(s->d_ctrl, 0, CTRL_INTS * sizeof(int), s->stream));
@@ -311,7 +313,7 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
 #undef CREATE_CUDA
   s->ws_bytes = CTRL_INTS * sizeof(int) + (size_t)nflags * sizeof(int) + (ft.size() + st.size()) * sizeof(int4) +
                 ntile * gbta::TS * (gbta::TS + gbta::SOLVE_NC) * sizeof(double) + (nt + 2) * sizeof(double) +
-                3 * ntile * sizeof(int);
+                3 * ntile * sizeof(int) + (size_t)(nt - 1) * s->g.B * sizeof(int);
   *out = s;
   g_last_error.clear();
   return GBTA_OK;
@@ -329,6 +331,7 @@ int gbta_destroy(gbta_solver* s) {
   cudaFree(s->d_arrow_part);
   cudaFree(s->d_faux);
   cudaFree(s->d_dpre);
+  cudaFree(s->d_kf);
   cudaFree(s->d_ld);
   cudaFree(s->d_sig);
   cudaFree(s->d_selws);
@@ -495,16 +498,19 @@ static int factor_async(gbta_solver* s, double* D, double* L, double* R, double*
   if (s->method == GBTA_METHOD_OZAKI)
     if (int r = ensure_digits(s)) return r;
   if (int r = reset_ticket(s)) return r;
-  if (s->g.nt > 1) gbta::launch_transpose_lslots(s->g, L, s->stream);
+  if (s->g.nt > 1) {
+    gbta::launch_transpose_lslots(s->g, L, s->stream);
+    gbta::launch_coupling_kfirst(s->g, L, s->d_kf, s->stream);
+  }
   gbta::launch_clear_feeders(s->g, s->d_flags, s->stream);
   const gbta::LaunchCtl lc = next_launch(s, s->n_ftasks);
   if (s->timing) GBTA_CUDA(cudaEventRecord(s->tev[0], s->stream));
   if (s->method == GBTA_METHOD_OZAKI)
     gbta::launch_factor_oz(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part,
-                           (__half*)s->d_digits, s->d_erow, lc, s->d_faux, s->d_dpre);
+                           (__half*)s->d_digits, s->d_erow, lc, s->d_faux, s->d_dpre, s->d_kf);
   else
     gbta::launch_factor(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part, lc, s->d_faux,
-                        s->d_dpre);
+                        s->d_dpre, s->d_kf);
   GBTA_CUDA(cudaGetLastError());
   if (s->timing) {
     GBTA_CUDA(cudaEventRecord(s->tev[1], s->stream));

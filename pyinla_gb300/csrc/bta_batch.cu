@@ -266,6 +266,7 @@ int build_args(gbta_batch* bt) {
     f.info = bt->d_info + k;
     f.feed_pre = bt->d_faux + q.faux_off;
     f.diag_pre = bt->d_faux + q.faux_off + (size_t)g.nt * g.B;
+    f.kf = g.nt > 1 ? bt->d_faux + q.faux_off + 3 * (size_t)g.nt * g.B : nullptr;
     f.c = batch_ctl(bt, flags, EP_FACTOR);
     gbta::SelinvArgs& s = sa[k];
     const size_t bb = (size_t)g.b * g.b;
@@ -351,7 +352,10 @@ int run_async(gbta_batch* bt, int phases, double* logdet_out) {
   const gbta::Ctl c = batch_ctl(bt, nullptr, 0);
   if (phases & GBTA_PHASE_FACTOR) {
     for (const BatchInst& q : bt->inst)
-      if (q.g.nt > 1) gbta::launch_transpose_lslots(q.g, q.L, st);
+      if (q.g.nt > 1) {
+        gbta::launch_transpose_lslots(q.g, q.L, st);
+        gbta::launch_coupling_kfirst(q.g, q.L, bt->d_faux + q.faux_off + 3 * (size_t)q.g.nt * q.g.B, st);
+      }
     for (const BatchInst& q : bt->inst)
       if (q.method == GBTA_METHOD_OZAKI) gbta::launch_row_exponents(q.g, q.D, q.T, q.g.a > 0, q.erow, st);
     gbta::k_factor_batch<<<grid_of(bt, (const void*)gbta::k_factor_batch, gbta::BATCH_FACTOR_SMEM, bt->n_forder), gbta::NT,
@@ -461,7 +465,8 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
     q.n_vtasks = g.nt * g.B + (g.a > 0 ? 1 : 0);
     q.flags_off = flags_total;
     q.faux_off = bt->nfaux_total;
-    bt->nfaux_total += 3 * (size_t)g.nt * g.B;   // feeder flags, then diagonal- and feeder-partial flags
+    // feeder flags, diagonal- and feeder-partial flags, then the coupling slots' kfirst
+    bt->nfaux_total += 3 * (size_t)g.nt * g.B + (size_t)(g.nt - 1) * g.B;
     flags_total += (size_t)g.nflags();
     const size_t ntile = (size_t)g.nt * g.B, bb = (size_t)g.b * g.b;
     o_ft[k] = off;

@@ -59,6 +59,31 @@ void launch_transpose_lslots(const Geom& g, double* L, cudaStream_t stream) {
   count_launches(1);
 }
 
+// One CTA per (L slot j, row tile r): scan the row tile's column tiles left to right
+// until one holds a nonzero (a NaN counts as nonzero).
+__global__ void __launch_bounds__(NT) k_coupling_kfirst(const double* __restrict__ L, Geom g, int* kf) {
+  const int j = blockIdx.x / g.B, r = blockIdx.x % g.B;
+  const double* rows = L + (size_t)j * g.b * g.b + (size_t)r * TS * g.b;
+  const int nr = min(TS, g.b - r * TS);
+  int k = 0;
+  for (; k < g.B; ++k) {
+    const int nc = min(TS, g.b - k * TS);
+    bool nz = false;
+    for (int idx = threadIdx.x; idx < nr * TS; idx += NT) {
+      const int rr = idx / TS, cc = idx % TS;
+      if (cc < nc && __ldg(rows + (size_t)rr * g.b + k * TS + cc) != 0.0) nz = true;
+    }
+    if (__syncthreads_or(nz)) break;
+  }
+  if (threadIdx.x == 0) kf[blockIdx.x] = k;
+}
+
+void launch_coupling_kfirst(const Geom& g, const double* L, int* kf, cudaStream_t stream) {
+  if (g.nt < 2) return;
+  k_coupling_kfirst<<<(g.nt - 1) * g.B, NT, 0, stream>>>(L, g, kf);
+  count_launches(1);
+}
+
 void launch_clear_feeders(const Geom& g, int* flags, cudaStream_t stream) {
   const int n = g.nt * g.B;
   const int blocks = (n + 255) / 256;
@@ -67,7 +92,8 @@ void launch_clear_feeders(const Geom& g, int* flags, cudaStream_t stream) {
 }
 
 void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow, const int4* tasks,
-                   int ntasks, double* tip_part, const LaunchCtl& lc, int* feed_aux, int* diag_pre) {
+                   int ntasks, double* tip_part, const LaunchCtl& lc, int* feed_aux, int* diag_pre,
+                   const int* kf) {
   FactorArgs p;
   p.D = D;
   p.L = L;
@@ -84,6 +110,7 @@ void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, in
   p.info = nullptr;
   p.feed_pre = feed_aux;
   p.diag_pre = diag_pre;
+  p.kf = kf;
   p.c.ctrl = lc.ctrl;
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;

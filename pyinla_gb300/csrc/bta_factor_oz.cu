@@ -47,7 +47,7 @@ size_t factor_oz_digit_bytes(const Geom& g) { return (size_t)g.nflags() * OZ_TIL
 
 void launch_factor_oz(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow, const int4* tasks,
                       int ntasks, double* tip_part, __half* digits, int* erow, const LaunchCtl& lc,
-                      int* feed_aux, int* diag_pre) {
+                      int* feed_aux, int* diag_pre, const int* kf) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_factor_oz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OZF_SMEM);
@@ -71,6 +71,7 @@ void launch_factor_oz(const Geom& g, double* D, double* L, double* R, double* T,
   p.info = nullptr;
   p.feed_pre = feed_aux;
   p.diag_pre = diag_pre;
+  p.kf = kf;
   p.c.ctrl = lc.ctrl;
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;

@@ -48,6 +48,8 @@ struct FactorArgs {
   int* feed_pre;        // [nt*B] flag: the feeder of diagonal tile (i, c) has its products
   int* diag_pre;        // [2*nt*B] flags: diagonal tile (i, c), then the feeder of column
                         // (i, c), holds its partial products (split loops; see FT_PART)
+  const int* kf;        // [(nt-1)*B] first column tile of each coupling-slot row tile that
+                        // can be nonzero (launch_coupling_kfirst), or null
   Ctl c;
 };
 
@@ -58,35 +60,65 @@ struct FactorArgs {
 // col = 0) and a tail (those last steps) when the task list splits them (FT_PART /
 // FT_TAIL).
 struct StepRange {
-  int n;      // steps
-  int mode;   // 0 full, 1 partial, 2 tail
-  int nprev;  // leading steps that are neighbour-block terms
+  int n;       // steps
+  int mode;    // 0 full, 1 partial, 2 tail
+  int nprev;   // leading steps that are neighbour-block terms
+  int n0;      // of those, the first neighbour's (the rest are the second's)
+  int ka, kb;  // column of the first neighbour's first term, and of the second's
+  int kin;     // column of the first own-block term
 };
-static __device__ __forceinline__ StepRange step_range(const Geom& g, int type, int mode, int i, int col) {
+// First column tile of coupling slot ls's row tile r that can be nonzero (FactorArgs::kf).
+static __device__ __forceinline__ int kfirst(const FactorArgs& p, int ls, int r) {
+  return p.kf ? __ldg(p.kf + ls * p.g.B + r) : 0;
+}
+// The steps of a task (type, mode) on target row tile r, column col of block i.  A
+// neighbour's term k multiplies its coupling tiles (r, k) and (col, k) (the arrow's
+// only (col, k)); an L target's own-block term k its own tile (r, k): terms on a
+// structurally zero tile are left out, so each neighbour's terms and the own block's
+// are a contiguous run of columns.
+static __device__ __forceinline__ StepRange step_range(const FactorArgs& p, int type, int mode, int i, int r,
+                                                       int col) {
+  const Geom& g = p.g;
+  StepRange sr;
+  sr.mode = mode;
+  sr.nprev = 0;
+  sr.n0 = 0;
+  sr.ka = sr.kb = 0;
   const int np = (type != FT_LOW) ? g.nprev(i) : 0;
-  if (mode == 1) return col == 0 ? StepRange{np * (g.B - 1), 1, np * (g.B - 1)} : StepRange{np * g.B + col - 1, 1, np * g.B};
-  if (mode == 2) return col == 0 ? StepRange{np, 2, np} : StepRange{1, 2, 0};
-  return StepRange{np * g.B + col, 0, np * g.B};
+  for (int q = 0; q < np; ++q) {
+    const int ls = g.lslot(g.prev(i, q));
+    int k0 = kfirst(p, ls, col), k1 = g.B;
+    if (type != FT_ARW) k0 = max(k0, kfirst(p, ls, r));
+    if (mode == 1 && col == 0) k1 = g.B - 1;           // all but each neighbour's last column
+    if (mode == 2) k0 = col == 0 ? max(k0, g.B - 1) : g.B;   // only those (col 0), none (col > 0)
+    const int cnt = max(0, k1 - k0);
+    if (q == 0) {
+      sr.ka = k0;
+      sr.n0 = cnt;
+    } else {
+      sr.kb = k0;
+    }
+    sr.nprev += cnt;
+  }
+  int kin = (type == FT_LOW) ? kfirst(p, g.lslot(i), r) : 0, kend = col;
+  if (mode == 1) kend = col - 1;                        // all but the last own column
+  if (mode == 2) kin = col == 0 ? col : max(kin, col - 1);   // only that one
+  sr.kin = kin;
+  sr.n = sr.nprev + max(0, kend - kin);
+  return sr;
 }
 // Step s of a range: a neighbour-block term (prev: neighbour pb, its column k) or a term
 // of the task's own block (column k).
-static __device__ __forceinline__ void step_src(const Geom& g, const StepRange& sr, int i, int col, int s, bool& prev,
+static __device__ __forceinline__ void step_src(const Geom& g, const StepRange& sr, int i, int s, bool& prev,
                                                 int& pb, int& k) {
   prev = s < sr.nprev;
-  if (!prev) {
-    pb = i;
-    k = sr.mode == 2 ? col - 1 : s - sr.nprev;
-    return;
-  }
-  if (sr.mode == 2) {          // the feeder tile of each neighbour's last column
-    pb = g.prev(i, s);
-    k = g.B - 1;
-  } else if (sr.mode == 1 && col == 0) {   // every neighbour column but the last
-    pb = g.prev(i, s / (g.B - 1));
-    k = s % (g.B - 1);
+  if (prev) {
+    const bool first = s < sr.n0;
+    pb = g.prev(i, first ? 0 : 1);
+    k = first ? sr.ka + s : sr.kb + (s - sr.n0);
   } else {
-    pb = g.prev(i, s / g.B);
-    k = s % g.B;
+    pb = i;
+    k = sr.kin + (s - sr.nprev);
   }
 }
 
@@ -330,7 +362,7 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
 
     // previous block columns: the Schur terms of the (one or two) neighbours eliminated
     // before block i, through their coupling slots (L tiles have none: Q(nxt(i), p) = 0)
-    const StepRange sr = step_range(g, type, dmode, i, col);
+    const StepRange sr = step_range(p, type, dmode, i, r, col);
     const int nsteps = sr.n;
     const int lsi = g.lslot(i);
     auto step_of = [&](int s) -> Step {
@@ -339,7 +371,7 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
       st.tb = true;
       bool isprev;
       int pb, k;
-      step_src(g, sr, i, col, s, isprev, pb, k);
+      step_src(g, sr, i, s, isprev, pb, k);
       if (isprev) {
         const int ls = g.lslot(pb);
         if (type == FT_ARW) {
@@ -405,9 +437,12 @@ static __device__ __forceinline__ bool factor_fp64_task(const FactorArgs& p, int
       return true;
     }
 
-    // Off-diagonal targets: X <- X * D_i(col,col)^{-T}.
-    if (!load_diag_factor(p, i, col, F, &s_ok)) return false;
-    offdiag_trsm(X, F, sm + 2 * TILE_SMEM, vec, type == FT_ARW, g.a);
+    // Off-diagonal targets: X <- X * D_i(col,col)^{-T}; a structurally zero coupling tile
+    // (no products, zero input) stays zero without the solve, so without its wait.
+    if (!(type == FT_LOW && col < kfirst(p, lsi, r))) {
+      if (!load_diag_factor(p, i, col, F, &s_ok)) return false;
+      offdiag_trsm(X, F, sm + 2 * TILE_SMEM, vec, type == FT_ARW, g.a);
+    }
     tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
     if (type == FT_OFFD) {
       // The factor's strict upper triangle is zero: clear the mirrored tile.
@@ -563,13 +598,13 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
 
     // ---- product loop over the final tiles left of the target (previous block
     //      column first, then columns k < col of this block)
-    const StepRange sr = step_range(g, type, dmode, i, col);
+    const StepRange sr = step_range(p, type, dmode, i, r, col);
     const int nsteps = sr.n;
     const int lsi = g.lslot(i);
     auto slots = [&](int s, int& sa, int& sb) {
       bool isprev;
       int pb, k;
-      step_src(g, sr, i, col, s, isprev, pb, k);
+      step_src(g, sr, i, s, isprev, pb, k);
       if (isprev) {
         const int ls = g.lslot(pb);
         sa = (type == FT_ARW) ? g.fR(pb, k) : g.fL(ls, r, k);
@@ -697,15 +732,18 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
       return true;
     }
 
-    // Off-diagonal targets: X <- X * D_i(col,col)^{-T}.
-    if (!cta_wait(c, c.flags + g.fD(i, col, col), nullptr, &s_ok)) return false;
-    trace_mark(c, t, 1);   // diagonal factor tile ready
-    tile_load(F, make_tile(p.D + i * bb, g.b, col * TS, col * TS, g.b, g.b));
-    __syncthreads();
-    tile_pad_identity(F, g.vrows(col));
-    __syncthreads();
-    offdiag_trsm(X, F, reinterpret_cast<double*>(stages), vec, type == FT_ARW, g.a);
-    trace_mark(c, t, 2);   // triangular solve done
+    // Off-diagonal targets: X <- X * D_i(col,col)^{-T}; a structurally zero coupling tile
+    // (no products, zero input) stays zero without the solve, so without its wait.
+    if (!(type == FT_LOW && col < kfirst(p, lsi, r))) {
+      if (!cta_wait(c, c.flags + g.fD(i, col, col), nullptr, &s_ok)) return false;
+      trace_mark(c, t, 1);   // diagonal factor tile ready
+      tile_load(F, make_tile(p.D + i * bb, g.b, col * TS, col * TS, g.b, g.b));
+      __syncthreads();
+      tile_pad_identity(F, g.vrows(col));
+      __syncthreads();
+      offdiag_trsm(X, F, reinterpret_cast<double*>(stages), vec, type == FT_ARW, g.a);
+      trace_mark(c, t, 2);   // triangular solve done
+    }
     tile_store(const_cast<double*>(tgt.p), tgt.ld, tgt.rows, tgt.cols, X);
     oz_store_digits(p.digits + (size_t)tgt_slot * OZ_TILE, X, tgt.rows, tgt.cols, erow_t);
     trace_mark(c, t, 3);   // tile and digits written

@@ -181,14 +181,24 @@ void count_launches(int n);
 // diag_pre: 2 * nt * B ints -- flags of the diagonal tiles' partial products, then of
 // the feeder tiles' partial products -- or null when the task list has no FT_PART /
 // FT_TAIL tasks.
+// kf: (nt - 1) * B ints from launch_coupling_kfirst (the products of structurally zero
+// coupling tiles are left out), or null (every product is formed).
 void launch_factor(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow,
                    const int4* tasks, int ntasks, double* tip_part, const LaunchCtl& lc, int* feed_aux = nullptr,
-                   int* diag_pre = nullptr);
+                   int* diag_pre = nullptr, const int* kf = nullptr);
 
 // Transpose, in place, the L slots below the separator (slots sep() .. nt-2): before a
 // factorization they hold the caller's Q(j+1, j), afterwards the factor needs Q(j, j+1).
 // No launch when the order is top-down.
 void launch_transpose_lslots(const Geom& g, double* L, cudaStream_t stream);
+
+// Structurally zero tiles of the factor's coupling slots.  The factor's slot is
+// L_j = Q_j F^{-T} with F the (lower triangular) factor of the diagonal block it
+// couples from, so its tile (r, k) is zero when the input's row tile r is zero in every
+// column tile <= k.  kf[j * B + r] = the first column tile of slot j's row tile r that
+// holds a nonzero (B: none), read from the L slots as the factorization sees them
+// (after launch_transpose_lslots).  Every product with a tile k < kf is exactly zero.
+void launch_coupling_kfirst(const Geom& g, const double* L, int* kf, cudaStream_t stream);
 
 // Zero the ready flags of the feeder tiles (Geom::feeder_kind): the FT_FEEDQ tasks of
 // a factorization add shares of the epoch to them.
@@ -200,7 +210,8 @@ constexpr int SOLVE_NC = 4;   // right-hand-side columns per solve launch
 size_t factor_oz_digit_bytes(const Geom& g);
 void launch_factor_oz(const Geom& g, double* D, double* L, double* R, double* T, int use_arrow,
                       const int4* tasks, int ntasks, double* tip_part, __half* digits, int* erow,
-                      const LaunchCtl& lc, int* feed_aux = nullptr, int* diag_pre = nullptr);
+                      const LaunchCtl& lc, int* feed_aux = nullptr, int* diag_pre = nullptr,
+                      const int* kf = nullptr);
 
 // Row exponents of the input matrix (before a tensor-core factorization).
 void launch_row_exponents(const Geom& g, const double* D, const double* T, int use_arrow, int* erow,

@@ -8,7 +8,10 @@ towards the middle block), with and without the split of the diagonal and feeder
 product loops into partial and tail tasks -- together with the flags each task body
 waits on (the product steps of step_range / step_src in csrc/bta_factor_task.cuh, the
 diagonal factor tile, the feeder and partial flags), and checks that every waited flag
-is published, by a smaller ticket.
+is published, by a smaller ticket.  With structurally zero coupling tiles (the kf
+array of launch_coupling_kfirst) the loops leave out the terms on them, and an L tile
+that is itself structurally zero skips its solve: the tests also check that the split
+loops then still cover exactly the live terms.
 """
 import pytest
 
@@ -98,29 +101,46 @@ def task_list(g, split=True):
     return t
 
 
-def steps(g, ttype, mode, i, col):
-    """(isprev, pb, k) of each product step, mirroring step_range / step_src."""
+def steps(g, ttype, mode, i, col, r=None, kf=None):
+    """(isprev, pb, k) of each product step, mirroring step_range / step_src: a
+    neighbour's term k uses its coupling tiles (r, k), (col, k) (the arrow's only
+    (col, k)), an L target's own-block term k its own tile (r, k); terms on a
+    structurally zero tile (k < kf[slot][row]) are left out."""
     B = g["B"]
+    r = col if r is None else r
+    kfirst = (lambda ls, row: 0) if kf is None else (lambda ls, row: kf[ls][row])
     np_ = g["nprev"](i) if ttype != "LOW" else 0
     out = []
+    for q in range(np_):
+        pb = g["prev"](i, q)
+        ls = g["lslot"](pb)
+        k0, k1 = kfirst(ls, col), B
+        if ttype != "ARW":
+            k0 = max(k0, kfirst(ls, r))
+        if mode == 1 and col == 0:
+            k1 = B - 1
+        if mode == 2:
+            k0 = max(k0, B - 1) if col == 0 else B
+        out += [(True, pb, k) for k in range(k0, k1)]
+    kin = kfirst(g["lslot"](i), r) if ttype == "LOW" else 0
+    kend = col
     if mode == 1:
-        if col == 0:
-            for s in range(np_ * (B - 1)): out.append((True, g["prev"](i, s // (B - 1)), s % (B - 1)))
-        else:
-            for s in range(np_ * B): out.append((True, g["prev"](i, s // B), s % B))
-            for k in range(col - 1): out.append((False, i, k))
-    elif mode == 2:
-        if col == 0:
-            for s in range(np_): out.append((True, g["prev"](i, s), B - 1))
-        else:
-            out.append((False, i, col - 1))
-    else:
-        for s in range(np_ * B): out.append((True, g["prev"](i, s // B), s % B))
-        for k in range(col): out.append((False, i, k))
+        kend = col - 1
+    if mode == 2:
+        kin = col if col == 0 else max(kin, col - 1)
+    out += [(False, i, k) for k in range(kin, kend)]
     return out
 
 
-def check(nt, b, a, twist=True, split=True):
+def full_steps_unskipped(g, ttype, i, col):
+    """The loop without skipping, written out directly: every neighbour column, then
+    the own block's columns k < col."""
+    B = g["B"]
+    np_ = g["nprev"](i) if ttype != "LOW" else 0
+    return [(True, g["prev"](i, q), k) for q in range(np_) for k in range(B)] + [(False, i, k) for k in range(col)]
+
+
+def check(nt, b, a, twist=True, split=True, kf=None):
     g = geom(nt, b, a, twist)
     B = g["B"]
     tl = task_list(g, split)
@@ -155,7 +175,7 @@ def check(nt, b, a, twist=True, split=True):
                     "FPARTL": "LOW", "DPART": "DIAG", "TAIL": "DIAG"}.get(ty, ty)
             if ty == "TAIL": waits.append(("dpart", i, c))
             if ty in ("PREOT", "PRELT"): waits.append(("fpart", i, c))
-            for isprev, pb, k in steps(g, kind, mode, i, c):
+            for isprev, pb, k in steps(g, kind, mode, i, c, r, kf):
                 if isprev:
                     ls = g["lslot"](pb)
                     sa = ("fR", pb, k) if kind == "ARW" else ("fL", ls, r, k)
@@ -165,7 +185,7 @@ def check(nt, b, a, twist=True, split=True):
                     sa = ("fR", i, k) if kind == "ARW" else (("fL", lsi, r, k) if kind == "LOW" else ("fD", i, r, k))
                     sb = ("fD", i, c, k)
                 waits += [sa, sb]
-            if ty in ("OFFD", "LOW", "ARW"):
+            if ty in ("OFFD", "ARW") or (ty == "LOW" and (kf is None or c >= kf[g["lslot"](i)][r])):
                 waits.append(("fD", i, c, c))
         for w in waits:
             if w not in prod:
@@ -200,3 +220,52 @@ def test_two_sided_order_halves_the_chain():
     top = [i for i in range(128) if g["nxt"](i) == i + 1]
     bottom = [i for i in range(128) if g["nxt"](i) == i - 1]
     assert len(top) == 64 and len(bottom) == 63 and g["nprev"](64) == 2
+
+
+def random_kf(g, seed):
+    """First nonzero column tile per coupling-slot row tile: banded (row tile r starts
+    near r - 2), with some empty row tiles (B) and some starting at 0."""
+    rng = __import__("random").Random(seed)
+    B = g["B"]
+    out = []
+    for _ in range(max(g["nt"] - 1, 0)):
+        row = []
+        for r in range(B):
+            u = rng.random()
+            row.append(B if u < 0.1 else (0 if u < 0.2 else max(0, r - rng.randint(0, 3))))
+        out.append(row)
+    return out
+
+
+@pytest.mark.parametrize("nt,b,a", SHAPES)
+def test_skipped_structural_zeros_keep_the_dag(nt, b, a):
+    g = geom(nt, b, a, True)
+    assert check(nt, b, a, True, True, random_kf(g, nt * 1000 + b))
+
+
+@pytest.mark.parametrize("nt,b,a", [(3, 96, 2), (5, 45, 5), (16, 128, 4), (17, 100, 3), (6, 5, 2)])
+def test_partial_and_tail_cover_the_live_steps(nt, b, a):
+    """Partial + tail = the full loop's steps, and the full loop = the unskipped loop
+    minus exactly the terms on structurally zero tiles."""
+    for twist in (True, False):
+        g = geom(nt, b, a, twist)
+        kf = random_kf(g, nt + b)
+        B = g["B"]
+        for i in range(nt):
+            for col in range(B):
+                for ttype, r in (("DIAG", col), ("OFFD", min(col + 1, B - 1)), ("LOW", 0), ("LOW", B - 1),
+                                 ("ARW", 0)):
+                    full = steps(g, ttype, 0, i, col, r, kf)
+                    split = steps(g, ttype, 1, i, col, r, kf) + steps(g, ttype, 2, i, col, r, kf)
+                    assert sorted(split) == sorted(full), (i, col, ttype, r)
+
+                    def live(st):
+                        isprev, pb, k = st
+                        if isprev:
+                            ls = g["lslot"](pb)
+                            ok = k >= kf[ls][col]
+                            return ok and (ttype == "ARW" or k >= kf[ls][r])
+                        return ttype != "LOW" or k >= kf[g["lslot"](i)][r]
+
+                    want = [st for st in full_steps_unskipped(g, ttype, i, col) if live(st)]
+                    assert full == want, (i, col, ttype, r)
