@@ -134,6 +134,12 @@ int gbta_set_ctas_per_sm(gbta_solver* s, int n);
  * returns how many were copied. */
 int gbta_set_trace(gbta_solver* s, int enable);
 long long gbta_get_trace(gbta_solver* s, long long* out, long long max_records);
+/* The task list of the factorization (which = 0) or of the selected inversion of the
+ * solver's current product method (which = 1), as the dataflow kernel takes it: one
+ * (type, block, row, column) int quadruple per ticket (out: 4 * max_tasks ints; the
+ * type word carries the split flags of the factorization's tasks).  Returns the number
+ * copied.  A measurement aid for reading traces (no reference counterpart). */
+long long gbta_get_task_list(gbta_solver* s, int which, int* out, long long max_tasks);
 
 /* Kernel timing (off by default; a measurement aid with no reference counterpart).
  * When enabled, the solver records CUDA events on its stream around the dataflow
@@ -145,6 +151,12 @@ long long gbta_get_trace(gbta_solver* s, long long* out, long long max_records);
  * timing was enabled). */
 int gbta_set_kernel_timing(gbta_solver* s, int enable);
 int gbta_kernel_ms(gbta_solver* s, double* ms);
+/* With kernel timing on: the tile-pair products (one 32 x 32 x 32 fp16 MMA of two digit
+ * planes each, 2 * 32^3 flops) that the tensor-core product loops of the last timed
+ * factorization (pairs[0]) and selected inversion (pairs[1]) issued, after the
+ * products of zero tiles and zero digit planes were left out; -1 where none was
+ * recorded (or the FP64 method ran: 0).  Synchronizes the solver's stream. */
+int gbta_kernel_pairs(gbta_solver* s, long long* pairs);
 
 /* Bytes of device workspace held by the solver (SerinvSolver.get_solver_memory,
  * structured_solver.py:540-550, minus the caller-owned block buffers). */

@@ -57,10 +57,12 @@ SIGNATURES = {
     "gbta_set_ctas_per_sm": (_c_int, [_vp, _c_int]),
     "gbta_set_trace": (_c_int, [_vp, _c_int]),
     "gbta_get_trace": (_c_ll, [_vp, _vp, _c_ll]),
+    "gbta_get_task_list": (_c_ll, [_vp, _c_int, _vp, _c_ll]),
     "gbta_set_twist": (_c_int, [_vp, _c_int]),
     "gbta_get_twist": (_c_int, [_vp]),
     "gbta_set_kernel_timing": (_c_int, [_vp, _c_int]),
     "gbta_kernel_ms": (_c_int, [_vp, _dp]),
+    "gbta_kernel_pairs": (_c_int, [_vp, ctypes.POINTER(ctypes.c_longlong)]),
     "gbta_workspace_bytes": (ctypes.c_size_t, [_vp]),
     "gbta_status": (_c_int, [_vp]),
     "gbta_pobtaf": (_c_int, [_vp, _vp, _vp, _vp, _vp]),

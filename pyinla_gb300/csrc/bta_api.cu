@@ -35,6 +35,7 @@ int fail(int code, const std::string& msg) {
 
 constexpr int CTRL_INTS = 8;
 constexpr int CTRL_INFO = 2, CTRL_ERR = 3;   // sticky status words of the control block
+constexpr int CTRL_MMA = 4;                  // words 4-5: the launch's tile-pair product count
 
 }  // namespace
 
@@ -60,6 +61,7 @@ struct gbta_solver {
   int* d_faux = nullptr;      // feeder "products done" flags [nt*B]
   int* d_dpre = nullptr;      // diagonal and feeder tiles' "partial stored" flags [2*nt*B]
   int* d_kf = nullptr;        // first nonzero column tile per coupling-slot row tile [(nt-1)*B]
+  bool fac_digits = false;    // d_digits holds the digit planes of the current factor
   double* d_ld = nullptr;   // logdet partials [nt + 1] + result [1]
   double* d_sig = nullptr;  // selected-inversion output blocks (lazy)
   double* d_selws = nullptr;  // selected-inversion pre-pass: diagonal inverses (lazy)
@@ -80,6 +82,7 @@ struct gbta_solver {
   bool timing = false;
   cudaEvent_t tev[6] = {};
   bool timed[3] = {false, false, false};
+  long long* h_pairs = nullptr;   // pinned: tile-pair products of the last timed factor, selinv
 };
 
 namespace gbta {
@@ -217,6 +220,7 @@ gbta::LaunchCtl next_launch(gbta_solver* s, int ntasks) {
 // status words).
 int reset_ticket(gbta_solver* s) {
   GBTA_CUDA(cudaMemsetAsync(s->d_ctrl, 0, 2 * sizeof(int), s->stream));
+  if (s->timing) GBTA_CUDA(cudaMemsetAsync(s->d_ctrl + CTRL_MMA, 0, sizeof(long long), s->stream));
   return GBTA_OK;
 }
 
@@ -341,6 +345,7 @@ int gbta_destroy(gbta_solver* s) {
   cudaFree(s->d_erow);
   cudaFree(s->d_tz);
   if (s->h_ctrl) cudaFreeHost(s->h_ctrl);
+  if (s->h_pairs) cudaFreeHost(s->h_pairs);
   for (cudaEvent_t ev : s->tev)
     if (ev) cudaEventDestroy(ev);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
@@ -378,11 +383,24 @@ int gbta_get_twist(const gbta_solver* s) { return s ? (s->g.twisted() ? 1 : 0) :
 
 int gbta_set_kernel_timing(gbta_solver* s, int enable) {
   if (int r = check_solver(s)) return r;
-  if (enable)
+  if (enable) {
     for (cudaEvent_t& ev : s->tev)
       if (!ev) GBTA_CUDA(cudaEventCreate(&ev));
+    if (!s->h_pairs) GBTA_CUDA(cudaMallocHost(&s->h_pairs, 2 * sizeof(long long)));
+    s->h_pairs[0] = s->h_pairs[1] = -1;
+  }
   s->timing = enable != 0;
   for (bool& t : s->timed) t = false;
+  return GBTA_OK;
+}
+
+int gbta_kernel_pairs(gbta_solver* s, long long* pairs) {
+  if (int r = check_solver(s)) return r;
+  if (!pairs) return fail(GBTA_ERR_ARG, "pairs is null");
+  pairs[0] = pairs[1] = -1;
+  if (!s->timing || !s->h_pairs) return GBTA_OK;
+  GBTA_CUDA(cudaStreamSynchronize(s->stream));
+  for (int k = 0; k < 2; ++k) pairs[k] = s->timed[k] ? s->h_pairs[k] : -1;
   return GBTA_OK;
 }
 
@@ -442,6 +460,16 @@ long long gbta_get_trace(gbta_solver* s, long long* out, long long max_records) 
   const long long n = s->trace_n < max_records ? s->trace_n : max_records;
   if (cudaStreamSynchronize(s->stream) != cudaSuccess) return 0;
   if (cudaMemcpy(out, s->d_trace, (size_t)n * 8 * sizeof(long long), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+  return n;
+}
+
+long long gbta_get_task_list(gbta_solver* s, int which, int* out, long long max_tasks) {
+  if (!s || !out || (which != 0 && which != 1)) return 0;
+  const int4* d = which == 0 ? s->d_ftasks : (s->method == GBTA_METHOD_OZAKI ? s->d_stasks_m : s->d_stasks);
+  const long long n0 = which == 0 ? s->n_ftasks : s->n_stasks;
+  const long long n = n0 < max_tasks ? n0 : max_tasks;
+  if (cudaStreamSynchronize(s->stream) != cudaSuccess) return 0;
+  if (cudaMemcpy(out, d, (size_t)n * sizeof(int4), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
   return n;
 }
 
@@ -505,6 +533,7 @@ static int factor_async(gbta_solver* s, double* D, double* L, double* R, double*
   gbta::launch_clear_feeders(s->g, s->d_flags, s->stream);
   const gbta::LaunchCtl lc = next_launch(s, s->n_ftasks);
   if (s->timing) GBTA_CUDA(cudaEventRecord(s->tev[0], s->stream));
+  s->fac_digits = s->method == GBTA_METHOD_OZAKI;
   if (s->method == GBTA_METHOD_OZAKI)
     gbta::launch_factor_oz(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part,
                            (__half*)s->d_digits, s->d_erow, lc, s->d_faux, s->d_dpre, s->d_kf);
@@ -515,6 +544,8 @@ static int factor_async(gbta_solver* s, double* D, double* L, double* R, double*
   if (s->timing) {
     GBTA_CUDA(cudaEventRecord(s->tev[1], s->stream));
     s->timed[0] = true;
+    GBTA_CUDA(cudaMemcpyAsync(s->h_pairs, s->d_ctrl + CTRL_MMA, sizeof(long long), cudaMemcpyDeviceToHost,
+                              s->stream));
   }
   return GBTA_OK;
 }
@@ -625,7 +656,12 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
       s->digit_bytes += bytes;
     }
   }
-  gbta::launch_selinv_prepare(g, D, L, R, use_arrow, s->d_selws, s->stream);
+  // with a tensor-core factorization's digit planes (until the inversion's own pre-pass
+  // overwrites them) the G tiles go through the tensor cores too
+  const bool tc_g = s->method == GBTA_METHOD_OZAKI && s->fac_digits;
+  gbta::launch_selinv_prepare(g, D, L, R, use_arrow, s->d_selws, s->stream, tc_g ? (__half*)s->d_digits : nullptr,
+                              s->d_erow, s->d_kf);
+  if (s->method == GBTA_METHOD_OZAKI) s->fac_digits = false;
   if (int r = reset_ticket(s)) return r;
   const gbta::LaunchCtl lc = next_launch(s, s->n_stasks);
   if (s->timing) GBTA_CUDA(cudaEventRecord(s->tev[2], s->stream));
@@ -640,6 +676,8 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
   if (s->timing) {
     GBTA_CUDA(cudaEventRecord(s->tev[3], s->stream));
     s->timed[1] = true;
+    GBTA_CUDA(cudaMemcpyAsync(s->h_pairs + 1, s->d_ctrl + CTRL_MMA, sizeof(long long),
+                              cudaMemcpyDeviceToHost, s->stream));
   }
   if (inplace)
     gbta::launch_selinv_finish_inplace(g, D, L, s->stream);

@@ -381,8 +381,12 @@ int run_async(gbta_batch* bt, int phases, double* logdet_out) {
     }
   }
   if (phases & GBTA_PHASE_SELINV) {
-    for (const BatchInst& q : bt->inst)
-      gbta::launch_selinv_prepare(q.g, q.D, q.L, q.R, q.g.a > 0, q.selws, st);
+    // tensor-core G tiles from the digit planes this run's factorization left
+    for (const BatchInst& q : bt->inst) {
+      const bool tc_g = q.method == GBTA_METHOD_OZAKI && (phases & GBTA_PHASE_FACTOR);
+      const int* kf = q.g.nt > 1 ? bt->d_faux + q.faux_off + 3 * (size_t)q.g.nt * q.g.B : nullptr;
+      gbta::launch_selinv_prepare(q.g, q.D, q.L, q.R, q.g.a > 0, q.selws, st, tc_g ? q.digits : nullptr, q.erow, kf);
+    }
     for (const BatchInst& q : bt->inst)
       if (q.method == GBTA_METHOD_OZAKI)
         gbta::launch_selinv_oz_prepare(q.g, q.D, q.L, q.R, q.g.a > 0, q.digits, q.erow,

@@ -26,6 +26,7 @@ enum {
   CTRL_ABORT = 1,    // set when any task fails; every wait returns early
   CTRL_INFO = 2,     // sticky: 1-based global row of the first non-positive pivot
   CTRL_ERR = 3,      // sticky: ERR_* code
+  CTRL_MMA = 4,      // words 4-5: tile-pair products issued by the launch (one 64-bit count)
   CTRL_N = 8
 };
 enum { ERR_NONE = 0, ERR_TIMEOUT = 1 };
@@ -259,6 +260,12 @@ __device__ __forceinline__ void cta_publish(const Ctl& c, int* flag) {
 __device__ __forceinline__ void cta_raise(int* flag, int v) {
   __syncthreads();
   if (threadIdx.x == 0) red_add_release(flag, v);
+}
+
+// Thread 0: add a task's tile-pair products (32 x 32 x 32 fp16 MMAs of two digit planes)
+// to the launch's count.
+__device__ __forceinline__ void count_pairs(const Ctl& c, unsigned long long n) {
+  if (threadIdx.x == 0 && n) atomicAdd(reinterpret_cast<unsigned long long*>(c.ctrl + CTRL_MMA), n);
 }
 
 // Pull the next ticket (CTA-uniform).

@@ -686,6 +686,7 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
     }
     if (!ok) return false;   // no copy is in flight here
     if (threadIdx.x == 0) pp->phase = ph;
+    count_pairs(c, (unsigned long long)nsteps * oz_pairs_from(0, 0));
     __syncthreads();
     trace_clear_marks(c, t);
     trace_mark(c, t, 0);   // product loop done

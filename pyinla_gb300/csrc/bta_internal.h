@@ -242,11 +242,14 @@ void launch_selinv(const Geom& g, const double* D, const double* L, const double
 
 // Selected-inversion pre-pass over the factor (both product methods): replaces every
 // off-diagonal pattern tile F(l,c) by G = F(l,c) F(c,c)^{-1} (in place) and writes
-// C_c = F(c,c)^{-T} F(c,c)^{-1} per diagonal tile into the second half of `ws`
-// (selinv_prepare_bytes; the first half holds F(c,c)^{-1}).
+// C_c = F(c,c)^{-T} F(c,c)^{-1} per diagonal tile into `ws` (selinv_prepare_bytes).
+// With fdig (the digit planes a tensor-core factorization left for every final tile,
+// rows relative to erow) the G tiles are formed on the tensor cores, skipping the
+// structurally zero coupling tiles of kf (or none: null); without, in FP64.
 size_t selinv_prepare_bytes(const Geom& g);
 void launch_selinv_prepare(const Geom& g, const double* D, double* L, double* R, int use_arrow, double* ws,
-                           cudaStream_t stream);
+                           cudaStream_t stream, const __half* fdig = nullptr, const int* erow = nullptr,
+                           const int* kf = nullptr);
 
 // Finish of a selected inversion with tensor-core products written in place over the
 // factor (its product loops read only digit planes, so Sigma can overwrite the factor

@@ -364,12 +364,30 @@ __device__ __forceinline__ void oz_step(OzAcc& acc, const __half* As, const __ha
   oz_step_t<false>(acc, As, Bs);
 }
 
+// Plane pairs (s, t) that oz_step_t<TA, SA, SB> multiplies.
+__host__ __device__ constexpr int oz_pairs_from(int SA, int SB) {
+  int n = 0;
+  for (int s = SA; s < OZ_S; ++s)
+    for (int t = SB; t < OZ_S && s + t < OZ_ND; ++t) ++n;
+  return n;
+}
+static_assert(oz_pairs_from(0, 0) == 43, "the 43 pairs s + t <= 8");
+// Leading zero planes that oz_step_z leaves out at most (A, B).
+constexpr int OZ_SA_MAX = 2, OZ_SB_MAX = 3;
+// ... and the pairs oz_step_z multiplies for runtime counts (0 when oz_pairs_vanish).
+__device__ __forceinline__ int oz_pairs_issued(int za, int zb) {
+  return oz_pairs_vanish(za, zb) ? 0
+                                 : oz_pairs_from(za < OZ_SA_MAX ? za : OZ_SA_MAX, zb < OZ_SB_MAX ? zb : OZ_SB_MAX);
+}
+
 // The tile step for runtime counts of zero leading planes za (A) and zb (B): the
-// variant that leaves out min(za, 2) A planes and min(zb, 3) B planes (compile-time
-// plane ranges keep the operands in registers).  Requires !oz_pairs_vanish(za, zb).
+// variant that leaves out min(za, OZ_SA_MAX) A planes and min(zb, OZ_SB_MAX) B planes
+// (compile-time plane ranges keep the operands in registers); the B planes it does not
+// read need not hold anything.  Requires !oz_pairs_vanish(za, zb).
 template <bool TA>
 __device__ __forceinline__ void oz_step_z(OzAcc& acc, const __half* As, const __half* Bs, int za, int zb) {
-  switch ((za < 2 ? za : 2) * 4 + (zb < 3 ? zb : 3)) {
+  static_assert(OZ_SA_MAX == 2 && OZ_SB_MAX == 3, "the variants below");
+  switch ((za < OZ_SA_MAX ? za : OZ_SA_MAX) * 4 + (zb < OZ_SB_MAX ? zb : OZ_SB_MAX)) {
     case 0: oz_step_t<TA, 0, 0>(acc, As, Bs); break;
     case 1: oz_step_t<TA, 0, 1>(acc, As, Bs); break;
     case 2: oz_step_t<TA, 0, 2>(acc, As, Bs); break;

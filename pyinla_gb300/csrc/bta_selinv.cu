@@ -60,9 +60,13 @@ static __device__ void smem_gram_lower(double* C, const double* W) {
 }
 
 // One CTA per diagonal factor tile F = D_i(c, c): finv = F^{-1}, cinv = F^{-T} F^{-1}
-// (identity-padded past the block edge).
-__global__ void __launch_bounds__(NT) k_diag_inverses(const double* D, Geom g, double* finv, double* cinv) {
+// (identity-padded past the block edge); with wdig, also the digit planes of W^T =
+// F^{-T} (row n of W^T relative to ew[n], the exponent of column n of W), the right
+// operand of the tensor-core G tiles.
+__global__ void __launch_bounds__(NT) k_diag_inverses(const double* D, Geom g, double* finv, double* cinv,
+                                                      __half* wdig, int* ew) {
   __shared__ double F[TILE_SMEM], W[TILE_SMEM], rd[TS];
+  __shared__ int es[TS];
   const int ic = blockIdx.x;
   const int i = ic / g.B, c = ic % g.B;
   const size_t bb = (size_t)g.b * g.b;
@@ -73,14 +77,111 @@ __global__ void __launch_bounds__(NT) k_diag_inverses(const double* D, Geom g, d
   __syncthreads();
   tile_diag_recip(F, rd);
   smem_trsm_rln(W, F, rd);   // W = F^{-1}
-  tile_store(finv + (size_t)ic * TS * TS, TS, TS, TS, W);
+  if (!wdig) tile_store(finv + (size_t)ic * TS * TS, TS, TS, TS, W);
   smem_gram_lower(F, W);
   tile_store(cinv + (size_t)ic * TS * TS, TS, TS, TS, F);
+  if (wdig) {
+    __syncthreads();
+    if (threadIdx.x < TS) {
+      const int n = threadIdx.x;
+      double m = 0.0;
+      for (int k = n; k < TS; ++k) m = fmax(m, fabs(W[k * LDS + n]));   // lower triangular
+      es[n] = (m > 0.0 && isfinite(m)) ? ilogb(m) + 1 : 0;
+      ew[(size_t)ic * TS + n] = es[n];
+    }
+    for (int idx = threadIdx.x; idx < TS * TS; idx += NT) {
+      const int n = idx / TS, k = idx % TS;
+      F[n * LDS + k] = W[k * LDS + n];
+    }
+    __syncthreads();
+    oz_store_digits(wdig + (size_t)ic * OZ_TILE, F, TS, TS, es);
+  }
+}
+
+// One CTA per off-diagonal pattern tile (the slots of k_g_tiles): G = F(l, c) F(c, c)^{-1}
+// on the tensor cores, from the digit planes the factorization left for F(l, c) (rows
+// relative to the row exponents erow) and those of F(c, c)^{-T} (k_diag_inverses): one
+// 43-pair tile step folded into FP64, written in place.  Coupling tiles that are
+// structurally zero (kf, launch_coupling_kfirst) stay zero.
+__global__ void __launch_bounds__(NT) k_g_tiles_oz(double* D, double* L, double* R, Geom g, int use_arrow,
+                                                   const __half* fdig, const int* erow, const __half* wdig,
+                                                   const int* ew, const int* kf) {
+  __shared__ __align__(16) __half As[OZ_OPER];
+  __shared__ __align__(16) __half Bs[OZ_OPER];
+  __shared__ double X[TILE_SMEM];
+  __shared__ int er[TS], ec[TS];
+  const int slot = blockIdx.x;
+  const int B = g.B;
+  const size_t bb = (size_t)g.b * g.b, ab = (size_t)g.a * g.b;
+  int i, c;
+  double* base;
+  int row0, rows;
+  long long grow0;   // global row of the tile's first row (row exponents)
+  if (slot < g.nt * B * B) {
+    i = slot / (B * B);
+    const int r = (slot / B) % B;
+    c = slot % B;
+    if (r <= c) return;
+    base = D + i * bb;
+    row0 = r * TS;
+    rows = g.b;
+    grow0 = (long long)i * g.b + r * TS;
+  } else if (slot < (2 * g.nt - 1) * B * B) {
+    const int s2 = slot - g.nt * B * B;
+    const int j = s2 / (B * B);   // L slot j: columns of block lcol(j), rows of the block after it
+    const int r = (s2 / B) % B;
+    c = s2 % B;
+    if (kf && c < kf[j * B + r]) return;
+    i = g.lcol(j);
+    base = L + j * bb;
+    row0 = r * TS;
+    rows = g.b;
+    grow0 = (long long)g.nxt(i) * g.b + r * TS;
+  } else if (slot < (2 * g.nt - 1) * B * B + g.nt * B) {
+    if (!use_arrow) return;
+    const int s3 = slot - (2 * g.nt - 1) * B * B;
+    i = s3 / B;
+    c = s3 % B;
+    base = R + i * ab;
+    row0 = 0;
+    rows = g.a;
+    grow0 = (long long)g.nt * g.b;
+  } else {
+    return;
+  }
+  const Tile t = make_tile(base, g.b, row0, c * TS, rows, g.b);
+  oz_load_async(As, fdig + (size_t)slot * OZ_TILE);
+  oz_load_async(Bs, wdig + (size_t)(i * B + c) * OZ_TILE);
+  cp_async_commit();
+  if (threadIdx.x < TS) {
+    er[threadIdx.x] = threadIdx.x < t.rows ? erow[grow0 + threadIdx.x] : 0;
+    ec[threadIdx.x] = ew[(size_t)(i * B + c) * TS + threadIdx.x];
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  OzAcc acc;
+  oz_clear_partials(acc);
+  int esum[2][4];
+#pragma unroll
+  for (int n = 0; n < 2; ++n)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      acc.v[n][q] = 0.0;
+      esum[n][q] = er[oz_row(n, q)] + ec[oz_col(n, q)];
+    }
+  oz_step(acc, As, Bs);
+  oz_fold_sub(acc, esum);   // acc.v = -G
+#pragma unroll
+  for (int n = 0; n < 2; ++n)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) X[oz_row(n, q) * LDS + oz_col(n, q)] = -acc.v[n][q];
+  __syncthreads();
+  tile_store(const_cast<double*>(t.p), g.b, t.rows, t.cols, X);
 }
 
 // One CTA per off-diagonal pattern tile F(l, c) of block column i (the slots of D_i
 // below the diagonal, block i's coupling slot lslot(i) and R_i): G = F(l, c) F(c, c)^{-1},
-// in place.
+// in place.  A zero tile (half the coupling tiles of a banded coupling) stays as it is.
 __global__ void __launch_bounds__(NT) k_g_tiles(double* D, double* L, double* R, Geom g, int use_arrow,
                                                 const double* finv) {
   __shared__ double X[TILE_SMEM], W[TILE_SMEM];
@@ -119,20 +220,41 @@ __global__ void __launch_bounds__(NT) k_g_tiles(double* D, double* L, double* R,
     return;
   }
   const Tile t = make_tile(base, g.b, row0, c * TS, rows, g.b);
-  tile_load(X, t);
+  {
+    double v[PER_THREAD];
+    tile_ldg(v, t);
+    bool nz = false;
+#pragma unroll
+    for (int k = 0; k < PER_THREAD; ++k) nz |= v[k] != 0.0;
+    if (!__syncthreads_or(nz)) return;
+    tile_sts(X, v);
+  }
   tile_load(W, make_tile(finv + (size_t)(i * B + c) * TS * TS, TS, 0, 0, TS, TS));
   smem_gemm_lower_right(X, W);
   tile_store(const_cast<double*>(t.p), g.b, t.rows, t.cols, X);
 }
 
-size_t selinv_prepare_bytes(const Geom& g) { return 2 * (size_t)g.nt * g.B * TS * TS * sizeof(double); }
+// Workspace per diagonal tile: F^{-1} (FP64), C = F^{-T} F^{-1} (FP64), the digit planes of
+// F^{-T} and its column exponents.
+size_t selinv_prepare_bytes(const Geom& g) {
+  return (size_t)g.nt * g.B * (2 * TS * TS * sizeof(double) + OZ_TILE * sizeof(__half) + TS * sizeof(int));
+}
 
 void launch_selinv_prepare(const Geom& g, const double* D, double* L, double* R, int use_arrow, double* ws,
-                           cudaStream_t stream) {
+                           cudaStream_t stream, const __half* fdig, const int* erow, const int* kf) {
+  const size_t ntile = (size_t)g.nt * g.B;
   double* finv = ws;
-  double* cinv = ws + (size_t)g.nt * g.B * TS * TS;
-  k_diag_inverses<<<g.nt * g.B, NT, 0, stream>>>(D, g, finv, cinv);
-  k_g_tiles<<<g.nflags(), NT, 0, stream>>>(const_cast<double*>(D), L, R, g, use_arrow, finv);
+  double* cinv = ws + ntile * TS * TS;
+  __half* wdig = reinterpret_cast<__half*>(cinv + ntile * TS * TS);
+  int* ew = reinterpret_cast<int*>(wdig + ntile * OZ_TILE);
+  if (fdig) {
+    k_diag_inverses<<<g.nt * g.B, NT, 0, stream>>>(D, g, finv, cinv, wdig, ew);
+    k_g_tiles_oz<<<g.nflags(), NT, 0, stream>>>(const_cast<double*>(D), L, R, g, use_arrow, fdig, erow, wdig, ew,
+                                                kf);
+  } else {
+    k_diag_inverses<<<g.nt * g.B, NT, 0, stream>>>(D, g, finv, cinv, nullptr, nullptr);
+    k_g_tiles<<<g.nflags(), NT, 0, stream>>>(const_cast<double*>(D), L, R, g, use_arrow, finv);
+  }
   count_launches(2);
 }
 

@@ -44,6 +44,7 @@ __global__ void __launch_bounds__(NT) k_fac_col_exponents(const double* D, const
 __global__ void __launch_bounds__(NT) k_fac_digits_t(const double* D, const double* L, const double* R, Geom g,
                                                      int use_arrow, const int* ecol, __half* dig, int* dz) {
   __shared__ int red[NT / 32];
+  __shared__ __align__(16) __half planes[OZ_TILE];   // the tile's planes, written out in 16-byte pieces
   const int slot = blockIdx.x;
   const int B = g.B;
   const size_t bb = (size_t)g.b * g.b, ab = (size_t)g.a * g.b;
@@ -74,6 +75,22 @@ __global__ void __launch_bounds__(NT) k_fac_digits_t(const double* D, const doub
   __half* dst = dig + (size_t)slot * OZ_TILE;
   int lz = OZ_S;
   // pairs of rows (m, m+1) of one column jj: adjacent in the transposed layout
+  double x0[PER_THREAD / 2], x1[PER_THREAD / 2];
+  bool nz = false;
+#pragma unroll
+  for (int q = 0; q < PER_THREAD / 2; ++q) {
+    const int p = threadIdx.x + q * NT;
+    const int jj = p % TS, m = 2 * (p / TS);
+    x0[q] = (m < t.rows && jj < t.cols) ? t.p[(size_t)m * t.ld + jj] : 0.0;
+    x1[q] = (m + 1 < t.rows && jj < t.cols) ? t.p[(size_t)(m + 1) * t.ld + jj] : 0.0;
+    nz |= x0[q] != 0.0 || x1[q] != 0.0;
+  }
+  // a zero tile: the inversion drops the products of a tile whose count is OZ_S and
+  // never reads its planes, so only the count is written
+  if (dz && !__syncthreads_or(nz)) {
+    if (threadIdx.x == 0) dz[slot] = OZ_S;
+    return;
+  }
 #pragma unroll
   for (int q = 0; q < PER_THREAD / 2; ++q) {
     const int p = threadIdx.x + q * NT;
@@ -81,19 +98,23 @@ __global__ void __launch_bounds__(NT) k_fac_digits_t(const double* D, const doub
     const int e = (jj < t.cols) ? ecol[(size_t)i * g.b + c * TS + jj] : 0;
     int d0[OZ_S], d1[OZ_S];
     if (m < t.rows && jj < t.cols)
-      oz_digits(t.p[(size_t)m * t.ld + jj], e, d0);
+      oz_digits(x0[q], e, d0);
     else
       oz_zero_digits(d0);
     if (m + 1 < t.rows && jj < t.cols)
-      oz_digits(t.p[(size_t)(m + 1) * t.ld + jj], e, d1);
+      oz_digits(x1[q], e, d1);
     else
       oz_zero_digits(d1);
-    unsigned* w = reinterpret_cast<unsigned*>(dst + oz_swz(jj, m));
+    unsigned* w = reinterpret_cast<unsigned*>(planes + oz_swz(jj, m));
 #pragma unroll
     for (int s = 0; s < OZ_S; ++s) w[s * (OZ_PLANE / 2)] = oz_digit_pair(d0[s], d1[s]);
     lz = min(lz, min(oz_lead_zeros(d0), oz_lead_zeros(d1)));
   }
-  lz = cta_min_int(lz, red);
+  lz = cta_min_int(lz, red);   // (contains the barriers that complete the planes)
+  // with the counts, the inversion reads no plane below min(lz, OZ_SB_MAX) (oz_step_z)
+  const int first = dz ? min(lz, OZ_SB_MAX) : 0;
+  for (int k = first * (OZ_PLANE / 8) + threadIdx.x; k < OZ_CHUNKS16; k += NT)
+    reinterpret_cast<uint4*>(dst)[k] = reinterpret_cast<const uint4*>(planes)[k];
   if (dz && threadIdx.x == 0) dz[slot] = lz;
 }
 

@@ -535,6 +535,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
 
     bool ok = true;
     int since_fold = 0;
+    unsigned long long npairs = 0;   // tile-pair products issued (thread 0's count is used)
     // trace marks: m0 first operand ready, m1 end of the last blocking wait in the
     // product loop, m2 ns spent in those waits, m3 product steps
     unsigned long long waited = 0;
@@ -578,6 +579,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         // the left tile was staged qcur planes down: its planes below qcur are zero
         // (all of them from OZ_S on: nothing to add)
         const int qcur = qst[s & 1], zcur = zst[s & 1];
+        npairs += oz_pairs_issued(qcur, zcur);
         if (oz_pairs_vanish(qcur, zcur)) {
         } else if (tcur) {
           oz_step_z<true>(acc, cur, cur + OZ_OPER, qcur, zcur);
@@ -613,6 +615,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
     }
     if (!ok) return false;   // no copy is in flight here
     if (threadIdx.x == 0) pp->phase = ph;
+    count_pairs(c, npairs);
     trace_put(c, t, 2, (long long)waited);
     trace_put(c, t, 3, np);
     __syncthreads();
@@ -673,6 +676,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
           }
         const int z2 = p.fdz ? p.fdz[fac_slot(g, i2, j2, c2)] : 0;
         if (Ed > NO_EXP && !oz_pairs_vanish(0, z2)) {
+          count_pairs(c, oz_pairs_issued(0, z2));
           oz_step_z<false>(a2, A0, B0, 0, z2);
           oz_fold_sub(a2, es);
         }
