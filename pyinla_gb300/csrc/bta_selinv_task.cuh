@@ -537,7 +537,9 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
     int since_fold = 0;
     unsigned long long npairs = 0;   // tile-pair products issued (thread 0's count is used)
     // trace marks: m0 first operand ready, m1 end of the last blocking wait in the
-    // product loop, m2 ns spent in those waits, m3 product steps
+    // product loop, m2 ns spent in those waits, m3 product steps (a diagonal task
+    // overwrites m2 and m3 with the times its product loop ended and it published the
+    // next column's sub-diagonal tile)
     unsigned long long waited = 0;
     trace_clear_marks(c, t);
     auto flags_of = [&](int s, const int*& f0, const int*& f1) {
@@ -636,6 +638,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       cta_publish(c, p.part_flag + i * g.B + col);
     } else {
       __syncthreads();   // (C_col was loaded into F before the product loop)
+      trace_mark(c, t, 2);   // (diagonal task) product loop done
       diag_from_cinv(X, F);
       const SigTile d = sig_dest(p, i, col, col);
       // Merged task list: this task also finishes the sub-diagonal tile of the next
@@ -689,6 +692,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         tile_store(const_cast<double*>(d2.t.p), d2.t.ld, d2.t.rows, d2.t.cols, X2);
         const int code2 = sig_store_digits(p, (int)(d2.flag - c.flags), X2, d2.t.rows, d2.t.cols, red4);
         cta_publish_val(c, const_cast<int*>(d2.flag), code2);
+        trace_mark(c, t, 3);   // (diagonal task) next column's sub-diagonal tile published
         // this tile: its digits are the ones in A0
         tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
         {
