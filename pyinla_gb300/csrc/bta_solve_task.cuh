@@ -161,12 +161,38 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
       smem_trsm_rln(Ws, Fs, rd);   // Ws = T^{-1}
       double s = (srow < g.a && scol < p.nc) ? __ldcg(p.B + (size_t)(arrow_row0 + srow) * p.ldb + scol) : 0.0;
       if (fwd) {
+        // every tile's partial: the flags are polled by all threads at once; thread t then
+        // sums the partials k = t (mod NT), RE entries per round, and the NT sums of an
+        // entry are combined in a fixed binary tree (a fixed order: reproducible)
         bool ok = true;
-        for (int k = 0; k < ntile; ++k) {
-          if (!(ok = cta_wait(c, c.flags + pflag(g, k), nullptr, &s_ok))) break;
-          s -= __ldcg(p.part + (size_t)k * TS * NC + threadIdx.x);
+        for (int k = threadIdx.x; k < ntile && ok; k += NT) ok = spin_ready(c, c.flags + pflag(g, k));
+        if (!__syncthreads_and(ok)) return false;
+        constexpr int RE = 8;
+        double* red = Ts;                // NT x RE doubles (free in the arrow task)
+        const int ne = g.a * NC;         // entries row * NC + q of the partials with row < a
+        for (int e0 = 0; e0 < ne; e0 += RE) {
+          double acc[RE];
+#pragma unroll
+          for (int e = 0; e < RE; ++e) acc[e] = 0.0;
+          for (int k = threadIdx.x; k < ntile; k += NT) {
+            const double* P = p.part + (size_t)k * TS * NC + e0;
+#pragma unroll
+            for (int e = 0; e < RE; ++e)
+              if (e0 + e < ne) acc[e] += __ldcg(P + e);
+          }
+#pragma unroll
+          for (int e = 0; e < RE; ++e) red[threadIdx.x * RE + e] = acc[e];
+          for (int st = NT / 2; st > 0; st >>= 1) {
+            __syncthreads();
+            if (threadIdx.x < st)
+#pragma unroll
+              for (int e = 0; e < RE; ++e) red[threadIdx.x * RE + e] += red[(threadIdx.x + st) * RE + e];
+          }
+          __syncthreads();
+          // entry row * NC + q is thread (row, q)'s right-hand side element
+          if (threadIdx.x >= e0 && threadIdx.x < e0 + RE && threadIdx.x < ne) s -= red[threadIdx.x - e0];
+          __syncthreads();
         }
-        if (!ok) return false;
       }
       Ss[threadIdx.x] = s;
       __syncthreads();
@@ -321,6 +347,8 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
       __syncthreads();
     }
     if (!ok) return false;
+    trace_clear_marks(c, t);
+    trace_mark(c, t, 0);   // every dependency but the neighbour done
     // u = Linv s (forward) or Linv^T s (backward)
     double u[NC];
     if (fwd)
@@ -330,6 +358,7 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
     // ---- the neighbour: y = u - M v_nb
     if (has_nb) {
       if (!cta_wait(c, nb.flag, nullptr, &s_ok)) return false;
+      trace_mark(c, t, 1);   // neighbour published
       vec_load(Vs, p, nb.vrow0, nb.vrows);
       __syncthreads();
       double res[NC];
@@ -345,7 +374,9 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
         if (q < p.nc && row < rows) p.B[(size_t)(row0 + row) * p.ldb + q] = u[q];
       }
     }
+    trace_mark(c, t, 2);   // solution tile computed and stored
     cta_publish(c, c.flags + vflag(g, i, r));   // the next tile's wait ends here
+    trace_mark(c, t, 3);   // published
     if (fwd && p.use_arrow) {
       // arrow partial R_i(:, r) y(i, r) (rows >= a of the staged tile are zero), off
       // the chain, under its own flag
