@@ -127,7 +127,7 @@ void launch_selinv_oz_prepare(const Geom& g, const double* D, const double* L, c
   count_launches(2);
 }
 
-__global__ void __launch_bounds__(NT, 1) k_selinv_oz(SelinvArgs p) {
+__global__ void __launch_bounds__(NT, OZS_CTAS_PER_SM) k_selinv_oz(SelinvArgs p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_ok, s_t, s_ready;
   __shared__ OzPipe pipe;

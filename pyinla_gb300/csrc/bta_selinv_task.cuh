@@ -342,6 +342,36 @@ static __device__ __forceinline__ int smem_tile_exponent7(const double* X, int r
   return e >= 0 ? 7 * ((e + 6) / 7) : -7 * ((-e) / 7);
 }
 
+// The same exponent for a tile held in the OzAcc register layout (v), valid part rows x
+// cols.  Writes red (NT / 32 words) and contains one __syncthreads(): the caller's
+// earlier reads of red must be behind a barrier, and shared-memory writes made before
+// the call are visible to every thread after it.
+static __device__ __forceinline__ int acc_tile_exponent7(const double (&v)[2][4], int rows, int cols,
+                                                         unsigned long long* red) {
+  unsigned long long m = 0;
+#pragma unroll
+  for (int n = 0; n < 2; ++n)
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+      if (oz_row(n, q) < rows && oz_col(n, q) < cols) {
+        const unsigned long long a = (unsigned long long)__double_as_longlong(v[n][q]) & 0x7fffffffffffffffull;
+        m = a > m ? a : m;
+      }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, m, o);
+    m = x > m ? x : m;
+  }
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+  __syncthreads();
+  unsigned long long r = red[0];
+#pragma unroll
+  for (int w = 1; w < NT / 32; ++w) r = red[w] > r ? red[w] : r;
+  if (!r) return NO_EXP;
+  const int e = ilogb_bits(r) + 1;   // |x| < 2^e
+  return e >= 0 ? 7 * ((e + 6) / 7) : -7 * ((-e) / 7);
+}
+
 // A Sigma tile's exponent (a multiple of 7 in [-1071, 1029], or NO_EXP) as the payload
 // of its flag word (below 2^EPOCH_SHIFT), and back.
 static __device__ __forceinline__ int sig_exp_code(int E) { return E == NO_EXP ? 0 : E / 7 + 256; }
@@ -367,15 +397,21 @@ static __device__ __forceinline__ int sig_shift(int E, int En) {
   return q < OZ_S ? q : OZ_S;
 }
 
-// OZS_STAGE: halves per stage (A, B digit planes).  X and F follow the two stages; W
-// (used only by the tip task, when no stage is in flight) reuses the first stage.
+// OZS_STAGE: halves per stage (A, B digit planes), two stages.  The FP64 tiles of the
+// epilogues live in the stages, used only when no copy is in flight: X, F and the
+// merged finish's X2 in the second, W (the tip task) and the merged finish's digit
+// planes in the first.  That keeps a CTA at 67 KB, so that three fit on an SM (with
+// the 168 registers of k_selinv_oz's launch bounds).
 constexpr int OZS_STAGE = 2 * OZ_OPER;
+static_assert(3 * TILE_SMEM * sizeof(double) <= OZS_STAGE * sizeof(__half), "X, F and X2 fit in a stage");
 // Step descriptors of a task's product loop, computed once per task (larger loops
 // compute the rest on the fly): left tile slot << 1 | transposed, right tile slot.
-constexpr int OZS_DESC = 512;
-constexpr size_t OZS_SMEM = 2 * OZS_STAGE * sizeof(__half) + 2 * TILE_SMEM * sizeof(double) + TS * sizeof(double) +
-                            TS * sizeof(int) + 4 * sizeof(double) + (SCAN_RING + 2) * sizeof(int) +
-                            OZS_DESC * sizeof(int2);
+// 256 cover the loops of blocks up to 4096 rows (at most 2 B steps).
+constexpr int OZS_DESC = 256;
+constexpr size_t OZS_SMEM = 2 * OZS_STAGE * sizeof(__half) + TS * sizeof(double) + TS * sizeof(int) +
+                            4 * sizeof(double) + (SCAN_RING + 2) * sizeof(int) + OZS_DESC * sizeof(int2);
+constexpr int OZS_CTAS_PER_SM = 3;
+static_assert(OZS_CTAS_PER_SM * (OZS_SMEM + 2048) <= 228 * 1024, "three CTAs per SM");
 
 // Task t of a tensor-core selected-inversion instance.  `raw` is OZS_SMEM bytes of
 // (16-byte aligned) shared memory.  Returns false when the launch is aborted.
@@ -388,10 +424,10 @@ constexpr size_t OZS_SMEM = 2 * OZS_STAGE * sizeof(__half) + 2 * TILE_SMEM * siz
 static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t, unsigned char* raw, int* s_okp,
                                                       int* s_readyp, OzPipe* pp) {
   __half* stages = reinterpret_cast<__half*>(raw);
-  double* X = reinterpret_cast<double*>(raw + 2 * OZS_STAGE * sizeof(__half));
-  double* F = X + TILE_SMEM;
-  double* W = reinterpret_cast<double*>(raw);   // aliases stage 0 (free in the tip task)
-  double* rd = F + TILE_SMEM;
+  double* X = reinterpret_cast<double*>(raw + OZS_STAGE * sizeof(__half));   // stage 1
+  double* F = X + TILE_SMEM;                                                 // stage 1
+  double* W = reinterpret_cast<double*>(raw);   // stage 0 (the tip task)
+  double* rd = reinterpret_cast<double*>(raw + 2 * OZS_STAGE * sizeof(__half));
   int* ecol_t = reinterpret_cast<int*>(rd + TS);
   double* red4 = reinterpret_cast<double*>(ecol_t + TS);
   int* ring = reinterpret_cast<int*>(red4 + 4);   // flag words of the steps found ready
@@ -429,16 +465,20 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       const int cc = col * TS + threadIdx.x;
       ecol_t[threadIdx.x] = cc < g.b ? p.ecol[(size_t)i * g.b + cc] : 0;
     }
-    // the diagonal task's C_col does not depend on other tasks: load it now, off the
-    // column chain (F is not used by the product loop)
-    if (type == ST_DIAG) tile_load(F, make_tile(p.cinv + (size_t)(i * g.B + col) * TS * TS, TS, 0, 0, TS, TS));
     __syncthreads();
+    // ST_OFF / ST_PART: acc.v = -(sum of the products) = Sigma(j, col) (or its partial);
+    // ST_DIAG starts from C_col = F^{-T} F^{-1} (identity-padded): acc.v = C_col - Z =
+    // Sigma(col, col), symmetrised after the loop
     OzAcc acc;
     oz_clear_partials(acc);
+    {
+      const double* cinv_t = p.cinv + (size_t)(i * g.B + col) * TS * TS;
 #pragma unroll
-    for (int n = 0; n < 2; ++n)
+      for (int n = 0; n < 2; ++n)
 #pragma unroll
-      for (int q = 0; q < 4; ++q) acc.v[n][q] = 0.0;
+        for (int q = 0; q < 4; ++q)
+          acc.v[n][q] = type == ST_DIAG ? __ldcg(cinv_t + oz_row(n, q) * TS + oz_col(n, q)) : 0.0;
+    }
     int E = NO_EXP;   // running exponent of the left operand (unset)
     int esum[2][4];
     auto set_esum = [&]() {
@@ -621,26 +661,45 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
     trace_put(c, t, 2, (long long)waited);
     trace_put(c, t, 3, np);
     __syncthreads();
-    // acc.v = -(sum of the products): ST_OFF: Sigma(j,col); ST_DIAG: -Z
+    unsigned long long* red = reinterpret_cast<unsigned long long*>(red4);
+    auto acc_to_x = [&](double* Y, const double (&v)[2][4]) {
 #pragma unroll
-    for (int n = 0; n < 2; ++n)
+      for (int n = 0; n < 2; ++n)
 #pragma unroll
-      for (int q = 0; q < 4; ++q) X[oz_row(n, q) * LDS + oz_col(n, q)] = acc.v[n][q];
+        for (int q = 0; q < 4; ++q) Y[oz_row(n, q) * LDS + oz_col(n, q)] = v[n][q];
+    };
+    // A finished Sigma tile leaves through its digit planes, which are all that the
+    // inversion's consumers read: they are written and the tile published first, the
+    // FP64 tile stored after (for the caller).
     if (type == ST_OFF) {
-      __syncthreads();
       const SigTile d = sig_dest(p, i, j, col);
+      acc_to_x(X, acc.v);
+      const int E = acc_tile_exponent7(acc.v, d.t.rows, d.t.cols, red);   // (its barrier covers X)
+      oz_store_digits_uniform(p.sdig + (size_t)(d.flag - c.flags) * OZ_TILE, X, d.t.rows, d.t.cols,
+                              E == NO_EXP ? 0 : E);
+      cta_publish_val(c, const_cast<int*>(d.flag), sig_exp_code(E));
       tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
-      const int code = sig_store_digits(p, (int)(d.flag - c.flags), X, d.t.rows, d.t.cols, red4);
-      cta_publish_val(c, const_cast<int*>(d.flag), code);
     } else if (type == ST_PART) {   // the partial sum, for the diagonal task that finishes the tile
+      acc_to_x(X, acc.v);
       __syncthreads();
       tile_store(p.part + (size_t)(i * g.B + col) * TS * TS, TS, TS, TS, X);
       cta_publish(c, p.part_flag + i * g.B + col);
     } else {
-      __syncthreads();   // (C_col was loaded into F before the product loop)
       trace_mark(c, t, 2);   // (diagonal task) product loop done
-      diag_from_cinv(X, F);
       const SigTile d = sig_dest(p, i, col, col);
+      // symmetrise: acc.v <- (acc.v + acc.v^T) / 2, through X
+      acc_to_x(X, acc.v);
+      __syncthreads();
+#pragma unroll
+      for (int n = 0; n < 2; ++n)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int r = oz_row(n, q), cc = oz_col(n, q);
+          acc.v[n][q] = 0.5 * (X[r * LDS + cc] + X[cc * LDS + r]);
+        }
+      __syncthreads();
+      acc_to_x(X, acc.v);
+      const int Ed = acc_tile_exponent7(acc.v, d.t.rows, d.t.cols, red);   // (its barrier covers X)
       // Merged task list: this task also finishes the sub-diagonal tile of the next
       // column, Sigma(j2, c2) of block column i2, whose last product needs this tile:
       // Sigma(j2, c2) = partial - Sigma(col, col) G(j2, c2) (the tile is symmetric, so
@@ -654,58 +713,59 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       if (p.merged && i2 >= 0) {
         __half* A0 = stages;   // stage 0: this tile's digits (no copy is in flight after the loop)
         __half* B0 = stages + OZ_OPER;
-        double* X2 = reinterpret_cast<double*>(stages + OZS_STAGE);   // stage 1: Sigma(j2, c2)
-        if (!cta_wait(c, p.part_flag + i2 * g.B + c2, nullptr, &s_ok)) return false;
-        tile_load(F, make_tile(p.part + (size_t)(i2 * g.B + c2) * TS * TS, TS, 0, 0, TS, TS));
+        double* X2 = F + TILE_SMEM;   // stage 1, after X and F: Sigma(j2, c2)
+        oz_load_async(B0, p.fdig + (size_t)fac_slot(g, i2, j2, c2) * OZ_TILE);
+        cp_async_commit();
         if (threadIdx.x < TS) {
           const int cc = c2 * TS + threadIdx.x;
           ecol_t[threadIdx.x] = cc < g.b ? p.ecol[(size_t)i2 * g.b + cc] : 0;
         }
-        oz_load_async(B0, p.fdig + (size_t)fac_slot(g, i2, j2, c2) * OZ_TILE);
-        cp_async_commit();
-        const int Ed = smem_tile_exponent7(X, d.t.rows, d.t.cols, red4);   // contains barriers
+        if (!cta_wait(c, p.part_flag + i2 * g.B + c2, nullptr, &s_ok)) return false;
+        OzAcc a2;   // starts from the partial (its loads overlap the slicing below)
+        oz_clear_partials(a2);
+        {
+          const double* P = p.part + (size_t)(i2 * g.B + c2) * TS * TS;
+#pragma unroll
+          for (int n = 0; n < 2; ++n)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) a2.v[n][q] = __ldcg(P + oz_row(n, q) * TS + oz_col(n, q));
+        }
         oz_store_digits_uniform(A0, X, d.t.rows, d.t.cols, Ed == NO_EXP ? 0 : Ed);
         cp_async_wait_all();
         __syncthreads();
-        OzAcc a2;
-        oz_clear_partials(a2);
         int es[2][4];
 #pragma unroll
         for (int n = 0; n < 2; ++n)
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            a2.v[n][q] = F[oz_row(n, q) * LDS + oz_col(n, q)];
-            es[n][q] = Ed + ecol_t[oz_col(n, q)];
-          }
+          for (int q = 0; q < 4; ++q) es[n][q] = Ed + ecol_t[oz_col(n, q)];
         const int z2 = p.fdz ? p.fdz[fac_slot(g, i2, j2, c2)] : 0;
         if (Ed > NO_EXP && !oz_pairs_vanish(0, z2)) {
           count_pairs(c, oz_pairs_issued(0, z2));
           oz_step_z<false>(a2, A0, B0, 0, z2);
           oz_fold_sub(a2, es);
         }
-#pragma unroll
-        for (int n = 0; n < 2; ++n)
-#pragma unroll
-          for (int q = 0; q < 4; ++q) X2[oz_row(n, q) * LDS + oz_col(n, q)] = a2.v[n][q];
-        __syncthreads();
         const SigTile d2 = sig_dest(p, i2, j2, c2);
-        tile_store(const_cast<double*>(d2.t.p), d2.t.ld, d2.t.rows, d2.t.cols, X2);
-        const int code2 = sig_store_digits(p, (int)(d2.flag - c.flags), X2, d2.t.rows, d2.t.cols, red4);
-        cta_publish_val(c, const_cast<int*>(d2.flag), code2);
+        acc_to_x(X2, a2.v);
+        const int E2 = acc_tile_exponent7(a2.v, d2.t.rows, d2.t.cols, red);   // (its barrier covers X2)
+        oz_store_digits_uniform(p.sdig + (size_t)(d2.flag - c.flags) * OZ_TILE, X2, d2.t.rows, d2.t.cols,
+                                E2 == NO_EXP ? 0 : E2);
+        cta_publish_val(c, const_cast<int*>(d2.flag), sig_exp_code(E2));
         trace_mark(c, t, 3);   // (diagonal task) next column's sub-diagonal tile published
+        tile_store(const_cast<double*>(d2.t.p), d2.t.ld, d2.t.rows, d2.t.cols, X2);
         // this tile: its digits are the ones in A0
-        tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
         {
           const uint4* src = reinterpret_cast<const uint4*>(A0);
           uint4* dst = reinterpret_cast<uint4*>(p.sdig + (size_t)(d.flag - c.flags) * OZ_TILE);
           for (int k = threadIdx.x; k < OZ_CHUNKS16; k += NT) dst[k] = src[k];
         }
         cta_publish_val(c, const_cast<int*>(d.flag), sig_exp_code(Ed));
+        tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
         fence_async_smem();   // stages 0 and 1 are refilled by bulk copies later
       } else {
+        oz_store_digits_uniform(p.sdig + (size_t)(d.flag - c.flags) * OZ_TILE, X, d.t.rows, d.t.cols,
+                                Ed == NO_EXP ? 0 : Ed);
+        cta_publish_val(c, const_cast<int*>(d.flag), sig_exp_code(Ed));
         tile_store(const_cast<double*>(d.t.p), d.t.ld, d.t.rows, d.t.cols, X);
-        const int code = sig_store_digits(p, (int)(d.flag - c.flags), X, d.t.rows, d.t.cols, red4);
-        cta_publish_val(c, const_cast<int*>(d.flag), code);
       }
     }
     trace_task(c, t, type, t_task0);
