@@ -313,9 +313,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         if e: e["fac"][1].record(); e["sol"][0].record()
         torch.mv(model._Aty_v.t(), tau_dev, out=mu)
         _lib.check(lib.gbta_pobtas_async(h.ptr, Dc.data_ptr(), Lc.data_ptr(), Rc.data_ptr(), Tc.data_ptr(),
-                                         mu.data_ptr(), 1, 0))
-        _lib.check(lib.gbta_pobtas_async(h.ptr, Dc.data_ptr(), Lc.data_ptr(), Rc.data_ptr(), Tc.data_ptr(),
-                                         mu.data_ptr(), 1, 1))
+                                         mu.data_ptr(), 1, 2))   # N then C in one launch
         if e: e["sol"][1].record(); e["sel"][0].record()
         _lib.check(lib.gbta_pobtasi_async(h.ptr, Dc.data_ptr(), Lc.data_ptr(), Rc.data_ptr(), Tc.data_ptr()))
         if e: e["sel"][1].record()
@@ -653,8 +651,7 @@ def run_batch41(args):
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record()
             _lib.check(lib.gbta_pobtaf_async(h.ptr, D.data_ptr(), L.data_ptr(), Rp, Tp))
-            _lib.check(lib.gbta_pobtas_async(h.ptr, D.data_ptr(), L.data_ptr(), Rp, Tp, x.data_ptr(), 1, 0))
-            _lib.check(lib.gbta_pobtas_async(h.ptr, D.data_ptr(), L.data_ptr(), Rp, Tp, x.data_ptr(), 1, 1))
+            _lib.check(lib.gbta_pobtas_async(h.ptr, D.data_ptr(), L.data_ptr(), Rp, Tp, x.data_ptr(), 1, 2))
             _lib.check(lib.gbta_pobtasi_async(h.ptr, D.data_ptr(), L.data_ptr(), Rp, Tp))
             e1.record()
             h.status()

@@ -26,7 +26,9 @@
  *
  * Right-hand sides: B is (N, nrhs) row-major with N = nt*b + a (N = nt*b for the
  * "bt" variants); the reference passes nrhs = 1.  trans = 0 solves L y = b
- * (Serinv trans="N"), trans = 1 solves L^T x = y (trans="C").
+ * (Serinv trans="N"), trans = 1 solves L^T x = y (trans="C"), and trans = 2 does both,
+ * N then C, in one launch (the reference's solve, structured_solver.py:102-149: the
+ * backward sweep's tasks follow the forward sweep's as soon as their tiles are solved).
  *
  * Return codes (int): 0 success; > 0 LAPACK-style info: the 1-based global row whose
  * pivot was not positive (non-SPD input, or NaN); < 0 an error (see gbta_last_error).
@@ -119,6 +121,17 @@ int gbta_get_method(const gbta_solver* s);
  * Sigma in every buffer. */
 int gbta_set_twist(gbta_solver* s, int twist);
 int gbta_get_twist(const gbta_solver* s);
+
+/* Overlapped selected inversion (off by default; no reference counterpart: the reference
+ * runs its calls one after the other).  With it on, a tensor-core gbta_pobtasi that follows
+ * this solver's gbta_pobtaf runs its whole pre-pass and inversion on a second stream from
+ * the factorization's completion, concurrently with the work enqueued on the solver's
+ * stream in between (the sweeps of gbta_pobtas), and writes Sigma into a workspace of the
+ * size of the blocks; the write-back into the caller's blocks is enqueued on the solver's
+ * stream, after that work and the inversion.  The blocks must hold the factor that
+ * gbta_pobtaf left until then (the sweeps only read them).  The sweeps then run one CTA
+ * per SM and the inversion two.  Status words of both streams are read by gbta_status. */
+int gbta_set_selinv_overlap(gbta_solver* s, int enable);
 
 /* Persistent CTAs per SM of the dataflow launches (0, the default: as many as the
  * kernel's registers and shared memory allow; GBTA_CTAS_PER_SM in the environment

@@ -58,6 +58,7 @@ SIGNATURES = {
     "gbta_set_trace": (_c_int, [_vp, _c_int]),
     "gbta_get_trace": (_c_ll, [_vp, _vp, _c_ll]),
     "gbta_get_task_list": (_c_ll, [_vp, _c_int, _vp, _c_ll]),
+    "gbta_set_selinv_overlap": (_c_int, [_vp, _c_int]),
     "gbta_set_twist": (_c_int, [_vp, _c_int]),
     "gbta_get_twist": (_c_int, [_vp]),
     "gbta_set_kernel_timing": (_c_int, [_vp, _c_int]),

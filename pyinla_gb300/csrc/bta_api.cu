@@ -62,6 +62,17 @@ struct gbta_solver {
   int* d_dpre = nullptr;      // diagonal and feeder tiles' "partial stored" flags [2*nt*B]
   int* d_kf = nullptr;        // first nonzero column tile per coupling-slot row tile [(nt-1)*B]
   bool fac_digits = false;    // d_digits holds the digit planes of the current factor
+  // Overlapped selected inversion (gbta_set_selinv_overlap): the inversion runs on a
+  // second stream from the factorization's completion, next to the sweeps enqueued after
+  // it, with its own control block and flags, into the Sigma workspace; the write-back
+  // into the caller's blocks comes on the solver's stream after both.
+  bool overlap = false;
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fac = nullptr;   // the last factorization's completion (solver's stream)
+  cudaEvent_t ev_sel = nullptr;   // the overlapped inversion's completion (side stream)
+  bool fac_evt = false;           // ev_fac belongs to the factor the blocks hold
+  int* d_ctrl2 = nullptr;         // control block of the side stream's launches
+  int* d_flags2 = nullptr;        // their ready flags
   double* d_ld = nullptr;   // logdet partials [nt + 1] + result [1]
   double* d_sig = nullptr;  // selected-inversion output blocks (lazy)
   double* d_selws = nullptr;  // selected-inversion pre-pass: diagonal inverses (lazy)
@@ -216,11 +227,28 @@ gbta::LaunchCtl next_launch(gbta_solver* s, int ntasks) {
   return lc;
 }
 
+// The same for a launch on the side stream (overlapped inversion).
+gbta::LaunchCtl next_side_launch(gbta_solver* s, int ntasks) {
+  const int e0 = s->epoch;
+  gbta::LaunchCtl lc = next_launch(s, ntasks);
+  if (s->epoch < e0)   // the epoch counter wrapped: the side flags start over too
+    cudaMemsetAsync(s->d_flags2, 0, (size_t)s->g.nflags() * sizeof(int), s->side);
+  lc.ctrl = s->d_ctrl2;
+  lc.flags = s->d_flags2;
+  lc.stream = s->side;
+  return lc;
+}
+
 // Reset the ticket counter and the abort flag of the next launch (not the sticky
 // status words).
 int reset_ticket(gbta_solver* s) {
   GBTA_CUDA(cudaMemsetAsync(s->d_ctrl, 0, 2 * sizeof(int), s->stream));
   if (s->timing) GBTA_CUDA(cudaMemsetAsync(s->d_ctrl + CTRL_MMA, 0, sizeof(long long), s->stream));
+  return GBTA_OK;
+}
+int reset_side_ticket(gbta_solver* s) {
+  GBTA_CUDA(cudaMemsetAsync(s->d_ctrl2, 0, 2 * sizeof(int), s->side));
+  if (s->timing) GBTA_CUDA(cudaMemsetAsync(s->d_ctrl2 + CTRL_MMA, 0, sizeof(long long), s->side));
   return GBTA_OK;
 }
 
@@ -288,6 +316,9 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   }
   CREATE_CUDA(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking));
   s->stream = s->own_stream;
+  CREATE_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+  CREATE_CUDA(cudaEventCreateWithFlags(&s->ev_fac, cudaEventDisableTiming));
+  CREATE_CUDA(cudaEventCreateWithFlags(&s->ev_sel, cudaEventDisableTiming));
 
   const std::vector<int4> ft = gbta::factor_task_list(s->g), st = gbta::selinv_task_list(s->g),
                           stm = gbta::selinv_task_list(s->g, true);
@@ -296,6 +327,10 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   const size_t ntile = (size_t)nt * s->g.B;
   CREATE_CUDA(cudaMalloc(&s->d_ctrl, CTRL_INTS * sizeof(int)));
   CREATE_CUDA(cudaMalloc(&s->d_flags, (size_t)nflags * sizeof(int)));
+  CREATE_CUDA(cudaMalloc(&s->d_ctrl2, CTRL_INTS * sizeof(int)));
+  CREATE_CUDA(cudaMalloc(&s->d_flags2, (size_t)nflags * sizeof(int)));
+  CREATE_CUDA(cudaMemsetAsync(s->d_ctrl2, 0, CTRL_INTS * sizeof(int), s->stream));
+  CREATE_CUDA(cudaMemsetAsync(s->d_flags2, 0, (size_t)nflags * sizeof(int), s->stream));
   CREATE_CUDA(cudaMalloc(&s->d_ftasks, ft.size() * sizeof(int4)));
   CREATE_CUDA(cudaMalloc(&s->d_stasks, st.size() * sizeof(int4)));
   CREATE_CUDA(cudaMalloc(&s->d_stasks_m, stm.size() * sizeof(int4)));
@@ -315,7 +350,7 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   CREATE_CUDA(cudaMemcpyAsync(s->d_stasks_m, stm.data(), stm.size() * sizeof(int4), cudaMemcpyHostToDevice, s->stream));
   CREATE_CUDA(cudaStreamSynchronize(s->stream));
 #undef CREATE_CUDA
-  s->ws_bytes = CTRL_INTS * sizeof(int) + (size_t)nflags * sizeof(int) + (ft.size() + st.size()) * sizeof(int4) +
+  s->ws_bytes = 2 * (CTRL_INTS * sizeof(int) + (size_t)nflags * sizeof(int)) + (ft.size() + st.size()) * sizeof(int4) +
                 ntile * gbta::TS * (gbta::TS + gbta::SOLVE_NC) * sizeof(double) + (nt + 2) * sizeof(double) +
                 3 * ntile * sizeof(int) + (size_t)(nt - 1) * s->g.B * sizeof(int);
   *out = s;
@@ -326,6 +361,7 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
 int gbta_destroy(gbta_solver* s) {
   if (!s) return GBTA_OK;
   if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->side) cudaStreamSynchronize(s->side);
   cudaFree(s->d_ctrl);
   cudaFree(s->d_flags);
   cudaFree(s->d_ftasks);
@@ -348,6 +384,11 @@ int gbta_destroy(gbta_solver* s) {
   if (s->h_pairs) cudaFreeHost(s->h_pairs);
   for (cudaEvent_t ev : s->tev)
     if (ev) cudaEventDestroy(ev);
+  cudaFree(s->d_ctrl2);
+  cudaFree(s->d_flags2);
+  if (s->ev_fac) cudaEventDestroy(s->ev_fac);
+  if (s->ev_sel) cudaEventDestroy(s->ev_sel);
+  if (s->side) cudaStreamDestroy(s->side);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
   delete s;
   return GBTA_OK;
@@ -433,6 +474,12 @@ int gbta_set_method(gbta_solver* s, int method) {
 
 int gbta_get_method(const gbta_solver* s) { return s ? s->method : -1; }
 
+int gbta_set_selinv_overlap(gbta_solver* s, int enable) {
+  if (int r = check_solver(s)) return r;
+  s->overlap = enable != 0;
+  return GBTA_OK;
+}
+
 int gbta_set_ctas_per_sm(gbta_solver* s, int n) {
   if (int r = check_solver(s)) return r;
   if (n < 0 || n > 8) return fail(GBTA_ERR_ARG, "ctas_per_sm must be in [0, 8]");
@@ -489,11 +536,18 @@ size_t gbta_workspace_bytes(const gbta_solver* s) {
 int gbta_status(gbta_solver* s) {
   if (int r = check_solver(s)) return r;
   GBTA_CUDA(cudaStreamSynchronize(s->stream));
+  GBTA_CUDA(cudaStreamSynchronize(s->side));
   GBTA_CUDA(cudaGetLastError());
-  GBTA_CUDA(cudaMemcpy(s->h_ctrl, s->d_ctrl, CTRL_INTS * sizeof(int), cudaMemcpyDeviceToHost));
-  const int info = s->h_ctrl[CTRL_INFO], err = s->h_ctrl[CTRL_ERR];
+  // the sticky words of both control blocks (the side stream's: an overlapped inversion)
+  int info = 0, err = 0;
+  for (int* ctrl : {s->d_ctrl, s->d_ctrl2}) {
+    GBTA_CUDA(cudaMemcpy(s->h_ctrl, ctrl, CTRL_INTS * sizeof(int), cudaMemcpyDeviceToHost));
+    if (s->h_ctrl[CTRL_ERR] != 0) err = s->h_ctrl[CTRL_ERR];
+    if (s->h_ctrl[CTRL_INFO] != 0 && info == 0) info = s->h_ctrl[CTRL_INFO];
+  }
   if (info != 0 || err != 0) {
     GBTA_CUDA(cudaMemsetAsync(s->d_ctrl, 0, CTRL_INTS * sizeof(int), s->stream));
+    GBTA_CUDA(cudaMemsetAsync(s->d_ctrl2, 0, CTRL_INTS * sizeof(int), s->stream));
     GBTA_CUDA(cudaStreamSynchronize(s->stream));
   }
   if (err == 1) return fail(GBTA_ERR_TIMEOUT, "a kernel wait exceeded the wait limit; the launch was abandoned");
@@ -541,6 +595,8 @@ static int factor_async(gbta_solver* s, double* D, double* L, double* R, double*
     gbta::launch_factor(s->g, D, L, R, T, use_arrow, s->d_ftasks, s->n_ftasks, s->d_tip_part, lc, s->d_faux,
                         s->d_dpre, s->d_kf);
   GBTA_CUDA(cudaGetLastError());
+  GBTA_CUDA(cudaEventRecord(s->ev_fac, s->stream));
+  s->fac_evt = true;
   if (s->timing) {
     GBTA_CUDA(cudaEventRecord(s->tev[1], s->stream));
     s->timed[0] = true;
@@ -570,14 +626,31 @@ static int solve_async(gbta_solver* s, const double* D, const double* L, const d
   if (!D || !B || (s->g.nt > 1 && !L)) return fail(GBTA_ERR_ARG, "D/L/B must be device pointers");
   if (use_arrow && (!R || !T)) return fail(GBTA_ERR_ARG, "R/T must be device pointers for the bta solve");
   if (nrhs < 1) return fail(GBTA_ERR_ARG, "nrhs must be >= 1");
-  if (trans != 0 && trans != 1) return fail(GBTA_ERR_ARG, "trans must be 0 (N) or 1 (C)");
-  const int ntasks = s->g.nt * s->g.B + (use_arrow ? 1 : 0);
+  if (trans != 0 && trans != 1 && trans != 2) return fail(GBTA_ERR_ARG, "trans must be 0 (N), 1 (C) or 2 (both)");
+  // both sweeps in one launch where the flag array has room for the second sweep's flags
+  // (every geometry but b <= 32), else one after the other
+  const bool both = trans == 2 && gbta::solve_both_fits(s->g);
+  const int ntasks = (s->g.nt * s->g.B + (use_arrow ? 1 : 0)) * (both ? 2 : 1);
   if (s->timing) GBTA_CUDA(cudaEventRecord(s->tev[4], s->stream));
   for (int c0 = 0; c0 < nrhs; c0 += gbta::SOLVE_NC) {
     const int nc = nrhs - c0 < gbta::SOLVE_NC ? nrhs - c0 : gbta::SOLVE_NC;
     if (int r = reset_ticket(s)) return r;
-    const gbta::LaunchCtl lc = next_launch(s, ntasks);
-    gbta::launch_solve(s->g, D, L, R, T, B + c0, nrhs, nc, trans, use_arrow, s->d_arrow_part, lc);
+    gbta::LaunchCtl lc = next_launch(s, ntasks);
+    // with the overlapped inversion the sweeps keep to one CTA per SM (the chain needs
+    // few; the inversion's CTAs take the rest of each SM)
+    if (s->overlap && s->ctas_per_sm == 0) lc.ctas_per_sm = 1;
+    if (both) {
+      gbta::launch_solve(s->g, D, L, R, T, B + c0, nrhs, nc, 0, use_arrow, s->d_arrow_part, lc, 1);
+    } else {
+      for (int tr = (trans == 1 ? 1 : 0); tr <= (trans == 0 ? 0 : 1); ++tr) {
+        if (tr == 1 && trans == 2) {   // the second sweep of trans = 2: its own launch
+          if (int r = reset_ticket(s)) return r;
+          lc = next_launch(s, ntasks);
+          if (s->overlap && s->ctas_per_sm == 0) lc.ctas_per_sm = 1;
+        }
+        gbta::launch_solve(s->g, D, L, R, T, B + c0, nrhs, nc, tr, use_arrow, s->d_arrow_part, lc);
+      }
+    }
     GBTA_CUDA(cudaGetLastError());
   }
   if (s->timing) {
@@ -624,10 +697,24 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
   if (use_arrow && (!R || !T)) return fail(GBTA_ERR_ARG, "R/T must be device pointers for the bta selected inversion");
   const gbta::Geom& g = s->g;
   const size_t bb = (size_t)g.b * g.b;
-  const bool inplace = s->method == GBTA_METHOD_OZAKI;   // Sigma over the factor (see below)
+  const bool ozaki = s->method == GBTA_METHOD_OZAKI;
+  // with a tensor-core factorization's digit planes (until the inversion's own pre-pass
+  // overwrites them) the G tiles go through the tensor cores too
+  const bool tc_g = ozaki && s->fac_digits;
+  // Overlapped: the whole inversion reads the factor's blocks only (the G tiles go to the
+  // Sigma workspace), so it runs on the side stream from the factorization's completion,
+  // next to whatever the solver's stream runs meanwhile (the sweeps), and the write-back
+  // follows on the solver's stream after both.  Not while tracing (one trace buffer).
+  const bool over = s->overlap && tc_g && s->fac_evt && !s->d_trace;
+  // The tensor-core method reads the factor only through its digit planes, sliced by the
+  // pre-pass, and the tip task reads T before it writes Sigma_T: without the overlap Sigma
+  // goes straight into the caller's buffers.  The FP64 method reads the factor tiles
+  // during the inversion, so Sigma goes to a workspace and is copied back.
+  const bool inplace = ozaki && !over;
   const size_t need = g.nt * bb + (g.nt - 1) * bb + (size_t)g.nt * g.a * g.b + (size_t)g.a * g.a;
   if (!inplace && s->sig_elems < need) {
     GBTA_CUDA(cudaStreamSynchronize(s->stream));
+    GBTA_CUDA(cudaStreamSynchronize(s->side));
     cudaFree(s->d_sig);
     s->d_sig = nullptr;
     s->sig_elems = 0;
@@ -639,15 +726,11 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
     GBTA_CUDA(cudaMalloc(&s->d_selws, gbta::selinv_prepare_bytes(g)));
   }
   const double* cinv = s->d_selws + (size_t)g.nt * g.B * gbta::TS * gbta::TS;
-  // The tensor-core method reads the factor only through its digit planes, sliced by the
-  // pre-pass, and the tip task reads T before it writes Sigma_T: Sigma goes straight
-  // into the caller's buffers.  The FP64 method reads the factor tiles during the
-  // inversion, so Sigma goes to a workspace and is copied back.
   double* SD = inplace ? D : s->d_sig;
   double* SL = inplace ? L : SD + g.nt * bb;
   double* SR = inplace ? R : SL + (g.nt - 1) * bb;
   double* ST = inplace ? T : SR + (size_t)g.nt * g.a * g.b;
-  if (s->method == GBTA_METHOD_OZAKI) {
+  if (ozaki) {
     if (int r = ensure_digits(s)) return r;
     if (!s->d_sdig) {
       GBTA_CUDA(cudaStreamSynchronize(s->stream));
@@ -656,28 +739,33 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
       s->digit_bytes += bytes;
     }
   }
-  // with a tensor-core factorization's digit planes (until the inversion's own pre-pass
-  // overwrites them) the G tiles go through the tensor cores too
-  const bool tc_g = s->method == GBTA_METHOD_OZAKI && s->fac_digits;
-  gbta::launch_selinv_prepare(g, D, L, R, use_arrow, s->d_selws, s->stream, tc_g ? (__half*)s->d_digits : nullptr,
-                              s->d_erow, s->d_kf);
-  if (s->method == GBTA_METHOD_OZAKI) s->fac_digits = false;
-  if (int r = reset_ticket(s)) return r;
-  const gbta::LaunchCtl lc = next_launch(s, s->n_stasks);
-  if (s->timing) GBTA_CUDA(cudaEventRecord(s->tev[2], s->stream));
-  if (s->method == GBTA_METHOD_OZAKI)
-    gbta::launch_selinv_oz(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks_m, s->n_stasks,
-                           (__half*)s->d_digits, s->d_erow, cinv, (__half*)s->d_sdig, s->d_tip_part, s->d_faux,
-                           lc,
-                           g.nflags() < (1 << 24) ? s->d_tz : nullptr);
+  cudaStream_t st = over ? s->side : s->stream;
+  if (over) GBTA_CUDA(cudaStreamWaitEvent(s->side, s->ev_fac, 0));
+  gbta::launch_selinv_prepare(g, D, L, R, use_arrow, s->d_selws, st, tc_g ? (__half*)s->d_digits : nullptr,
+                              s->d_erow, s->d_kf, over ? SD : nullptr, over ? SL : nullptr, over ? SR : nullptr);
+  if (ozaki) s->fac_digits = false;
+  s->fac_evt = false;
+  if (int r = over ? reset_side_ticket(s) : reset_ticket(s)) return r;
+  gbta::LaunchCtl lc = over ? next_side_launch(s, s->n_stasks) : next_launch(s, s->n_stasks);
+  // (its grid is the full one: the CTAs that find no slot next to the sweeps' CTAs,
+  // which were launched first and keep one per SM, start when those exit)
+  if (s->timing) GBTA_CUDA(cudaEventRecord(s->tev[2], st));
+  if (ozaki)   // (its pre-pass reads the G tiles: from the workspace when overlapped)
+    gbta::launch_selinv_oz(g, over ? SD : D, over ? SL : L, over ? SR : R, T, SD, SL, SR, ST, use_arrow,
+                           s->d_stasks_m, s->n_stasks, (__half*)s->d_digits, s->d_erow, cinv, (__half*)s->d_sdig,
+                           s->d_tip_part, s->d_faux, lc, g.nflags() < (1 << 24) ? s->d_tz : nullptr);
   else
     gbta::launch_selinv(g, D, L, R, T, SD, SL, SR, ST, use_arrow, s->d_stasks, s->n_stasks, cinv, lc);
   GBTA_CUDA(cudaGetLastError());
   if (s->timing) {
-    GBTA_CUDA(cudaEventRecord(s->tev[3], s->stream));
+    GBTA_CUDA(cudaEventRecord(s->tev[3], st));
     s->timed[1] = true;
-    GBTA_CUDA(cudaMemcpyAsync(s->h_pairs + 1, s->d_ctrl + CTRL_MMA, sizeof(long long),
-                              cudaMemcpyDeviceToHost, s->stream));
+    GBTA_CUDA(cudaMemcpyAsync(s->h_pairs + 1, (over ? s->d_ctrl2 : s->d_ctrl) + CTRL_MMA, sizeof(long long),
+                              cudaMemcpyDeviceToHost, st));
+  }
+  if (over) {
+    GBTA_CUDA(cudaEventRecord(s->ev_sel, s->side));
+    GBTA_CUDA(cudaStreamWaitEvent(s->stream, s->ev_sel, 0));
   }
   if (inplace)
     gbta::launch_selinv_finish_inplace(g, D, L, s->stream);

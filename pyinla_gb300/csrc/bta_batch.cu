@@ -313,6 +313,8 @@ int build_args(gbta_batch* bt) {
       v.trans = dir;
       v.part = q.arrow_part;
       v.ntasks = q.n_vtasks;
+      v.both = 0;
+      v.bflag0 = 0;
       v.c = batch_ctl(bt, flags, dir == 0 ? EP_SOLVE_N : EP_SOLVE_C);
     }
   }
@@ -542,6 +544,7 @@ int gbta_batch_create(int n, const int* b, const int* nt, const int* a, const in
                                    (int)gbta::BATCH_SELINV_SMEM));
   // the largest shared-memory carveout, so that two CTAs fit on an SM
   CREATE_CUDA(cudaFuncSetAttribute(gbta::k_factor_batch, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  CREATE_CUDA(cudaFuncSetAttribute(gbta::k_solve_batch, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   CREATE_CUDA(cudaFuncSetAttribute(gbta::k_selinv_batch, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
 #undef CREATE_CUDA
   *out = bt;

@@ -232,9 +232,12 @@ void launch_selinv_oz(const Geom& g, const double* D, const double* L, const dou
                       int ntasks, __half* fdig, int* ecol, const double* cinv, __half* sdig, double* part,
                       int* part_flag, const LaunchCtl& lc, int* fdz = nullptr);
 
+// both: the forward and then the backward sweep in one launch (needs 3 nt B + 2 flags,
+// solve_both_fits); trans is then ignored.
 void launch_solve(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                   double* Bv, int ldb, int nc, int trans, int use_arrow, double* arrow_part,
-                  const LaunchCtl& lc);
+                  const LaunchCtl& lc, int both = 0);
+inline bool solve_both_fits(const Geom& g) { return 3LL * g.nt * g.B + 2 <= g.nflags(); }
 
 void launch_selinv(const Geom& g, const double* D, const double* L, const double* R, const double* T,
                    double* SD, double* SL, double* SR, double* ST, int use_arrow, const int4* tasks,
@@ -245,11 +248,14 @@ void launch_selinv(const Geom& g, const double* D, const double* L, const double
 // C_c = F(c,c)^{-T} F(c,c)^{-1} per diagonal tile into `ws` (selinv_prepare_bytes).
 // With fdig (the digit planes a tensor-core factorization left for every final tile,
 // rows relative to erow) the G tiles are formed on the tensor cores, skipping the
-// structurally zero coupling tiles of kf (or none: null); without, in FP64.
+// structurally zero coupling tiles of kf (or none: null); without, in FP64.  With GD
+// (and GL, GR; tensor-core path only) the G tiles go to those blocks instead and the
+// factor's blocks are only read, so the pre-pass can run next to kernels that read them.
 size_t selinv_prepare_bytes(const Geom& g);
 void launch_selinv_prepare(const Geom& g, const double* D, double* L, double* R, int use_arrow, double* ws,
                            cudaStream_t stream, const __half* fdig = nullptr, const int* erow = nullptr,
-                           const int* kf = nullptr);
+                           const int* kf = nullptr, double* GD = nullptr, double* GL = nullptr,
+                           double* GR = nullptr);
 
 // Finish of a selected inversion with tensor-core products written in place over the
 // factor (its product loops read only digit planes, so Sigma can overwrite the factor

@@ -101,11 +101,13 @@ __global__ void __launch_bounds__(NT) k_diag_inverses(const double* D, Geom g, d
 // One CTA per off-diagonal pattern tile (the slots of k_g_tiles): G = F(l, c) F(c, c)^{-1}
 // on the tensor cores, from the digit planes the factorization left for F(l, c) (rows
 // relative to the row exponents erow) and those of F(c, c)^{-T} (k_diag_inverses): one
-// 43-pair tile step folded into FP64, written in place.  Coupling tiles that are
-// structurally zero (kf, launch_coupling_kfirst) stay zero.
+// 43-pair tile step folded into FP64, written into the blocks D, L, R (the factor's
+// own, in place, or a separate set; the kernel reads no FP64 factor tile).  Coupling
+// tiles that are structurally zero (kf, launch_coupling_kfirst) are zero in place and
+// written as zeros into a separate set (zero_skipped).
 __global__ void __launch_bounds__(NT) k_g_tiles_oz(double* D, double* L, double* R, Geom g, int use_arrow,
                                                    const __half* fdig, const int* erow, const __half* wdig,
-                                                   const int* ew, const int* kf) {
+                                                   const int* ew, const int* kf, int zero_skipped) {
   __shared__ __align__(16) __half As[OZ_OPER];
   __shared__ __align__(16) __half Bs[OZ_OPER];
   __shared__ double X[TILE_SMEM];
@@ -131,7 +133,11 @@ __global__ void __launch_bounds__(NT) k_g_tiles_oz(double* D, double* L, double*
     const int j = s2 / (B * B);   // L slot j: columns of block lcol(j), rows of the block after it
     const int r = (s2 / B) % B;
     c = s2 % B;
-    if (kf && c < kf[j * B + r]) return;
+    if (kf && c < kf[j * B + r]) {
+      if (zero_skipped) tile_store_zero(L + j * bb + (size_t)r * TS * g.b + c * TS, g.b, min(TS, g.b - r * TS),
+                                        min(TS, g.b - c * TS));
+      return;
+    }
     i = g.lcol(j);
     base = L + j * bb;
     row0 = r * TS;
@@ -241,7 +247,15 @@ size_t selinv_prepare_bytes(const Geom& g) {
 }
 
 void launch_selinv_prepare(const Geom& g, const double* D, double* L, double* R, int use_arrow, double* ws,
-                           cudaStream_t stream, const __half* fdig, const int* erow, const int* kf) {
+                           cudaStream_t stream, const __half* fdig, const int* erow, const int* kf, double* GD,
+                           double* GL, double* GR) {
+  static bool attr_set = false;   // the largest shared-memory carveout (see launch_solve)
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_diag_inverses, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_g_tiles_oz, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_g_tiles, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    attr_set = true;
+  }
   const size_t ntile = (size_t)g.nt * g.B;
   double* finv = ws;
   double* cinv = ws + ntile * TS * TS;
@@ -249,8 +263,9 @@ void launch_selinv_prepare(const Geom& g, const double* D, double* L, double* R,
   int* ew = reinterpret_cast<int*>(wdig + ntile * OZ_TILE);
   if (fdig) {
     k_diag_inverses<<<g.nt * g.B, NT, 0, stream>>>(D, g, finv, cinv, wdig, ew);
-    k_g_tiles_oz<<<g.nflags(), NT, 0, stream>>>(const_cast<double*>(D), L, R, g, use_arrow, fdig, erow, wdig, ew,
-                                                kf);
+    const bool sep = GD != nullptr;
+    k_g_tiles_oz<<<g.nflags(), NT, 0, stream>>>(sep ? GD : const_cast<double*>(D), sep ? GL : L, sep ? GR : R, g,
+                                                use_arrow, fdig, erow, wdig, ew, kf, sep ? 1 : 0);
   } else {
     k_diag_inverses<<<g.nt * g.B, NT, 0, stream>>>(D, g, finv, cinv, nullptr, nullptr);
     k_g_tiles<<<g.nflags(), NT, 0, stream>>>(const_cast<double*>(D), L, R, g, use_arrow, finv);

@@ -122,6 +122,12 @@ __global__ void __launch_bounds__(NT) k_fac_digits_t(const double* D, const doub
 // inversion with tensor-core products).
 void launch_selinv_oz_prepare(const Geom& g, const double* D, const double* L, const double* R, int use_arrow,
                               __half* fdig, int* ecol, int* fdz, cudaStream_t stream) {
+  static bool attr_set = false;   // the largest shared-memory carveout (see launch_solve)
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_fac_col_exponents, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(k_fac_digits_t, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    attr_set = true;
+  }
   k_fac_col_exponents<<<g.nt * g.B, NT, 0, stream>>>(D, L, R, g, use_arrow, ecol);
   k_fac_digits_t<<<g.nflags(), NT, 0, stream>>>(D, L, R, g, use_arrow, ecol, fdig, fdz);
   count_launches(2);

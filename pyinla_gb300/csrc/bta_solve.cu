@@ -15,8 +15,16 @@ __global__ void __launch_bounds__(NT, 1) k_solve(SolveArgs p) {
 }
 
 void launch_solve(const Geom& g, const double* D, const double* L, const double* R, const double* T, double* Bv,
-                  int ldb, int nc, int trans, int use_arrow, double* arrow_part, const LaunchCtl& lc) {
+                  int ldb, int nc, int trans, int use_arrow, double* arrow_part, const LaunchCtl& lc, int both) {
   // One launch covers nc <= NC right-hand-side columns starting at Bv (row stride ldb).
+  // The largest shared-memory carveout, as the other dataflow kernels: an SM keeps its
+  // split while any CTA is resident, so a sweep CTA on the default split would keep the
+  // selected inversion's CTAs (overlapped with the sweeps) off that SM.
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute(k_solve, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    attr_set = true;
+  }
   SolveArgs p;
   p.D = D;
   p.L = L;
@@ -29,7 +37,9 @@ void launch_solve(const Geom& g, const double* D, const double* L, const double*
   p.use_arrow = use_arrow;
   p.trans = trans;
   p.part = arrow_part;
-  p.ntasks = g.nt * g.B + (use_arrow ? 1 : 0);
+  p.ntasks = (g.nt * g.B + (use_arrow ? 1 : 0)) * (both ? 2 : 1);
+  p.both = both;
+  p.bflag0 = 2 * g.nt * g.B + 1;   // after the tiles' and the forward partials' flags
   p.c.ctrl = lc.ctrl;
   p.c.flags = lc.flags;
   p.c.epoch = lc.epoch;

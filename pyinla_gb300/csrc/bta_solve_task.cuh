@@ -38,7 +38,9 @@ struct SolveArgs {
   int use_arrow;
   int trans;
   double* part;     // [nt*B][TS*NC] arrow partials
-  int ntasks;       // nt*B (+1 with the arrow)
+  int ntasks;       // nt*B (+1 with the arrow); both sweeps: twice that
+  int both;         // one launch for the forward sweep and then the backward sweep
+  int bflag0;       // (both) offset of the backward sweep's tile and arrow flags
   Ctl c;
 };
 
@@ -107,7 +109,14 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
   const int ntile = g.nt * g.B;
   const size_t bb = (size_t)g.b * g.b, ab = (size_t)g.a * g.b;
   const int arrow_row0 = g.nt * g.b;
-  const bool fwd = p.trans == 0;
+  // With p.both the tickets of the forward sweep come first and those of the backward
+  // sweep follow (its tasks also wait for the forward sweep's tile they start from); the
+  // backward sweep's flags sit at p.bflag0.
+  const int nsweep = ntile + (p.use_arrow ? 1 : 0);
+  const bool fwd = p.both ? t < nsweep : p.trans == 0;
+  const int fo = (p.both && !fwd) ? p.bflag0 : 0;   // offset of this sweep's flags
+  const int tt = t;                                  // the ticket (trace record)
+  if (p.both && !fwd) t -= nsweep;
   {
     const unsigned long long t_task0 = c.trace ? gtimer() : 0ull;
     // ticket -> tile in the elimination order of the blocks (Geom): forward, the tiles of
@@ -159,6 +168,7 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
       __syncthreads();
       tile_diag_recip(Fs, rd);
       smem_trsm_rln(Ws, Fs, rd);   // Ws = T^{-1}
+      if (p.both && !fwd && !cta_wait(c, c.flags + ntile, nullptr, &s_ok)) return false;   // the forward y_a
       double s = (srow < g.a && scol < p.nc) ? __ldcg(p.B + (size_t)(arrow_row0 + srow) * p.ldb + scol) : 0.0;
       if (fwd) {
         // every tile's partial: the flags are polled by all threads at once; thread t then
@@ -206,8 +216,8 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
         for (int q = 0; q < p.nc; ++q)
           if (row < g.a) p.B[(size_t)(arrow_row0 + row) * p.ldb + q] = res[q];
       }
-      cta_publish(c, c.flags + ntile);
-      trace_task(c, t, 1, t_task0);
+      cta_publish(c, c.flags + fo + ntile);
+      trace_task(c, tt, 1, t_task0);
       return true;
     }
 
@@ -234,14 +244,14 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
         nb.t = make_tile(p.D + i * bb, g.b, r * TS, (r - 1) * TS, g.b, g.b);
         nb.vrow0 = i * g.b + (r - 1) * TS;
         nb.vrows = g.vrows(r - 1);
-        nb.flag = c.flags + vflag(g, i, r - 1);
+        nb.flag = c.flags + fo + vflag(g, i, r - 1);
       } else if (np > 0) {
         const int p0 = g.prev(i, 0);
         has_nb = true;
         nb.t = make_tile(p.L + g.lslot(p0) * bb, g.b, 0, (g.B - 1) * TS, g.b, g.b);
         nb.vrow0 = p0 * g.b + (g.B - 1) * TS;
         nb.vrows = g.vrows(g.B - 1);
-        nb.flag = c.flags + vflag(g, p0, g.B - 1);
+        nb.flag = c.flags + fo + vflag(g, p0, g.B - 1);
       }
     } else {
       if (r < g.B - 1) {
@@ -249,13 +259,13 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
         nb.t = make_tile(p.D + i * bb, g.b, (r + 1) * TS, r * TS, g.b, g.b);
         nb.vrow0 = i * g.b + (r + 1) * TS;
         nb.vrows = g.vrows(r + 1);
-        nb.flag = c.flags + vflag(g, i, r + 1);
+        nb.flag = c.flags + fo + vflag(g, i, r + 1);
       } else if (nx >= 0) {
         has_nb = true;
         nb.t = make_tile(p.L + lsi * bb, g.b, 0, r * TS, g.b, g.b);
         nb.vrow0 = nx * g.b;
         nb.vrows = g.vrows(0);
-        nb.flag = c.flags + vflag(g, nx, 0);
+        nb.flag = c.flags + fo + vflag(g, nx, 0);
       }
     }
     if (has_nb) {
@@ -277,6 +287,7 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
       }
     }
     // ---- the other dependencies (all solved before the neighbour): s -= A_k v_k
+    if (p.both && !fwd && !cta_wait(c, c.flags + vflag(g, i, r), nullptr, &s_ok)) return false;   // the forward y
     Ss[threadIdx.x] = (srow < rows && scol < p.nc) ? __ldcg(p.B + (size_t)(row0 + srow) * p.ldb + scol) : 0.0;
     __syncthreads();
     int ndep, nfirst, n0 = 0;
@@ -301,13 +312,13 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
           d.t = make_tile(p.L + g.lslot(pb) * bb, g.b, r * TS, k * TS, g.b, g.b);
           d.vrow0 = pb * g.b + k * TS;
           d.vrows = g.vrows(k);
-          d.flag = c.flags + vflag(g, pb, k);
+          d.flag = c.flags + fo + vflag(g, pb, k);
         } else {
           const int k = st - nfirst;   // k < r - 1
           d.t = make_tile(p.D + i * bb, g.b, r * TS, k * TS, g.b, g.b);
           d.vrow0 = i * g.b + k * TS;
           d.vrows = g.vrows(k);
-          d.flag = c.flags + vflag(g, i, k);
+          d.flag = c.flags + fo + vflag(g, i, k);
         }
       } else {
         int s2 = st;
@@ -315,7 +326,7 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
           d.t = make_tile(p.R + i * ab, g.b, 0, r * TS, g.a, g.b);
           d.vrow0 = arrow_row0;
           d.vrows = g.a;
-          d.flag = c.flags + ntile;
+          d.flag = c.flags + fo + ntile;
         } else {
           if (p.use_arrow) --s2;
           if (s2 < nfirst) {
@@ -323,13 +334,13 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
             d.t = make_tile(p.L + lsi * bb, g.b, k * TS, r * TS, g.b, g.b);
             d.vrow0 = nx * g.b + k * TS;
             d.vrows = g.vrows(k);
-            d.flag = c.flags + vflag(g, nx, k);
+            d.flag = c.flags + fo + vflag(g, nx, k);
           } else {
             const int k = g.B - 1 - (s2 - nfirst);   // D_i rows B-1 down to r+2
             d.t = make_tile(p.D + i * bb, g.b, k * TS, r * TS, g.b, g.b);
             d.vrow0 = i * g.b + k * TS;
             d.vrows = g.vrows(k);
-            d.flag = c.flags + vflag(g, i, k);
+            d.flag = c.flags + fo + vflag(g, i, k);
           }
         }
       }
@@ -347,8 +358,8 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
       __syncthreads();
     }
     if (!ok) return false;
-    trace_clear_marks(c, t);
-    trace_mark(c, t, 0);   // every dependency but the neighbour done
+    trace_clear_marks(c, tt);
+    trace_mark(c, tt, 0);   // every dependency but the neighbour done
     // u = Linv s (forward) or Linv^T s (backward)
     double u[NC];
     if (fwd)
@@ -358,7 +369,7 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
     // ---- the neighbour: y = u - M v_nb
     if (has_nb) {
       if (!cta_wait(c, nb.flag, nullptr, &s_ok)) return false;
-      trace_mark(c, t, 1);   // neighbour published
+      trace_mark(c, tt, 1);   // neighbour published
       vec_load(Vs, p, nb.vrow0, nb.vrows);
       __syncthreads();
       double res[NC];
@@ -374,9 +385,9 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
         if (q < p.nc && row < rows) p.B[(size_t)(row0 + row) * p.ldb + q] = u[q];
       }
     }
-    trace_mark(c, t, 2);   // solution tile computed and stored
-    cta_publish(c, c.flags + vflag(g, i, r));   // the next tile's wait ends here
-    trace_mark(c, t, 3);   // published
+    trace_mark(c, tt, 2);   // solution tile computed and stored
+    cta_publish(c, c.flags + fo + vflag(g, i, r));   // the next tile's wait ends here
+    trace_mark(c, tt, 3);   // published
     if (fwd && p.use_arrow) {
       // arrow partial R_i(:, r) y(i, r) (rows >= a of the staged tile are zero), off
       // the chain, under its own flag
@@ -390,7 +401,7 @@ static __device__ __forceinline__ bool solve_task(const SolveArgs& p, int t, uns
       }
       cta_publish(c, c.flags + pflag(g, gi));
     }
-    trace_task(c, t, 0, t_task0);
+    trace_task(c, tt, 0, t_task0);
   }
   return true;
 }

@@ -72,6 +72,12 @@ class BtaHandle:
         """Persistent CTAs per SM of the dataflow launches (0: as many as fit)."""
         _lib.check(self.lib.gbta_set_ctas_per_sm(self.ptr, int(n)))
 
+    def set_selinv_overlap(self, enable: bool) -> None:
+        """Run a (tensor-core) selected inversion that follows this handle's
+        factorization concurrently with the sweeps enqueued in between, into a
+        workspace of the size of the blocks (gbta_set_selinv_overlap)."""
+        _lib.check(self.lib.gbta_set_selinv_overlap(self.ptr, 1 if enable else 0))
+
     def method(self) -> int:
         return int(self.lib.gbta_get_method(self.ptr))
 

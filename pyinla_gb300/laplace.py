@@ -185,9 +185,7 @@ class KronLaplaceModel(KronGaussianModel):
                                          1 if has_arrow else 0, x.data_ptr(), qpx.data_ptr()))
             dx = self._spmv(self._At, grad) - qpx
             _lib.check(lib.gbta_pobtaf_async(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T))
-            _lib.check(lib.gbta_pobtas_async(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T, dx.data_ptr(), 1,
-                                             0))
-            _lib.check(lib.gbta_pobtas(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T, dx.data_ptr(), 1, 1))
+            _lib.check(lib.gbta_pobtas(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T, dx.data_ptr(), 1, 2))
             it += 1
             if float(torch.linalg.vector_norm(dx)) < self.eps_inner:
                 break

@@ -259,6 +259,9 @@ class KronGaussianModel:
         self._coef = torch.empty(2 * self.K * nt + self.nv, dtype=f64, device=dev)
         self._contract_out = torch.empty(4 * self.K * nt + 2 * self.nv * (nt + 1), dtype=f64, device=dev)
         self.h = BtaHandle.get(b, nt, a)
+        # an evaluation with the gradient runs the selected inversion after the mean's
+        # sweeps: let it run next to them
+        self.h.set_selinv_overlap(True)
         self.last = {}
         # separable priors: logdet and tr(Q_prior^-1 dQ_prior) from the ns x ns spatial
         # factors (see _separable_prior_terms); "selinv" forces the prior's selected inverse
@@ -438,9 +441,8 @@ class KronGaussianModel:
         tau_t = self.torch.from_numpy(coef.tau_y).to(self.mu.device)
         self.mu.copy_(tau_t @ self._Aty_v)
         bvec = self.mu.clone()
-        _lib.check(lib.gbta_pobtas_async(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T,
-                                         self.mu.data_ptr(), 1, 0))
-        _lib.check(lib.gbta_pobtas(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T, self.mu.data_ptr(), 1, 1))
+        # N then C in one launch (trans = 2)
+        _lib.check(lib.gbta_pobtas(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T, self.mu.data_ptr(), 1, 2))
         quad = float(self.torch.dot(self.mu, bvec))   # mu^T Q_cond mu = mu^T b
         ty = np.asarray(self.lik_theta_indices(), dtype=np.int64)
         # gaussian.py:58-60 at eta = 0, summed over the variates' likelihoods

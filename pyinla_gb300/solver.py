@@ -44,6 +44,9 @@ class GB300SerinvSolver:
         self.A_arrow_bottom_blocks = torch.empty((nt, a, b), dtype=f64, device=dev) if a > 0 else None
         self.A_arrow_tip_block = torch.empty((a, a), dtype=f64, device=dev) if a > 0 else None
         self._h = BtaHandle.get(b, nt, a)
+        # selected_inversion follows cholesky and solve (structured_solver.py's order): it
+        # runs next to the sweeps
+        self._h.set_selinv_overlap(True)
         self._torch = torch
         # index structures derived from the sparsity pattern of the matrices passed in
         # (the same at every theta): input scatter indices, output gather indices and
@@ -107,11 +110,9 @@ class GB300SerinvSolver:
         h.set_stream(current_stream_ptr())
         D, L, R, T = self._ptrs(sparsity)
         if R is not None:
-            _lib.check(h.lib.gbta_pobtas_async(h.ptr, D, L, R, T, x.data_ptr(), nrhs, 0))
-            _lib.check(h.lib.gbta_pobtas(h.ptr, D, L, R, T, x.data_ptr(), nrhs, 1))
+            _lib.check(h.lib.gbta_pobtas(h.ptr, D, L, R, T, x.data_ptr(), nrhs, 2))   # N then C, one launch
         else:
-            _lib.check(h.lib.gbta_pobts(h.ptr, D, L, x.data_ptr(), nrhs, 0))
-            _lib.check(h.lib.gbta_pobts(h.ptr, D, L, x.data_ptr(), nrhs, 1))
+            _lib.check(h.lib.gbta_pobts(h.ptr, D, L, x.data_ptr(), nrhs, 2))
         if on_dev:
             if x.data_ptr() != rhs.data_ptr():
                 rhs[:n].copy_(x)
