@@ -130,7 +130,10 @@ int gbta_get_twist(const gbta_solver* s);
  * size of the blocks; the write-back into the caller's blocks is enqueued on the solver's
  * stream, after that work and the inversion.  The blocks must hold the factor that
  * gbta_pobtaf left until then (the sweeps only read them).  The sweeps then run one CTA
- * per SM and the inversion two.  Status words of both streams are read by gbta_status. */
+ * per SM and the inversion's CTAs fill the rest of each SM.  An inversion with no sweep
+ * enqueued since the factorization runs in place on the solver's stream as without the
+ * option (there is nothing to overlap).  Status words of both streams are read by
+ * gbta_status. */
 int gbta_set_selinv_overlap(gbta_solver* s, int enable);
 
 /* Persistent CTAs per SM of the dataflow launches (0, the default: as many as the

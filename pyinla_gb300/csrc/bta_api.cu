@@ -71,6 +71,7 @@ struct gbta_solver {
   cudaEvent_t ev_fac = nullptr;   // the last factorization's completion (solver's stream)
   cudaEvent_t ev_sel = nullptr;   // the overlapped inversion's completion (side stream)
   bool fac_evt = false;           // ev_fac belongs to the factor the blocks hold
+  bool swept = false;             // sweeps were enqueued since that factorization
   int* d_ctrl2 = nullptr;         // control block of the side stream's launches
   int* d_flags2 = nullptr;        // their ready flags
   double* d_ld = nullptr;   // logdet partials [nt + 1] + result [1]
@@ -597,6 +598,7 @@ static int factor_async(gbta_solver* s, double* D, double* L, double* R, double*
   GBTA_CUDA(cudaGetLastError());
   GBTA_CUDA(cudaEventRecord(s->ev_fac, s->stream));
   s->fac_evt = true;
+  s->swept = false;
   if (s->timing) {
     GBTA_CUDA(cudaEventRecord(s->tev[1], s->stream));
     s->timed[0] = true;
@@ -653,6 +655,7 @@ static int solve_async(gbta_solver* s, const double* D, const double* L, const d
     }
     GBTA_CUDA(cudaGetLastError());
   }
+  s->swept = true;
   if (s->timing) {
     GBTA_CUDA(cudaEventRecord(s->tev[5], s->stream));
     s->timed[2] = true;
@@ -704,8 +707,10 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
   // Overlapped: the whole inversion reads the factor's blocks only (the G tiles go to the
   // Sigma workspace), so it runs on the side stream from the factorization's completion,
   // next to whatever the solver's stream runs meanwhile (the sweeps), and the write-back
-  // follows on the solver's stream after both.  Not while tracing (one trace buffer).
-  const bool over = s->overlap && tc_g && s->fac_evt && !s->d_trace;
+  // follows on the solver's stream after both.  Only when sweeps were enqueued since the
+  // factorization (with nothing to overlap the write-back is pure cost), and not while
+  // tracing (one trace buffer).
+  const bool over = s->overlap && tc_g && s->fac_evt && s->swept && !s->d_trace;
   // The tensor-core method reads the factor only through its digit planes, sliced by the
   // pre-pass, and the tip task reads T before it writes Sigma_T: without the overlap Sigma
   // goes straight into the caller's buffers.  The FP64 method reads the factor tiles

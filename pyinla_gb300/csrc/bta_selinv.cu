@@ -275,32 +275,64 @@ void launch_selinv_prepare(const Geom& g, const double* D, double* L, double* R,
 
 // Copy Sigma back into the caller's buffers; D_i and T become full symmetric, and the
 // coupling slots below the separator (Sigma(j, j+1)) are transposed to the caller's
-// Sigma(j+1, j).
-__global__ void k_writeback(const double* SD, const double* SL, const double* SR, const double* ST, double* D,
-                            double* L, double* R, double* T, Geom g, int use_arrow) {
-  const size_t bb = (size_t)g.b * g.b;
-  const size_t nD = g.nt * bb, nL = (g.nt - 1) * bb, nR = use_arrow ? (size_t)g.nt * g.a * g.b : 0;
-  const size_t nT = use_arrow ? (size_t)g.a * g.a : 0;
-  const size_t total = nD + nL + nR + nT;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-    if (e < nD) {
-      const size_t blk = e / bb, rem = e % bb;
-      const int r = (int)(rem / g.b), cc = (int)(rem % g.b);
-      const bool lower = (r / TS) >= (cc / TS);   // tiles on/below the diagonal are stored
-      D[e] = lower ? SD[blk * bb + (size_t)r * g.b + cc] : SD[blk * bb + (size_t)cc * g.b + r];
-    } else if (e < nD + nL) {
-      const size_t blk = (e - nD) / bb, rem = (e - nD) % bb;
-      if ((int)blk >= g.sep()) {
-        const int r = (int)(rem / g.b), cc = (int)(rem % g.b);
-        L[e - nD] = SL[blk * bb + (size_t)cc * g.b + r];
-      } else {
-        L[e - nD] = SL[e - nD];
+// Sigma(j+1, j).  One 32 x 32 destination tile per step of a CTA (256 threads, four
+// rows each): a tile that is a transpose of a stored tile (above a diagonal block's
+// diagonal, or a coupling slot past the separator) is staged through shared memory so
+// that reads and writes both run along rows; the arrow rows and the tip, which are
+// plain copies, are spread over all threads after the tiles.
+__global__ void __launch_bounds__(256) k_writeback(const double* SD, const double* SL, const double* SR,
+                                                   const double* ST, double* D, double* L, double* R, double* T,
+                                                   Geom g, int use_arrow) {
+  __shared__ double A[TS][TS + 1];
+  const int B = g.B, b = g.b;
+  const size_t bb = (size_t)b * b;
+  const long long perblk = (long long)B * B;
+  const long long nDt = (long long)g.nt * perblk, nLt = (long long)(g.nt - 1) * perblk;
+  const int cc = threadIdx.x & 31, r8 = threadIdx.x >> 5;
+  for (long long t = blockIdx.x; t < nDt + nLt; t += gridDim.x) {
+    const bool isD = t < nDt;
+    const long long u = isD ? t : t - nDt;
+    const int blk = (int)(u / perblk), q = (int)(u % perblk);
+    const int Rt = q / B, Ct = q % B;
+    const double* src = (isD ? SD : SL) + (size_t)blk * bb;
+    double* dst = (isD ? D : L) + (size_t)blk * bb;
+    const bool trans = isD ? Rt < Ct : blk >= g.sep();   // uniform over the CTA
+    if (!trans) {
+      const int c = Ct * TS + cc;
+      double v[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int r = Rt * TS + r8 + 8 * k;
+        v[k] = (r < b && c < b) ? __ldcs(src + (size_t)r * b + c) : 0.0;
       }
-    } else if (e < nD + nL + nR) {
-      R[e - nD - nL] = SR[e - nD - nL];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int r = Rt * TS + r8 + 8 * k;
+        if (r < b && c < b) __stcs(dst + (size_t)r * b + c, v[k]);
+      }
     } else {
-      T[e - nD - nL - nR] = ST[e - nD - nL - nR];
+      // destination tile (Rt, Ct) = transpose of source tile (Ct, Rt)
+      __syncthreads();   // the previous transposed tile's reads of A are done
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int r = Ct * TS + r8 + 8 * k, c = Rt * TS + cc;
+        A[r8 + 8 * k][cc] = (r < b && c < b) ? __ldcs(src + (size_t)r * b + c) : 0.0;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int r = Rt * TS + r8 + 8 * k, c = Ct * TS + cc;
+        if (r < b && c < b) __stcs(dst + (size_t)r * b + c, A[cc][r8 + 8 * k]);
+      }
     }
+  }
+  const size_t nR = use_arrow ? (size_t)g.nt * g.a * g.b : 0;
+  const size_t nT = use_arrow ? (size_t)g.a * g.a : 0;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < nR + nT; e += (size_t)gridDim.x * blockDim.x) {
+    if (e < nR)
+      R[e] = SR[e];
+    else
+      T[e - nR] = ST[e - nR];
   }
 }
 
@@ -374,7 +406,7 @@ void launch_selinv(const Geom& g, const double* D, const double* L, const double
 
 void launch_selinv_writeback(const Geom& g, const double* SD, const double* SL, const double* SR, const double* ST,
                              double* D, double* L, double* R, double* T, int use_arrow, cudaStream_t stream) {
-  k_writeback<<<1024, 256, 0, stream>>>(SD, SL, SR, ST, D, L, R, T, g, use_arrow);
+  k_writeback<<<152 * 8, 256, 0, stream>>>(SD, SL, SR, ST, D, L, R, T, g, use_arrow);
   count_launches(1);
 }
 

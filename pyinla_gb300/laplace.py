@@ -192,8 +192,7 @@ class KronLaplaceModel(KronGaussianModel):
         self.last_iterations = it
         logdet_c = self._logdet(self.Dc, self.Tc, with_tip=has_arrow)
         xqx = float(torch.dot(x, qpx))
-        _lib.check(lib.gbta_pobtf(h.ptr, self.Dp.data_ptr(), self.Lp.data_ptr()))
-        logdet_p = self._logdet(self.Dp, self.Tp, with_tip=False)
+        logdet_p = self._prior_logdet(theta, ptrs)
         self.x_latent = x
         lik = float(lik)
         lp = self.log_prior(theta)

@@ -264,8 +264,10 @@ class KronGaussianModel:
         self.h.set_selinv_overlap(True)
         self.last = {}
         # separable priors: logdet and tr(Q_prior^-1 dQ_prior) from the ns x ns spatial
-        # factors (see _separable_prior_terms); "selinv" forces the prior's selected inverse
+        # factors (see _separable_prior_terms); "selinv" factors the whole prior (bt) for
+        # its logdet and takes the trace from its selected inverse, as the reference does
         self.prior_trace = "separable"
+        self._sep_prior_grad = None
         sep = spec.separable_prior(spec.theta0) if hasattr(spec, "theta0") else None
         self._sep_base = None
         if sep is not None:
@@ -359,10 +361,11 @@ class KronGaussianModel:
         _lib.check(code)
         return float(out.value)
 
-    def _spatial_logdet_and_traces(self, w: np.ndarray):
+    def _spatial_logdet_and_traces(self, w: np.ndarray, traces: bool = True):
         """logdet Q_s and tr(Q_s^-1 S_j) for Q_s = sum_j w_j S_j (ns x ns), on the device:
         Kronecker assembly with one time block, factorization, logdet, selected
-        inversion (the full inverse of a single block) and the trace contractions."""
+        inversion (the full inverse of a single block) and the trace contractions (the
+        last two only with ``traces``; the traces are None without)."""
         h, lib = self._sep_h, self._sep_h.lib
         h.set_stream(current_stream_ptr())
         J = len(self._sep_base)
@@ -374,6 +377,8 @@ class KronGaussianModel:
         _lib.check(lib.gbta_pobtf(h.ptr, self._sep_D.data_ptr(), None))
         out = ctypes.c_double(0.0)
         _lib.check(lib.gbta_logdet(h.ptr, self._sep_D.data_ptr(), None, 0, ctypes.byref(out)))
+        if not traces:
+            return float(out.value), None
         _lib.check(lib.gbta_pobtsi(h.ptr, self._sep_D.data_ptr(), None))
         _lib.check(lib.gbta_contract_kron(
             h.ptr, self.ns, 1, J, self._sep_rowptr.data_ptr(), self._sep_col.data_ptr(), self._sep_uval.data_ptr(),
@@ -382,8 +387,9 @@ class KronGaussianModel:
         tr = self._sep_out.cpu().numpy()[:J].copy()
         return float(out.value), tr
 
-    def _separable_prior_terms(self, theta):
-        """logdet_bt Q_prior and its theta-gradient for a separable prior:
+    def _separable_prior_terms(self, theta, gradient: bool = True):
+        """logdet_bt Q_prior and (with ``gradient``, else None) its theta-gradient for a
+        separable prior:
         Q_re = (W^T (x) I) blockdiag_k(c_k T_k (x) Q_s,k) (W (x) I) with |det W| = 1 gives
             logdet = sum_k nt ns log c_k + ns logdet T_k + nt logdet Q_s,k,
             d logdet = sum_k nt ns dlog c_k + ns dlogdet T_k + nt sum_j dw_kj tr(Q_s,k^-1 S_j),
@@ -399,13 +405,28 @@ class KronGaussianModel:
         for part in parts:
             key = tuple(np.asarray(part.w, dtype=np.float64).tolist())
             if key not in cache:
-                cache[key] = self._spatial_logdet_and_traces(part.w)
+                cache[key] = self._spatial_logdet_and_traces(part.w, traces=gradient)
             ld_s, tr_s = cache[key]
             r = part.rho
             logdet += nt * ns * np.log(part.c) - ns * (nt - 1) * np.log1p(-r * r) + nt * ld_s
-            dlogdet_t = 2.0 * r * (nt - 1) / (1.0 - r * r)
-            grad += nt * ns * part.dlogc + ns * dlogdet_t * part.drho + nt * (part.dw @ tr_s)
-        return logdet, grad
+            if gradient:
+                dlogdet_t = 2.0 * r * (nt - 1) / (1.0 - r * r)
+                grad += nt * ns * part.dlogc + ns * dlogdet_t * part.drho + nt * (part.dw @ tr_s)
+        return logdet, (grad if gradient else None)
+
+    def _prior_logdet(self, theta, ptrs, gradient: bool = False) -> float:
+        """logdet_bt Q_prior, the tip excluded (pyinla.py:1102-1103).  A separable prior
+        takes it from its ns x ns spatial factors (with ``gradient`` also the trace the
+        adjoint needs, kept for _adjoint_gradient), with no factorization of the whole
+        prior; otherwise the prior is assembled and factored (bt) as the reference does."""
+        self._sep_prior_grad = None
+        if self._sep_base is not None and self.prior_trace == "separable":
+            logdet, self._sep_prior_grad = self._separable_prior_terms(theta, gradient=gradient)
+            return logdet
+        h = self.h
+        self._assemble(ptrs, self.Dp, self.Lp, self.Rp, self.Tp, with_lik=False)
+        _lib.check(h.lib.gbta_pobtf(h.ptr, self.Dp.data_ptr(), self.Lp.data_ptr()))
+        return self._logdet(self.Dp, self.Tp, with_tip=False)
 
     def _split(self, out: np.ndarray):
         K, nt = self.K, self.nt
@@ -427,10 +448,8 @@ class KronGaussianModel:
         coef = self.coefficients(theta)
         ptrs = self._upload_coef(coef)
         has_arrow = self.nb > 0
-        # prior: bt factorization, tip excluded from the logdet (pyinla.py:1102-1103)
-        self._assemble(ptrs, self.Dp, self.Lp, self.Rp, self.Tp, with_lik=False)
-        _lib.check(lib.gbta_pobtf(h.ptr, self.Dp.data_ptr(), self.Lp.data_ptr()))
-        logdet_p = self._logdet(self.Dp, self.Tp, with_tip=False)
+        # prior logdet, tip excluded (pyinla.py:1102-1103)
+        logdet_p = self._prior_logdet(theta, ptrs, gradient=gradient)
         # conditional: bta factorization (pyinla.py:650-662)
         self._assemble(ptrs, self.Dc, self.Lc, self.Rc, self.Tc, with_lik=True)
         R, T = (self.Rc.data_ptr(), self.Tc.data_ptr()) if has_arrow else (None, None)
@@ -442,7 +461,16 @@ class KronGaussianModel:
         self.mu.copy_(tau_t @ self._Aty_v)
         bvec = self.mu.clone()
         # N then C in one launch (trans = 2)
-        _lib.check(lib.gbta_pobtas(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T, self.mu.data_ptr(), 1, 2))
+        if gradient:
+            # the conditional's selected inverse (for the gradient's traces) is queued right
+            # behind the sweeps: it reads the factor only, so it runs on the solver's side
+            # stream next to them, and Sigma lands in the blocks after both
+            _lib.check(lib.gbta_pobtas_async(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T,
+                                             self.mu.data_ptr(), 1, 2))
+            _lib.check(lib.gbta_pobtasi_async(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T))
+            h.status()
+        else:
+            _lib.check(lib.gbta_pobtas(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T, self.mu.data_ptr(), 1, 2))
         quad = float(self.torch.dot(self.mu, bvec))   # mu^T Q_cond mu = mu^T b
         ty = np.asarray(self.lik_theta_indices(), dtype=np.int64)
         # gaussian.py:58-60 at eta = 0, summed over the variates' likelihoods
@@ -504,16 +532,17 @@ class KronGaussianModel:
         lib = h.lib
         dc = self.coefficient_derivatives(theta)
         has_arrow = self.nb > 0
-        # conditional selected inverse (in place over the factor) + contractions with mu
-        R, T = (self.Rc.data_ptr(), self.Tc.data_ptr()) if has_arrow else (None, None)
-        _lib.check(lib.gbta_pobtasi(h.ptr, self.Dc.data_ptr(), self.Lc.data_ptr(), R, T))
+        # contractions of the conditional's selected inverse (over the factor's blocks,
+        # computed in evaluate) with mu
         cc, dd, qc, qd, lc, lq = self._split(self._contract(
             self.Dc, self.Lc if self.nt > 1 else None, self.Rc if has_arrow else None,
             self.Tc if has_arrow else None, self.mu))
         # prior trace tr(Q_prior^-1 dQ_prior): from the spatial factors for a separable
         # prior, else from the prior's selected inverse (bt)
         tr_prior = None
-        if self._sep_base is not None and self.prior_trace == "separable":
+        if self._sep_prior_grad is not None:   # from evaluate's separable prior terms
+            tr_prior = self._sep_prior_grad
+        elif self._sep_base is not None and self.prior_trace == "separable":
             _, tr_prior = self._separable_prior_terms(theta)
         else:
             _lib.check(lib.gbta_pobtsi(h.ptr, self.Dp.data_ptr(), self.Lp.data_ptr()))

@@ -184,10 +184,12 @@ def test_separable_prior_logdet_and_trace(built, kind):
         spec = CoregionalSpdeAr1.synthetic(4, 4, 2, nv, 900, seed=23, m_side=5)
         theta = spec.theta0 + 0.1 * np.cos(np.arange(3 * nv))
     m = KronGaussianModel(spec)
-    m.evaluate(theta)
-    ld_sep, tr_sep = m._separable_prior_terms(theta)
-    assert abs(ld_sep - m.last["logdet_prior"]) <= 1e-10 * abs(m.last["logdet_prior"])
+    f_sep = m.evaluate(theta)                   # prior logdet from the spatial factors
+    ld_sep = m.last["logdet_prior"]
     _, g_sep = m.evaluate(theta, gradient=True)
-    m.prior_trace = "selinv"
+    m.prior_trace = "selinv"                    # the whole prior factored (bt), as the reference
+    f_bt = m.evaluate(theta)
+    assert abs(ld_sep - m.last["logdet_prior"]) <= 1e-10 * abs(m.last["logdet_prior"])
+    assert abs(f_sep - f_bt) <= 1e-10 * abs(f_bt)
     _, g_sel = m.evaluate(theta, gradient=True)
     assert relerr(g_sep, g_sel) < 1e-9, (g_sep, g_sel)
