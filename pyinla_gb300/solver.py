@@ -76,20 +76,33 @@ class GB300SerinvSolver:
 
     # ------------------------------------------------------------------ API
     def cholesky(self, A, sparsity: str) -> None:
-        """Map the sparse matrix into BTA blocks and factor it (structured_solver.py:72-100)."""
+        """Map the sparse matrix into BTA blocks and factor it (structured_solver.py:72-100).
+
+        For a CSR / CSC matrix whose format, shape and sizes match the pattern seen
+        before, the scatter and the factorization are queued with that pattern's
+        indices first and the full comparison of the index arrays runs on the host
+        while the device works; on a mismatch both are redone with the new pattern."""
         self._check_sparsity(sparsity)
-        self._spmatrix_to_structured(A, sparsity)
         tic = time.perf_counter()
-        self._sync()
         h = self._h
         h.set_stream(current_stream_ptr())
+        verify = self._spmatrix_to_structured(A, sparsity, verify_later=True)
+        self._factor_async(sparsity)
+        if verify is not None and not self._same_pattern(A, verify):
+            h.lib.gbta_status(h.ptr)   # drain the queued work; its result is discarded
+            self._in_cache = None
+            self._spmatrix_to_structured(A, sparsity)
+            self._factor_async(sparsity)
+        h.status()
+        self.t_cholesky += time.perf_counter() - tic
+
+    def _factor_async(self, sparsity: str) -> None:
+        h = self._h
         D, L, R, T = self._ptrs(sparsity)
         if sparsity == "bta" and self.arrowhead_blocksize > 0:
-            _lib.check(h.lib.gbta_pobtaf(h.ptr, D, L, R, T))
+            _lib.check(h.lib.gbta_pobtaf_async(h.ptr, D, L, R, T))
         else:
-            _lib.check(h.lib.gbta_pobtf(h.ptr, D, L))
-        self._sync()
-        self.t_cholesky += time.perf_counter() - tic
+            _lib.check(h.lib.gbta_pobtf_async(h.ptr, D, L))
 
     def solve(self, rhs, sparsity: str):
         """Forward then backward sweep, overwriting and returning ``rhs``
@@ -136,23 +149,38 @@ class GB300SerinvSolver:
         return float(out.value)
 
     def selected_inversion(self, sparsity: str) -> None:
-        """Overwrite the factor blocks with Sigma on the BTA pattern (structured_solver.py:168-190)."""
+        """Overwrite the factor blocks with Sigma on the BTA pattern (structured_solver.py:168-190).
+
+        The bta form returns once the work is queued on the current stream (as the
+        reference's device backend does): stream-ordered readers of the blocks see
+        Sigma, and a failure is raised by the next call that waits for the device
+        (``_structured_to_spmatrix``, ``cholesky``, ``solve``, ``logdet``)."""
         self._check_sparsity(sparsity)
         h = self._h
         h.set_stream(current_stream_ptr())
         D, L, R, T = self._ptrs(sparsity)
         if R is not None:
-            _lib.check(h.lib.gbta_pobtasi(h.ptr, D, L, R, T))
+            _lib.check(h.lib.gbta_pobtasi_async(h.ptr, D, L, R, T))
         else:
             _lib.check(h.lib.gbta_pobtsi(h.ptr, D, L))
 
-    @staticmethod
-    def _same_pattern(A, key) -> bool:
-        """A (CSR or CSC) has the sparsity pattern recorded in key."""
+    def _same_pattern(self, A, key) -> bool:
+        """A (CSR or CSC) has the sparsity pattern recorded in key (the index arrays
+        compared by torch's multi-threaded CPU kernels where the dtypes agree)."""
         fmt, shape, indptr, indices = key
-        return (A.format == fmt and A.shape == shape and A.indptr.size == indptr.size
-                and A.indices.size == indices.size and np.array_equal(A.indptr, indptr)
-                and np.array_equal(A.indices, indices))
+        if not self._same_shape(A, key):
+            return False
+        return self._equal(A.indptr, indptr) and self._equal(A.indices, indices)
+
+    def _equal(self, x: np.ndarray, y: np.ndarray) -> bool:
+        if x.dtype == y.dtype and x.flags.c_contiguous and y.flags.c_contiguous:
+            return bool(self._torch.equal(self._torch.from_numpy(x), self._torch.from_numpy(y)))
+        return bool(np.array_equal(x, y))
+
+    def _host_copy(self, x):
+        """A fresh host copy (numpy) of a host tensor or array, by torch's multi-threaded copy."""
+        t = x if isinstance(x, self._torch.Tensor) else self._torch.from_numpy(x)
+        return t.clone().numpy()
 
     @staticmethod
     def _pattern_key(A):
@@ -170,15 +198,27 @@ class GB300SerinvSolver:
         stage.copy_(src)
         return stage.to("cuda")   # (blocking: the staging buffer is reused by the next call)
 
-    def _spmatrix_to_structured(self, A, sparsity: str) -> None:
+    @staticmethod
+    def _same_shape(A, key) -> bool:
+        """The cheap part of _same_pattern: format, shape and array sizes."""
+        fmt, shape, indptr, indices = key
+        return A.format == fmt and A.shape == shape and A.indptr.size == indptr.size and A.indices.size == indices.size
+
+    def _spmatrix_to_structured(self, A, sparsity: str, verify_later: bool = False):
         """Zero-fill and scatter the symmetric sparse matrix into the BTA blocks
         (structured_solver.py:192-250) with one device scatter.  For CSR / CSC input
         the scatter indices are kept per sparsity pattern, so a matrix with the
-        pattern of an earlier call moves only its values."""
+        pattern of an earlier call moves only its values.  With ``verify_later`` a
+        matrix whose format, shape and sizes match the kept pattern is scattered with
+        it at once and the pattern key is returned: the caller compares the index
+        arrays (``_same_pattern``) while the device works.  Returns None otherwise."""
         self._check_sparsity(sparsity)
         torch = self._torch
+        verify = None
         if sps.issparse(A) and A.format in ("csr", "csc"):
-            if self._in_cache is None or not self._same_pattern(A, self._in_cache[0]):
+            if verify_later and self._in_cache is not None and self._same_shape(A, self._in_cache[0]):
+                verify = self._in_cache[0]
+            elif self._in_cache is None or not self._same_pattern(A, self._in_cache[0]):
                 coo = A.tocoo()   # entries in the order of A.data
                 rows = torch.from_numpy(coo.row.astype(np.int64)).cuda()
                 cols = torch.from_numpy(coo.col.astype(np.int64)).cuda()
@@ -197,6 +237,7 @@ class GB300SerinvSolver:
         D, L, R, T = self._ptrs("bta")
         _lib.check(h.lib.gbta_scatter_coo(h.ptr, rows.data_ptr(), cols.data_ptr(), vals.data_ptr(), nnz,
                                           D, L, R, T, 1 if R is not None else 0))
+        return verify
 
     def _output_structure(self, A, sparsity: str):
         """Gather indices of the lower BTA pattern of A and the structure of the
@@ -245,10 +286,12 @@ class GB300SerinvSolver:
         if host is None or host.numel() < data.numel():
             host = torch.empty(data.numel(), dtype=torch.float64, pin_memory=True)
             self._pinned["out"] = host
-        host[: data.numel()].copy_(data)
+        host[: data.numel()].copy_(data, non_blocking=True)
+        # (while the device works)
+        indices, indptr = self._host_copy(st["indices"]), self._host_copy(st["indptr"])
+        h.status()   # waits for the copy; raises a failure of the queued work
         cls = sps.csc_matrix if st["format"] == "csc" else sps.csr_matrix
-        return cls((host[: data.numel()].numpy().copy(), st["indices"].copy(), st["indptr"].copy()),
-                   shape=st["shape"])
+        return cls((self._host_copy(host[: data.numel()]), indices, indptr), shape=st["shape"])
 
     def get_solver_memory(self) -> int:
         """Bytes of the block buffers plus the library workspace (structured_solver.py:540-550)."""
