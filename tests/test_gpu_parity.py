@@ -336,3 +336,39 @@ def test_drop_in_solver_pattern_cache(torch):
         s2.selected_inversion("bta")
         S3 = s2._structured_to_spmatrix(B, "bta")
         assert np.abs((S3 - S2).toarray()).max() <= RTOL * np.abs(S2.data).max()
+
+
+def test_drop_in_solver_pattern_change_same_sizes(torch):
+    """A matrix whose index arrays differ from the kept pattern's while its format,
+    shape and sizes match (two entries of one column stored in the other order) is
+    first scattered and factored with the kept indices while the arrays are compared,
+    then redone with its own: the results are those of the matrix in its first order."""
+    import scipy.sparse as sps
+
+    from pyinla_gb300.solver import GB300SerinvSolver
+
+    g, D, L, R, T, rhs = _golden("ragged")
+    A = sps.csc_matrix(orc.bta_to_dense(D, L, R, T))
+    s = GB300SerinvSolver(None, diagonal_blocksize=int(g["b"]), n_diag_blocks=int(g["nt"]),
+                          arrowhead_blocksize=int(g["a"]))
+    s.cholesky(A, sparsity="bta")
+    ld1 = s.logdet("bta")
+    s.selected_inversion("bta")
+    S1 = s._structured_to_spmatrix(A, "bta")
+    B = A.copy()
+    j = next(j for j in range(B.shape[1]) if B.indptr[j + 1] - B.indptr[j] >= 2
+             and B.data[B.indptr[j]] != B.data[B.indptr[j] + 1])
+    p, q = B.indptr[j], B.indptr[j] + 1
+    B.indices[[p, q]] = B.indices[[q, p]]
+    B.data[[p, q]] = B.data[[q, p]]
+    B.has_sorted_indices = False
+    assert not np.array_equal(B.indices, A.indices)
+    s.cholesky(B, sparsity="bta")
+    ld2 = s.logdet("bta")
+    s.selected_inversion("bta")
+    S2 = s._structured_to_spmatrix(B, "bta")
+    assert abs(ld2 - ld1) <= 1e-12 * abs(ld1)
+    assert np.abs((S2 - S1).toarray()).max() <= RTOL * np.abs(S1.data).max()
+    # and back to the first order
+    s.cholesky(A, sparsity="bta")
+    assert abs(s.logdet("bta") - ld1) <= 1e-12 * abs(ld1)
