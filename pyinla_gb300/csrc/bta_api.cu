@@ -70,6 +70,7 @@ struct gbta_solver {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fac = nullptr;   // the last factorization's completion (solver's stream)
   cudaEvent_t ev_sel = nullptr;   // the overlapped inversion's completion (side stream)
+  cudaEvent_t ev_swp = nullptr;   // the last sweeps' completion (solver's stream)
   bool fac_evt = false;           // ev_fac belongs to the factor the blocks hold
   bool swept = false;             // sweeps were enqueued since that factorization
   int* d_ctrl2 = nullptr;         // control block of the side stream's launches
@@ -320,6 +321,7 @@ int gbta_create(int b, int nt, int a, gbta_solver** out) {
   CREATE_CUDA(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
   CREATE_CUDA(cudaEventCreateWithFlags(&s->ev_fac, cudaEventDisableTiming));
   CREATE_CUDA(cudaEventCreateWithFlags(&s->ev_sel, cudaEventDisableTiming));
+  CREATE_CUDA(cudaEventCreateWithFlags(&s->ev_swp, cudaEventDisableTiming));
 
   const std::vector<int4> ft = gbta::factor_task_list(s->g), st = gbta::selinv_task_list(s->g),
                           stm = gbta::selinv_task_list(s->g, true);
@@ -389,6 +391,7 @@ int gbta_destroy(gbta_solver* s) {
   cudaFree(s->d_flags2);
   if (s->ev_fac) cudaEventDestroy(s->ev_fac);
   if (s->ev_sel) cudaEventDestroy(s->ev_sel);
+  if (s->ev_swp) cudaEventDestroy(s->ev_swp);
   if (s->side) cudaStreamDestroy(s->side);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
   delete s;
@@ -656,6 +659,7 @@ static int solve_async(gbta_solver* s, const double* D, const double* L, const d
     GBTA_CUDA(cudaGetLastError());
   }
   s->swept = true;
+  GBTA_CUDA(cudaEventRecord(s->ev_swp, s->stream));
   if (s->timing) {
     GBTA_CUDA(cudaEventRecord(s->tev[5], s->stream));
     s->timed[2] = true;
@@ -708,9 +712,16 @@ static int selinv_async(gbta_solver* s, double* D, double* L, double* R, double*
   // Sigma workspace), so it runs on the side stream from the factorization's completion,
   // next to whatever the solver's stream runs meanwhile (the sweeps), and the write-back
   // follows on the solver's stream after both.  Only when sweeps were enqueued since the
-  // factorization (with nothing to overlap the write-back is pure cost), and not while
-  // tracing (one trace buffer).
-  const bool over = s->overlap && tc_g && s->fac_evt && s->swept && !s->d_trace;
+  // factorization and have not finished yet (with nothing to overlap, the write-back is
+  // pure cost), and not while tracing (one trace buffer).
+  bool sweeping = false;
+  if (s->overlap && s->swept) {
+    const cudaError_t q = cudaEventQuery(s->ev_swp);
+    if (q != cudaSuccess && q != cudaErrorNotReady)
+      return fail(GBTA_ERR_CUDA, std::string("cudaEventQuery: ") + cudaGetErrorString(q));
+    sweeping = q == cudaErrorNotReady;
+  }
+  const bool over = s->overlap && tc_g && s->fac_evt && sweeping && !s->d_trace;
   // The tensor-core method reads the factor only through its digit planes, sliced by the
   // pre-pass, and the tip task reads T before it writes Sigma_T: without the overlap Sigma
   // goes straight into the caller's buffers.  The FP64 method reads the factor tiles

@@ -4,7 +4,8 @@ overlapped with them (gbta_set_selinv_overlap).
 The combined launch runs the same tile tasks as the forward and backward launches one
 after the other, and the overlapped inversion the same pre-pass and product loops into a
 workspace (written back afterwards) as the in-place one: results must be bit-identical
-to the plain calls, and agree with the oracle (the reference's recurrence,
+to the plain calls (the overlap is taken only while the sweeps are in flight, so the
+stream is held by a short spin kernel first), and agree with the oracle (the reference's recurrence,
 src/pyinla/solvers/structured_solver.py:83-190) at 1e-10.  b = 32 has one tile per block
 row, where the flag array has no room for the second sweep's flags and trans = 2 falls
 back to two launches.
@@ -43,6 +44,10 @@ def run(torch, D, L, R, T, rhs, b, nt, a, combined, overlap):
     x = torch.from_numpy(np.ascontiguousarray(rhs)).cuda()
     nrhs = 1 if rhs.ndim == 1 else rhs.shape[1]
     Rp, Tp = (Rd.data_ptr(), Td.data_ptr()) if a else (None, None)
+    # the inversion overlaps only sweeps that are still in flight when it is called:
+    # hold the stream (a bounded spin kernel of ~10 ms) so that they are
+    h.set_stream(torch.cuda.current_stream().cuda_stream)
+    torch.cuda._sleep(20_000_000)
     _lib.check(lib.gbta_pobtaf_async(h.ptr, Dd.data_ptr(), Ld.data_ptr(), Rp, Tp))
     if a:
         if combined:
@@ -52,13 +57,17 @@ def run(torch, D, L, R, T, rhs, b, nt, a, combined, overlap):
                 _lib.check(lib.gbta_pobtas_async(h.ptr, Dd.data_ptr(), Ld.data_ptr(), Rp, Tp, x.data_ptr(), nrhs, tr))
         _lib.check(lib.gbta_pobtasi(h.ptr, Dd.data_ptr(), Ld.data_ptr(), Rp, Tp))
     else:
-        for tr in ((2,) if combined else (0, 1)):
-            _lib.check(lib.gbta_pobts(h.ptr, Dd.data_ptr(), Ld.data_ptr(), x.data_ptr(), nrhs, tr))
+        if combined:   # queued (the bt sweeps without the arrow), so that they are in flight
+            _lib.check(lib.gbta_pobtas_async(h.ptr, Dd.data_ptr(), Ld.data_ptr(), None, None, x.data_ptr(), nrhs, 2))
+        else:
+            for tr in (0, 1):
+                _lib.check(lib.gbta_pobts(h.ptr, Dd.data_ptr(), Ld.data_ptr(), x.data_ptr(), nrhs, tr))
         _lib.check(lib.gbta_pobtsi(h.ptr, Dd.data_ptr(), Ld.data_ptr()))
     h.status()
     out = [t.cpu().numpy() for t in (x, Dd, Ld, Rd, Td)]
+    ws = h.workspace_bytes()
     h.close()
-    return out
+    return out, ws
 
 
 @pytest.mark.parametrize("b,nt,a,nrhs", [(96, 6, 3, 1), (64, 5, 0, 1), (32, 5, 2, 1), (70, 4, 4, 6)])
@@ -67,10 +76,13 @@ def test_combined_sweeps_and_overlapped_inversion(torch, b, nt, a, nrhs):
     if not a:
         R, T = np.zeros((nt, 0, b)), np.zeros((0, 0))
         rhs = rhs[: nt * b]
-    plain = run(torch, D, L, R, T, rhs, b, nt, a, combined=False, overlap=False)
-    both = run(torch, D, L, R, T, rhs, b, nt, a, combined=True, overlap=True)
+    plain, ws_plain = run(torch, D, L, R, T, rhs, b, nt, a, combined=False, overlap=False)
+    both, ws_both = run(torch, D, L, R, T, rhs, b, nt, a, combined=True, overlap=True)
     for got, want in zip(both, plain):
         assert np.array_equal(got, want)
+    # the overlapped inversion ran (into its Sigma workspace; the plain one works in place)
+    sig = 8 * (nt * b * b + (nt - 1) * b * b + nt * a * b + a * a)
+    assert ws_both - ws_plain >= sig, (ws_both, ws_plain, sig)
     # against the oracle: solution and selected inverse
     Dn, Ln, Rn, Tn = [np.array(v, copy=True) for v in (D, L, R, T)]
     xo = np.array(rhs, copy=True)
