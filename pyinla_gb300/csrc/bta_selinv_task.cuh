@@ -687,6 +687,37 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
     } else {
       trace_mark(c, t, 2);   // (diagonal task) product loop done
       const SigTile d = sig_dest(p, i, col, col);
+      // The merged finish below (Sigma(j2, c2) of block column i2) reads its right tile's
+      // digit planes, column exponents and zero-plane count from global memory: all three
+      // are copied into shared memory asynchronously from here (stage 0 is free after the
+      // loop), so that their latency passes under the symmetrisation instead of on the
+      // column chain.
+      // (the target's indices are recomputed after the symmetrisation rather than kept
+      // live across it: the kernel runs at its register limit)
+      auto merged_target = [&](int& i2, int& c2, int& j2) {
+        i2 = col > 0 ? i : (g.nprev(i) == 1 ? g.prev(i, 0) : -1);
+        c2 = col > 0 ? col - 1 : g.B - 1;
+        j2 = col > 0 ? col : g.B;
+        return p.merged && i2 >= 0;
+      };
+      int i2, c2, j2;
+      if (merged_target(i2, c2, j2)) {
+        oz_load_async(stages + OZ_OPER, p.fdig + (size_t)fac_slot(g, i2, j2, c2) * OZ_TILE);
+        if (threadIdx.x < TS) {
+          const int cc = c2 * TS + threadIdx.x;
+          if (cc < g.b)
+            cp_async4(ecol_t + threadIdx.x, p.ecol + (size_t)i2 * g.b + cc);
+          else
+            ecol_t[threadIdx.x] = 0;
+        }
+        if (threadIdx.x == 0) {   // (s_val[1] is free once the task has read its step count)
+          if (p.fdz)
+            cp_async4(s_val + 1, p.fdz + fac_slot(g, i2, j2, c2));
+          else
+            s_val[1] = 0;
+        }
+        cp_async_commit();
+      }
       // symmetrise: acc.v <- (acc.v + acc.v^T) / 2, through X
       acc_to_x(X, acc.v);
       __syncthreads();
@@ -708,18 +739,10 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
       // follow (its other consumers are later columns' products).  After column (i, 0)
       // the chain goes on in the one neighbour eliminated before i (none for the first
       // block of a chain; two for the separator, whose next tiles ordinary tasks form).
-      const int i2 = col > 0 ? i : (g.nprev(i) == 1 ? g.prev(i, 0) : -1);
-      const int c2 = col > 0 ? col - 1 : g.B - 1, j2 = col > 0 ? col : g.B;
-      if (p.merged && i2 >= 0) {
+      if (merged_target(i2, c2, j2)) {
         __half* A0 = stages;   // stage 0: this tile's digits (no copy is in flight after the loop)
-        __half* B0 = stages + OZ_OPER;
+        __half* B0 = stages + OZ_OPER;   // (its copy was issued above)
         double* X2 = F + TILE_SMEM;   // stage 1, after X and F: Sigma(j2, c2)
-        oz_load_async(B0, p.fdig + (size_t)fac_slot(g, i2, j2, c2) * OZ_TILE);
-        cp_async_commit();
-        if (threadIdx.x < TS) {
-          const int cc = c2 * TS + threadIdx.x;
-          ecol_t[threadIdx.x] = cc < g.b ? p.ecol[(size_t)i2 * g.b + cc] : 0;
-        }
         if (!cta_wait(c, p.part_flag + i2 * g.B + c2, nullptr, &s_ok)) return false;
         OzAcc a2;   // starts from the partial (its loads overlap the slicing below)
         oz_clear_partials(a2);
@@ -733,12 +756,12 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         oz_store_digits_uniform(A0, X, d.t.rows, d.t.cols, Ed == NO_EXP ? 0 : Ed);
         cp_async_wait_all();
         __syncthreads();
+        const int z2 = s_val[1];
         int es[2][4];
 #pragma unroll
         for (int n = 0; n < 2; ++n)
 #pragma unroll
           for (int q = 0; q < 4; ++q) es[n][q] = Ed + ecol_t[oz_col(n, q)];
-        const int z2 = p.fdz ? p.fdz[fac_slot(g, i2, j2, c2)] : 0;
         if (Ed > NO_EXP && !oz_pairs_vanish(0, z2)) {
           count_pairs(c, oz_pairs_issued(0, z2));
           oz_step_z<false>(a2, A0, B0, 0, z2);
