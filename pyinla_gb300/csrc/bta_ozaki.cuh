@@ -63,44 +63,58 @@ __device__ __forceinline__ int oz_row_exponent(double q) {
   return ilogb(sqrt(q)) + 2;
 }
 
-// The eight balanced digits of x relative to 2^E, as biased fields f_s = d_s + 64
-// (f_0 in [0, 128], the others in [0, 127]).  N + sum_s 64 * 128^(7-s) is non-negative
-// and its 7-bit fields are the biased digits, so the balanced decomposition costs
-// shifts and masks only (no carries to propagate).
-__device__ __forceinline__ void oz_digits(double x, int E, int (&f)[OZ_S]) {
+// The fixed-point value N = round(x 2^(55 - E)) (ties away from zero, |N| <= 2^55) of
+// x relative to 2^E, from the bits of x with integer instructions only and no branch
+// (lanes whose values sit in different binades take the same path): the 53-bit
+// significand m is shifted left by sh in [0, 2] or right, with rounding, by -sh; sh > 2
+// saturates (only reachable for x beyond the bound 2^(E-1)); zero, infinities and NaN
+// give 0.
+__device__ __forceinline__ long long oz_fixed(double x, int E) {
   const long long bits = __double_as_longlong(x);
   const int ex = (int)((bits >> 52) & 0x7ff);
-  long long N = 0;
-  if (ex != 0x7ff && (bits & 0x7fffffffffffffffll) != 0) {
-    const unsigned long long m = (bits & 0xfffffffffffffull) | (ex ? (1ull << 52) : 0ull);
-    const int sh = (ex ? ex : 1) - 1075 + 55 - E;   // |N| = round(|x| 2^(55 - E)) = round(m 2^sh)
-    unsigned long long F = 0;
-    if (sh >= 0)
-      F = (sh <= 2) ? (m << sh) : ~0ull;
-    else if (sh > -54)
-      F = (m + (1ull << (-sh - 1))) >> (-sh);         // round half up on the magnitude
-    if (F > (1ull << 55)) F = 1ull << 55;             // only reachable for out-of-bound input
-    N = bits < 0 ? -(long long)F : (long long)F;
-  }
+  const unsigned long long mag = (unsigned long long)bits & 0x7fffffffffffffffull;
+  const unsigned long long m = (bits & 0xfffffffffffffull) | (ex ? (1ull << 52) : 0ull);
+  const int sh = (ex ? ex : 1) - 1075 + 55 - E;   // |x| 2^(55 - E) = m 2^sh
+  const int ls = sh > 0 ? (sh < 2 ? sh : 2) : 0;
+  const int rs = sh >= 0 ? 0 : (sh > -63 ? -sh : 63);   // (a shift of 54 or more gives 0)
+  const unsigned long long half = rs > 0 ? (1ull << (rs - 1)) : 0ull;
+  unsigned long long F = ((m << ls) + half) >> rs;
+  F = sh > 2 ? (1ull << 55) : F;
+  F = F > (1ull << 55) ? (1ull << 55) : F;
+  F = (ex == 0x7ff || mag == 0) ? 0ull : F;
+  const long long sg = bits >> 63;   // 0 or -1
+  return ((long long)F ^ sg) - sg;
+}
+
+// The eight digit planes of two elements (fixed-point values N0, N1) as fp16 pairs, one
+// 32-bit word per plane (N0's digit in the low half).  The balanced base-128 digits are
+// the 7-bit fields of P = N + sum_s 64 * 128^s (non-negative, so no carries: each field
+// is d_s + 64; the top field d_0 + 64 is in [0, 128]).  P is split into two 28-bit
+// words holding planes 0-3 and 4-7, so that each plane of both elements comes from
+// 32-bit shifts and masks; the fp16 bit pattern 0x6400 + f is the integer 1024 + f, so
+// one half2 subtraction of 1088 turns both fields into their digits exactly.  Returns
+// the number of leading planes in which both digits are zero.
+__device__ __forceinline__ int oz_pair_planes(long long N0, long long N1, unsigned (&w)[OZ_S]) {
   constexpr unsigned long long BIAS = 0x0081020408102040ull;   // sum_{s=0..7} 64 * 128^s
-  const unsigned long long P = (unsigned long long)N + BIAS;
-  f[0] = (int)(P >> 49);
+  const unsigned long long P0 = (unsigned long long)N0 + BIAS, P1 = (unsigned long long)N1 + BIAS;
+  const unsigned h0 = (unsigned)(P0 >> 28), l0 = (unsigned)P0 & 0xfffffffu;
+  const unsigned h1 = (unsigned)(P1 >> 28), l1 = (unsigned)P1 & 0xfffffffu;
+  const __half h1088 = __ushort_as_half((unsigned short)0x6440);
+  const __half2 off = __halves2half2(h1088, h1088);
+  int lz = 0;
 #pragma unroll
-  for (int s = 1; s < OZ_S; ++s) f[s] = (int)((P >> (OZ_W * (OZ_S - 1 - s))) & 127);
-}
-
-__device__ __forceinline__ void oz_zero_digits(int (&f)[OZ_S]) {
-#pragma unroll
-  for (int s = 0; s < OZ_S; ++s) f[s] = OZ_ZERO;
-}
-
-// Number of leading zero digits (0 .. OZ_S; OZ_S for x = 0) of a digit vector.
-__device__ __forceinline__ int oz_lead_zeros(const int (&f)[OZ_S]) {
-  int z = 0;
-#pragma unroll
-  for (int s = 0; s < OZ_S; ++s)
-    if (z == s && f[s] == OZ_ZERO) z = s + 1;
-  return z;
+  for (int s = 0; s < OZ_S; ++s) {
+    const unsigned a = s < 4 ? h0 : l0, b = s < 4 ? h1 : l1;
+    const int k = OZ_W * (3 - (s & 3));   // 21, 14, 7, 0 within the 28-bit word
+    const unsigned mk = s == 0 ? 0xffu : 0x7fu;
+    const unsigned lo = (a >> k) & mk;
+    const unsigned hi = (k <= 16 ? (b << (16 - k)) : (b >> (k - 16))) & (mk << 16);
+    const unsigned f = lo | hi | 0x64006400u;
+    if (lz == s && f == 0x64406440u) lz = s + 1;   // both fields 64: both digits 0
+    const __half2 hv = __hsub2(*reinterpret_cast<const __half2*>(&f), off);
+    w[s] = *reinterpret_cast<const unsigned*>(&hv);
+  }
+  return lz;
 }
 
 // Minimum of v over the CTA (every thread gets it); red: NT / 32 ints of shared memory.
@@ -125,16 +139,6 @@ __device__ __forceinline__ bool oz_pairs_vanish(int za, int zb) {
   return za >= OZ_S || zb >= OZ_S || za + zb > OZ_ND - 1;
 }
 
-// Two digits given by their biased fields (0 <= f <= 128) as an exact fp16 pair
-// without conversion instructions: the fp16 bit pattern 0x6400 + f is the integer
-// 1024 + f, so (0x6400 + f) - 1088 = f - 64 = d exactly (1088 = 0x6440), one half2
-// subtraction for both.
-__device__ __forceinline__ unsigned oz_digit_pair(int f0, int f1) {
-  const unsigned bits = (unsigned)(0x6400 + f0) | ((unsigned)(0x6400 + f1) << 16);
-  const __half h1088 = __ushort_as_half((unsigned short)0x6440);
-  const __half2 h = __hsub2(*reinterpret_cast<const __half2*>(&bits), __halves2half2(h1088, h1088));
-  return *reinterpret_cast<const unsigned*>(&h);
-}
 
 // Write the digit planes of the valid part of a shared FP64 tile X (rows x cols)
 // to dst ([plane][row][col] halves), row r relative to 2^Eof(r).  Each thread converts
@@ -145,18 +149,13 @@ __device__ __forceinline__ void oz_store_digits_e(__half* dst, const double* X, 
   for (int q = 0; q < PER_THREAD / 2; ++q) {
     const int p = threadIdx.x + q * NT;
     const int r = p / (TS / 2), c = 2 * (p % (TS / 2));
-    int d0[OZ_S], d1[OZ_S];
-    if (r < rows && c < cols)
-      oz_digits(X[r * LDS + c], Eof(r), d0);
-    else
-      oz_zero_digits(d0);
-    if (r < rows && c + 1 < cols)
-      oz_digits(X[r * LDS + c + 1], Eof(r), d1);
-    else
-      oz_zero_digits(d1);
+    const long long n0 = (r < rows && c < cols) ? oz_fixed(X[r * LDS + c], Eof(r)) : 0ll;
+    const long long n1 = (r < rows && c + 1 < cols) ? oz_fixed(X[r * LDS + c + 1], Eof(r)) : 0ll;
+    unsigned wv[OZ_S];
+    oz_pair_planes(n0, n1, wv);
     unsigned* w = reinterpret_cast<unsigned*>(dst + oz_swz(r, c));
 #pragma unroll
-    for (int s = 0; s < OZ_S; ++s) w[s * (OZ_PLANE / 2)] = oz_digit_pair(d0[s], d1[s]);
+    for (int s = 0; s < OZ_S; ++s) w[s * (OZ_PLANE / 2)] = wv[s];
   }
 }
 
@@ -166,18 +165,13 @@ __device__ __forceinline__ void oz_store_digits_rows(__half* dst, const double* 
                                                      const int* E) {
   static_assert(FEED_ROWS * TS / 2 == NT, "one column pair of the row group per thread");
   const int r = row0 + threadIdx.x / (TS / 2), c = 2 * (threadIdx.x % (TS / 2));
-  int d0[OZ_S], d1[OZ_S];
-  if (r < rows && c < cols)
-    oz_digits(X[r * LDS + c], E[r], d0);
-  else
-    oz_zero_digits(d0);
-  if (r < rows && c + 1 < cols)
-    oz_digits(X[r * LDS + c + 1], E[r], d1);
-  else
-    oz_zero_digits(d1);
+  const long long n0 = (r < rows && c < cols) ? oz_fixed(X[r * LDS + c], E[r]) : 0ll;
+  const long long n1 = (r < rows && c + 1 < cols) ? oz_fixed(X[r * LDS + c + 1], E[r]) : 0ll;
+  unsigned wv[OZ_S];
+  oz_pair_planes(n0, n1, wv);
   unsigned* w = reinterpret_cast<unsigned*>(dst + oz_swz(r, c));
 #pragma unroll
-  for (int s = 0; s < OZ_S; ++s) w[s * (OZ_PLANE / 2)] = oz_digit_pair(d0[s], d1[s]);
+  for (int s = 0; s < OZ_S; ++s) w[s * (OZ_PLANE / 2)] = wv[s];
 }
 
 // Rows relative to per-row exponents E[row].

@@ -96,19 +96,13 @@ __global__ void __launch_bounds__(NT) k_fac_digits_t(const double* D, const doub
     const int p = threadIdx.x + q * NT;
     const int jj = p % TS, m = 2 * (p / TS);
     const int e = (jj < t.cols) ? ecol[(size_t)i * g.b + c * TS + jj] : 0;
-    int d0[OZ_S], d1[OZ_S];
-    if (m < t.rows && jj < t.cols)
-      oz_digits(x0[q], e, d0);
-    else
-      oz_zero_digits(d0);
-    if (m + 1 < t.rows && jj < t.cols)
-      oz_digits(x1[q], e, d1);
-    else
-      oz_zero_digits(d1);
+    const long long n0 = (m < t.rows && jj < t.cols) ? oz_fixed(x0[q], e) : 0ll;
+    const long long n1 = (m + 1 < t.rows && jj < t.cols) ? oz_fixed(x1[q], e) : 0ll;
+    unsigned wv[OZ_S];
+    lz = min(lz, oz_pair_planes(n0, n1, wv));
     unsigned* w = reinterpret_cast<unsigned*>(planes + oz_swz(jj, m));
 #pragma unroll
-    for (int s = 0; s < OZ_S; ++s) w[s * (OZ_PLANE / 2)] = oz_digit_pair(d0[s], d1[s]);
-    lz = min(lz, min(oz_lead_zeros(d0), oz_lead_zeros(d1)));
+    for (int s = 0; s < OZ_S; ++s) w[s * (OZ_PLANE / 2)] = wv[s];
   }
   lz = cta_min_int(lz, red);   // (contains the barriers that complete the planes)
   // with the counts, the inversion reads no plane below min(lz, OZ_SB_MAX) (oz_step_z)
