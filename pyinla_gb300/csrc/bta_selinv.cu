@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(NT) k_g_tiles_oz(double* D, double* L, double*
       esum[n][q] = er[oz_row(n, q)] + ec[oz_col(n, q)];
     }
   oz_step(acc, As, Bs);
-  oz_fold_sub(acc, esum);   // acc.v = -G
+  oz_fold_sub_short(acc, esum);   // acc.v = -G (one step)
 #pragma unroll
   for (int n = 0; n < 2; ++n)
 #pragma unroll

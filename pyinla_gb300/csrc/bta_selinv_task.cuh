@@ -641,7 +641,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
             En = sig_exp_decode(*s_val, c.epoch);
           }
           if ((En > E && En != NO_EXP) || since_fold == OZ_CHUNK) {
-            if (E > NO_EXP) oz_fold_sub(acc, esum);
+            if (E > NO_EXP) oz_fold_sub_steps(acc, esum, since_fold);
             since_fold = 0;
             if (En > E && En != NO_EXP) {
               E = En;
@@ -651,7 +651,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
           if (!have) stage(nst, nt_, sig_shift(E, En), s + 1);
           tcur = nt_.trans;
         } else if (E > NO_EXP) {
-          oz_fold_sub(acc, esum);   // acc.v = -(sum)
+          oz_fold_sub_steps(acc, esum, since_fold);   // acc.v = -(sum)
         }
       }
     }
@@ -765,7 +765,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         if (Ed > NO_EXP && !oz_pairs_vanish(0, z2)) {
           count_pairs(c, oz_pairs_issued(0, z2));
           oz_step_z<false>(a2, A0, B0, 0, z2);
-          oz_fold_sub(a2, es);
+          oz_fold_sub_short(a2, es);   // (one step)
         }
         const SigTile d2 = sig_dest(p, i2, j2, c2);
         acc_to_x(X2, a2.v);
