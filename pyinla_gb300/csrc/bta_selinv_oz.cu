@@ -12,27 +12,34 @@ namespace gbta {
 // coupling slot, R_i).
 __global__ void __launch_bounds__(NT) k_fac_col_exponents(const double* D, const double* L, const double* R, Geom g,
                                                           int use_arrow, int* ecol) {
-  __shared__ double red[NT];
+  // the maximum magnitude as the integer maximum of the magnitude bits (the order of
+  // non-negative doubles; no FP64 instruction), NaN and infinity giving exponent 0
+  __shared__ unsigned long long red[NT];
   const int ic = blockIdx.x;
   const int i = ic / g.B, c = ic % g.B;
   const size_t bb = (size_t)g.b * g.b, ab = (size_t)g.a * g.b;
   const int j = threadIdx.x % TS, r0 = threadIdx.x / TS;   // 4 row groups
   const int col = c * TS + j;
-  double m = 0.0;
+  auto mag = [](double x) {
+    return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+  };
+  unsigned long long m = 0;
   if (col < g.b) {
-    for (int row = (c + 1) * TS + r0; row < g.b; row += NT / TS) m = fmax(m, fabs(D[i * bb + (size_t)row * g.b + col]));
+    for (int row = (c + 1) * TS + r0; row < g.b; row += NT / TS) m = max(m, mag(D[i * bb + (size_t)row * g.b + col]));
     if (g.nxt(i) >= 0) {
       const size_t ls = (size_t)g.lslot(i);
-      for (int row = r0; row < g.b; row += NT / TS) m = fmax(m, fabs(L[ls * bb + (size_t)row * g.b + col]));
+      for (int row = r0; row < g.b; row += NT / TS) m = max(m, mag(L[ls * bb + (size_t)row * g.b + col]));
     }
     if (use_arrow)
-      for (int row = r0; row < g.a; row += NT / TS) m = fmax(m, fabs(R[i * ab + (size_t)row * g.b + col]));
+      for (int row = r0; row < g.a; row += NT / TS) m = max(m, mag(R[i * ab + (size_t)row * g.b + col]));
   }
   red[threadIdx.x] = m;
   __syncthreads();
   if (threadIdx.x < TS) {
-    double mm = fmax(fmax(red[threadIdx.x], red[threadIdx.x + TS]), fmax(red[threadIdx.x + 2 * TS], red[threadIdx.x + 3 * TS]));
-    if (col < g.b) ecol[(size_t)i * g.b + col] = (mm > 0.0 && isfinite(mm)) ? ilogb(mm) + 1 : 0;
+    const unsigned long long mm =
+        max(max(red[threadIdx.x], red[threadIdx.x + TS]), max(red[threadIdx.x + 2 * TS], red[threadIdx.x + 3 * TS]));
+    const bool finite = mm < 0x7ff0000000000000ull;
+    if (col < g.b) ecol[(size_t)i * g.b + col] = (mm != 0 && finite) ? ilogb_bits(mm) + 1 : 0;
   }
 }
 
