@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(NT) k_diag_inverses(const double* D, Geom g, d
 // own, in place, or a separate set; the kernel reads no FP64 factor tile).  Coupling
 // tiles that are structurally zero (kf, launch_coupling_kfirst) are zero in place and
 // written as zeros into a separate set (zero_skipped).
-__global__ void __launch_bounds__(NT) k_g_tiles_oz(double* D, double* L, double* R, Geom g, int use_arrow,
+__global__ void __launch_bounds__(NT, 3) k_g_tiles_oz(double* D, double* L, double* R, Geom g, int use_arrow,
                                                    const __half* fdig, const int* erow, const __half* wdig,
                                                    const int* ew, const int* kf, int zero_skipped) {
   __shared__ __align__(16) __half As[OZ_OPER];
