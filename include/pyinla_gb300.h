@@ -129,16 +129,18 @@ int gbta_get_twist(const gbta_solver* s);
  * stream in between (the sweeps of gbta_pobtas), and writes Sigma into a workspace of the
  * size of the blocks; the write-back into the caller's blocks is enqueued on the solver's
  * stream, after that work and the inversion.  The blocks must hold the factor that
- * gbta_pobtaf left until then (the sweeps only read them).  The sweeps then run one CTA
- * per SM and the inversion's CTAs fill the rest of each SM.  An inversion with no sweep
- * enqueued since the factorization runs in place on the solver's stream as without the
- * option (there is nothing to overlap).  Status words of both streams are read by
- * gbta_status. */
+ * gbta_pobtaf left until then (the sweeps only read them).  The sweeps keep one CTA per
+ * SM and the inversion's CTAs fill the rest of each SM.  An inversion called when no
+ * sweep enqueued since the factorization is still in flight runs in place on the
+ * solver's stream as without the option (there is nothing to overlap).  Status words
+ * of both streams are read by gbta_status. */
 int gbta_set_selinv_overlap(gbta_solver* s, int enable);
 
 /* Persistent CTAs per SM of the dataflow launches (0, the default: as many as the
- * kernel's registers and shared memory allow; GBTA_CTAS_PER_SM in the environment
- * sets the initial value).  No reference counterpart (a launch-shape setting). */
+ * kernel's registers and shared memory allow for the factorization and the selected
+ * inversion, one for the sweeps, whose latency-bound chain runs fastest so;
+ * GBTA_CTAS_PER_SM in the environment sets the initial value).  No reference
+ * counterpart (a launch-shape setting). */
 int gbta_set_ctas_per_sm(gbta_solver* s, int n);
 
 /* Task tracing (off by default).  When enabled, every dataflow kernel launched by

@@ -641,9 +641,11 @@ static int solve_async(gbta_solver* s, const double* D, const double* L, const d
     const int nc = nrhs - c0 < gbta::SOLVE_NC ? nrhs - c0 : gbta::SOLVE_NC;
     if (int r = reset_ticket(s)) return r;
     gbta::LaunchCtl lc = next_launch(s, ntasks);
-    // with the overlapped inversion the sweeps keep to one CTA per SM (the chain needs
-    // few; the inversion's CTAs take the rest of each SM)
-    if (s->overlap && s->ctas_per_sm == 0) lc.ctas_per_sm = 1;
+    // the sweeps run one CTA per SM unless set otherwise: their chain needs few, and
+    // more spend the SMs' issue slots and memory traffic on waiting tasks (alone at
+    // nt = 128, b = 1024: 9.7 ms against 12.4 ms with as many as fit), and next to an
+    // overlapped inversion its CTAs take the rest of each SM
+    if (s->ctas_per_sm == 0) lc.ctas_per_sm = 1;
     if (both) {
       gbta::launch_solve(s->g, D, L, R, T, B + c0, nrhs, nc, 0, use_arrow, s->d_arrow_part, lc, 1);
     } else {
@@ -651,7 +653,7 @@ static int solve_async(gbta_solver* s, const double* D, const double* L, const d
         if (tr == 1 && trans == 2) {   // the second sweep of trans = 2: its own launch
           if (int r = reset_ticket(s)) return r;
           lc = next_launch(s, ntasks);
-          if (s->overlap && s->ctas_per_sm == 0) lc.ctas_per_sm = 1;
+          if (s->ctas_per_sm == 0) lc.ctas_per_sm = 1;
         }
         gbta::launch_solve(s->g, D, L, R, T, B + c0, nrhs, nc, tr, use_arrow, s->d_arrow_part, lc);
       }
