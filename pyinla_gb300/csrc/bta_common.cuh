@@ -544,6 +544,14 @@ template <int N> __device__ __forceinline__ void nbar_sync_n(int id) {
 // updated through pivot j, from its owner to the pivot warp (64 threads).
 constexpr int POTRF_BAR_L = 1, POTRF_BAR_C = 9;
 
+// x > 0 (false for zeros and NaN, true for +inf) by integer compares on the bits: a
+// double compare is an FP64-unit instruction, and on the pivot chain it would occupy
+// that unit for a full slot per pivot.
+__device__ __forceinline__ bool positive_bits(double x) {
+  const long long b = __double_as_longlong(x);
+  return b > 0 && b <= 0x7ff0000000000000ll;
+}
+
 // 1/d with the third-order refinement in three dependent FMAs (for a chain that counts
 // FP64 instructions): e = 1 - d y, y <- y + y (e + e^2).
 __device__ __forceinline__ double rcp3_fma(double d) {
@@ -634,7 +642,7 @@ static __device__ int smem_potrf(double* S) {
     const double u0 = S[r * LDS];       // column 0 of U is column 0 of S
     const double a1 = S[r * LDS + 1];   // column 1 takes no update before pivot 0
     double dk = __shfl_sync(0xffffffffu, u0, 0);   // lane k keeps d_k
-    if (r == 0 && !(dk > 0.0)) atomicMin(&s_info, 1);
+    if (r == 0 && !positive_bits(dk)) atomicMin(&s_info, 1);
     double wp = u0 * rcp3_fma(dk);
     s_wring[0][r] = wp;
     nbar_arrive(POTRF_BAR_L);
@@ -647,7 +655,7 @@ static __device__ int smem_potrf(double* S) {
       const double d = __shfl_sync(0xffffffffu, a, k);
       if (r == k) dk = d;
       S[r * LDS + k] = u;
-      if (r == 0 && !(d > 0.0)) atomicMin(&s_info, k + 1);
+      if (r == 0 && !positive_bits(d)) atomicMin(&s_info, k + 1);
       if (k < TS - 1) {
         const double sk = rcp3_fma(d);
         // Column k+1, updated through pivot k-1 by its owner, is awaited and loaded
