@@ -718,7 +718,8 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
         }
         cp_async_commit();
       }
-      // symmetrise: acc.v <- (acc.v + acc.v^T) / 2, through X
+      // symmetrise: the lower triangle mirrored into the upper one, through X (selects
+      // only: no FP64 instruction on the chain)
       acc_to_x(X, acc.v);
       __syncthreads();
 #pragma unroll
@@ -726,7 +727,7 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           const int r = oz_row(n, q), cc = oz_col(n, q);
-          acc.v[n][q] = 0.5 * (X[r * LDS + cc] + X[cc * LDS + r]);
+          if (r < cc) acc.v[n][q] = X[cc * LDS + r];
         }
       __syncthreads();
       acc_to_x(X, acc.v);
