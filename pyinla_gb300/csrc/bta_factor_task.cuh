@@ -674,7 +674,7 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
           }
         }
         oz_step(acc, cur, cur + OZ_OPER);
-        if ((s + 1) % OZ_CHUNK == 0 || !more) oz_fold_sub(acc, esum);
+        if ((s + 1) % OZ_CHUNK == 0) oz_fold_sub(acc, esum);   // (the last fold follows the loop)
         if (more && !issued) {
           slots(s + 1, na, nb);
           if (!(ok = cta_wait(c, c.flags + na, na == nb ? nullptr : c.flags + nb, &s_ok))) break;
@@ -685,6 +685,17 @@ static __device__ __forceinline__ bool factor_oz_task(const FactorArgs& p, int t
       }
     }
     if (!ok) return false;   // no copy is in flight here
+    {
+      // the steps since the last fold, folded out of the loop: the short form when there
+      // are at most OZ_SHORT of them (a diagonal tail's last fold is on the column chain)
+      const int rest = nsteps % OZ_CHUNK;
+      if (rest != 0) {
+        if (rest <= OZ_SHORT)
+          oz_fold_sub_short(acc, esum);
+        else
+          oz_fold_sub(acc, esum);
+      }
+    }
     if (threadIdx.x == 0) pp->phase = ph;
     count_pairs(c, (unsigned long long)nsteps * oz_pairs_from(0, 0));
     __syncthreads();
