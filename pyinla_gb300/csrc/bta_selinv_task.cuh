@@ -650,12 +650,11 @@ static __device__ __forceinline__ bool selinv_oz_task(const SelinvArgs& p, int t
           }
           if (!have) stage(nst, nt_, sig_shift(E, En), s + 1);
           tcur = nt_.trans;
-        } else if (E > NO_EXP) {
-          oz_fold_sub_steps(acc, esum, since_fold);   // acc.v = -(sum)
         }
       }
     }
     if (!ok) return false;   // no copy is in flight here
+    if (np > 0 && E > NO_EXP) oz_fold_sub_steps(acc, esum, since_fold);   // acc.v = -(sum)
     if (threadIdx.x == 0) pp->phase = ph;
     count_pairs(c, npairs);
     trace_put(c, t, 2, (long long)waited);
